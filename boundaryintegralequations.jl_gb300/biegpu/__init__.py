@@ -1,0 +1,14 @@
+"""biegpu - GB300-native collocation BEM hot path of BoundaryIntegralEquations.jl.
+
+The compute path is libbiegpu.so (CUDA, sm_103a) behind a C ABI
+(include/biegpu.h); this package is its Python host side, mirroring the
+reference's Julia API for the path:
+
+  * ``Mesh3d`` and mesh builders (:mod:`biegpu.mesh`)
+  * ``assemble_parallel`` -> (F, G, C)  (:mod:`biegpu.assembly`)
+"""
+from ._capi import BIEError, lib, library_path  # noqa: F401
+from .assembly import Context, assemble_parallel, get_context, quadrature_rule  # noqa: F401
+from .mesh import Mesh3d, ellipsoid, icosphere, load_comsol, read_comsol  # noqa: F401
+
+__version__ = "0.1.0"

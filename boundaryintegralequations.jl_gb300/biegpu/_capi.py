@@ -1,0 +1,147 @@
+"""ctypes binding of libbiegpu.so (the C ABI declared in include/biegpu.h).
+
+This is the Python counterpart of the ``ccall`` glue a Julia caller uses: the
+same entry points, the same plain pointers and sizes.  There is no CPU
+fallback: if the library cannot be built or loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import _build
+
+BIE_OK = 0
+BIE_ERR_INVALID = -1
+BIE_ERR_CUDA = -2
+BIE_ERR_NOT_CONVERGED = -3
+BIE_ERR_TIMEOUT = -4
+BIE_ERR_NOMEM = -5
+BIE_ERR_UNSUPPORTED = -6
+
+BIE_TRI_LINEAR = 1
+BIE_TRI_QUADRATIC = 2
+
+BIE_F = 1
+BIE_G = 2
+BIE_C = 4
+
+BIE_PREC_FP64 = 0
+BIE_PREC_MIXED = 1
+
+KIND = {"linear": BIE_TRI_LINEAR, "quadratic": BIE_TRI_QUADRATIC}
+PRECISION = {"fp64": BIE_PREC_FP64, "mixed": BIE_PREC_MIXED}
+
+_ERRNAMES = {
+    BIE_ERR_INVALID: "invalid argument",
+    BIE_ERR_CUDA: "CUDA error",
+    BIE_ERR_NOT_CONVERGED: "not converged",
+    BIE_ERR_TIMEOUT: "device wait timed out",
+    BIE_ERR_NOMEM: "out of memory",
+    BIE_ERR_UNSUPPORTED: "unsupported",
+}
+
+
+class BIEError(RuntimeError):
+    """A libbiegpu call returned a negative status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{_ERRNAMES.get(code, 'error')} ({code}): {message}")
+        self.code = code
+        self.message = message
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("n_coordinates", C.c_int64),
+        ("coordinates", C.POINTER(C.c_double)),
+        ("n_elements", C.c_int64),
+        ("shape_kind", C.c_int32),
+        ("physics_kind", C.c_int32),
+        ("topology", C.POINTER(C.c_int64)),
+        ("physics_topology", C.POINTER(C.c_int64)),
+        ("n_sources", C.c_int64),
+        ("sources", C.POINTER(C.c_double)),
+        ("quad_n", C.c_int32),
+        ("quad_m", C.c_int32),
+    ]
+
+
+class Peaks(C.Structure):
+    _fields_ = [("fp64_flops", C.c_double), ("fp32_flops", C.c_double)]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("kernel_launches", C.c_int64),
+        ("timed_launches", C.c_int64),
+        ("timed_ms", C.c_double),
+        ("algorithmic_flops", C.c_double),
+        ("quadrature_evals", C.c_int64),
+    ]
+
+
+_lib = None
+_lock = threading.Lock()
+
+_P = C.c_void_p
+_D = C.c_double
+_I = C.c_int
+_I64 = C.c_int64
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "bie_version": (C.c_char_p, []),
+    "bie_last_error": (C.c_char_p, []),
+    "bie_quadrature_rule": (_I, [_I, _I, _I, _P, _P, _P, _I, C.POINTER(_I)]),
+    "bie_ctx_create": (_I, [C.POINTER(_P), C.POINTER(MeshDesc), _I]),
+    "bie_ctx_destroy": (_I, [_P]),
+    "bie_ctx_stream": (_I, [_P, C.POINTER(_P)]),
+    "bie_measure_peaks": (_I, [_I, C.POINTER(Peaks)]),
+    "bie_ctx_set_timing": (_I, [_P, _I]),
+    "bie_ctx_stats": (_I, [_P, C.POINTER(Stats), _I]),
+    "bie_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
+    "bie_assemble_device": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
+}
+
+
+def library_path() -> Path:
+    return _build.LIB_PATH
+
+
+def lib():
+    """Load libbiegpu.so (building it first if it is missing or stale)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            L = C.CDLL(str(path))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+        return _lib
+
+
+def measure_peaks(device: int = 0) -> dict:
+    """Measured FP64 / FP32 FMA throughput of a device in FLOP/s."""
+    p = Peaks()
+    check(lib().bie_measure_peaks(int(device), C.byref(p)))
+    return {"fp64_flops": p.fp64_flops, "fp32_flops": p.fp32_flops}
+
+
+def check(status: int) -> None:
+    if status != BIE_OK:
+        msg = lib().bie_last_error().decode(errors="replace")
+        raise BIEError(status, msg)
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data

@@ -1,0 +1,151 @@
+"""Dense collocation assembly on the GPU, mirroring ``assemble_parallel!``.
+
+``assemble_parallel(mesh, k, sources; fOn, gOn, cOn, n, m)`` has the argument
+meaning, defaults (n = m = 4) and return value (F, G, C) of the reference's
+dispatcher (src/3d/assembly_collocation.jl:259-268): F and G are
+``len(targets) x N`` complex128 matrices in column-major (Fortran) order, the
+memory layout of Julia's ``Matrix{ComplexF64}``, and C is a complex vector.
+Everything is computed by libbiegpu.so on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import weakref
+
+import numpy as np
+
+from . import _capi
+from .mesh import Mesh3d
+
+
+def quadrature_rule(n: int, m: int, node: int):
+    """(u, v, w) of the collocation rule clustered at element node ``node`` (1..6),
+    computed by libbiegpu's host code (no GPU needed)."""
+    cap = 2 * n * (m + 1) + 8
+    u, v, w = (np.zeros(cap) for _ in range(3))
+    cnt = C.c_int()
+    _capi.check(_capi.lib().bie_quadrature_rule(n, m, node, u.ctypes.data, v.ctypes.data,
+                                                w.ctypes.data, cap, C.byref(cnt)))
+    q = cnt.value
+    return u[:q].copy(), v[:q].copy(), w[:q].copy()
+
+
+class Context:
+    """A libbiegpu context: one mesh, one quadrature order (n, m), one device."""
+
+    def __init__(self, mesh: Mesh3d, n: int = 4, m: int = 4, device: int = 0):
+        L = _capi.lib()
+        self.mesh = mesh
+        self.n, self.m, self.device = int(n), int(m), int(device)
+        # keep the arrays alive while the descriptor points at them
+        self._coords = np.asfortranarray(mesh.coordinates, dtype=np.float64)
+        self._topo = np.asfortranarray(mesh.topology, dtype=np.int64)
+        self._ptopo = np.asfortranarray(mesh.physics_topology, dtype=np.int64)
+        self._src = np.asfortranarray(mesh.sources, dtype=np.float64)
+        desc = _capi.MeshDesc(
+            n_coordinates=self._coords.shape[1],
+            coordinates=self._coords.ctypes.data_as(C.POINTER(C.c_double)),
+            n_elements=self._topo.shape[1],
+            shape_kind=_capi.KIND[mesh.shape_function],
+            physics_kind=_capi.KIND[mesh.physics_function],
+            topology=self._topo.ctypes.data_as(C.POINTER(C.c_int64)),
+            physics_topology=self._ptopo.ctypes.data_as(C.POINTER(C.c_int64)),
+            n_sources=self._src.shape[1],
+            sources=self._src.ctypes.data_as(C.POINTER(C.c_double)),
+            quad_n=self.n,
+            quad_m=self.m,
+        )
+        h = C.c_void_p()
+        _capi.check(L.bie_ctx_create(C.byref(h), C.byref(desc), self.device))
+        self._h = h
+        self._finalizer = weakref.finalize(self, L.bie_ctx_destroy, h)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def n_sources(self) -> int:
+        return self.mesh.n_sources
+
+    def close(self) -> None:
+        self._finalizer()
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _capi.check(_capi.lib().bie_ctx_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def set_timing(self, on: bool) -> None:
+        _capi.check(_capi.lib().bie_ctx_set_timing(self._h, 1 if on else 0))
+
+    def stats(self, reset: bool = False) -> dict:
+        st = _capi.Stats()
+        _capi.check(_capi.lib().bie_ctx_stats(self._h, C.byref(st), 1 if reset else 0))
+        return {name: getattr(st, name) for name, _ in st._fields_}
+
+    # ---- host-buffer assembly (the reference-facing call) -----------------
+    def assemble(self, k, targets=None, fOn=True, gOn=True, cOn=True, precision="fp64",
+                 out=None):
+        """(F, G, C) on the host; ``targets`` is 3 x M (None = mesh sources)."""
+        k = complex(k)
+        N = self.n_sources
+        if targets is not None:
+            t = np.asfortranarray(targets, dtype=np.float64)
+            if t.ndim != 2 or t.shape[0] != 3:
+                raise ValueError("targets must be a 3 x M array")
+            M = t.shape[1]
+        else:
+            t, M = None, N
+        flags = (_capi.BIE_F if fOn else 0) | (_capi.BIE_G if gOn else 0) | (_capi.BIE_C if cOn else 0)
+        if out is not None:
+            F, G, Cv = out
+        else:
+            F = np.empty((M, N), dtype=np.complex128, order="F") if fOn else None
+            G = np.empty((M, N), dtype=np.complex128, order="F") if gOn else None
+            Cv = np.empty(M, dtype=np.complex128) if cOn else None
+        _capi.check(_capi.lib().bie_assemble(
+            self._h, k.real, k.imag, _capi.ptr(t), M, flags, _capi.PRECISION[precision],
+            _capi.ptr(F), _capi.ptr(G), _capi.ptr(Cv)))
+        return F, G, Cv
+
+    # ---- device-buffer assembly (torch tensors, enqueued on the context stream)
+    def assemble_device(self, k, F=None, G=None, Cv=None, targets=None, precision="fp64"):
+        """Fill device tensors: F, G complex128 of shape (N, M) in row-major torch
+        terms (= column-major M x N), Cv complex128 (M,).  Asynchronous."""
+        k = complex(k)
+        M = self.n_sources if targets is None else int(targets.shape[-1] if targets.ndim == 2 and targets.shape[0] == 3 else targets.shape[0])
+        flags = (_capi.BIE_F if F is not None else 0) | (_capi.BIE_G if G is not None else 0) | \
+                (_capi.BIE_C if Cv is not None else 0)
+        _capi.check(_capi.lib().bie_assemble_device(
+            self._h, k.real, k.imag, _capi.ptr(targets), M, flags, _capi.PRECISION[precision],
+            _capi.ptr(F), _capi.ptr(G), _capi.ptr(Cv)))
+
+
+_CTX_CACHE: "weakref.WeakKeyDictionary[Mesh3d, dict]" = weakref.WeakKeyDictionary()
+
+
+def get_context(mesh: Mesh3d, n: int = 4, m: int = 4, device: int = 0) -> Context:
+    """Cached context per (mesh object, n, m, device)."""
+    d = _CTX_CACHE.setdefault(mesh, {})
+    key = (int(n), int(m), int(device))
+    if key not in d:
+        d[key] = Context(mesh, n=n, m=m, device=device)
+    return d[key]
+
+
+def assemble_parallel(mesh: Mesh3d, k, sources=None, fOn=True, gOn=True, cOn=True,
+                      sparse=False, m=4, n=4, progress=True, depth=2, offset=None,
+                      precision="fp64", device=0):
+    """GPU ``assemble_parallel!``: returns (F, G, C).
+
+    ``sources`` are the collocation/field points (3 x M); passing
+    ``mesh.sources`` (or None) assembles the square BEM matrices.  ``progress``
+    is accepted and ignored.  ``sparse=True`` (the near-field-only assembly)
+    is not part of this library yet and raises.
+    """
+    if sparse:
+        raise NotImplementedError("sparse (near-field) assembly is not provided by libbiegpu yet")
+    ctx = get_context(mesh, n=n, m=m, device=device)
+    targets = None if sources is None or sources is mesh.sources else sources
+    return ctx.assemble(k, targets=targets, fOn=fOn, gOn=gOn, cOn=cOn, precision=precision)

@@ -1,0 +1,295 @@
+// K1: dense FP64 collocation assembly of F (double layer), G (single layer) and
+// C (k = 0 double-layer row sums) for 3- and 6-node triangles.
+//
+// Replaces the hot loop of assemble_parallel! (src/3d/assembly_collocation.jl:
+// 314-349 and 424-476) with computing_integrals! (:213-252), the kernels
+// greens3d!, freens3d!, freens3dk0! (src/3d/kernels.jl:13-55), the nearest
+// physics node rule choice find_closest_corner (:102-115) and the
+// accumulation mygemm_vec! (src/2d/assembly_collocation.jl:142-150).
+//
+// Work decomposition (one GPU):
+//   grid.x  tiles of 128 target rows, one thread per row i
+//   grid.y  S element slices (contiguous ranges of the Morton-ordered element
+//           records), so that even a few thousand rows fill all 152 SMs
+// Each block stages a chunk of element records (quadrature points, normals,
+// jacobian x weight for every clustered rule, the physics-node coordinates and
+// indices) in shared memory; every thread walks the chunk for its own row.
+// F and G are column-major M x N complex128 (the layout of Julia's
+// Matrix{ComplexF64}); a warp's 32 consecutive rows give one coalesced 512-byte
+// access per node.  A (row, node) entry whose node is touched by one slice only
+// is updated with a plain read-modify-write by the one thread that owns the row;
+// nodes shared between slices are updated with FP64 atomics.  C is accumulated
+// per slice and reduced by a second kernel.
+#include "bie_internal.h"
+
+#include <algorithm>
+
+namespace bie {
+
+namespace {
+
+constexpr double kInv4Pi = 0.07957747154594767;   // 1 / (4 pi)
+constexpr int kThreads = 128;
+
+struct RuleInfo {
+    int Q[kMaxRules];
+    int off[kMaxRules];
+};
+
+// Julia's 3-argument hypot (maximum-abs scaling, IEEE-rounded division and
+// square root, ((a^2 + b^2) + c^2) summation), evaluated bit-exactly.
+__device__ __forceinline__ double julia_hypot3(double x, double y, double z) {
+    const double m = fmax(fmax(fabs(x), fabs(y)), fabs(z));
+    if (m == 0.0) return 0.0;
+    const double a = __ddiv_rn(x, m), b = __ddiv_rn(y, m), c = __ddiv_rn(z, m);
+    const double s = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
+    return __dmul_rn(m, __dsqrt_rn(s));
+}
+
+// find_closest_corner (src/3d/assembly_collocation.jl:102-115): index of the
+// physics node nearest to the target, strict '<' so the first of equal
+// distances wins.  Squared distances decide whenever the runner-up is more
+// than 1e-12 (relative) farther; only near-ties are re-decided with the exact
+// Julia hypot so the choice is the reference's in every case.
+template <int NP>
+__device__ __forceinline__ int nearest_node(const double *r, double tx, double ty, double tz) {
+    double d2[NP];
+#pragma unroll
+    for (int a = 0; a < NP; ++a) {
+        const double dx = r[3 * a + 0] - tx, dy = r[3 * a + 1] - ty, dz = r[3 * a + 2] - tz;
+        d2[a] = dx * dx + dy * dy + dz * dz;
+    }
+    int c = 0;
+    double b = d2[0];
+#pragma unroll
+    for (int a = 1; a < NP; ++a)
+        if (d2[a] < b) {
+            b = d2[a];
+            c = a;
+        }
+    const double lim = b * (1.0 + 1e-12);
+    bool tie = false;
+#pragma unroll
+    for (int a = 0; a < NP; ++a) tie |= (a != c) && (d2[a] <= lim);
+    if (tie) {
+        double best = __longlong_as_double(0x7ff0000000000000LL);
+        c = 0;
+#pragma unroll
+        for (int a = 0; a < NP; ++a) {
+            const double h = julia_hypot3(__dsub_rn(r[3 * a + 0], tx), __dsub_rn(r[3 * a + 1], ty),
+                                          __dsub_rn(r[3 * a + 2], tz));
+            if (h < best) {
+                best = h;
+                c = a;
+            }
+        }
+    }
+    return c;
+}
+
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(kThreads)
+assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
+                     int64_t E, int S, const uint32_t *__restrict__ smask,
+                     const double *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
+                     const double *__restrict__ tgt, int64_t M, double kre, double kim,
+                     int flags, double2 *__restrict__ F, double2 *__restrict__ G,
+                     double *__restrict__ Cpart, int chunk,
+                     unsigned long long *__restrict__ qpe_count) {
+    extern __shared__ __align__(16) double smem[];
+    double *s_phi = smem;                                   // nphi doubles (padded even)
+    double *s_rec = smem + ((nphi + 1) & ~1);               // chunk * stride doubles
+    uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);
+
+    const int s = blockIdx.y;
+    const int64_t e0 = (int64_t)s * E / S;
+    const int64_t e1 = (int64_t)(s + 1) * E / S;
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = i < M;
+    const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
+
+    double tx = 0, ty = 0, tz = 0;
+    if (active) {
+        tx = tgt[3 * i + 0];
+        ty = tgt[3 * i + 1];
+        tz = tgt[3 * i + 2];
+    }
+    for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+
+    double cacc = 0.0;
+    unsigned long long nqpe = 0;
+    for (int64_t cb = e0; cb < e1; cb += chunk) {
+        const int n = (int)min((int64_t)chunk, e1 - cb);
+        __syncthreads();   // previous chunk fully consumed
+        {
+            const double2 *src = reinterpret_cast<const double2 *>(rec + cb * stride);
+            double2 *dst = reinterpret_cast<double2 *>(s_rec);
+            const int n2 = n * stride / 2;
+            for (int t = threadIdx.x; t < n2; t += kThreads) dst[t] = src[t];
+            for (int t = threadIdx.x; t < n; t += kThreads) s_mask[t] = smask[cb + t];
+        }
+        __syncthreads();
+        if (!active) continue;
+
+        for (int el = 0; el < n; ++el) {
+            const double *r = s_rec + (size_t)el * stride;
+            const int c = nearest_node<NP>(r, tx, ty, tz);
+            const int Q = ri.Q[c];
+            nqpe += Q;
+            const double *g = r + ri.off[c];
+            const double *ph = s_phi + (size_t)c * qmax * NP;
+
+            double fr[NP], fi[NP], gr[NP], gi[NP];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.0;
+            double ce = 0.0;
+
+            for (int q = 0; q < Q; ++q) {
+                const double dx = g[q] - tx;
+                const double dy = g[Q + q] - ty;
+                const double dz = g[2 * Q + q] - tz;
+                const double r2 = dx * dx + dy * dy + dz * dz;
+                const double rinv = rsqrt(r2);
+                const double rr = r2 * rinv;
+                const double jw = g[6 * Q + q];
+                const double dn = g[3 * Q + q] * dx + g[4 * Q + q] * dy + g[5 * Q + q] * dz;
+                double sn, cs;
+                sincos(kre * rr, &sn, &cs);
+                if (CPLX_K) {
+                    const double damp = exp(-kim * rr);
+                    sn *= damp;
+                    cs *= damp;
+                }
+                // G: e^{ikr} / (4 pi r) * jw
+                const double wg = rinv * kInv4Pi * jw;
+                const double Gr = cs * wg, Gi = sn * wg;
+                // C: -(x - y).n / (4 pi r^3) * jw ; F: e^{ikr} (ikr - 1) (x - y).n / (4 pi r^3) * jw
+                const double tq = dn * (rinv * rinv * rinv) * kInv4Pi * jw;
+                ce -= tq;
+                const double ar = CPLX_K ? (-1.0 - kim * rr) : -1.0;
+                const double ai = kre * rr;
+                const double Fr = (cs * ar - sn * ai) * tq;
+                const double Fi = (cs * ai + sn * ar) * tq;
+                const double *pq = ph + q * NP;
+#pragma unroll
+                for (int a = 0; a < NP; ++a) {
+                    const double p = pq[a];
+                    fr[a] += Fr * p;
+                    fi[a] += Fi * p;
+                    gr[a] += Gr * p;
+                    gi[a] += Gi * p;
+                }
+            }
+            cacc += ce;
+
+            const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
+            const uint32_t m = s_mask[el];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
+                if ((m >> a) & 1u) {
+                    if (doF) {
+                        atomicAdd(&F[off].x, fr[a]);
+                        atomicAdd(&F[off].y, fi[a]);
+                    }
+                    if (doG) {
+                        atomicAdd(&G[off].x, gr[a]);
+                        atomicAdd(&G[off].y, gi[a]);
+                    }
+                } else {
+                    if (doF) {
+                        double2 v = F[off];
+                        v.x += fr[a];
+                        v.y += fi[a];
+                        F[off] = v;
+                    }
+                    if (doG) {
+                        double2 v = G[off];
+                        v.x += gr[a];
+                        v.y += gi[a];
+                        G[off] = v;
+                    }
+                }
+            }
+        }
+    }
+    if (active && doC) Cpart[(int64_t)s * M + i] = cacc;
+    // one atomic per warp for the evaluation counter
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+__global__ void reduce_c_kernel(const double *__restrict__ Cpart, int S, int64_t M,
+                                double2 *__restrict__ C) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    double acc = 0.0;
+    for (int s = 0; s < S; ++s) acc += Cpart[(int64_t)s * M + i];
+    C[i] = make_double2(acc, 0.0);
+}
+
+template <int NP, bool CPLX>
+void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int chunk,
+               double *Cpart) {
+    const RecordLayout &L = c.lay;
+    RuleInfo ri{};
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = L.Q[r];
+        ri.off[r] = L.rule_off[r];
+    }
+    auto kern = assemble_fp64_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((a.M + kThreads - 1) / kThreads), (unsigned)S);
+    cudaEvent_t t0 = c.timer_begin();
+    kern<<<grid, kThreads, smem, c.stream>>>(
+        c.d_records, L.stride, L.nidx_off, c.n_elements, S,
+        c.d_shared_mask + (size_t)level * c.n_elements, c.d_phi, L.R * L.qmax * L.NP, L.qmax,
+        ri, a.targets, a.M, a.k_re, a.k_im, a.flags, reinterpret_cast<double2 *>(a.F),
+        reinterpret_cast<double2 *>(a.G), Cpart, chunk, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    c.timer_end(t0);
+    ++c.kernel_launches;
+}
+
+}  // namespace
+
+void launch_assemble_fp64(Ctx &c, const AssembleArgs &a) {
+    const RecordLayout &L = c.lay;
+    const int64_t N = c.n_sources;
+    if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
+    if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));
+    if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;
+
+    // slices: enough blocks for ~8 per SM, power of two, at most one per element
+    const int64_t row_tiles = (a.M + kThreads - 1) / kThreads;
+    int level = 0;
+    while (level + 1 < kMaxLevels && row_tiles * (int64_t(1) << level) < 8LL * c.num_sms &&
+           (int64_t(2) << level) <= c.n_elements)
+        ++level;
+    const int S = 1 << level;
+
+    // element chunk: ~40 KB of records per block
+    const size_t rec_bytes = (size_t)L.stride * sizeof(double);
+    int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (40u << 10) / rec_bytes));
+    const size_t phi_d = (size_t)((L.R * L.qmax * L.NP + 1) & ~1);
+    const size_t smem = phi_d * sizeof(double) + (size_t)chunk * rec_bytes + (size_t)chunk * 4;
+
+    double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
+    const bool cplx = a.k_im != 0.0;
+    if (L.NP == 3) {
+        if (cplx) launch_np<3, true>(c, a, S, level, smem, chunk, Cpart);
+        else launch_np<3, false>(c, a, S, level, smem, chunk, Cpart);
+    } else {
+        if (cplx) launch_np<6, true>(c, a, S, level, smem, chunk, Cpart);
+        else launch_np<6, false>(c, a, S, level, smem, chunk, Cpart);
+    }
+    if (a.flags & BIE_C) {
+        reduce_c_kernel<<<(unsigned)((a.M + 255) / 256), 256, 0, c.stream>>>(
+            Cpart, S, a.M, reinterpret_cast<double2 *>(a.C));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+}
+
+}  // namespace bie

@@ -1,0 +1,153 @@
+// Internal declarations shared by the host set-up code and the CUDA kernels of
+// libbiegpu.so.  Nothing here crosses the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/biegpu.h"
+
+namespace bie {
+
+// ----------------------------------------------------------------------------
+// Errors: every internal failure throws bie::Error; the C-ABI wrappers catch it,
+// store the message in a thread-local string and return the code.
+// ----------------------------------------------------------------------------
+struct Error {
+    int code;
+    std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string &msg);
+void cuda_check(cudaError_t e, const char *what);
+#define BIE_CUDA(call) ::bie::cuda_check((call), #call)
+
+// ----------------------------------------------------------------------------
+// Quadrature rules on the reference triangle (u, v >= 0, u + v <= 1).
+// ----------------------------------------------------------------------------
+struct Rule {
+    std::vector<double> u, v, w;
+    int size() const { return (int)w.size(); }
+};
+
+// Gauss-Legendre nodes/weights on [-1, 1], ascending nodes.
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w);
+// Duffy rule clustered at element node `corner` (1, 2, 3) built from an n x m
+// tensor Gauss grid; node 1 = rotated rule, node 2 = plain Duffy rule, node 3 =
+// plain Duffy with u and v swapped.  src/3d/quadrature.jl:70-113.
+Rule duffy_corner_rule(int n, int m, int corner);
+// Two half-Duffy triangles split at edge midpoint `vertex` (4, 5, 6), m rounded
+// up to even.  src/3d/quadrature.jl:116-144.
+Rule duffy_midpoint_rule(int n, int m, int vertex);
+// Symmetric triangle rules with n in {1, 3, 4, 7, 12, 13} points
+// (src/3d/adaptive_integration.jl:13-64).
+Rule triangle_gauss_rule(int n);
+
+// Shape functions of the 3- and 6-node triangles (src/3d/surface_functions.jl:191-236).
+int  n_nodes_of_kind(int kind);
+void shape_values(int kind, double u, double v, double *N);
+void shape_derivs(int kind, double u, double v, double *dNu, double *dNv);
+
+// ----------------------------------------------------------------------------
+// Per-element record consumed by the assembly kernels (doubles, element-major).
+//   [0, 3*NP)                       physics-node coordinates, a-major (x, y, z)
+//   rule r at rule_off[r]:          x[Q_r] y[Q_r] z[Q_r] nx[Q_r] ny[Q_r] nz[Q_r] jw[Q_r]
+//   nidx_off:                       NP int32 physics-node indices (0-based)
+// The stride is even so every record starts on a 16-byte boundary.
+// ----------------------------------------------------------------------------
+constexpr int kMaxRules = 6;
+constexpr int kMaxNP = 6;
+constexpr int kMaxQ = 64;
+constexpr int kMaxLevels = 8;   // element slicings 1, 2, 4, ..., 128
+
+struct RecordLayout {
+    int NP = 0;                 // physics nodes per element (3 or 6)
+    int R = 0;                  // number of clustered rules (3 or 6)
+    int Q[kMaxRules] = {};      // points per rule
+    int rule_off[kMaxRules] = {};
+    int nidx_off = 0;
+    int stride = 0;             // doubles per record
+    int qmax = 0;
+};
+
+enum ScratchSlot {
+    kScratchTargets = 0,   // uploaded target points (host entry points)
+    kScratchF = 1,         // device F (host entry points)
+    kScratchG = 2,         // device G (host entry points)
+    kScratchCpart = 3,     // per-slice partial C row sums
+    kScratchC = 4,         // device C (host entry points)
+    kScratchCount = 8
+};
+
+struct Ctx {
+    std::mutex mu;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+
+    // mesh (host copies, 0-based)
+    int shape_kind = 0, physics_kind = 0;
+    int64_t n_coords = 0, n_elements = 0, n_sources = 0;
+    int NS = 0;                          // geometry nodes per element
+    std::vector<double> coords;          // 3 x Nc
+    std::vector<int32_t> topo;           // NS x E
+    std::vector<int32_t> ptopo;          // NP x E
+    std::vector<double> sources;         // 3 x N
+    int quad_n = 0, quad_m = 0;
+
+    // clustered rules and physics interpolation tables Phi[r][q][a]
+    RecordLayout lay;
+    std::vector<Rule> rules;
+    std::vector<double> phi;             // R x qmax x NP
+
+    // element order (Morton order of centroids); records follow this order
+    std::vector<int32_t> order;
+
+    // device data
+    double *d_records = nullptr;         // E x stride, Morton order
+    double *d_phi = nullptr;             // R x qmax x NP
+    double *d_sources = nullptr;         // 3 x N (AoS)
+    uint32_t *d_shared_mask = nullptr;   // kMaxLevels x E: bit a set -> node a is
+                                         // touched by elements of another slice
+
+    // grow-only device scratch, indexed by the kScratch* slots below
+    void *d_scratch[8] = {};
+    size_t scratch_bytes[8] = {};
+    void *scratch(int slot, size_t bytes);
+
+    // launch statistics (bie_ctx_stats)
+    bool timing = false;
+    int64_t kernel_launches = 0;
+    int64_t timed_launches = 0;
+    double timed_ms = 0.0;
+    unsigned long long *d_qpe = nullptr;     // device counter of quadrature evaluations
+    std::vector<cudaEvent_t> ev_free;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
+    cudaEvent_t take_event();
+    // Bracket the dominant kernel of a call: timer_begin() before its launch,
+    // timer_end() after; both are no-ops while timing is off.
+    cudaEvent_t timer_begin();
+    void timer_end(cudaEvent_t a);
+    void collect_timers();   // synchronises the stream
+};
+
+// Host set-up (bie_setup.cpp)
+void build_context(Ctx &c, const bie_mesh_desc &d, int device);
+void destroy_context(Ctx &c);
+
+// Kernel launchers (bie_assemble.cu)
+struct AssembleArgs {
+    double k_re, k_im;
+    const double *targets;   // device, 3 x M AoS
+    int64_t M;
+    int flags;
+    double *F, *G, *C;       // device outputs (interleaved complex), may be null
+};
+void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
+
+// FMA throughput probe (bie_peaks.cu)
+void measure_peaks(int device, bie_peaks &out);
+
+}  // namespace bie

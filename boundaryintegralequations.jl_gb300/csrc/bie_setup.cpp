@@ -1,0 +1,556 @@
+// Host-side set-up of a libbiegpu context: quadrature rules, shape functions,
+// per-element quadrature geometry, element ordering and slicing.
+//
+// Reference behaviour followed (BoundaryIntegralEquations.jl):
+//   Gauss-Legendre on [0,1]           src/2d/quadrature.jl:5-11
+//   Duffy rules clustered at nodes    src/3d/quadrature.jl:70-113
+//   midpoint (two half-Duffy) rules   src/3d/quadrature.jl:116-144
+//   triangle shape functions          src/3d/surface_functions.jl:191-236
+//   rule per closest node, tables     src/3d/assembly_collocation.jl:122-136, 284-305, 369-413
+//   element interpolation + jacobian  src/3d/assembly_collocation.jl:27-66, src/3d/jacobian.jl:78-87
+#include "bie_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace bie {
+
+[[noreturn]] void fail(int code, const std::string &msg) { throw Error{code, msg}; }
+
+void cuda_check(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) {
+        int code = (e == cudaErrorMemoryAllocation) ? BIE_ERR_NOMEM : BIE_ERR_CUDA;
+        fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gauss-Legendre: Newton iteration on the three-term Legendre recurrence, run in
+// long double and rounded once, so the nodes/weights are correctly rounded to
+// within an ulp of the exact values (the reference takes them from
+// FastGaussQuadrature.gausslegendre, which is accurate to the same level).
+// ---------------------------------------------------------------------------
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+    if (n < 1) fail(BIE_ERR_INVALID, "gauss_legendre: n must be >= 1");
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    const long double pi = 3.141592653589793238462643383279502884L;
+    for (int i = 0; i < (n + 1) / 2; ++i) {
+        // initial guess for the (i+1)-th largest root
+        long double z = std::cos(pi * (i + 0.75L) / (n + 0.5L));
+        long double pn = 0, dpn = 1;
+        for (int it = 0; it < 100; ++it) {
+            long double p0 = 1, p1 = z;
+            for (int j = 2; j <= n; ++j) {
+                long double p2 = ((2 * j - 1) * z * p1 - (j - 1) * p0) / j;
+                p0 = p1;
+                p1 = p2;
+            }
+            pn = (n == 1) ? z : p1;
+            long double pm = (n == 1) ? 1.0L : p0;
+            dpn = n * (z * pn - pm) / (z * z - 1.0L);
+            long double dz = pn / dpn;
+            z -= dz;
+            if (std::fabs((double)dz) < 1e-19) break;
+        }
+        // re-evaluate the derivative at the converged root for the weight
+        {
+            long double p0 = 1, p1 = z;
+            for (int j = 2; j <= n; ++j) {
+                long double p2 = ((2 * j - 1) * z * p1 - (j - 1) * p0) / j;
+                p0 = p1;
+                p1 = p2;
+            }
+            long double pm = (n == 1) ? 1.0L : p0;
+            long double pnn = (n == 1) ? z : p1;
+            dpn = n * (z * pnn - pm) / (z * z - 1.0L);
+        }
+        long double wi = 2.0L / ((1.0L - z * z) * dpn * dpn);
+        // ascending order: the largest root goes last
+        x[n - 1 - i] = (double)z;
+        x[i] = (double)(-z);
+        w[n - 1 - i] = (double)wi;
+        w[i] = (double)wi;
+    }
+    if (n % 2 == 1) x[n / 2] = 0.0;
+}
+
+// nodes/weights mapped to [0, 1]
+static void gl01(int n, std::vector<double> &x, std::vector<double> &w) {
+    gauss_legendre(n, x, w);
+    for (int i = 0; i < n; ++i) {
+        w[i] = 0.5 * w[i];
+        x[i] = 0.5 * (x[i] + 1.0);
+    }
+}
+
+// tensor grid with the u index fastest: point j*n + i has (x_i, y_j, wy_j*wx_i)
+static void tensor01(int n, int m, std::vector<double> &u, std::vector<double> &v,
+                     std::vector<double> &w) {
+    std::vector<double> xn, wn, xm, wm;
+    gl01(n, xn, wn);
+    gl01(m, xm, wm);
+    u.resize(n * m);
+    v.resize(n * m);
+    w.resize(n * m);
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < n; ++i) {
+            u[j * n + i] = xn[i];
+            v[j * n + i] = xm[j];
+            w[j * n + i] = wm[j] * wn[i];
+        }
+}
+
+Rule duffy_corner_rule(int n, int m, int corner) {
+    if (corner < 1 || corner > 3) fail(BIE_ERR_INVALID, "duffy_corner_rule: corner must be 1..3");
+    std::vector<double> u, v, w;
+    tensor01(n, m, u, v, w);
+    Rule r;
+    const int Q = n * m;
+    r.u.resize(Q);
+    r.v.resize(Q);
+    r.w.resize(Q);
+    for (int q = 0; q < Q; ++q) {
+        double xi, eta, wt;
+        if (corner == 1) {          // collapsed towards node 1
+            xi = u[q] * v[q];
+            eta = (1.0 - u[q]) * v[q];
+            wt = w[q] * v[q];
+        } else {                    // collapsed towards node 3 (plain Duffy)
+            xi = u[q];
+            eta = v[q] * (1.0 - u[q]);
+            wt = w[q] * std::fabs(1.0 - u[q]);
+        }
+        if (corner == 3) std::swap(xi, eta);   // mirror: clusters at node 3
+        r.u[q] = xi;
+        r.v[q] = eta;
+        r.w[q] = wt;
+    }
+    return r;
+}
+
+Rule duffy_midpoint_rule(int n, int m, int vertex) {
+    if (vertex < 4 || vertex > 6) fail(BIE_ERR_INVALID, "duffy_midpoint_rule: vertex must be 4..6");
+    const int me = ((m + 1) / 2) * 2;
+    std::vector<double> u, v, w;
+    tensor01(n, me, u, v, w);
+    const int H = n * me;
+    std::vector<double> X(2 * H), Y(2 * H), W(2 * H);
+    for (int q = 0; q < H; ++q) {
+        X[q] = 0.5 * u[q];
+        Y[q] = v[q] * (1.0 - u[q]);
+        W[q] = w[q] * (0.5 * (1.0 - u[q]));
+        X[H + q] = (u[q] - 0.5) * v[q] + 0.5;
+        Y[H + q] = v[q] * (1.0 - u[q]);
+        W[H + q] = w[q] * (0.5 * v[q]);
+    }
+    Rule r;
+    r.w = W;
+    r.u.resize(2 * H);
+    r.v.resize(2 * H);
+    for (int q = 0; q < 2 * H; ++q) {
+        if (vertex == 4) {
+            r.u[q] = X[q];
+            r.v[q] = Y[q];
+        } else if (vertex == 5) {
+            r.u[q] = (1.0 - X[q]) - Y[q];
+            r.v[q] = X[q];
+        } else {
+            r.u[q] = Y[q];
+            r.v[q] = (1.0 - X[q]) - Y[q];
+        }
+    }
+    return r;
+}
+
+Rule triangle_gauss_rule(int n) {
+    // Symmetric rules on the unit triangle (weights sum to 1/2).  These are the
+    // standard published Strang-Fix / Dunavant tables, in the same point order as
+    // gauss_points_triangle (src/3d/adaptive_integration.jl:13-64).
+    static const double r1[] = {1.0 / 3, 1.0 / 3, 0.5};
+    static const double r3[] = {1.0 / 6, 1.0 / 6, 1.0 / 6, 2.0 / 3, 1.0 / 6, 1.0 / 6,
+                                1.0 / 6, 2.0 / 3, 1.0 / 6};
+    static const double r4[] = {1.0 / 3, 1.0 / 3, -9.0 / 32, 0.2, 0.6, 25.0 / 96,
+                                0.2, 0.2, 25.0 / 96, 0.6, 0.2, 25.0 / 96};
+    static const double r7[] = {
+        1.0 / 3, 1.0 / 3, 0.1125,
+        0.797426985353087, 0.101286507323456, 0.0629695902724135,
+        0.101286507323456, 0.797426985353087, 0.0629695902724135,
+        0.101286507323456, 0.101286507323456, 0.0629695902724135,
+        0.059715871789770, 0.470142064105115, 0.066197076394253,
+        0.470142064105115, 0.059715871789770, 0.066197076394253,
+        0.470142064105115, 0.470142064105115, 0.066197076394253};
+    static const double r12[] = {
+        0.873821971016996, 0.063089014491502, 0.0254224531851035,
+        0.063089014491502, 0.873821971016996, 0.0254224531851035,
+        0.063089014491502, 0.063089014491502, 0.0254224531851035,
+        0.501426509658279, 0.249286745170910, 0.0583931378631895,
+        0.249286745170910, 0.501426509658279, 0.0583931378631895,
+        0.249286745170910, 0.249286745170910, 0.0583931378631895,
+        0.636502499121399, 0.310352451033785, 0.041425537809187,
+        0.636502499121399, 0.053145049844816, 0.041425537809187,
+        0.310352451033785, 0.636502499121399, 0.041425537809187,
+        0.310352451033785, 0.053145049844816, 0.041425537809187,
+        0.053145049844816, 0.636502499121399, 0.041425537809187,
+        0.053145049844816, 0.310352451033785, 0.041425537809187};
+    static const double r13[] = {
+        1.0 / 3, 1.0 / 3, -0.074785022233835,
+        0.479308067841923, 0.260345966079038, 0.087807628716602,
+        0.260345966079038, 0.479308067841923, 0.087807628716602,
+        0.260345966079038, 0.260345966079038, 0.087807628716602,
+        0.869739794195568, 0.065130102902216, 0.0266736178044195,
+        0.065130102902216, 0.869739794195568, 0.0266736178044195,
+        0.065130102902216, 0.065130102902216, 0.0266736178044195,
+        0.638444188569809, 0.312865496004875, 0.0385568804451285,
+        0.638444188569809, 0.048690315425316, 0.0385568804451285,
+        0.312865496004875, 0.638444188569809, 0.0385568804451285,
+        0.312865496004875, 0.048690315425316, 0.0385568804451285,
+        0.048690315425316, 0.638444188569809, 0.0385568804451285,
+        0.048690315425316, 0.312865496004875, 0.0385568804451285};
+    const double *t = nullptr;
+    switch (n) {
+        case 1: t = r1; break;
+        case 3: t = r3; break;
+        case 4: t = r4; break;
+        case 7: t = r7; break;
+        case 12: t = r12; break;
+        case 13: t = r13; break;
+        default: fail(BIE_ERR_UNSUPPORTED, "triangle rule with n=" + std::to_string(n) +
+                                              " points (supported: 1,3,4,7,12,13)");
+    }
+    Rule r;
+    for (int i = 0; i < n; ++i) {
+        r.u.push_back(t[3 * i]);
+        r.v.push_back(t[3 * i + 1]);
+        r.w.push_back(t[3 * i + 2]);
+    }
+    return r;
+}
+
+int n_nodes_of_kind(int kind) {
+    if (kind == BIE_TRI_LINEAR) return 3;
+    if (kind == BIE_TRI_QUADRATIC) return 6;
+    fail(BIE_ERR_UNSUPPORTED, "unknown element kind " + std::to_string(kind));
+}
+
+void shape_values(int kind, double u, double v, double *N) {
+    if (kind == BIE_TRI_LINEAR) {
+        N[0] = (1.0 - u) - v;
+        N[1] = u;
+        N[2] = v;
+    } else {
+        const double l = (1.0 - v) - u;
+        N[0] = l * ((1.0 - 2.0 * v) - 2.0 * u);
+        N[1] = u * (2.0 * u - 1.0);
+        N[2] = v * (2.0 * v - 1.0);
+        N[3] = 4.0 * u * l;
+        N[4] = 4.0 * u * v;
+        N[5] = 4.0 * v * l;
+    }
+}
+
+void shape_derivs(int kind, double u, double v, double *dNu, double *dNv) {
+    if (kind == BIE_TRI_LINEAR) {
+        dNu[0] = -1; dNu[1] = 1; dNu[2] = 0;
+        dNv[0] = -1; dNv[1] = 0; dNv[2] = 1;
+    } else {
+        const double l = (1.0 - v) - u;
+        const double d1 = -(2.0 * l - 1.0) - 2.0 * l;
+        dNu[0] = d1; dNu[1] = 4.0 * u - 1.0; dNu[2] = 0.0;
+        dNu[3] = 4.0 * l - 4.0 * u; dNu[4] = 4.0 * v; dNu[5] = -4.0 * v;
+        dNv[0] = d1; dNv[1] = 0.0; dNv[2] = 4.0 * v - 1.0;
+        dNv[3] = -4.0 * u; dNv[4] = 4.0 * u; dNv[5] = 4.0 * l - 4.0 * v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Morton code of a point in the unit cube (10 bits per axis)
+// ---------------------------------------------------------------------------
+static uint32_t spread10(uint32_t x) {
+    x &= 0x3ff;
+    x = (x | (x << 16)) & 0x030000ff;
+    x = (x | (x << 8)) & 0x0300f00f;
+    x = (x | (x << 4)) & 0x030c30c3;
+    x = (x | (x << 2)) & 0x09249249;
+    return x;
+}
+
+void *Ctx::scratch(int slot, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    if (scratch_bytes[slot] < bytes) {
+        if (d_scratch[slot]) BIE_CUDA(cudaFree(d_scratch[slot]));
+        d_scratch[slot] = nullptr;
+        scratch_bytes[slot] = 0;
+        BIE_CUDA(cudaMalloc(&d_scratch[slot], bytes));
+        scratch_bytes[slot] = bytes;
+    }
+    return d_scratch[slot];
+}
+
+cudaEvent_t Ctx::take_event() {
+    if (!ev_free.empty()) {
+        cudaEvent_t e = ev_free.back();
+        ev_free.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    BIE_CUDA(cudaEventCreate(&e));
+    return e;
+}
+
+cudaEvent_t Ctx::timer_begin() {
+    if (!timing) return nullptr;
+    cudaEvent_t a = take_event();
+    BIE_CUDA(cudaEventRecord(a, stream));
+    return a;
+}
+
+void Ctx::timer_end(cudaEvent_t a) {
+    if (!timing || !a) return;
+    cudaEvent_t b = take_event();
+    BIE_CUDA(cudaEventRecord(b, stream));
+    ev_pending.emplace_back(a, b);
+    ++timed_launches;
+}
+
+void Ctx::collect_timers() {
+    BIE_CUDA(cudaStreamSynchronize(stream));
+    for (auto &p : ev_pending) {
+        float ms = 0.f;
+        BIE_CUDA(cudaEventElapsedTime(&ms, p.first, p.second));
+        timed_ms += ms;
+        ev_free.push_back(p.first);
+        ev_free.push_back(p.second);
+    }
+    ev_pending.clear();
+}
+
+void build_context(Ctx &c, const bie_mesh_desc &d, int device) {
+    // ---- validation -------------------------------------------------------
+    if (d.n_coordinates <= 0 || d.n_elements <= 0 || d.n_sources <= 0)
+        fail(BIE_ERR_INVALID, "mesh sizes must be positive");
+    if (!d.coordinates || !d.topology || !d.physics_topology || !d.sources)
+        fail(BIE_ERR_INVALID, "mesh arrays must not be NULL");
+    if (d.n_coordinates > INT32_MAX || d.n_sources > INT32_MAX || d.n_elements > INT32_MAX)
+        fail(BIE_ERR_INVALID, "mesh too large for 32-bit node indices");
+    const int NS = n_nodes_of_kind(d.shape_kind);
+    const int NP = n_nodes_of_kind(d.physics_kind);
+    if (d.shape_kind == BIE_TRI_LINEAR && d.physics_kind == BIE_TRI_QUADRATIC)
+        fail(BIE_ERR_UNSUPPORTED, "quadratic physics on linear geometry is not supported");
+    if (d.quad_n < 1 || d.quad_m < 1 || d.quad_n > 32 || d.quad_m > 32)
+        fail(BIE_ERR_INVALID, "quad_n and quad_m must be in 1..32");
+    c.shape_kind = d.shape_kind;
+    c.physics_kind = d.physics_kind;
+    c.n_coords = d.n_coordinates;
+    c.n_elements = d.n_elements;
+    c.n_sources = d.n_sources;
+    c.NS = NS;
+    c.quad_n = d.quad_n;
+    c.quad_m = d.quad_m;
+    const int64_t E = d.n_elements;
+
+    c.coords.assign(d.coordinates, d.coordinates + 3 * d.n_coordinates);
+    c.sources.assign(d.sources, d.sources + 3 * d.n_sources);
+    for (double x : c.coords)
+        if (!std::isfinite(x)) fail(BIE_ERR_INVALID, "non-finite mesh coordinate");
+    for (double x : c.sources)
+        if (!std::isfinite(x)) fail(BIE_ERR_INVALID, "non-finite source coordinate");
+    c.topo.resize((size_t)NS * E);
+    c.ptopo.resize((size_t)NP * E);
+    for (int64_t i = 0; i < NS * E; ++i) {
+        int64_t t = d.topology[i];
+        if (t < 1 || t > d.n_coordinates)
+            fail(BIE_ERR_INVALID, "topology index out of range at entry " + std::to_string(i));
+        c.topo[i] = (int32_t)(t - 1);
+    }
+    for (int64_t i = 0; i < NP * E; ++i) {
+        int64_t t = d.physics_topology[i];
+        if (t < 1 || t > d.n_sources)
+            fail(BIE_ERR_INVALID, "physics_topology index out of range at entry " + std::to_string(i));
+        c.ptopo[i] = (int32_t)(t - 1);
+    }
+
+    // ---- clustered rules ---------------------------------------------------
+    // Linear geometry: three rules clustered at the corners.  Quadratic geometry:
+    // one rule per physics node (corners, then edge midpoints 4-6).
+    const int R = (d.shape_kind == BIE_TRI_LINEAR) ? 3 : NP;
+    c.rules.clear();
+    for (int r = 0; r < R; ++r)
+        c.rules.push_back(r < 3 ? duffy_corner_rule(d.quad_n, d.quad_m, r + 1)
+                                : duffy_midpoint_rule(d.quad_n, d.quad_m, r + 1));
+    RecordLayout &L = c.lay;
+    L = RecordLayout{};
+    L.NP = NP;
+    L.R = R;
+    int off = 3 * NP;
+    for (int r = 0; r < R; ++r) {
+        L.Q[r] = c.rules[r].size();
+        if (L.Q[r] > kMaxQ)
+            fail(BIE_ERR_INVALID, "quadrature rule has more than 64 points; reduce quad_n/quad_m");
+        L.qmax = std::max(L.qmax, L.Q[r]);
+        L.rule_off[r] = off;
+        off += 7 * L.Q[r];
+    }
+    L.nidx_off = off;
+    off += (NP + 1) / 2;
+    L.stride = (off + 1) & ~1;
+
+    // physics interpolation at each rule's points: Phi[r][q][a]
+    c.phi.assign((size_t)R * L.qmax * NP, 0.0);
+    for (int r = 0; r < R; ++r)
+        for (int q = 0; q < L.Q[r]; ++q)
+            shape_values(d.physics_kind, c.rules[r].u[q], c.rules[r].v[q],
+                         &c.phi[((size_t)r * L.qmax + q) * NP]);
+
+    // ---- element order: Morton order of element centroids -------------------
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < d.n_coordinates; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], c.coords[3 * i + k]);
+            hi[k] = std::max(hi[k], c.coords[3 * i + k]);
+        }
+    std::vector<uint32_t> key(E);
+    for (int64_t e = 0; e < E; ++e) {
+        uint32_t code = 0;
+        for (int k = 0; k < 3; ++k) {
+            double s = 0;
+            for (int a = 0; a < 3; ++a) s += c.coords[3 * (int64_t)c.topo[NS * e + a] + k];
+            s /= 3.0;
+            double span = hi[k] - lo[k];
+            double t = span > 0 ? (s - lo[k]) / span : 0.0;
+            uint32_t qk = (uint32_t)std::min(1023.0, std::max(0.0, t * 1023.0));
+            code |= spread10(qk) << k;
+        }
+        key[e] = code;
+    }
+    c.order.resize(E);
+    std::iota(c.order.begin(), c.order.end(), 0);
+    std::stable_sort(c.order.begin(), c.order.end(),
+                     [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+
+    // ---- element records (quadrature geometry per rule) ---------------------
+    std::vector<double> rec((size_t)E * L.stride, 0.0);
+    std::vector<double> N(NS), dNu(NS), dNv(NS);
+    for (int64_t p = 0; p < E; ++p) {
+        const int64_t e = c.order[p];
+        double *R0 = &rec[(size_t)p * L.stride];
+        for (int a = 0; a < NP; ++a)
+            for (int k = 0; k < 3; ++k)
+                R0[3 * a + k] = c.sources[3 * (int64_t)c.ptopo[NP * e + a] + k];
+        for (int r = 0; r < R; ++r) {
+            const int Q = L.Q[r];
+            double *g = R0 + L.rule_off[r];
+            for (int q = 0; q < Q; ++q) {
+                const double u = c.rules[r].u[q], v = c.rules[r].v[q];
+                shape_values(d.shape_kind, u, v, N.data());
+                shape_derivs(d.shape_kind, u, v, dNu.data(), dNv.data());
+                double x[3] = {0, 0, 0}, t[3] = {0, 0, 0}, s[3] = {0, 0, 0};
+                for (int a = 0; a < NS; ++a) {
+                    const double *X = &c.coords[3 * (int64_t)c.topo[NS * e + a]];
+                    for (int k = 0; k < 3; ++k) {
+                        x[k] += X[k] * N[a];
+                        t[k] += X[k] * dNu[a];
+                        s[k] += X[k] * dNv[a];
+                    }
+                }
+                double nrm[3] = {t[1] * s[2] - t[2] * s[1], t[2] * s[0] - t[0] * s[2],
+                                 t[0] * s[1] - t[1] * s[0]};
+                double jac = std::hypot(std::hypot(nrm[0], nrm[1]), nrm[2]);
+                if (!(jac > 0)) fail(BIE_ERR_INVALID, "degenerate element " + std::to_string(e + 1));
+                g[0 * Q + q] = x[0];
+                g[1 * Q + q] = x[1];
+                g[2 * Q + q] = x[2];
+                g[3 * Q + q] = -nrm[0] / jac;
+                g[4 * Q + q] = -nrm[1] / jac;
+                g[5 * Q + q] = -nrm[2] / jac;
+                g[6 * Q + q] = jac * c.rules[r].w[q];
+            }
+        }
+        int32_t *nid = reinterpret_cast<int32_t *>(R0 + L.nidx_off);
+        for (int a = 0; a < NP; ++a) nid[a] = c.ptopo[NP * e + a];
+    }
+
+    // ---- shared-node masks for the element slicings S = 2^l ------------------
+    // Slice s of S covers sorted positions [s*E/S, (s+1)*E/S).  A node is shared
+    // at level l when elements of two different slices touch it; writes to a
+    // shared node use atomics, all other writes are plain read-modify-writes by
+    // the single thread that owns the (row, node) entry.
+    std::vector<uint32_t> masks((size_t)kMaxLevels * E, 0u);
+    std::vector<int32_t> first(d.n_sources);
+    std::vector<uint8_t> shared(d.n_sources);
+    for (int l = 0; l < kMaxLevels; ++l) {
+        const int64_t S = int64_t(1) << l;
+        std::fill(first.begin(), first.end(), -1);
+        std::fill(shared.begin(), shared.end(), 0);
+        for (int64_t s = 0; s < S; ++s) {
+            const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
+            for (int64_t p = p0; p < p1; ++p) {
+                const int64_t e = c.order[p];
+                for (int a = 0; a < NP; ++a) {
+                    int32_t nd = c.ptopo[NP * e + a];
+                    if (first[nd] < 0) first[nd] = (int32_t)s;
+                    else if (first[nd] != (int32_t)s) shared[nd] = 1;
+                }
+            }
+        }
+        for (int64_t p = 0; p < E; ++p) {
+            const int64_t e = c.order[p];
+            uint32_t m = 0;
+            for (int a = 0; a < NP; ++a)
+                if (shared[c.ptopo[NP * e + a]]) m |= 1u << a;
+            masks[(size_t)l * E + p] = m;
+        }
+    }
+
+    // ---- device upload --------------------------------------------------------
+    int ndev = 0;
+    BIE_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev)
+        fail(BIE_ERR_INVALID, "device " + std::to_string(device) + " not present (" +
+                                  std::to_string(ndev) + " visible)");
+    c.device = device;
+    BIE_CUDA(cudaSetDevice(device));
+    BIE_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    BIE_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    BIE_CUDA(cudaMalloc(&c.d_records, rec.size() * sizeof(double)));
+    BIE_CUDA(cudaMalloc(&c.d_phi, c.phi.size() * sizeof(double)));
+    BIE_CUDA(cudaMalloc(&c.d_sources, c.sources.size() * sizeof(double)));
+    BIE_CUDA(cudaMalloc(&c.d_shared_mask, masks.size() * sizeof(uint32_t)));
+    BIE_CUDA(cudaMalloc(&c.d_qpe, sizeof(unsigned long long)));
+    BIE_CUDA(cudaMemset(c.d_qpe, 0, sizeof(unsigned long long)));
+    BIE_CUDA(cudaMemcpy(c.d_records, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMemcpy(c.d_phi, c.phi.data(), c.phi.size() * sizeof(double), cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMemcpy(c.d_sources, c.sources.data(), c.sources.size() * sizeof(double),
+                        cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMemcpy(c.d_shared_mask, masks.data(), masks.size() * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice));
+}
+
+void destroy_context(Ctx &c) {
+    if (c.device >= 0) cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    cudaFree(c.d_records);
+    cudaFree(c.d_phi);
+    cudaFree(c.d_sources);
+    cudaFree(c.d_shared_mask);
+    cudaFree(c.d_qpe);
+    for (int i = 0; i < kScratchCount; ++i) cudaFree(c.d_scratch[i]);
+    for (auto &p : c.ev_pending) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    for (auto e : c.ev_free) cudaEventDestroy(e);
+    c.ev_pending.clear();
+    c.ev_free.clear();
+    c.d_qpe = nullptr;
+    if (c.stream) cudaStreamDestroy(c.stream);
+    c.d_records = nullptr;
+    c.d_phi = nullptr;
+    c.d_sources = nullptr;
+    c.d_shared_mask = nullptr;
+    c.stream = nullptr;
+}
+
+}  // namespace bie

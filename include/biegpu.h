@@ -1,0 +1,187 @@
+/*
+ * biegpu.h - C ABI of libbiegpu.so, the GB300 (sm_103a) collocation-BEM hot path.
+ *
+ * The library replaces the dense collocation assembly and the operator
+ * application of BoundaryIntegralEquations.jl (3D, triangular elements).
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, returns an
+ * int status (BIE_OK == 0, negative on failure) and never lets a C++ exception
+ * cross the boundary.  `bie_last_error()` gives a thread-local message for the
+ * last failing call made by the calling thread.
+ *
+ * Array conventions (identical to Julia's column-major storage, so a Julia
+ * caller passes `pointer(A)` directly):
+ *   - point sets are 3 x n column-major doubles: x0 y0 z0 x1 y1 z1 ...
+ *   - connectivities are n_per_element x E column-major int64, 1-based
+ *     (Julia's `mesh.topology`, `mesh.physics_topology`); they are checked and
+ *     converted to 0-based on upload.
+ *   - complex outputs are interleaved (re, im) doubles, the memory layout of
+ *     Julia's ComplexF64; matrices are column-major M x N with leading
+ *     dimension M.
+ *
+ * Threading: each context owns one CUDA stream; calls on one context are
+ * serialised by a mutex inside the library.  Different contexts may be used
+ * from different host threads.
+ */
+#ifndef BIEGPU_H
+#define BIEGPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define BIE_API __attribute__((visibility("default")))
+#else
+#define BIE_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define BIE_OK                 0
+#define BIE_ERR_INVALID       -1  /* bad argument: sizes, indices, NaN, NULL */
+#define BIE_ERR_CUDA          -2  /* a CUDA runtime call failed             */
+#define BIE_ERR_NOT_CONVERGED -3  /* iterative solver hit maxiter           */
+#define BIE_ERR_TIMEOUT       -4  /* a bounded device wait gave up          */
+#define BIE_ERR_NOMEM         -5  /* device or host allocation failed       */
+#define BIE_ERR_UNSUPPORTED   -6  /* element kind / option not implemented  */
+
+/* ---- element kinds (Julia: TriangularLinear, TriangularQuadratic) ----- */
+#define BIE_TRI_LINEAR    1   /* 3-node triangle, N = [1-u-v, u, v]            */
+#define BIE_TRI_QUADRATIC 2   /* 6-node triangle, nodes 1 2 3 corners, 4 5 6 mid */
+
+/* ---- assembly selection flags (Julia keywords fOn, gOn, cOn) ---------- */
+#define BIE_F 1   /* double-layer matrix F  */
+#define BIE_G 2   /* single-layer matrix G  */
+#define BIE_C 4   /* free-term row sums C   */
+
+/* ---- arithmetic of an assembly or operator application ---------------- */
+#define BIE_PREC_FP64  0  /* plain FP64 throughout (the reference's arithmetic) */
+#define BIE_PREC_MIXED 1  /* FP32 regular pairs, FP64 near-singular pairs and C  */
+
+typedef struct bie_ctx bie_ctx;
+
+/*
+ * Mesh description.  Mirrors the fields of `Mesh3d` that the collocation
+ * assembly reads (src/utils/mesh.jl:23-34): `coordinates`, `topology`,
+ * `sources`, `physics_topology` and the element kinds of `shape_function` and
+ * `physics_function`.  `quad_n`, `quad_m` are the `n`, `m` keywords of
+ * `assemble_parallel!` (src/3d/assembly_collocation.jl:259-260).
+ * The library copies everything it needs; the caller keeps ownership.
+ */
+typedef struct bie_mesh_desc {
+    int64_t        n_coordinates;     /* N_c                                    */
+    const double  *coordinates;       /* 3 x N_c                                */
+    int64_t        n_elements;        /* E                                      */
+    int32_t        shape_kind;        /* BIE_TRI_LINEAR | BIE_TRI_QUADRATIC     */
+    int32_t        physics_kind;      /* BIE_TRI_LINEAR | BIE_TRI_QUADRATIC     */
+    const int64_t *topology;          /* n_shape x E, 1-based into coordinates  */
+    const int64_t *physics_topology;  /* n_phys x E, 1-based into sources       */
+    int64_t        n_sources;         /* N (collocation nodes = matrix columns) */
+    const double  *sources;           /* 3 x N                                  */
+    int32_t        quad_n;            /* Gauss-Legendre points along u (>= 1)   */
+    int32_t        quad_m;            /* Gauss-Legendre points along v (>= 1)   */
+} bie_mesh_desc;
+
+/* Library version string, e.g. "biegpu 0.1.0 sm_103a". */
+BIE_API const char *bie_version(void);
+
+/* Message of the last failing call on this host thread ("" if none). */
+BIE_API const char *bie_last_error(void);
+
+/*
+ * Quadrature rule on the reference triangle clustered at element node `node`
+ * (1, 2, 3: Duffy rules collapsed at that corner, from an n x m Gauss grid;
+ * 4, 5, 6: two half-Duffy triangles split at that edge midpoint, m rounded up
+ * to even).  Host-only (needs no GPU).  Writes at most `capacity` points to
+ * u, v, w and the rule size to *count.
+ * Replaces rotated_triangular_quadpoints / triangularQuadpoints /
+ * rotated_midpoint_triangular_quadpoints as chosen by create_rotated_element
+ * (src/3d/quadrature.jl:70-144; src/3d/assembly_collocation.jl:122-136, 384-389).
+ */
+BIE_API int bie_quadrature_rule(int n, int m, int node, double *u, double *v, double *w,
+                                int capacity, int *count);
+
+/*
+ * Create a context on CUDA device `device`: validates and uploads the mesh,
+ * builds the Duffy rules clustered at each element node and the per-element
+ * quadrature geometry (points, unit normals, jacobian x weight).
+ * Replaces the set-up half of `assemble_parallel!` for triangles:
+ * create_rotated_element / rotated_midpoint_triangular_quadpoints and
+ * interpolate_elements (src/3d/assembly_collocation.jl:122-136, 27-66,
+ * 284-305, 369-413; src/3d/quadrature.jl:70-144; src/3d/jacobian.jl:78-87).
+ */
+BIE_API int bie_ctx_create(bie_ctx **out, const bie_mesh_desc *desc, int device);
+
+/* Release every device and host resource of a context. NULL is a no-op. */
+BIE_API int bie_ctx_destroy(bie_ctx *ctx);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that enqueue
+ * their own work or record events around the device entry points. */
+BIE_API int bie_ctx_stream(bie_ctx *ctx, void **stream);
+
+/*
+ * Launch statistics of a context, for profiling.  `kernel_launches` counts every
+ * kernel libbiegpu enqueued on the context; with timing on, the dominant
+ * compute kernel of each call (assembly or operator application) is bracketed
+ * by CUDA events on the context stream and `timed_ms` sums their durations
+ * over `timed_launches` launches.  Not part of the reference API (its only
+ * instrumentation is ProgressMeter and @time in examples).
+ */
+typedef struct bie_stats {
+    int64_t kernel_launches;
+    int64_t timed_launches;
+    double  timed_ms;
+    double  algorithmic_flops;   /* flops of the timed launches, counted as
+                                    32 + 8 n_phys per quadrature-point evaluation */
+    int64_t quadrature_evals;    /* (target, quadrature point) evaluations */
+} bie_stats;
+
+/*
+ * Measured FMA throughput of a device (dependency-free FMA chains on every SM,
+ * ~0.1 s): the denominators of the FP64 / FP32 pipe rooflines of the assembly
+ * and operator kernels.  Values in FLOP/s (an FMA counts 2).
+ */
+typedef struct bie_peaks {
+    double fp64_flops;
+    double fp32_flops;
+} bie_peaks;
+BIE_API int bie_measure_peaks(int device, bie_peaks *out);
+
+BIE_API int bie_ctx_set_timing(bie_ctx *ctx, int on);
+/* Synchronises the context stream, then fills *out; `reset` != 0 zeroes the counters. */
+BIE_API int bie_ctx_stats(bie_ctx *ctx, bie_stats *out, int reset);
+
+/*
+ * Dense collocation assembly into HOST buffers.
+ * Replaces `assemble_parallel!(mesh, k, targets; fOn, gOn, cOn, m, n)`
+ * (src/3d/assembly_collocation.jl:259-268, triangle methods :270-353 and
+ * :355-479) returning (F, G, C).
+ *   k = k_re + i k_im (the reference accepts real or complex k).
+ *   targets: 3 x M collocation / field points; NULL means the mesh sources.
+ *   flags: BIE_F | BIE_G | BIE_C.  precision: BIE_PREC_*.
+ *   F, G: M x N complex (interleaved doubles), C: M complex.  A buffer whose
+ *   flag is off may be NULL and is not touched.
+ * Outputs are fully overwritten (the reference starts from zeros).
+ * Blocks until the results are in the host buffers.
+ */
+BIE_API int bie_assemble(bie_ctx *ctx, double k_re, double k_im,
+                 const double *targets, int64_t n_targets,
+                 int flags, int precision,
+                 double *F, double *G, double *C);
+
+/*
+ * Same as bie_assemble with DEVICE pointers for targets (3 x M doubles, may be
+ * NULL for the mesh sources) and outputs.  Enqueued on the context stream and
+ * returns without synchronising.
+ */
+BIE_API int bie_assemble_device(bie_ctx *ctx, double k_re, double k_im,
+                        const double *d_targets, int64_t n_targets,
+                        int flags, int precision,
+                        double *d_F, double *d_G, double *d_C);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BIEGPU_H */

@@ -1,0 +1,103 @@
+"""ORACLE - test infrastructure only (never imported by the product path).
+
+CPU checker for libbiegpu.so:
+  * ``bem_oracle.c`` - C99/OpenMP restatement of the reference's dense
+    collocation assembly (see its header for the file:line map);
+  * ``analytic.py`` - the reference's analytic sphere solutions.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
+may use this package.
+
+Parity status: the Julia reference cannot run here (no Julia toolchain), so the
+restatement is pinned by reproducing the reference's own known-answer tests:
+the rigid-sphere error table (test/3d/assembly_test.jl:12-44), the sphere
+area (test/3d/fmm_test.jl:11-28) and the rule weight sums
+(test/3d/surface_functions_test.jl:13-53).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "bem_oracle.c"
+LIB = HERE / "libbemoracle.so"
+_lib = None
+_lock = threading.Lock()
+
+
+def build(force: bool = False) -> Path:
+    """Compile the C restatement with gcc (FMA contraction off, OpenMP)."""
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    cc = os.environ.get("CC") or shutil.which("gcc") or "cc"
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [cc, "-O2", "-std=gnu99", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           str(SRC), "-o", str(tmp), "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = C.CDLL(str(build()))
+            P, D, I, I64 = C.c_void_p, C.c_double, C.c_int, C.c_int64
+            L.oracle_assemble.restype = I
+            L.oracle_assemble.argtypes = [P, I64, P, I, P, I, I64, P, I64, P, I64, I, I, D, D, I,
+                                          P, P, P, I]
+            L.oracle_rule.restype = I
+            L.oracle_rule.argtypes = [I, I, I, P, P, P]
+            L.oracle_total_weight.restype = D
+            L.oracle_total_weight.argtypes = [P, P, I, I64, I, I]
+            _lib = L
+        return _lib
+
+
+_KIND = {"linear": 1, "quadratic": 2}
+
+
+def rule(n: int, m: int, corner: int):
+    """(u, v, w) of the rule clustered at element node ``corner`` (1..6)."""
+    size = 2 * n * (m + 1) + 8
+    u, v, w = (np.zeros(size) for _ in range(3))
+    q = lib().oracle_rule(n, m, corner, u.ctypes.data, v.ctypes.data, w.ctypes.data)
+    return u[:q].copy(), v[:q].copy(), w[:q].copy()
+
+
+def total_weight(mesh, n: int = 2, m: int = 2) -> float:
+    c = np.asfortranarray(mesh.coordinates, dtype=np.float64)
+    t = np.asfortranarray(mesh.topology, dtype=np.int64)
+    return lib().oracle_total_weight(c.ctypes.data, t.ctypes.data, _KIND[mesh.shape_function],
+                                     t.shape[1], n, m)
+
+
+def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, threads=0):
+    """Reference-algorithm (F, G, C) on the CPU; F, G are M x N Fortran-ordered."""
+    k = complex(k)
+    c = np.asfortranarray(mesh.coordinates, dtype=np.float64)
+    t = np.asfortranarray(mesh.topology, dtype=np.int64)
+    pt = np.asfortranarray(mesh.physics_topology, dtype=np.int64)
+    s = np.asfortranarray(mesh.sources, dtype=np.float64)
+    tg = s if targets is None else np.asfortranarray(targets, dtype=np.float64)
+    N, M = s.shape[1], tg.shape[1]
+    F = np.zeros((M, N), dtype=np.complex128, order="F") if fOn else None
+    G = np.zeros((M, N), dtype=np.complex128, order="F") if gOn else None
+    Cv = np.zeros(M, dtype=np.complex128) if cOn else None
+    flags = (1 if fOn else 0) | (2 if gOn else 0) | (4 if cOn else 0)
+    addr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+    lib().oracle_assemble(c.ctypes.data, c.shape[1], t.ctypes.data, _KIND[mesh.shape_function],
+                          pt.ctypes.data, _KIND[mesh.physics_function], t.shape[1], s.ctypes.data,
+                          N, tg.ctypes.data, M, n, m, k.real, k.imag, flags, addr(F), addr(G),
+                          addr(Cv), int(threads))
+    return F, G, Cv

@@ -1,0 +1,70 @@
+"""Mesh builders and the COMSOL reader (host side, no GPU)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from biegpu import mesh as bm
+
+
+@pytest.mark.parametrize("f", [1, 2, 5, 16, 17])
+def test_icosphere_counts(f):
+    P, T = bm.icosphere_arrays(f)
+    assert P.shape == (3, 10 * f * f + 2)
+    assert T.shape == (3, 20 * f * f)
+    assert np.allclose(np.linalg.norm(P, axis=0), 1.0)
+    # every edge shared by exactly two triangles (closed surface)
+    e = np.sort(np.concatenate([T[[0, 1]], T[[1, 2]], T[[2, 0]]], axis=1), axis=0)
+    _, cnt = np.unique(e, axis=1, return_counts=True)
+    assert np.all(cnt == 2)
+
+
+def test_icosphere_outward_orientation_and_inward_normals():
+    m = bm.icosphere(4)
+    X = m.coordinates[:, m.topology - 1]
+    n = np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0], axis=0)
+    c = X.mean(axis=1)
+    assert np.all(np.sum(n * c, axis=0) > 0)          # counter-clockwise seen from outside
+    assert np.all(np.sum(m.normals * m.sources, axis=0) < -0.99)   # negated nodal normals
+
+
+def test_quadratic_promotion():
+    f = 17
+    m = bm.icosphere(f, geometry="quadratic")
+    V, E = 10 * f * f + 2, 20 * f * f
+    assert m.sources.shape == (3, V + 3 * E // 2)    # 2892 vertices + 8670 midpoints = 11562
+    assert m.topology.shape == (6, E)
+    assert np.allclose(np.linalg.norm(m.coordinates, axis=0), 1.0)
+    # midpoint node 4 lies between corners 1 and 2 (before projection)
+    X = m.coordinates[:, m.topology - 1]
+    mid = 0.5 * (X[:, 0] + X[:, 1])
+    mid /= np.linalg.norm(mid, axis=0)
+    assert np.allclose(mid, X[:, 3])
+
+
+def test_linear_physics_on_quadratic_geometry():
+    m = bm.icosphere(3, geometry="quadratic", physics="linear")
+    assert m.physics_topology.shape[0] == 3
+    assert m.sources.shape[1] == 10 * 9 + 2
+
+
+def test_ellipsoid_axes():
+    m = bm.ellipsoid(6)
+    ext = m.coordinates.max(axis=1)
+    assert np.allclose(ext, [1.0, 2 / 3, 1 / 3], atol=2e-2)
+
+
+def test_tangents_orthonormal():
+    m = bm.icosphere(3)
+    assert np.allclose(np.sum(m.normals * m.tangents, axis=0), 0.0, atol=1e-14)
+    assert np.allclose(np.sum(m.tangents * m.sangents, axis=0), 0.0, atol=1e-14)
+
+
+def test_comsol_reader(reference_meshes):
+    # test/3d/meshing_test.jl:23 - 840 triangles, physics nodes = sources
+    for go in ["linear", "quadratic"]:
+        m = bm.load_comsol(reference_meshes / "sphere_1m", go, "linear" if go == "linear" else "geometry")
+        assert m.topology.shape[1] == 840
+        assert m.sources.shape[1] == len(np.unique(m.physics_topology))
+    C, T, ents = bm.read_comsol(reference_meshes / "sphere_1m")
+    assert C.shape == (3, 1682) and T.shape == (6, 840)

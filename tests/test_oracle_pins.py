@@ -1,0 +1,80 @@
+"""Pins the CPU oracle to the reference's own known-answer tests.
+
+* rigid-sphere scattering error table, test/3d/assembly_test.jl:12-44
+  (continuous physics rows: linear/linear, quadratic/linear, quadratic/geometry)
+* total quadrature weight = sphere area 4 pi, test/3d/fmm_test.jl:11-28
+* rule weights sum to 1/2, test/3d/surface_functions_test.jl:16,37
+* mesh sizes, test/3d/meshing_test.jl:23
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle.analytic as an
+from biegpu import mesh as bm
+
+# test/3d/assembly_test.jl:22-23 (geometry x physics)
+ERROR_TABLE = {("linear", "linear"): 0.037, ("quadratic", "linear"): 0.048,
+               ("quadratic", "geometry"): 2.8e-5}
+
+
+@pytest.mark.parametrize("go,po", list(ERROR_TABLE))
+def test_rigid_sphere_error_table(reference_meshes, go, po):
+    freq, c = 100.0, 340.0
+    k = 2 * np.pi * freq / c
+    mesh = bm.load_comsol(reference_meshes / "sphere_1m", go, po)
+    assert mesh.topology.shape[1] == 840
+    # assemble_parallel!(mesh, k, mesh.sources; gOn=false) with default n = m = 4
+    F, _, C = oracle.assemble(mesh, k, n=4, m=4, gOn=False)
+    pI = an.incoming_wave([np.pi / 2, 0.0], 1.0, mesh.sources, k)
+    A = F + np.diag(1.0 - C)
+    p = np.linalg.solve(A, pI)
+    theta = np.arccos(np.clip(mesh.sources[0] / 1.0, -1.0, 1.0))
+    pa, _ = an.plane_wave_scattering_sphere(k, 1.0, 1.0, theta, 1e-6)
+    err = np.linalg.norm(pa - p) / np.linalg.norm(pa)
+    assert err <= ERROR_TABLE[(go, po)]
+
+
+@pytest.mark.parametrize("go,tol", [("linear", 1e-1), ("quadratic", 1e-5)])
+def test_sphere_area(reference_meshes, go, tol):
+    mesh = bm.load_comsol(reference_meshes / "sphere_1m_extremely_fine", go,
+                          "linear" if go == "linear" else "geometry")
+    assert abs(oracle.total_weight(mesh, n=2, m=2) - 4 * np.pi) <= tol
+
+
+def test_oracle_rule_weights():
+    for node in range(1, 7):
+        for n, m in [(2, 2), (3, 3), (4, 4)]:
+            _, _, w = oracle.rule(n, m, node)
+            assert abs(w.sum() - 0.5) < 1e-14
+
+
+def test_oracle_c_is_half_on_smooth_sphere():
+    # the k = 0 double layer gives the free term 1/2 on a smooth surface
+    mesh = bm.icosphere(4, geometry="quadratic")
+    _, _, C = oracle.assemble(mesh, 1.0, n=4, m=4, fOn=False, gOn=False)
+    assert np.max(np.abs(C.real - 0.5)) < 5e-3
+
+
+def test_oracle_rowsum_identity_at_k0():
+    # partition of unity: sum_j F(k=0)[i, j] equals C[i] (same rules, same points)
+    mesh = bm.icosphere(3)
+    F, _, C = oracle.assemble(mesh, 0.0, n=2, m=2, gOn=False)
+    assert np.max(np.abs(F.sum(axis=1) - C)) < 1e-12
+
+
+def test_pulsating_sphere_quadratic():
+    # examples/3d_pulsating_sphere.jl: interior field vs the analytic solution
+    k = 2 * np.pi * 54.59 / 343.0
+    Z0 = 1.21 * 343.0
+    mesh = bm.icosphere(5, geometry="quadratic")
+    F, G, C = oracle.assemble(mesh, k, n=2, m=2)
+    vs = 1j * Z0 * k * np.ones(mesh.n_sources)
+    p = np.linalg.solve(np.diag(1.0 - C) - F, G @ vs)
+    z = np.linspace(0.1, 0.9, 20)
+    X = np.vstack([0 * z, 0 * z, z])
+    Fp, Gp, _ = oracle.assemble(mesh, k, targets=X, n=2, m=2)
+    pa = an.pulsating_sphere_interior(k, 1.0, Z0, 1.0, z)
+    assert np.linalg.norm(Fp @ p + Gp @ vs - pa) / np.linalg.norm(pa) < 5e-3
