@@ -50,6 +50,13 @@ def workload(name: str):
         desc = {"workload": "rigid_sphere_p2", "mesh": "geodesic sphere f=17, 6-node triangles, r=1",
                 "nodes": mesh.n_sources, "elements": mesh.n_elements, "quad_n": 2, "quad_m": 2,
                 "ka": "1..10 cycled", "outputs": "F, G complex128 N x N + C"}
+    elif name == "small_p2":
+        # profiling case: same kernel, 2562 nodes (F, G = 210 MB, larger than L2)
+        mesh = bm.icosphere(8, geometry="quadratic")
+        ks = [float(ka) for ka in range(1, 11)]
+        desc = {"workload": "small_p2", "mesh": "geodesic sphere f=8, 6-node triangles, r=1",
+                "nodes": mesh.n_sources, "elements": mesh.n_elements, "quad_n": 2, "quad_m": 2,
+                "ka": "1..10 cycled", "outputs": "F, G complex128 N x N + C"}
     elif name == "pulsating_sphere":
         mesh = bm.icosphere(32)
         ks = [2 * np.pi * 200 / 343]

@@ -27,7 +27,7 @@ import numpy as np
 KIND_NODES = {"linear": 3, "quadratic": 6}
 
 
-@dataclass
+@dataclass(eq=False)   # identity hash: contexts are cached per mesh object
 class Mesh3d:
     sources: np.ndarray            # 3 x N   collocation nodes
     coordinates: np.ndarray        # 3 x Nc  geometry nodes
