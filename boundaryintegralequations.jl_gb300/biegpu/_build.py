@@ -22,6 +22,7 @@ SOURCES = [
     "bie_capi.cpp",
     "bie_setup.cpp",
     "bie_assemble.cu",
+    "bie_assemble_mixed.cu",
     "bie_peaks.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -21,6 +21,7 @@
 // nodes shared between slices are updated with FP64 atomics.  C is accumulated
 // per slice and reduced by a second kernel.
 #include "bie_internal.h"
+#include "bie_device.cuh"
 
 #include <algorithm>
 
@@ -28,64 +29,8 @@ namespace bie {
 
 namespace {
 
-constexpr double kInv4Pi = 0.07957747154594767;   // 1 / (4 pi)
+using dev::RuleInfo;
 constexpr int kThreads = 128;
-
-struct RuleInfo {
-    int Q[kMaxRules];
-    int off[kMaxRules];
-};
-
-// Julia's 3-argument hypot (maximum-abs scaling, IEEE-rounded division and
-// square root, ((a^2 + b^2) + c^2) summation), evaluated bit-exactly.
-__device__ __forceinline__ double julia_hypot3(double x, double y, double z) {
-    const double m = fmax(fmax(fabs(x), fabs(y)), fabs(z));
-    if (m == 0.0) return 0.0;
-    const double a = __ddiv_rn(x, m), b = __ddiv_rn(y, m), c = __ddiv_rn(z, m);
-    const double s = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(c, c));
-    return __dmul_rn(m, __dsqrt_rn(s));
-}
-
-// find_closest_corner (src/3d/assembly_collocation.jl:102-115): index of the
-// physics node nearest to the target, strict '<' so the first of equal
-// distances wins.  Squared distances decide whenever the runner-up is more
-// than 1e-12 (relative) farther; only near-ties are re-decided with the exact
-// Julia hypot so the choice is the reference's in every case.
-template <int NP>
-__device__ __forceinline__ int nearest_node(const double *r, double tx, double ty, double tz) {
-    double d2[NP];
-#pragma unroll
-    for (int a = 0; a < NP; ++a) {
-        const double dx = r[3 * a + 0] - tx, dy = r[3 * a + 1] - ty, dz = r[3 * a + 2] - tz;
-        d2[a] = dx * dx + dy * dy + dz * dz;
-    }
-    int c = 0;
-    double b = d2[0];
-#pragma unroll
-    for (int a = 1; a < NP; ++a)
-        if (d2[a] < b) {
-            b = d2[a];
-            c = a;
-        }
-    const double lim = b * (1.0 + 1e-12);
-    bool tie = false;
-#pragma unroll
-    for (int a = 0; a < NP; ++a) tie |= (a != c) && (d2[a] <= lim);
-    if (tie) {
-        double best = __longlong_as_double(0x7ff0000000000000LL);
-        c = 0;
-#pragma unroll
-        for (int a = 0; a < NP; ++a) {
-            const double h = julia_hypot3(__dsub_rn(r[3 * a + 0], tx), __dsub_rn(r[3 * a + 1], ty),
-                                          __dsub_rn(r[3 * a + 2], tz));
-            if (h < best) {
-                best = h;
-                c = a;
-            }
-        }
-    }
-    return c;
-}
 
 template <int NP, bool CPLX_K>
 __global__ void __launch_bounds__(kThreads)
@@ -133,54 +78,12 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
 
         for (int el = 0; el < n; ++el) {
             const double *r = s_rec + (size_t)el * stride;
-            const int c = nearest_node<NP>(r, tx, ty, tz);
+            const int c = dev::nearest_node<NP>(r, tx, ty, tz);
             const int Q = ri.Q[c];
             nqpe += Q;
-            const double *g = r + ri.off[c];
-            const double *ph = s_phi + (size_t)c * qmax * NP;
-
             double fr[NP], fi[NP], gr[NP], gi[NP];
-#pragma unroll
-            for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.0;
-            double ce = 0.0;
-
-            for (int q = 0; q < Q; ++q) {
-                const double dx = g[q] - tx;
-                const double dy = g[Q + q] - ty;
-                const double dz = g[2 * Q + q] - tz;
-                const double r2 = dx * dx + dy * dy + dz * dz;
-                const double rinv = rsqrt(r2);
-                const double rr = r2 * rinv;
-                const double jw = g[6 * Q + q];
-                const double dn = g[3 * Q + q] * dx + g[4 * Q + q] * dy + g[5 * Q + q] * dz;
-                double sn, cs;
-                sincos(kre * rr, &sn, &cs);
-                if (CPLX_K) {
-                    const double damp = exp(-kim * rr);
-                    sn *= damp;
-                    cs *= damp;
-                }
-                // G: e^{ikr} / (4 pi r) * jw
-                const double wg = rinv * kInv4Pi * jw;
-                const double Gr = cs * wg, Gi = sn * wg;
-                // C: -(x - y).n / (4 pi r^3) * jw ; F: e^{ikr} (ikr - 1) (x - y).n / (4 pi r^3) * jw
-                const double tq = dn * (rinv * rinv * rinv) * kInv4Pi * jw;
-                ce -= tq;
-                const double ar = CPLX_K ? (-1.0 - kim * rr) : -1.0;
-                const double ai = kre * rr;
-                const double Fr = (cs * ar - sn * ai) * tq;
-                const double Fi = (cs * ai + sn * ar) * tq;
-                const double *pq = ph + q * NP;
-#pragma unroll
-                for (int a = 0; a < NP; ++a) {
-                    const double p = pq[a];
-                    fr[a] += Fr * p;
-                    fi[a] += Fi * p;
-                    gr[a] += Gr * p;
-                    gi[a] += Gi * p;
-                }
-            }
-            cacc += ce;
+            cacc += dev::element_fp64<NP, CPLX_K>(r + ri.off[c], Q, s_phi + (size_t)c * qmax * NP,
+                                                  tx, ty, tz, kre, kim, fr, fi, gr, gi);
 
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
             const uint32_t m = s_mask[el];
@@ -220,15 +123,6 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
     if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
 }
 
-__global__ void reduce_c_kernel(const double *__restrict__ Cpart, int S, int64_t M,
-                                double2 *__restrict__ C) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M) return;
-    double acc = 0.0;
-    for (int s = 0; s < S; ++s) acc += Cpart[(int64_t)s * M + i];
-    C[i] = make_double2(acc, 0.0);
-}
-
 template <int NP, bool CPLX>
 void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int chunk,
                double *Cpart) {
@@ -254,6 +148,18 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int
 
 }  // namespace
 
+int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile) {
+    const int64_t row_tiles = (M + threads_per_row_tile - 1) / threads_per_row_tile;
+    int level = 0;
+    while (level + 1 < kMaxLevels && row_tiles * (int64_t(1) << level) < 8LL * c.num_sms &&
+           (int64_t(2) << level) <= c.n_elements)
+        ++level;
+    return level;
+}
+
+void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
+                     double *C);
+
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
     const int64_t N = c.n_sources;
@@ -262,11 +168,7 @@ void launch_assemble_fp64(Ctx &c, const AssembleArgs &a) {
     if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;
 
     // slices: enough blocks for ~8 per SM, power of two, at most one per element
-    const int64_t row_tiles = (a.M + kThreads - 1) / kThreads;
-    int level = 0;
-    while (level + 1 < kMaxLevels && row_tiles * (int64_t(1) << level) < 8LL * c.num_sms &&
-           (int64_t(2) << level) <= c.n_elements)
-        ++level;
+    const int level = choose_slice_level(c, a.M, kThreads);
     const int S = 1 << level;
 
     // element chunk: ~40 KB of records per block
@@ -284,12 +186,31 @@ void launch_assemble_fp64(Ctx &c, const AssembleArgs &a) {
         if (cplx) launch_np<6, true>(c, a, S, level, smem, chunk, Cpart);
         else launch_np<6, false>(c, a, S, level, smem, chunk, Cpart);
     }
-    if (a.flags & BIE_C) {
-        reduce_c_kernel<<<(unsigned)((a.M + 255) / 256), 256, 0, c.stream>>>(
-            Cpart, S, a.M, reinterpret_cast<double2 *>(a.C));
-        BIE_CUDA(cudaGetLastError());
-        ++c.kernel_launches;
-    }
+    if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, nullptr, a.M, a.C);
+}
+
+// ---------------------------------------------------------------------------
+// C = sum over slices of the partial row sums (+ optional extra term)
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void reduce_c_kernel(const double *__restrict__ Cpart, int S,
+                                const double *__restrict__ Cextra, int64_t M,
+                                double2 *__restrict__ C) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    double acc = 0.0;
+    for (int s = 0; s < S; ++s) acc += Cpart[(int64_t)s * M + i];
+    if (Cextra) acc += Cextra[i];
+    C[i] = make_double2(acc, 0.0);
+}
+}  // namespace
+
+void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
+                     double *C) {
+    reduce_c_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+        Cpart, S, Cextra, M, reinterpret_cast<double2 *>(C));
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
 }
 
 }  // namespace bie

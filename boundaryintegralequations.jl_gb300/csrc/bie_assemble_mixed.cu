@@ -1,0 +1,478 @@
+// K2: mixed-precision dense collocation assembly (BIE_PREC_MIXED).
+//
+// Same result as K1 (assemble_parallel!, src/3d/assembly_collocation.jl:270-479)
+// to a stated relative error, with the regular (target, element) pairs on the
+// FP32 pipe and the pairs that need FP64 moved to a sparse FP64 correction:
+//
+//   * regular pairs: quadrature points stored relative to the element centroid
+//     c_e in FP32.  Per pair, D = c_e - t and r0 = |D| are formed in
+//     double-float arithmetic and the phase k r0 is reduced modulo 2 pi there,
+//     so the per-point phase  k r0 + k (r - r0)  with
+//     r - r0 = (2 D.d + |d|^2) / (r + r0)  stays accurate to ~1e-7 even for
+//     k r ~ 20.  sin/cos are evaluated with a quadrant reduction and Taylor
+//     polynomials on the FMA pipe.  Per-node sums are FP32 over the <= 8 points
+//     of one element; F and G accumulate across elements in complex64 and are
+//     widened to complex128 by a separate pass.
+//   * near pairs (target within one element size of the centroid, or within half
+//     an element size of a physics node: the singular and near-singular
+//     elements, which include every element containing the target node) and
+//     pairs whose nearest physics node is a near-tie (runner-up within 1e-5)
+//     are not integrated in FP32: they are appended to a list and integrated in
+//     FP64 by a correction kernel with the exact reference rule choice, then
+//     added to F, G and C.  If the list is full the pair is integrated in FP64
+//     in place (slower, same result).
+//   * C (free term): per-pair FP32 sums accumulated in double-float per row,
+//     the near pairs in FP64.
+#include "bie_internal.h"
+#include "bie_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace bie {
+
+namespace {
+
+using dev::df;
+using dev::RuleInfo;
+constexpr int kThreads = 128;
+constexpr float kTwoPiA = 6.28125f;                 // 2 pi = A + B + C (A has 8 bits)
+constexpr float kTwoPiB = 1.9353071795864769e-3f;
+constexpr float kTwoPiC = 1.0253376606e-11f;        // (2 pi - A) - B, rounded
+constexpr float kInv2Pi = 0.15915494309189535f;
+
+struct Fp64View {
+    const double *rec;
+    int stride;
+    int nidx_off;
+    const double *phi;   // global, R x qmax x NP
+    int qmax;
+    RuleInfo ri;
+};
+
+// FP64 integration of one deferred pair (exact rule choice), used in place when
+// the deferred list is full.
+template <int NP, bool CPLX>
+__device__ __noinline__ void pair_fp64_inplace(const Fp64View v, int64_t p, double tx, double ty,
+                                               double tz, double kre, double kim, float *fr,
+                                               float *fi, float *gr, float *gi, double *ce) {
+    const double *r = v.rec + (size_t)p * v.stride;
+    const int c = dev::nearest_node<NP>(r, tx, ty, tz);
+    double dfr[NP], dfi[NP], dgr[NP], dgi[NP];
+    *ce = dev::element_fp64<NP, CPLX>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP,
+                                      tx, ty, tz, kre, kim, dfr, dfi, dgr, dgi);
+#pragma unroll
+    for (int a = 0; a < NP; ++a) {
+        fr[a] = (float)dfr[a];
+        fi[a] = (float)dfi[a];
+        gr[a] = (float)dgr[a];
+        gi[a] = (float)dgi[a];
+    }
+}
+
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(kThreads)
+assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
+                      const uint32_t *__restrict__ smask, const float *__restrict__ phi, int nphi,
+                      int qmax, RuleInfo ri, const double *__restrict__ tgt, int64_t M, double kre,
+                      double kim, int flags, float2 *__restrict__ F32, float2 *__restrict__ G32,
+                      double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
+                      unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
+                      unsigned long long *__restrict__ qpe_count) {
+    extern __shared__ __align__(16) float smemf[];
+    float *s_phi = smemf;                                   // nphi floats (padded to 4)
+    float *s_rec = smemf + ((nphi + 3) & ~3);               // chunk * stride floats
+    uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);
+
+    const int s = blockIdx.y;
+    const int64_t e0 = (int64_t)s * E / S;
+    const int64_t e1 = (int64_t)(s + 1) * E / S;
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = i < M;
+    const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
+
+    double tx = 0, ty = 0, tz = 0;
+    if (active) {
+        tx = tgt[3 * i + 0];
+        ty = tgt[3 * i + 1];
+        tz = tgt[3 * i + 2];
+    }
+    const df Tx = dev::df_from_double(tx), Ty = dev::df_from_double(ty), Tz = dev::df_from_double(tz);
+    const df K = dev::df_from_double(kre);
+    const float kf = K.hi;
+    const float kimf = (float)kim;
+    for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+
+    df cacc = {0.f, 0.f};
+    unsigned long long nqpe = 0;
+    for (int64_t cb = e0; cb < e1; cb += chunk) {
+        const int n = (int)min((int64_t)chunk, e1 - cb);
+        __syncthreads();
+        {
+            const float4 *src = reinterpret_cast<const float4 *>(rec + cb * stride);
+            float4 *dst = reinterpret_cast<float4 *>(s_rec);
+            const int n4 = n * stride / 4;
+            for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
+            for (int t = threadIdx.x; t < n; t += kThreads) s_mask[t] = smask[cb + t];
+        }
+        __syncthreads();
+        if (!active) continue;
+
+        for (int el = 0; el < n; ++el) {
+            const float *r = s_rec + (size_t)el * stride;
+            // D = c_e - t in double-float
+            const df Dx = dev::df_sub({r[0], r[3]}, Tx);
+            const df Dy = dev::df_sub({r[1], r[4]}, Ty);
+            const df Dz = dev::df_sub({r[2], r[5]}, Tz);
+            const float Dfx = Dx.hi, Dfy = Dy.hi, Dfz = Dz.hi;
+
+            // nearest physics node in FP32, with near / tie detection
+            float d2[NP];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                const float ax = Dfx + r[8 + 3 * a], ay = Dfy + r[9 + 3 * a], az = Dfz + r[10 + 3 * a];
+                d2[a] = ax * ax + ay * ay + az * az;
+            }
+            int c = 0;
+            float b = d2[0];
+#pragma unroll
+            for (int a = 1; a < NP; ++a)
+                if (d2[a] < b) {
+                    b = d2[a];
+                    c = a;
+                }
+            const float lim = b * (1.0f + 1e-5f);
+            bool tie = false;
+#pragma unroll
+            for (int a = 0; a < NP; ++a) tie |= (a != c) && (d2[a] <= lim);
+            const float r0f2 = Dfx * Dfx + Dfy * Dfy + Dfz * Dfz;
+            const float near2 = r[6];
+            const bool deferred = tie || r0f2 < near2 || 4.0f * b < near2;
+
+            float fr[NP], fi[NP], gr[NP], gi[NP];
+            float ce = 0.f;
+            bool have = true;
+            if (deferred) {
+                const unsigned int slot = atomicAdd(defer_count, 1u);
+                if (slot < defer_cap) {
+                    defer[slot] = make_int2((int)i, (int)(cb + el));
+                    have = false;
+                } else {
+                    double ced;
+                    pair_fp64_inplace<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, fr, fi, gr,
+                                                  gi, &ced);
+                    ce = (float)(-ced);   // stored with the sign of the FP32 path below
+                }
+            } else {
+                // pair quantities in double-float: r0 = |D|, phase k r0 mod 2 pi
+                const df r0sq = dev::df_add(dev::df_add(dev::df_sqr(Dx), dev::df_sqr(Dy)), dev::df_sqr(Dz));
+                const df r0 = dev::df_sqrt(r0sq);
+                const df kr0 = dev::df_mul(K, r0);
+                const float nrev = rintf(kr0.hi * kInv2Pi);
+                float th0 = __fmaf_rn(-nrev, kTwoPiA, kr0.hi);
+                th0 = __fmaf_rn(-nrev, kTwoPiB, th0);
+                th0 = __fmaf_rn(-nrev, kTwoPiC, th0);
+                th0 += kr0.lo;
+                const float r0h = r0.hi;
+
+                const int Q = ri.Q[c];
+                nqpe += Q;
+                const float *g = r + ri.off[c];
+                const float *ph = s_phi + (size_t)c * qmax * NP;
+#pragma unroll
+                for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.f;
+                for (int q = 0; q < Q; ++q) {
+                    const float ox = g[q], oy = g[Q + q], oz = g[2 * Q + q];
+                    const float dx = Dfx + ox, dy = Dfy + oy, dz = Dfz + oz;   // x_q - t
+                    const float r2 = dx * dx + dy * dy + dz * dz;
+                    const float rinv = rsqrtf(r2);
+                    const float rr = r2 * rinv;
+                    // r - r0 = (2 D.o + |o|^2) / (r + r0), free of cancellation
+                    const float num = __fmaf_rn(2.0f, Dfx * ox + Dfy * oy + Dfz * oz, g[7 * Q + q]);
+                    const float dr = __fdividef(num, rr + r0h);
+                    float sn, cs;
+                    dev::sincos_f32(__fmaf_rn(kf, dr, th0), &sn, &cs);
+                    if (CPLX_K) {
+                        const float damp = __expf(-kimf * rr);
+                        sn *= damp;
+                        cs *= damp;
+                    }
+                    const float dn = g[3 * Q + q] * dx + g[4 * Q + q] * dy + g[5 * Q + q] * dz;
+                    const float wg = rinv * g[6 * Q + q];          // jw / (4 pi r)
+                    const float Gr = cs * wg, Gi = sn * wg;
+                    const float tq = dn * (rinv * rinv) * wg;        // (x-t).n jw / (4 pi r^3)
+                    ce += tq;
+                    const float ar = CPLX_K ? (-1.0f - kimf * rr) : -1.0f;
+                    const float ai = kf * rr;
+                    const float Fr = (cs * ar - sn * ai) * tq;
+                    const float Fi = (cs * ai + sn * ar) * tq;
+                    const float *pq = ph + q * NP;
+#pragma unroll
+                    for (int a = 0; a < NP; ++a) {
+                        const float p = pq[a];
+                        fr[a] = __fmaf_rn(Fr, p, fr[a]);
+                        fi[a] = __fmaf_rn(Fi, p, fi[a]);
+                        gr[a] = __fmaf_rn(Gr, p, gr[a]);
+                        gi[a] = __fmaf_rn(Gi, p, gi[a]);
+                    }
+                }
+            }
+            if (!have) continue;
+            // C row sum in double-float (C = -sum tq)
+            {
+                const df t = dev::two_sum(cacc.hi, -ce);
+                cacc = dev::fast_two_sum(t.hi, __fadd_rn(t.lo, cacc.lo));
+            }
+            const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
+            const uint32_t m = s_mask[el];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
+                if ((m >> a) & 1u) {
+                    if (doF) {
+                        atomicAdd(&F32[off].x, fr[a]);
+                        atomicAdd(&F32[off].y, fi[a]);
+                    }
+                    if (doG) {
+                        atomicAdd(&G32[off].x, gr[a]);
+                        atomicAdd(&G32[off].y, gi[a]);
+                    }
+                } else {
+                    if (doF) {
+                        float2 w = F32[off];
+                        w.x += fr[a];
+                        w.y += fi[a];
+                        F32[off] = w;
+                    }
+                    if (doG) {
+                        float2 w = G32[off];
+                        w.x += gr[a];
+                        w.y += gi[a];
+                        G32[off] = w;
+                    }
+                }
+            }
+        }
+    }
+    if (active && doC) Cpart[(int64_t)s * M + i] = dev::f2d(cacc.hi) + dev::f2d(cacc.lo);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+// complex64 -> complex128, two entries per thread per iteration (16-byte stores)
+__global__ void widen_kernel(const float4 *__restrict__ in, double2 *__restrict__ out, int64_t n2,
+                             const float2 *__restrict__ in_tail, double2 *__restrict__ out_tail,
+                             int tail) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += stride) {
+        const float4 v = in[j];
+        out[2 * j] = make_double2(dev::f2d(v.x), dev::f2d(v.y));
+        out[2 * j + 1] = make_double2(dev::f2d(v.z), dev::f2d(v.w));
+    }
+    if (tail && blockIdx.x == 0 && threadIdx.x == 0) {
+        const float2 v = in_tail[0];
+        out_tail[0] = make_double2(dev::f2d(v.x), dev::f2d(v.y));
+    }
+}
+
+// FP64 integration of the deferred pairs; results added with FP64 atomics.
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(128)
+correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restrict__ defer_count,
+                    unsigned int defer_cap, Fp64View v, const double *__restrict__ tgt, int64_t M,
+                    double kre, double kim, int flags, double2 *__restrict__ F,
+                    double2 *__restrict__ G, double *__restrict__ Cnear,
+                    unsigned long long *__restrict__ qpe_count) {
+    const unsigned int n = min(*defer_count, defer_cap);
+    const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
+    unsigned long long nqpe = 0;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int2 pr = defer[j];
+        const int64_t i = pr.x;
+        const double *r = v.rec + (size_t)pr.y * v.stride;
+        const double tx = tgt[3 * i], ty = tgt[3 * i + 1], tz = tgt[3 * i + 2];
+        const int c = dev::nearest_node<NP>(r, tx, ty, tz);
+        nqpe += v.ri.Q[c];
+        double fr[NP], fi[NP], gr[NP], gi[NP];
+        const double ce = dev::element_fp64<NP, CPLX_K>(r + v.ri.off[c], v.ri.Q[c],
+                                                        v.phi + (size_t)c * v.qmax * NP, tx, ty, tz,
+                                                        kre, kim, fr, fi, gr, gi);
+        const int32_t *nid = reinterpret_cast<const int32_t *>(r + v.nidx_off);
+#pragma unroll
+        for (int a = 0; a < NP; ++a) {
+            const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
+            if (doF) {
+                atomicAdd(&F[off].x, fr[a]);
+                atomicAdd(&F[off].y, fi[a]);
+            }
+            if (doG) {
+                atomicAdd(&G[off].x, gr[a]);
+                atomicAdd(&G[off].y, gi[a]);
+            }
+        }
+        if (doC) atomicAdd(&Cnear[i], ce);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+template <int NP, bool CPLX>
+void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int chunk,
+               float2 *F32, float2 *G32, double *Cpart, int2 *defer, unsigned int *dcount,
+               unsigned int dcap, double *Cnear) {
+    const RecordLayout &L = c.lay;
+    const MixedLayout &X = c.mlay;
+    RuleInfo ri{}, ri64{};
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = L.Q[r];
+        ri.off[r] = X.rule_off[r];
+        ri64.Q[r] = L.Q[r];
+        ri64.off[r] = L.rule_off[r];
+    }
+    Fp64View v{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
+    auto kern = assemble_mixed_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((a.M + kThreads - 1) / kThreads), (unsigned)S);
+    cudaEvent_t t0 = c.timer_begin();
+    kern<<<grid, kThreads, smem, c.stream>>>(
+        c.d_mrecords, X.stride, X.nidx_off, c.n_elements, S,
+        c.d_shared_mask + (size_t)level * c.n_elements, c.d_mphi, L.R * L.qmax * L.NP, L.qmax, ri,
+        a.targets, a.M, a.k_re, a.k_im, a.flags, F32, G32, Cpart, chunk, defer, dcount, dcap, v,
+        c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    c.timer_end(t0);
+    ++c.kernel_launches;
+
+    const int64_t N = c.n_sources;
+    const int64_t total = a.M * N;                 // complex entries per matrix
+    const int64_t n2 = total / 2;
+    const int tail = (int)(total & 1);
+    const unsigned wgrid = (unsigned)std::min<int64_t>((n2 + 255) / 256, 8LL * c.num_sms * 8);
+    if (a.flags & BIE_F) {
+        widen_kernel<<<std::max(1u, wgrid), 256, 0, c.stream>>>(
+            reinterpret_cast<const float4 *>(F32), reinterpret_cast<double2 *>(a.F), n2,
+            F32 + 2 * n2, reinterpret_cast<double2 *>(a.F) + 2 * n2, tail);
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+    if (a.flags & BIE_G) {
+        widen_kernel<<<std::max(1u, wgrid), 256, 0, c.stream>>>(
+            reinterpret_cast<const float4 *>(G32), reinterpret_cast<double2 *>(a.G), n2,
+            G32 + 2 * n2, reinterpret_cast<double2 *>(a.G) + 2 * n2, tail);
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+    correct_fp64_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+        defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
+        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+}
+
+}  // namespace
+
+void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
+    const RecordLayout &L = c.lay;
+    MixedLayout &X = c.mlay;
+    X = MixedLayout{};
+    const int NP = L.NP;
+    int off = 8 + 3 * NP;
+    for (int r = 0; r < L.R; ++r) {
+        X.rule_off[r] = off;
+        off += 8 * L.Q[r];
+    }
+    X.nidx_off = off;
+    off += NP;
+    X.stride = (off + 3) & ~3;
+    const int64_t E = c.n_elements;
+    std::vector<float> rec((size_t)E * X.stride, 0.f);
+    for (int64_t p = 0; p < E; ++p) {
+        const int64_t e = c.order[p];
+        const double *R0 = &rec64[(size_t)p * L.stride];
+        float *W = &rec[(size_t)p * X.stride];
+        double cen[3] = {0, 0, 0}, hmax = 0;
+        for (int a = 0; a < 3; ++a)
+            for (int k = 0; k < 3; ++k) cen[k] += c.coords[3 * (int64_t)c.topo[c.NS * e + a] + k] / 3.0;
+        for (int a = 0; a < 3; ++a) {
+            const double *A = &c.coords[3 * (int64_t)c.topo[c.NS * e + a]];
+            const double *B = &c.coords[3 * (int64_t)c.topo[c.NS * e + (a + 1) % 3]];
+            hmax = std::max(hmax, std::sqrt((A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) +
+                                            (A[2] - B[2]) * (A[2] - B[2])));
+        }
+        for (int k = 0; k < 3; ++k) {
+            const float hi = (float)cen[k];
+            W[k] = hi;
+            W[3 + k] = (float)(cen[k] - (double)hi);
+        }
+        W[6] = (float)(hmax * hmax);   // near: centroid within one element size
+        for (int a = 0; a < NP; ++a)
+            for (int k = 0; k < 3; ++k) W[8 + 3 * a + k] = (float)(R0[3 * a + k] - cen[k]);
+        for (int r = 0; r < L.R; ++r) {
+            const int Q = L.Q[r];
+            const double *g = R0 + L.rule_off[r];
+            float *w = W + X.rule_off[r];
+            for (int q = 0; q < Q; ++q) {
+                const double ox = g[q] - cen[0], oy = g[Q + q] - cen[1], oz = g[2 * Q + q] - cen[2];
+                w[q] = (float)ox;
+                w[Q + q] = (float)oy;
+                w[2 * Q + q] = (float)oz;
+                w[3 * Q + q] = (float)g[3 * Q + q];
+                w[4 * Q + q] = (float)g[4 * Q + q];
+                w[5 * Q + q] = (float)g[5 * Q + q];
+                w[6 * Q + q] = (float)(g[6 * Q + q] * 0.07957747154594767);
+                // |o|^2 of the rounded offsets, so that 2 D.o + |o|^2 = |D + o|^2 - |D|^2
+                const double fx = (float)ox, fy = (float)oy, fz = (float)oz;
+                w[7 * Q + q] = (float)(fx * fx + fy * fy + fz * fz);
+            }
+        }
+        int32_t *nid = reinterpret_cast<int32_t *>(W + X.nidx_off);
+        for (int a = 0; a < NP; ++a) nid[a] = c.ptopo[NP * e + a];
+    }
+    std::vector<float> phi32(c.phi.size());
+    for (size_t j = 0; j < phi32.size(); ++j) phi32[j] = (float)c.phi[j];
+    BIE_CUDA(cudaMalloc(&c.d_mrecords, rec.size() * sizeof(float)));
+    BIE_CUDA(cudaMalloc(&c.d_mphi, phi32.size() * sizeof(float)));
+    BIE_CUDA(cudaMemcpy(c.d_mrecords, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMemcpy(c.d_mphi, phi32.data(), phi32.size() * sizeof(float), cudaMemcpyHostToDevice));
+}
+
+void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
+    const RecordLayout &L = c.lay;
+    const int64_t N = c.n_sources;
+    const size_t mat32 = (size_t)a.M * N * 8;
+    float2 *F32 = (a.flags & BIE_F) ? static_cast<float2 *>(c.scratch(kScratchF32, mat32)) : nullptr;
+    float2 *G32 = (a.flags & BIE_G) ? static_cast<float2 *>(c.scratch(kScratchG32, mat32)) : nullptr;
+    if (F32) BIE_CUDA(cudaMemsetAsync(F32, 0, mat32, c.stream));
+    if (G32) BIE_CUDA(cudaMemsetAsync(G32, 0, mat32, c.stream));
+    if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;
+
+    // deferred-pair list: M x 32 entries + counter + near C (M doubles)
+    const unsigned int dcap = (unsigned int)std::min<int64_t>(a.M * 32 + 4096, (int64_t)1 << 30);
+    const size_t dbytes = (size_t)dcap * sizeof(int2);
+    char *dbuf = static_cast<char *>(c.scratch(kScratchDefer, dbytes + 256 + (size_t)a.M * 8));
+    int2 *defer = reinterpret_cast<int2 *>(dbuf);
+    unsigned int *dcount = reinterpret_cast<unsigned int *>(dbuf + dbytes);
+    double *Cnear = reinterpret_cast<double *>(dbuf + dbytes + 256);
+    BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
+
+    const int level = choose_slice_level(c, a.M, kThreads);
+    const int S = 1 << level;
+    const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (40u << 10) / rec_bytes));
+    const size_t phi_f = (size_t)((L.R * L.qmax * L.NP + 3) & ~3);
+    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes + (size_t)chunk * 4;
+    double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
+    const bool cplx = a.k_im != 0.0;
+    if (L.NP == 3) {
+        if (cplx) launch_np<3, true>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        else launch_np<3, false>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+    } else {
+        if (cplx) launch_np<6, true>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        else launch_np<6, false>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+    }
+    if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
+}
+
+}  // namespace bie

@@ -54,8 +54,8 @@ void check_assemble_args(bie::Ctx &c, double kr, double ki, int64_t M, int flags
 }
 
 void run_assemble(bie::Ctx &c, const bie::AssembleArgs &a, int precision) {
-    (void)precision;   // the mixed-precision kernel is selected here once it exists
-    bie::launch_assemble_fp64(c, a);
+    if (precision == BIE_PREC_MIXED) bie::launch_assemble_mixed(c, a);
+    else bie::launch_assemble_fp64(c, a);
 }
 
 }  // namespace

@@ -78,7 +78,24 @@ enum ScratchSlot {
     kScratchG = 2,         // device G (host entry points)
     kScratchCpart = 3,     // per-slice partial C row sums
     kScratchC = 4,         // device C (host entry points)
+    kScratchF32 = 5,       // complex64 F accumulator (mixed precision)
+    kScratchG32 = 6,       // complex64 G accumulator (mixed precision)
+    kScratchDefer = 7,     // deferred (target, element) pairs + counter + near C
     kScratchCount = 8
+};
+
+// Mixed-precision element record (32-bit words, same element order as the FP64
+// records):
+//   [0,3) centroid hi, [3,6) centroid lo (double-float), [6] near radius^2
+//   [8, 8+3*NP)                      physics-node offsets from the centroid
+//   rule r at rule_off[r]:           dx[Q] dy[Q] dz[Q] nx[Q] ny[Q] nz[Q] jw/4pi[Q] |d|^2[Q]
+//                                    (quadrature points relative to the centroid)
+//   nidx_off:                        NP int32 physics-node indices
+// The stride is a multiple of 4 words (16 bytes).
+struct MixedLayout {
+    int rule_off[kMaxRules] = {};
+    int nidx_off = 0;
+    int stride = 0;
 };
 
 struct Ctx {
@@ -111,6 +128,9 @@ struct Ctx {
     double *d_sources = nullptr;         // 3 x N (AoS)
     uint32_t *d_shared_mask = nullptr;   // kMaxLevels x E: bit a set -> node a is
                                          // touched by elements of another slice
+    MixedLayout mlay;
+    float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
+    float *d_mphi = nullptr;             // R x qmax x NP (FP32)
 
     // grow-only device scratch, indexed by the kScratch* slots below
     void *d_scratch[8] = {};
@@ -146,6 +166,14 @@ struct AssembleArgs {
     double *F, *G, *C;       // device outputs (interleaved complex), may be null
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
+int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
+void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
+                     double *C);
+
+// Mixed-precision assembly (bie_assemble_mixed.cu)
+// host: builds d_mrecords / d_mphi from the FP64 records (E x lay.stride) and uploads them
+void build_mixed_records(Ctx &c, const std::vector<double> &rec64);
+void launch_assemble_mixed(Ctx &c, const AssembleArgs &a);
 
 // FMA throughput probe (bie_peaks.cu)
 void measure_peaks(int device, bie_peaks &out);

@@ -526,6 +526,7 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device) {
                         cudaMemcpyHostToDevice));
     BIE_CUDA(cudaMemcpy(c.d_shared_mask, masks.data(), masks.size() * sizeof(uint32_t),
                         cudaMemcpyHostToDevice));
+    build_mixed_records(c, rec);
 }
 
 void destroy_context(Ctx &c) {
@@ -535,6 +536,10 @@ void destroy_context(Ctx &c) {
     cudaFree(c.d_phi);
     cudaFree(c.d_sources);
     cudaFree(c.d_shared_mask);
+    cudaFree(c.d_mrecords);
+    cudaFree(c.d_mphi);
+    c.d_mrecords = nullptr;
+    c.d_mphi = nullptr;
     cudaFree(c.d_qpe);
     for (int i = 0; i < kScratchCount; ++i) cudaFree(c.d_scratch[i]);
     for (auto &p : c.ev_pending) {
