@@ -192,6 +192,52 @@ def run_reference(args):
     }))
 
 
+def timed_steps(ctx, stream, ks, F, G, Cv, flush, steps, warmup, precision, barrier):
+    """W untimed + K timed assemblies; CUDA events on the library stream around each
+    step, an L2 flush (256 MB write) before each step outside the events."""
+    import torch
+    for w in range(warmup):
+        ctx.assemble_device(ks[w % len(ks)], F, G, Cv, precision=precision)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ctx.set_timing(True)
+    ctx.stats(reset=True)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(s & 0xFF)
+            starts[s].record(stream)
+        ctx.assemble_device(ks[s % len(ks)], F, G, Cv, precision=precision)
+        with torch.cuda.stream(stream):
+            ends[s].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier()
+    st = ctx.stats(reset=True)
+    ctx.set_timing(False)
+    dev_ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
+    return dev_ms, wall, st
+
+
+def roofline_entry(st, kernel, bound, peak_flops, workload_name, nphys):
+    kernel_ms = st["timed_ms"] / max(st["timed_launches"], 1)
+    flops = st["algorithmic_flops"] / max(st["timed_launches"], 1)
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    peak = peak_flops / 1e12
+    tr = ncu_traffic(kernel, workload_name)
+    return {"bound": bound, "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak,
+            "peak_source": f"measured {bound.upper()} FMA-chain throughput (bie_measure_peaks) on this GPU",
+            "traffic": tr.get("dram_bytes_per_launch") if tr else None,
+            "traffic_how": tr.get("how") if tr else None,
+            "flops_per_launch": flops, "kernel_ms": kernel_ms,
+            "qpe_per_launch": st["quadrature_evals"] / max(st["timed_launches"], 1),
+            "flops_per_qpe": f"32 + 8 n_phys (n_phys={nphys})"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,9 +245,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="rigid_sphere_p2")
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed",
+                    help="arithmetic of the headline path (the plain FP64 path is always timed beside it)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -226,10 +274,17 @@ def main():
         if dist is not None:
             dist.barrier()
 
+    def max_over_ranks(x):
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+        if dist is not None:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     mesh, ks, desc = workload(args.workload)
     # weak scaling: every rank assembles its own share of the frequency list
     ks = ks[rank % len(ks):] + ks[:rank % len(ks)]
     N = mesh.n_sources
+    nphys = 3 if mesh.physics_function == "linear" else 6
     ctx = biegpu.Context(mesh, n=2, m=2, device=local)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=f"cuda:{local}")
     dev = torch.device(f"cuda:{local}")
@@ -238,53 +293,42 @@ def main():
     Cv = torch.empty(N, dtype=torch.complex128, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     entries_per_step = 2.0 * N * N
-
-    for w in range(args.warmup):
-        ctx.assemble_device(ks[w % len(ks)], F, G, Cv, precision=args.precision)
-    torch.cuda.synchronize()
-
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ctx.set_timing(True)
-    ctx.stats(reset=True)
-    barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        for s in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(s & 0xFF)
-                starts[s].record(stream)
-            ctx.assemble_device(ks[s % len(ks)], F, G, Cv, precision=args.precision)
-            with torch.cuda.stream(stream):
-                ends[s].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-    barrier()
-    st = ctx.stats(reset=True)
-    ctx.set_timing(False)
-    dev_ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends))
-    t = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    dev_ms = float(t.item())
-    value = entries_per_step * args.steps * world / (dev_ms * 1e-3)
-
-    # ---- roofline of the dominant kernel (FP64 pipe bound) -----------------
-    kernel_ms = st["timed_ms"] / max(st["timed_launches"], 1)
-    flops_per_launch = st["algorithmic_flops"] / max(st["timed_launches"], 1)
     peaks = biegpu._capi.measure_peaks(local)
-    achieved = flops_per_launch / (kernel_ms * 1e-3) / 1e12
-    peak = peaks["fp64_flops"] / 1e12
-    roofline = {"bound": "fp64", "kernel": "assemble_fp64_kernel", "achieved": achieved, "peak": peak,
-                "unit": "TFLOP/s", "frac": achieved / peak,
-                "peak_source": "measured FP64 FMA-chain throughput (bie_measure_peaks) on this GPU",
-                "traffic": ncu_traffic("assemble_fp64_kernel", args.workload),
-                "flops_per_launch": flops_per_launch, "kernel_ms": kernel_ms,
-                "qpe_per_launch": st["quadrature_evals"] / max(st["timed_launches"], 1),
-                "flops_per_qpe": "32 + 8 n_phys (n_phys=%d)" % (3 if mesh.physics_function == "linear" else 6),
-                "fp32_peak_tflops": peaks["fp32_flops"] / 1e12}
+
+    with ClockSampler(local) as clk:
+        dev_ms, wall, st = timed_steps(ctx, stream, ks, F, G, Cv, flush, args.steps, args.warmup,
+                                       args.precision, barrier)
+    dev_ms = max_over_ranks(dev_ms)
+    value = entries_per_step * args.steps * world / (dev_ms * 1e-3)
     gpu_launches = st["kernel_launches"]
+    if args.precision == "mixed":
+        roofline = roofline_entry(st, "assemble_mixed_kernel", "fp32", peaks["fp32_flops"], args.workload, nphys)
+    else:
+        roofline = roofline_entry(st, "assemble_fp64_kernel", "fp64", peaks["fp64_flops"], args.workload, nphys)
+
+    # ---- the plain FP64 GPU path, and the mixed path's error against it ------
+    plain = None
+    accuracy = None
+    if args.precision == "mixed" and not args.no_fp64:
+        p_ms, _, pst = timed_steps(ctx, stream, ks, F, G, Cv, flush, max(2, args.steps // 2), 1, "fp64", barrier)
+        p_ms = max_over_ranks(p_ms)
+        psteps = max(2, args.steps // 2)
+        plain = {"value": entries_per_step * psteps * world / (p_ms * 1e-3), "unit": UNIT,
+                 "ms_per_step": p_ms / psteps,
+                 "roofline": roofline_entry(pst, "assemble_fp64_kernel", "fp64", peaks["fp64_flops"],
+                                            args.workload, nphys)}
+        kerr = max(ks)
+        ctx.assemble_device(kerr, F, G, Cv, precision="fp64")
+        F2 = torch.empty_like(F)
+        G2 = torch.empty_like(F)
+        C2 = torch.empty_like(Cv)
+        ctx.assemble_device(kerr, F2, G2, C2, precision="mixed")
+        torch.cuda.synchronize()
+        accuracy = {"k": kerr, "vs": "plain FP64 GPU assembly (same inputs)",
+                    "F_rel_fro": float(torch.linalg.norm(F2 - F) / torch.linalg.norm(F)),
+                    "G_rel_fro": float(torch.linalg.norm(G2 - G) / torch.linalg.norm(G)),
+                    "C_rel": float(torch.linalg.norm(C2 - Cv) / torch.linalg.norm(Cv))}
+        del F2, G2, C2
 
     # ---- end to end through the host-buffer C-ABI call -----------------------
     e2e = None
@@ -299,20 +343,18 @@ def main():
         tg[...] = mesh.sources
         ctx.assemble(ks[0], targets=tg, out=(Fh, Gh, Ch), precision=args.precision)   # warm-up
         barrier()
-        t0 = time.perf_counter()
         n_e2e = max(1, min(args.steps, 5))
+        t0 = time.perf_counter()
         for s in range(n_e2e):
             ctx.assemble(ks[s % len(ks)], targets=tg, out=(Fh, Gh, Ch), precision=args.precision)
-        e2e_s = time.perf_counter() - t0
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        if dist is not None:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
         e2e = {"value": entries_per_step * n_e2e * world / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": int(tg.nbytes), "d2h_bytes_per_step": int(Fh.nbytes + Gh.nbytes + Ch.nbytes),
                "steps": n_e2e, "call": "bie_assemble (host buffers, pinned)"}
 
     if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
         return
     cpu = None
     if not args.no_cpu_baseline:
@@ -324,12 +366,15 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "wall_ms_per_step": 1e3 * wall / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if args.precision == "mixed" else "f64",
         "precision": args.precision, "data": "synthetic",
         "config": dict(desc, l2="256 MB L2 flush between steps; each step writes 4.3 GB", parallelism=f"replicas{world}"),
-        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
+        "roofline": roofline, "plain_fp64": plain, "accuracy": accuracy,
+        "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
         "clocks": clk.summary(), "gpu": torch.cuda.get_device_name(dev),
-        "measured_peaks_file": {k: measured_peaks().get(k) for k in ("hbm_gbs", "bf16_tflops")},
+        "peaks": {"fp64_tflops": peaks["fp64_flops"] / 1e12, "fp32_tflops": peaks["fp32_flops"] / 1e12,
+                  "hbm_gbs_measured_file": measured_peaks().get("hbm_gbs")},
     }
     print(json.dumps(out))
     if dist is not None:

@@ -8,11 +8,12 @@
 //     c_e in FP32.  Per pair, D = c_e - t and r0 = |D| are formed in
 //     double-float arithmetic and the phase k r0 is reduced modulo 2 pi there,
 //     so the per-point phase  k r0 + k (r - r0)  with
-//     r - r0 = (2 D.d + |d|^2) / (r + r0)  stays accurate to ~1e-7 even for
-//     k r ~ 20.  sin/cos are evaluated with a quadrant reduction and Taylor
-//     polynomials on the FMA pipe.  Per-node sums are FP32 over the <= 8 points
-//     of one element; F and G accumulate across elements in complex64 and are
-//     widened to complex128 by a separate pass.
+//     r - r0 = (2 D.o + |o|^2) / (r + r0)  (o = x_q - c_e) stays accurate to
+//     ~1e-7 even for k r ~ 20.  sin/cos are evaluated with a quadrant reduction
+//     and Taylor polynomials on the FMA pipe.  Per-node sums are FP32 over the
+//     <= 8 points of one element; F and G accumulate across elements in
+//     complex64 with vector FP32 reductions (no read-modify-write round trip)
+//     and are widened to complex128 by a streaming pass.
 //   * near pairs (target within one element size of the centroid, or within half
 //     an element size of a physics node: the singular and near-singular
 //     elements, which include every element containing the target node) and
@@ -41,6 +42,11 @@ constexpr float kTwoPiB = 1.9353071795864769e-3f;
 constexpr float kTwoPiC = 1.0253376606e-11f;        // (2 pi - A) - B, rounded
 constexpr float kInv2Pi = 0.15915494309189535f;
 
+template <int NP>
+struct PhiPad {
+    static constexpr int value = NP <= 4 ? 4 : 8;   // Phi rows padded for 16-byte loads
+};
+
 struct Fp64View {
     const double *rec;
     int stride;
@@ -49,6 +55,14 @@ struct Fp64View {
     int qmax;
     RuleInfo ri;
 };
+
+// sqrt of a positive double-float: float estimate from rsqrt, one correction
+__device__ __forceinline__ df df_sqrt_fast(df a) {
+    const float ri = rsqrtf(a.hi);
+    const float y = a.hi * ri;
+    const float e = __fadd_rn(__fmaf_rn(-y, y, a.hi), a.lo);
+    return dev::fast_two_sum(y, e * (0.5f * ri));
+}
 
 // FP64 integration of one deferred pair (exact rule choice), used in place when
 // the deferred list is full.
@@ -71,18 +85,18 @@ __device__ __noinline__ void pair_fp64_inplace(const Fp64View v, int64_t p, doub
 }
 
 template <int NP, bool CPLX_K>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
 assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
-                      const uint32_t *__restrict__ smask, const float *__restrict__ phi, int nphi,
-                      int qmax, RuleInfo ri, const double *__restrict__ tgt, int64_t M, double kre,
-                      double kim, int flags, float2 *__restrict__ F32, float2 *__restrict__ G32,
+                      const float *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
+                      const double *__restrict__ tgt, int64_t M, double kre, double kim, int flags,
+                      float2 *__restrict__ F32, float2 *__restrict__ G32,
                       double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
                       unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
                       unsigned long long *__restrict__ qpe_count) {
+    constexpr int NPP = PhiPad<NP>::value;
     extern __shared__ __align__(16) float smemf[];
     float *s_phi = smemf;                                   // nphi floats (padded to 4)
     float *s_rec = smemf + ((nphi + 3) & ~3);               // chunk * stride floats
-    uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);
 
     const int s = blockIdx.y;
     const int64_t e0 = (int64_t)s * E / S;
@@ -113,7 +127,6 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             float4 *dst = reinterpret_cast<float4 *>(s_rec);
             const int n4 = n * stride / 4;
             for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
-            for (int t = threadIdx.x; t < n; t += kThreads) s_mask[t] = smask[cb + t];
         }
         __syncthreads();
         if (!active) continue;
@@ -121,9 +134,11 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
         for (int el = 0; el < n; ++el) {
             const float *r = s_rec + (size_t)el * stride;
             // D = c_e - t in double-float
-            const df Dx = dev::df_sub({r[0], r[3]}, Tx);
-            const df Dy = dev::df_sub({r[1], r[4]}, Ty);
-            const df Dz = dev::df_sub({r[2], r[5]}, Tz);
+            const float4 h0 = *reinterpret_cast<const float4 *>(r);       // c_hi xyz, c_lo x
+            const float4 h1 = *reinterpret_cast<const float4 *>(r + 4);   // c_lo yz, near2, -
+            const df Dx = dev::df_sub({h0.x, h0.w}, Tx);
+            const df Dy = dev::df_sub({h0.y, h1.x}, Ty);
+            const df Dz = dev::df_sub({h0.z, h1.y}, Tz);
             const float Dfx = Dx.hi, Dfy = Dy.hi, Dfz = Dz.hi;
 
             // nearest physics node in FP32, with near / tie detection
@@ -146,27 +161,25 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
 #pragma unroll
             for (int a = 0; a < NP; ++a) tie |= (a != c) && (d2[a] <= lim);
             const float r0f2 = Dfx * Dfx + Dfy * Dfy + Dfz * Dfz;
-            const float near2 = r[6];
+            const float near2 = h1.z;
             const bool deferred = tie || r0f2 < near2 || 4.0f * b < near2;
 
             float fr[NP], fi[NP], gr[NP], gi[NP];
             float ce = 0.f;
-            bool have = true;
             if (deferred) {
                 const unsigned int slot = atomicAdd(defer_count, 1u);
                 if (slot < defer_cap) {
                     defer[slot] = make_int2((int)i, (int)(cb + el));
-                    have = false;
-                } else {
-                    double ced;
-                    pair_fp64_inplace<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, fr, fi, gr,
-                                                  gi, &ced);
-                    ce = (float)(-ced);   // stored with the sign of the FP32 path below
+                    continue;
                 }
+                double ced;
+                pair_fp64_inplace<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, fr, fi, gr, gi,
+                                              &ced);
+                ce = (float)(-ced);   // stored with the sign of the FP32 path below
             } else {
                 // pair quantities in double-float: r0 = |D|, phase k r0 mod 2 pi
                 const df r0sq = dev::df_add(dev::df_add(dev::df_sqr(Dx), dev::df_sqr(Dy)), dev::df_sqr(Dz));
-                const df r0 = dev::df_sqrt(r0sq);
+                const df r0 = df_sqrt_fast(r0sq);
                 const df kr0 = dev::df_mul(K, r0);
                 const float nrev = rintf(kr0.hi * kInv2Pi);
                 float th0 = __fmaf_rn(-nrev, kTwoPiA, kr0.hi);
@@ -177,18 +190,19 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
 
                 const int Q = ri.Q[c];
                 nqpe += Q;
-                const float *g = r + ri.off[c];
-                const float *ph = s_phi + (size_t)c * qmax * NP;
+                const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
+                const float *ph = s_phi + (size_t)c * qmax * NPP;
 #pragma unroll
                 for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.f;
                 for (int q = 0; q < Q; ++q) {
-                    const float ox = g[q], oy = g[Q + q], oz = g[2 * Q + q];
-                    const float dx = Dfx + ox, dy = Dfy + oy, dz = Dfz + oz;   // x_q - t
+                    const float4 A = g4[2 * q];       // o = x_q - c_e, jw / 4 pi
+                    const float4 B = g4[2 * q + 1];   // n, |o|^2
+                    const float dx = Dfx + A.x, dy = Dfy + A.y, dz = Dfz + A.z;   // x_q - t
                     const float r2 = dx * dx + dy * dy + dz * dz;
                     const float rinv = rsqrtf(r2);
                     const float rr = r2 * rinv;
                     // r - r0 = (2 D.o + |o|^2) / (r + r0), free of cancellation
-                    const float num = __fmaf_rn(2.0f, Dfx * ox + Dfy * oy + Dfz * oz, g[7 * Q + q]);
+                    const float num = __fmaf_rn(2.0f, Dfx * A.x + Dfy * A.y + Dfz * A.z, B.w);
                     const float dr = __fdividef(num, rr + r0h);
                     float sn, cs;
                     dev::sincos_f32(__fmaf_rn(kf, dr, th0), &sn, &cs);
@@ -197,60 +211,40 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                         sn *= damp;
                         cs *= damp;
                     }
-                    const float dn = g[3 * Q + q] * dx + g[4 * Q + q] * dy + g[5 * Q + q] * dz;
-                    const float wg = rinv * g[6 * Q + q];          // jw / (4 pi r)
+                    const float dn = B.x * dx + B.y * dy + B.z * dz;
+                    const float wg = rinv * A.w;                      // jw / (4 pi r)
                     const float Gr = cs * wg, Gi = sn * wg;
-                    const float tq = dn * (rinv * rinv) * wg;        // (x-t).n jw / (4 pi r^3)
+                    const float tq = dn * (rinv * rinv) * wg;         // (x-t).n jw / (4 pi r^3)
                     ce += tq;
                     const float ar = CPLX_K ? (-1.0f - kimf * rr) : -1.0f;
                     const float ai = kf * rr;
                     const float Fr = (cs * ar - sn * ai) * tq;
                     const float Fi = (cs * ai + sn * ar) * tq;
-                    const float *pq = ph + q * NP;
+                    float p[NPP];
+                    *reinterpret_cast<float4 *>(p) = *reinterpret_cast<const float4 *>(ph + q * NPP);
+                    if (NPP == 8)
+                        *reinterpret_cast<float4 *>(p + 4) = *reinterpret_cast<const float4 *>(ph + q * NPP + 4);
 #pragma unroll
                     for (int a = 0; a < NP; ++a) {
-                        const float p = pq[a];
-                        fr[a] = __fmaf_rn(Fr, p, fr[a]);
-                        fi[a] = __fmaf_rn(Fi, p, fi[a]);
-                        gr[a] = __fmaf_rn(Gr, p, gr[a]);
-                        gi[a] = __fmaf_rn(Gi, p, gi[a]);
+                        fr[a] = __fmaf_rn(Fr, p[a], fr[a]);
+                        fi[a] = __fmaf_rn(Fi, p[a], fi[a]);
+                        gr[a] = __fmaf_rn(Gr, p[a], gr[a]);
+                        gi[a] = __fmaf_rn(Gi, p[a], gi[a]);
                     }
                 }
             }
-            if (!have) continue;
             // C row sum in double-float (C = -sum tq)
             {
                 const df t = dev::two_sum(cacc.hi, -ce);
                 cacc = dev::fast_two_sum(t.hi, __fadd_rn(t.lo, cacc.lo));
             }
+            // F, G: vector FP32 reductions (fire-and-forget, no return value)
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
-            const uint32_t m = s_mask[el];
 #pragma unroll
             for (int a = 0; a < NP; ++a) {
                 const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
-                if ((m >> a) & 1u) {
-                    if (doF) {
-                        atomicAdd(&F32[off].x, fr[a]);
-                        atomicAdd(&F32[off].y, fi[a]);
-                    }
-                    if (doG) {
-                        atomicAdd(&G32[off].x, gr[a]);
-                        atomicAdd(&G32[off].y, gi[a]);
-                    }
-                } else {
-                    if (doF) {
-                        float2 w = F32[off];
-                        w.x += fr[a];
-                        w.y += fi[a];
-                        F32[off] = w;
-                    }
-                    if (doG) {
-                        float2 w = G32[off];
-                        w.x += gr[a];
-                        w.y += gi[a];
-                        G32[off] = w;
-                    }
-                }
+                if (doF) atomicAdd(F32 + off, make_float2(fr[a], fi[a]));
+                if (doG) atomicAdd(G32 + off, make_float2(gr[a], gi[a]));
             }
         }
     }
@@ -319,9 +313,9 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
 }
 
 template <int NP, bool CPLX>
-void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int chunk,
-               float2 *F32, float2 *G32, double *Cpart, int2 *defer, unsigned int *dcount,
-               unsigned int dcap, double *Cnear) {
+void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, float2 *F32,
+               float2 *G32, double *Cpart, int2 *defer, unsigned int *dcount, unsigned int dcap,
+               double *Cnear) {
     const RecordLayout &L = c.lay;
     const MixedLayout &X = c.mlay;
     RuleInfo ri{}, ri64{};
@@ -337,10 +331,9 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int
     dim3 grid((unsigned)((a.M + kThreads - 1) / kThreads), (unsigned)S);
     cudaEvent_t t0 = c.timer_begin();
     kern<<<grid, kThreads, smem, c.stream>>>(
-        c.d_mrecords, X.stride, X.nidx_off, c.n_elements, S,
-        c.d_shared_mask + (size_t)level * c.n_elements, c.d_mphi, L.R * L.qmax * L.NP, L.qmax, ri,
-        a.targets, a.M, a.k_re, a.k_im, a.flags, F32, G32, Cpart, chunk, defer, dcount, dcap, v,
-        c.d_qpe);
+        c.d_mrecords, X.stride, X.nidx_off, c.n_elements, S, c.d_mphi,
+        L.R * L.qmax * PhiPad<NP>::value, L.qmax, ri, a.targets, a.M, a.k_re, a.k_im, a.flags,
+        F32, G32, Cpart, chunk, defer, dcount, dcap, v, c.d_qpe);
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;
@@ -378,7 +371,8 @@ void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
     MixedLayout &X = c.mlay;
     X = MixedLayout{};
     const int NP = L.NP;
-    int off = 8 + 3 * NP;
+    const int NPP = NP <= 4 ? 4 : 8;
+    int off = (8 + 3 * NP + 3) & ~3;
     for (int r = 0; r < L.R; ++r) {
         X.rule_off[r] = off;
         off += 8 * L.Q[r];
@@ -401,11 +395,11 @@ void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
             hmax = std::max(hmax, std::sqrt((A[0] - B[0]) * (A[0] - B[0]) + (A[1] - B[1]) * (A[1] - B[1]) +
                                             (A[2] - B[2]) * (A[2] - B[2])));
         }
-        for (int k = 0; k < 3; ++k) {
-            const float hi = (float)cen[k];
-            W[k] = hi;
-            W[3 + k] = (float)(cen[k] - (double)hi);
-        }
+        // header: c_hi x y z, c_lo x | c_lo y z, near radius^2, 0
+        for (int k = 0; k < 3; ++k) W[k] = (float)cen[k];
+        W[3] = (float)(cen[0] - (double)W[0]);
+        W[4] = (float)(cen[1] - (double)W[1]);
+        W[5] = (float)(cen[2] - (double)W[2]);
         W[6] = (float)(hmax * hmax);   // near: centroid within one element size
         for (int a = 0; a < NP; ++a)
             for (int k = 0; k < 3; ++k) W[8 + 3 * a + k] = (float)(R0[3 * a + k] - cen[k]);
@@ -414,24 +408,29 @@ void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
             const double *g = R0 + L.rule_off[r];
             float *w = W + X.rule_off[r];
             for (int q = 0; q < Q; ++q) {
-                const double ox = g[q] - cen[0], oy = g[Q + q] - cen[1], oz = g[2 * Q + q] - cen[2];
-                w[q] = (float)ox;
-                w[Q + q] = (float)oy;
-                w[2 * Q + q] = (float)oz;
-                w[3 * Q + q] = (float)g[3 * Q + q];
-                w[4 * Q + q] = (float)g[4 * Q + q];
-                w[5 * Q + q] = (float)g[5 * Q + q];
-                w[6 * Q + q] = (float)(g[6 * Q + q] * 0.07957747154594767);
+                const float ox = (float)(g[q] - cen[0]), oy = (float)(g[Q + q] - cen[1]),
+                            oz = (float)(g[2 * Q + q] - cen[2]);
+                float *P = w + 8 * q;
+                P[0] = ox;
+                P[1] = oy;
+                P[2] = oz;
+                P[3] = (float)(g[6 * Q + q] * 0.07957747154594767);    // jw / (4 pi)
+                P[4] = (float)g[3 * Q + q];
+                P[5] = (float)g[4 * Q + q];
+                P[6] = (float)g[5 * Q + q];
                 // |o|^2 of the rounded offsets, so that 2 D.o + |o|^2 = |D + o|^2 - |D|^2
-                const double fx = (float)ox, fy = (float)oy, fz = (float)oz;
-                w[7 * Q + q] = (float)(fx * fx + fy * fy + fz * fz);
+                P[7] = (float)((double)ox * ox + (double)oy * oy + (double)oz * oz);
             }
         }
         int32_t *nid = reinterpret_cast<int32_t *>(W + X.nidx_off);
         for (int a = 0; a < NP; ++a) nid[a] = c.ptopo[NP * e + a];
     }
-    std::vector<float> phi32(c.phi.size());
-    for (size_t j = 0; j < phi32.size(); ++j) phi32[j] = (float)c.phi[j];
+    // Phi[r][q][a] padded to NPP columns
+    std::vector<float> phi32((size_t)L.R * L.qmax * NPP, 0.f);
+    for (int r = 0; r < L.R; ++r)
+        for (int q = 0; q < L.qmax; ++q)
+            for (int a = 0; a < NP; ++a)
+                phi32[((size_t)r * L.qmax + q) * NPP + a] = (float)c.phi[((size_t)r * L.qmax + q) * NP + a];
     BIE_CUDA(cudaMalloc(&c.d_mrecords, rec.size() * sizeof(float)));
     BIE_CUDA(cudaMalloc(&c.d_mphi, phi32.size() * sizeof(float)));
     BIE_CUDA(cudaMemcpy(c.d_mrecords, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -459,18 +458,19 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
 
     const int level = choose_slice_level(c, a.M, kThreads);
     const int S = 1 << level;
+    const int NPP = L.NP <= 4 ? 4 : 8;
     const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
-    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (40u << 10) / rec_bytes));
-    const size_t phi_f = (size_t)((L.R * L.qmax * L.NP + 3) & ~3);
-    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes + (size_t)chunk * 4;
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
+    const size_t phi_f = (size_t)((L.R * L.qmax * NPP + 3) & ~3);
+    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes;
     double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
     const bool cplx = a.k_im != 0.0;
     if (L.NP == 3) {
-        if (cplx) launch_np<3, true>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        else launch_np<3, false>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        if (cplx) launch_np<3, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        else launch_np<3, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
     } else {
-        if (cplx) launch_np<6, true>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        else launch_np<6, false>(c, a, S, level, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        if (cplx) launch_np<6, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        else launch_np<6, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
     }
     if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
 }
