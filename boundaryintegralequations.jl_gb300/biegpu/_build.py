@@ -23,6 +23,8 @@ SOURCES = [
     "bie_setup.cpp",
     "bie_assemble.cu",
     "bie_assemble_mixed.cu",
+    "bie_matvec.cu",
+    "bie_solver.cu",
     "bie_peaks.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -82,6 +82,49 @@ class Stats(C.Structure):
     ]
 
 
+BIE_OP_DENSE = 0
+BIE_OP_MATRIX_FREE = 1
+
+
+class Operator(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("A", C.c_void_p),
+        ("A32", C.c_void_p),
+        ("k_re", C.c_double),
+        ("k_im", C.c_double),
+        ("scale_re", C.c_double),
+        ("scale_im", C.c_double),
+        ("diag", C.c_void_p),
+    ]
+
+
+class GmresOpts(C.Structure):
+    _fields_ = [
+        ("restart", C.c_int32),
+        ("maxiter", C.c_int32),
+        ("reltol", C.c_double),
+        ("abstol", C.c_double),
+        ("precision", C.c_int32),
+        ("refine", C.c_int32),
+        ("inner_reltol", C.c_double),
+        ("max_refine", C.c_int32),
+        ("initially_nonzero", C.c_int32),
+    ]
+
+
+class GmresInfo(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32),
+        ("restarts", C.c_int32),
+        ("refinements", C.c_int32),
+        ("converged", C.c_int32),
+        ("matvecs", C.c_int64),
+        ("residual_norm", C.c_double),
+        ("rhs_norm", C.c_double),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -103,6 +146,10 @@ SIGNATURES = {
     "bie_ctx_stats": (_I, [_P, C.POINTER(Stats), _I]),
     "bie_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
     "bie_assemble_device": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
+    "bie_matvec": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
+    "bie_matvec_device": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
+    "bie_gmres_device": (_I, [_P, C.POINTER(Operator), _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
+    "bie_round_c64_device": (_I, [_P, _P, _P, _I64]),
 }
 
 

@@ -26,6 +26,7 @@
 //     the near pairs in FP64.
 #include "bie_internal.h"
 #include "bie_device.cuh"
+#include "bie_mixed.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -37,15 +38,7 @@ namespace {
 using dev::df;
 using dev::RuleInfo;
 constexpr int kThreads = 128;
-constexpr float kTwoPiA = 6.28125f;                 // 2 pi = A + B + C (A has 8 bits)
-constexpr float kTwoPiB = 1.9353071795864769e-3f;
-constexpr float kTwoPiC = 1.0253376606e-11f;        // (2 pi - A) - B, rounded
-constexpr float kInv2Pi = 0.15915494309189535f;
-
-template <int NP>
-struct PhiPad {
-    static constexpr int value = NP <= 4 ? 4 : 8;   // Phi rows padded for 16-byte loads
-};
+using mixed::PhiPad;
 
 struct Fp64View {
     const double *rec;
@@ -55,14 +48,6 @@ struct Fp64View {
     int qmax;
     RuleInfo ri;
 };
-
-// sqrt of a positive double-float: float estimate from rsqrt, one correction
-__device__ __forceinline__ df df_sqrt_fast(df a) {
-    const float ri = rsqrtf(a.hi);
-    const float y = a.hi * ri;
-    const float e = __fadd_rn(__fmaf_rn(-y, y, a.hi), a.lo);
-    return dev::fast_two_sum(y, e * (0.5f * ri));
-}
 
 // FP64 integration of one deferred pair (exact rule choice), used in place when
 // the deferred list is full.
@@ -111,7 +96,7 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
         ty = tgt[3 * i + 1];
         tz = tgt[3 * i + 2];
     }
-    const df Tx = dev::df_from_double(tx), Ty = dev::df_from_double(ty), Tz = dev::df_from_double(tz);
+    const mixed::Target T{dev::df_from_double(tx), dev::df_from_double(ty), dev::df_from_double(tz)};
     const df K = dev::df_from_double(kre);
     const float kf = K.hi;
     const float kimf = (float)kim;
@@ -133,40 +118,10 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
 
         for (int el = 0; el < n; ++el) {
             const float *r = s_rec + (size_t)el * stride;
-            // D = c_e - t in double-float
-            const float4 h0 = *reinterpret_cast<const float4 *>(r);       // c_hi xyz, c_lo x
-            const float4 h1 = *reinterpret_cast<const float4 *>(r + 4);   // c_lo yz, near2, -
-            const df Dx = dev::df_sub({h0.x, h0.w}, Tx);
-            const df Dy = dev::df_sub({h0.y, h1.x}, Ty);
-            const df Dz = dev::df_sub({h0.z, h1.y}, Tz);
-            const float Dfx = Dx.hi, Dfy = Dy.hi, Dfz = Dz.hi;
-
-            // nearest physics node in FP32, with near / tie detection
-            float d2[NP];
-#pragma unroll
-            for (int a = 0; a < NP; ++a) {
-                const float ax = Dfx + r[8 + 3 * a], ay = Dfy + r[9 + 3 * a], az = Dfz + r[10 + 3 * a];
-                d2[a] = ax * ax + ay * ay + az * az;
-            }
-            int c = 0;
-            float b = d2[0];
-#pragma unroll
-            for (int a = 1; a < NP; ++a)
-                if (d2[a] < b) {
-                    b = d2[a];
-                    c = a;
-                }
-            const float lim = b * (1.0f + 1e-5f);
-            bool tie = false;
-#pragma unroll
-            for (int a = 0; a < NP; ++a) tie |= (a != c) && (d2[a] <= lim);
-            const float r0f2 = Dfx * Dfx + Dfy * Dfy + Dfz * Dfz;
-            const float near2 = h1.z;
-            const bool deferred = tie || r0f2 < near2 || 4.0f * b < near2;
-
+            const mixed::PairSetup P = mixed::pair_setup<NP>(r, T);
             float fr[NP], fi[NP], gr[NP], gi[NP];
             float ce = 0.f;
-            if (deferred) {
+            if (P.deferred) {
                 const unsigned int slot = atomicAdd(defer_count, 1u);
                 if (slot < defer_cap) {
                     defer[slot] = make_int2((int)i, (int)(cb + el));
@@ -177,67 +132,31 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                                               &ced);
                 ce = (float)(-ced);   // stored with the sign of the FP32 path below
             } else {
-                // pair quantities in double-float: r0 = |D|, phase k r0 mod 2 pi
-                const df r0sq = dev::df_add(dev::df_add(dev::df_sqr(Dx), dev::df_sqr(Dy)), dev::df_sqr(Dz));
-                const df r0 = df_sqrt_fast(r0sq);
-                const df kr0 = dev::df_mul(K, r0);
-                const float nrev = rintf(kr0.hi * kInv2Pi);
-                float th0 = __fmaf_rn(-nrev, kTwoPiA, kr0.hi);
-                th0 = __fmaf_rn(-nrev, kTwoPiB, th0);
-                th0 = __fmaf_rn(-nrev, kTwoPiC, th0);
-                th0 += kr0.lo;
-                const float r0h = r0.hi;
-
+                const mixed::Phase ph = mixed::pair_phase(P, K);
+                const int c = P.c;
                 const int Q = ri.Q[c];
                 nqpe += Q;
                 const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
-                const float *ph = s_phi + (size_t)c * qmax * NPP;
+                const float *phc = s_phi + (size_t)c * qmax * NPP;
 #pragma unroll
                 for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.f;
                 for (int q = 0; q < Q; ++q) {
-                    const float4 A = g4[2 * q];       // o = x_q - c_e, jw / 4 pi
-                    const float4 B = g4[2 * q + 1];   // n, |o|^2
-                    const float dx = Dfx + A.x, dy = Dfy + A.y, dz = Dfz + A.z;   // x_q - t
-                    const float r2 = dx * dx + dy * dy + dz * dz;
-                    const float rinv = rsqrtf(r2);
-                    const float rr = r2 * rinv;
-                    // r - r0 = (2 D.o + |o|^2) / (r + r0), free of cancellation
-                    const float num = __fmaf_rn(2.0f, Dfx * A.x + Dfy * A.y + Dfz * A.z, B.w);
-                    const float dr = __fdividef(num, rr + r0h);
-                    float sn, cs;
-                    dev::sincos_f32(__fmaf_rn(kf, dr, th0), &sn, &cs);
-                    if (CPLX_K) {
-                        const float damp = __expf(-kimf * rr);
-                        sn *= damp;
-                        cs *= damp;
-                    }
-                    const float dn = B.x * dx + B.y * dy + B.z * dz;
-                    const float wg = rinv * A.w;                      // jw / (4 pi r)
-                    const float Gr = cs * wg, Gi = sn * wg;
-                    const float tq = dn * (rinv * rinv) * wg;         // (x-t).n jw / (4 pi r^3)
-                    ce += tq;
-                    const float ar = CPLX_K ? (-1.0f - kimf * rr) : -1.0f;
-                    const float ai = kf * rr;
-                    const float Fr = (cs * ar - sn * ai) * tq;
-                    const float Fi = (cs * ai + sn * ar) * tq;
+                    const mixed::QpeValues v = mixed::qpe<CPLX_K>(g4[2 * q], g4[2 * q + 1], P, ph, kf, kimf);
+                    ce += v.tq;
                     float p[NPP];
-                    *reinterpret_cast<float4 *>(p) = *reinterpret_cast<const float4 *>(ph + q * NPP);
+                    *reinterpret_cast<float4 *>(p) = *reinterpret_cast<const float4 *>(phc + q * NPP);
                     if (NPP == 8)
-                        *reinterpret_cast<float4 *>(p + 4) = *reinterpret_cast<const float4 *>(ph + q * NPP + 4);
+                        *reinterpret_cast<float4 *>(p + 4) = *reinterpret_cast<const float4 *>(phc + q * NPP + 4);
 #pragma unroll
                     for (int a = 0; a < NP; ++a) {
-                        fr[a] = __fmaf_rn(Fr, p[a], fr[a]);
-                        fi[a] = __fmaf_rn(Fi, p[a], fi[a]);
-                        gr[a] = __fmaf_rn(Gr, p[a], gr[a]);
-                        gi[a] = __fmaf_rn(Gi, p[a], gi[a]);
+                        fr[a] = __fmaf_rn(v.Fr, p[a], fr[a]);
+                        fi[a] = __fmaf_rn(v.Fi, p[a], fi[a]);
+                        gr[a] = __fmaf_rn(v.Gr, p[a], gr[a]);
+                        gi[a] = __fmaf_rn(v.Gi, p[a], gi[a]);
                     }
                 }
             }
-            // C row sum in double-float (C = -sum tq)
-            {
-                const df t = dev::two_sum(cacc.hi, -ce);
-                cacc = dev::fast_two_sum(t.hi, __fadd_rn(t.lo, cacc.lo));
-            }
+            mixed::df_accum(cacc, -ce);   // C = -sum tq
             // F, G: vector FP32 reductions (fire-and-forget, no return value)
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
 #pragma unroll
@@ -447,8 +366,8 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     if (G32) BIE_CUDA(cudaMemsetAsync(G32, 0, mat32, c.stream));
     if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;
 
-    // deferred-pair list: M x 32 entries + counter + near C (M doubles)
-    const unsigned int dcap = (unsigned int)std::min<int64_t>(a.M * 32 + 4096, (int64_t)1 << 30);
+    // deferred-pair list: M x 64 entries + counter + near C (M doubles)
+    const unsigned int dcap = (unsigned int)std::min<int64_t>(a.M * 64 + 4096, (int64_t)1 << 30);
     const size_t dbytes = (size_t)dcap * sizeof(int2);
     char *dbuf = static_cast<char *>(c.scratch(kScratchDefer, dbytes + 256 + (size_t)a.M * 8));
     int2 *defer = reinterpret_cast<int2 *>(dbuf);

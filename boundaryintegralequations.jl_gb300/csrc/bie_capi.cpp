@@ -53,6 +53,18 @@ void check_assemble_args(bie::Ctx &c, double kr, double ki, int64_t M, int flags
         bie::fail(BIE_ERR_INVALID, "M x N output too large");
 }
 
+void check_matvec_args(bie::Ctx &c, double kr, double ki, int64_t M, int precision, const void *x,
+                       const void *v, const void *yF, const void *yG) {
+    (void)c;
+    if (!std::isfinite(kr) || !std::isfinite(ki)) bie::fail(BIE_ERR_INVALID, "k must be finite");
+    if (M <= 0) bie::fail(BIE_ERR_INVALID, "number of targets must be positive");
+    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED)
+        bie::fail(BIE_ERR_INVALID, "unknown precision");
+    if (!x && !v) bie::fail(BIE_ERR_INVALID, "neither x nor v given");
+    if (x && !yF) bie::fail(BIE_ERR_INVALID, "x given without yF");
+    if (v && !yG) bie::fail(BIE_ERR_INVALID, "v given without yG");
+}
+
 void run_assemble(bie::Ctx &c, const bie::AssembleArgs &a, int precision) {
     if (precision == BIE_PREC_MIXED) bie::launch_assemble_mixed(c, a);
     else bie::launch_assemble_fp64(c, a);
@@ -182,6 +194,95 @@ int bie_assemble(bie_ctx *ctx, double k_re, double k_im, const double *targets, 
         if (flags & BIE_C)
             BIE_CUDA(cudaMemcpyAsync(C, a.C, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
         BIE_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int bie_matvec(bie_ctx *ctx, double k_re, double k_im, const double *targets, int64_t n_targets,
+               const double *x, const double *v, double *yF, double *yG, int precision) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        const int64_t M = targets ? n_targets : c.n_sources;
+        check_matvec_args(c, k_re, k_im, M, precision, x, v, yF, yG);
+        BIE_CUDA(cudaSetDevice(c.device));
+        const int64_t N = c.n_sources;
+        // device staging: targets | x | v | yF | yG  (solver workspace slot is not used here)
+        const size_t tb = targets ? (size_t)M * 24 : 0;
+        char *buf = static_cast<char *>(c.scratch(bie::kScratchTargets, tb + 2 * (size_t)N * 16 +
+                                                                               2 * (size_t)M * 16 + 64));
+        double *dt = targets ? reinterpret_cast<double *>(buf) : c.d_sources;
+        double *dx = reinterpret_cast<double *>(buf + ((tb + 15) & ~size_t(15)));
+        double *dv = dx + 2 * N;
+        double *dyF = dv + 2 * N;
+        double *dyG = dyF + 2 * M;
+        if (targets) {
+            for (int64_t i = 0; i < 3 * M; ++i)
+                if (!std::isfinite(targets[i])) bie::fail(BIE_ERR_INVALID, "non-finite target");
+            BIE_CUDA(cudaMemcpyAsync(dt, targets, tb, cudaMemcpyHostToDevice, c.stream));
+        }
+        if (x) BIE_CUDA(cudaMemcpyAsync(dx, x, (size_t)N * 16, cudaMemcpyHostToDevice, c.stream));
+        if (v) BIE_CUDA(cudaMemcpyAsync(dv, v, (size_t)N * 16, cudaMemcpyHostToDevice, c.stream));
+        bie::MatvecArgs a{k_re, k_im, dt, M, x ? dx : nullptr, v ? dv : nullptr, dyF, dyG, precision};
+        bie::launch_matvec(c, a);
+        if (x) BIE_CUDA(cudaMemcpyAsync(yF, dyF, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
+        if (v) BIE_CUDA(cudaMemcpyAsync(yG, dyG, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int bie_matvec_device(bie_ctx *ctx, double k_re, double k_im, const double *d_targets,
+                      int64_t n_targets, const double *d_x, const double *d_v, double *d_yF,
+                      double *d_yG, int precision) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        const int64_t M = d_targets ? n_targets : c.n_sources;
+        check_matvec_args(c, k_re, k_im, M, precision, d_x, d_v, d_yF, d_yG);
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie::MatvecArgs a{k_re, k_im, d_targets ? d_targets : c.d_sources, M, d_x, d_v, d_yF, d_yG,
+                          precision};
+        bie::launch_matvec(c, a);
+    });
+}
+
+int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b, double *d_x,
+                     const bie_gmres_opts *opts, bie_gmres_info *info) {
+    int converged = 1;
+    const int st = guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!op || !d_b || !d_x) bie::fail(BIE_ERR_INVALID, "op, b and x must not be NULL");
+        if (op->kind != BIE_OP_DENSE && op->kind != BIE_OP_MATRIX_FREE)
+            bie::fail(BIE_ERR_INVALID, "unknown operator kind");
+        if (op->kind == BIE_OP_DENSE && !op->A) bie::fail(BIE_ERR_INVALID, "dense operator without A");
+        if (!std::isfinite(op->k_re) || !std::isfinite(op->k_im) || !std::isfinite(op->scale_re) ||
+            !std::isfinite(op->scale_im))
+            bie::fail(BIE_ERR_INVALID, "k and scale must be finite");
+        bie_gmres_opts o{};
+        if (opts) o = *opts;
+        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
+            bie::fail(BIE_ERR_INVALID, "unknown precision");
+        if (!(o.reltol >= 0) || !(o.abstol >= 0)) bie::fail(BIE_ERR_INVALID, "tolerances must be >= 0");
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie_gmres_info inf{};
+        bie::run_gmres(c, *op, d_b, d_x, o, inf);
+        if (info) *info = inf;
+        converged = inf.converged;
+    });
+    if (st == BIE_OK && !converged) {
+        g_last_error = "GMRES reached maxiter before the tolerance";
+        return BIE_ERR_NOT_CONVERGED;
+    }
+    return st;
+}
+
+int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!d_in || !d_out || n < 0) bie::fail(BIE_ERR_INVALID, "bad arguments");
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        if (n > 0) bie::round_to_c64(c, d_in, d_out, n);
     });
 }
 

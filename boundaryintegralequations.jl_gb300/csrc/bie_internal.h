@@ -81,7 +81,11 @@ enum ScratchSlot {
     kScratchF32 = 5,       // complex64 F accumulator (mixed precision)
     kScratchG32 = 6,       // complex64 G accumulator (mixed precision)
     kScratchDefer = 7,     // deferred (target, element) pairs + counter + near C
-    kScratchCount = 8
+    kScratchMatvecXi = 8,  // interpolated densities of the matrix-free products
+    kScratchMatvecPart = 9,// per-slice partial products
+    kScratchSolver = 10,   // GMRES workspace
+    kScratchSolverPart = 11,  // GMRES reduction partials and small coefficient vectors
+    kScratchCount = 12
 };
 
 // Mixed-precision element record (32-bit words, same element order as the FP64
@@ -133,8 +137,8 @@ struct Ctx {
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)
 
     // grow-only device scratch, indexed by the kScratch* slots below
-    void *d_scratch[8] = {};
-    size_t scratch_bytes[8] = {};
+    void *d_scratch[kScratchCount] = {};
+    size_t scratch_bytes[kScratchCount] = {};
     void *scratch(int slot, size_t bytes);
 
     // launch statistics (bie_ctx_stats)
@@ -169,6 +173,23 @@ void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
 void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
                      double *C);
+
+// Matrix-free products yF = F x, yG = G v (bie_matvec.cu); all pointers device
+struct MatvecArgs {
+    double k_re, k_im;
+    const double *targets;   // 3 x M AoS
+    int64_t M;
+    const double *x;         // N complex, input of F (null: skip F)
+    const double *v;         // N complex, input of G (null: skip G)
+    double *yF, *yG;         // M complex outputs
+    int precision;
+};
+void launch_matvec(Ctx &c, const MatvecArgs &a);
+
+// GMRES (bie_solver.cu); b, x device, N = n_sources
+void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
+               bie_gmres_info &info);
+void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
 
 // Mixed-precision assembly (bie_assemble_mixed.cu)
 // host: builds d_mrecords / d_mphi from the FP64 records (E x lay.stride) and uploads them

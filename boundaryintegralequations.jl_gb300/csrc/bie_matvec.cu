@@ -1,0 +1,515 @@
+// K3: matrix-free operator application  yF = F x,  yG = G v  (F, G as assembled
+// by assemble_parallel!, src/3d/assembly_collocation.jl:270-479, never stored).
+//
+// This is the GPU counterpart of the LinearMaps operators fed to gmres
+// (FMMFOperator / FMMGOperator._unsafe_mul!, src/3d/fast_multipole_method.jl:
+// 238-247, 392-404): each product recomputes the kernel values on the fly, so
+// an N = 40k operator needs O(N) memory instead of a 26 GB matrix.
+//
+// Mixed precision (BIE_PREC_MIXED):
+//   1. interp: xi[e, r, q] = sum_a Phi_r[q][a] x[node_a(e)] for every element,
+//      rule and quadrature point (complex64), likewise for v.
+//   2. one thread per target row (x element slices for occupancy) evaluates the
+//      regular pairs with the shared mixed-precision pair code and accumulates
+//      yF += F_q xiF_q, yG += G_q xiG_q: FP32 per element, double-float across
+//      elements (compensated), written once per (row, slice).
+//   3. near pairs and nearest-node near-ties are integrated in FP64 by a
+//      correction kernel (same rule as the assembly) and added atomically.
+//   4. y = sum over slices + correction.
+// FP64 (BIE_PREC_FP64): the FP64 element integrals of the assembly kernel,
+// dotted with x and v per element, accumulated in FP64.
+#include "bie_internal.h"
+#include "bie_device.cuh"
+#include "bie_mixed.cuh"
+
+#include <algorithm>
+
+namespace bie {
+
+namespace {
+
+using dev::df;
+using dev::RuleInfo;
+constexpr int kThreads = 128;
+
+// xi[p][slot] for slot in [0, QT): rule r covers [xoff[r], xoff[r] + Q_r)
+__global__ void interp_kernel(const double *__restrict__ rec64, int stride64, int nidx_off,
+                              const double *__restrict__ phi, int qmax, int NP, int R, RuleInfo ri,
+                              int QT, int QTp, int64_t E, const double2 *__restrict__ x,
+                              const double2 *__restrict__ v, float2 *__restrict__ xiF,
+                              float2 *__restrict__ xiG) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= E * QT) return;
+    const int64_t p = j / QT;
+    int slot = (int)(j - p * QT);
+    int r = 0;
+    while (r + 1 < R && slot >= ri.Q[r]) {
+        slot -= ri.Q[r];
+        ++r;
+    }
+    const int q = slot;
+    const int32_t *nid = reinterpret_cast<const int32_t *>(rec64 + (size_t)p * stride64 + nidx_off);
+    const double *ph = phi + ((size_t)r * qmax + q) * NP;
+    double fr = 0, fi = 0, gr = 0, gi = 0;
+    for (int a = 0; a < NP; ++a) {
+        const double w = ph[a];
+        if (x) {
+            const double2 xa = x[nid[a]];
+            fr += w * xa.x;
+            fi += w * xa.y;
+        }
+        if (v) {
+            const double2 va = v[nid[a]];
+            gr += w * va.x;
+            gi += w * va.y;
+        }
+    }
+    const int64_t o = p * QTp + (j - p * QT);
+    if (xiF) xiF[o] = make_float2((float)fr, (float)fi);
+    if (xiG) xiG[o] = make_float2((float)gr, (float)gi);
+}
+
+struct Fp64Rec {
+    const double *rec;
+    int stride;
+    int nidx_off;
+    const double *phi;   // global, R x qmax x NP
+    int qmax;
+    RuleInfo ri;
+};
+
+// FP64 element integral of one pair dotted with x and v (deferred-list overflow)
+template <int NP, bool CPLX>
+__device__ __noinline__ void pair_fp64_dot(const Fp64Rec v, int64_t p, double tx, double ty,
+                                           double tz, double kre, double kim,
+                                           const double2 *x, const double2 *vin, double2 *yf,
+                                           double2 *yg) {
+    const double *r = v.rec + (size_t)p * v.stride;
+    const int c = dev::nearest_node<NP>(r, tx, ty, tz);
+    double fr[NP], fi[NP], gr[NP], gi[NP];
+    dev::element_fp64<NP, CPLX>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP, tx,
+                                ty, tz, kre, kim, fr, fi, gr, gi);
+    const int32_t *nid = reinterpret_cast<const int32_t *>(r + v.nidx_off);
+    double a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+    for (int a = 0; a < NP; ++a) {
+        if (x) {
+            const double2 xa = x[nid[a]];
+            a0 += fr[a] * xa.x - fi[a] * xa.y;
+            a1 += fr[a] * xa.y + fi[a] * xa.x;
+        }
+        if (vin) {
+            const double2 va = vin[nid[a]];
+            b0 += gr[a] * va.x - gi[a] * va.y;
+            b1 += gr[a] * va.y + gi[a] * va.x;
+        }
+    }
+    *yf = make_double2(a0, a1);
+    *yg = make_double2(b0, b1);
+}
+
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(kThreads, 4)
+matvec_mixed_kernel(const float *__restrict__ rec, int stride, int64_t E, int S, RuleInfo ri,
+                    RuleInfo rxi, int QTp, const float2 *__restrict__ xiF,
+                    const float2 *__restrict__ xiG, const double *__restrict__ tgt, int64_t M,
+                    double kre, double kim, double2 *__restrict__ yFpart,
+                    double2 *__restrict__ yGpart, int chunk, int2 *__restrict__ defer,
+                    unsigned int *__restrict__ defer_count, unsigned int defer_cap,
+                    Fp64Rec v64, const double2 *__restrict__ x64, const double2 *__restrict__ v64in,
+                    unsigned long long *__restrict__ qpe_count) {
+    extern __shared__ __align__(16) float smemf[];
+    float *s_rec = smemf;                                               // chunk * stride
+    float2 *s_xiF = reinterpret_cast<float2 *>(s_rec + (size_t)chunk * stride);
+    float2 *s_xiG = s_xiF + (xiF ? (size_t)chunk * QTp : 0);
+
+    const int s = blockIdx.y;
+    const int64_t e0 = (int64_t)s * E / S;
+    const int64_t e1 = (int64_t)(s + 1) * E / S;
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = i < M;
+    const bool doF = xiF != nullptr, doG = xiG != nullptr;
+
+    double tx = 0, ty = 0, tz = 0;
+    if (active) {
+        tx = tgt[3 * i + 0];
+        ty = tgt[3 * i + 1];
+        tz = tgt[3 * i + 2];
+    }
+    const mixed::Target T{dev::df_from_double(tx), dev::df_from_double(ty), dev::df_from_double(tz)};
+    const df K = dev::df_from_double(kre);
+    const float kf = K.hi;
+    const float kimf = (float)kim;
+
+    df yFr = {0.f, 0.f}, yFi = {0.f, 0.f}, yGr = {0.f, 0.f}, yGi = {0.f, 0.f};
+    unsigned long long nqpe = 0;
+    for (int64_t cb = e0; cb < e1; cb += chunk) {
+        const int n = (int)min((int64_t)chunk, e1 - cb);
+        __syncthreads();
+        {
+            const float4 *src = reinterpret_cast<const float4 *>(rec + cb * stride);
+            float4 *dst = reinterpret_cast<float4 *>(s_rec);
+            const int n4 = n * stride / 4;
+            for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
+            const int nx = n * QTp;
+            if (doF)
+                for (int t = threadIdx.x; t < nx; t += kThreads) s_xiF[t] = xiF[cb * QTp + t];
+            if (doG)
+                for (int t = threadIdx.x; t < nx; t += kThreads) s_xiG[t] = xiG[cb * QTp + t];
+        }
+        __syncthreads();
+        if (!active) continue;
+
+        for (int el = 0; el < n; ++el) {
+            const float *r = s_rec + (size_t)el * stride;
+            const mixed::PairSetup P = mixed::pair_setup<NP>(r, T);
+            if (P.deferred) {
+                const unsigned int slot = atomicAdd(defer_count, 1u);
+                if (slot < defer_cap) {
+                    defer[slot] = make_int2((int)i, (int)(cb + el));
+                } else {   // list full: integrate this pair in FP64 in place
+                    double2 pf, pg;
+                    pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in, &pf, &pg);
+                    if (doF) {
+                        mixed::df_accum(yFr, (float)pf.x);
+                        mixed::df_accum(yFi, (float)pf.y);
+                    }
+                    if (doG) {
+                        mixed::df_accum(yGr, (float)pg.x);
+                        mixed::df_accum(yGi, (float)pg.y);
+                    }
+                }
+                continue;
+            }
+            const mixed::Phase ph = mixed::pair_phase(P, K);
+            const int c = P.c;
+            const int Q = ri.Q[c];
+            nqpe += Q;
+            const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
+            const float2 *xf = s_xiF + (size_t)el * QTp + rxi.off[c];
+            const float2 *xg = s_xiG + (size_t)el * QTp + rxi.off[c];
+            float afr = 0.f, afi = 0.f, agr = 0.f, agi = 0.f;
+            for (int q = 0; q < Q; ++q) {
+                const mixed::QpeValues w = mixed::qpe<CPLX_K>(g4[2 * q], g4[2 * q + 1], P, ph, kf, kimf);
+                if (doF) {
+                    const float2 a = xf[q];
+                    afr = __fmaf_rn(w.Fr, a.x, __fmaf_rn(-w.Fi, a.y, afr));
+                    afi = __fmaf_rn(w.Fr, a.y, __fmaf_rn(w.Fi, a.x, afi));
+                }
+                if (doG) {
+                    const float2 a = xg[q];
+                    agr = __fmaf_rn(w.Gr, a.x, __fmaf_rn(-w.Gi, a.y, agr));
+                    agi = __fmaf_rn(w.Gr, a.y, __fmaf_rn(w.Gi, a.x, agi));
+                }
+            }
+            if (doF) {
+                mixed::df_accum(yFr, afr);
+                mixed::df_accum(yFi, afi);
+            }
+            if (doG) {
+                mixed::df_accum(yGr, agr);
+                mixed::df_accum(yGi, agi);
+            }
+        }
+    }
+    if (active) {
+        if (doF) yFpart[(int64_t)s * M + i] = make_double2(dev::f2d(yFr.hi) + dev::f2d(yFr.lo),
+                                                           dev::f2d(yFi.hi) + dev::f2d(yFi.lo));
+        if (doG) yGpart[(int64_t)s * M + i] = make_double2(dev::f2d(yGr.hi) + dev::f2d(yGr.lo),
+                                                           dev::f2d(yGi.hi) + dev::f2d(yGi.lo));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+// FP64 matrix-free product: per (row, element) the FP64 element integrals of
+// the assembly, dotted with x / v.
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(kThreads)
+matvec_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
+                   const double *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
+                   const double2 *__restrict__ x, const double2 *__restrict__ v,
+                   const double *__restrict__ tgt, int64_t M, double kre, double kim,
+                   double2 *__restrict__ yFpart, double2 *__restrict__ yGpart, int chunk,
+                   unsigned long long *__restrict__ qpe_count) {
+    extern __shared__ __align__(16) double smem[];
+    double *s_phi = smem;
+    double *s_rec = smem + ((nphi + 1) & ~1);
+    const int s = blockIdx.y;
+    const int64_t e0 = (int64_t)s * E / S;
+    const int64_t e1 = (int64_t)(s + 1) * E / S;
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = i < M;
+    double tx = 0, ty = 0, tz = 0;
+    if (active) {
+        tx = tgt[3 * i + 0];
+        ty = tgt[3 * i + 1];
+        tz = tgt[3 * i + 2];
+    }
+    for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+    double yfr = 0, yfi = 0, ygr = 0, ygi = 0;
+    unsigned long long nqpe = 0;
+    for (int64_t cb = e0; cb < e1; cb += chunk) {
+        const int n = (int)min((int64_t)chunk, e1 - cb);
+        __syncthreads();
+        {
+            const double2 *src = reinterpret_cast<const double2 *>(rec + cb * stride);
+            double2 *dst = reinterpret_cast<double2 *>(s_rec);
+            const int n2 = n * stride / 2;
+            for (int t = threadIdx.x; t < n2; t += kThreads) dst[t] = src[t];
+        }
+        __syncthreads();
+        if (!active) continue;
+        for (int el = 0; el < n; ++el) {
+            const double *r = s_rec + (size_t)el * stride;
+            const int c = dev::nearest_node<NP>(r, tx, ty, tz);
+            nqpe += ri.Q[c];
+            double fr[NP], fi[NP], gr[NP], gi[NP];
+            dev::element_fp64<NP, CPLX_K>(r + ri.off[c], ri.Q[c], s_phi + (size_t)c * qmax * NP, tx,
+                                          ty, tz, kre, kim, fr, fi, gr, gi);
+            const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                if (x) {
+                    const double2 xa = x[nid[a]];
+                    yfr += fr[a] * xa.x - fi[a] * xa.y;
+                    yfi += fr[a] * xa.y + fi[a] * xa.x;
+                }
+                if (v) {
+                    const double2 va = v[nid[a]];
+                    ygr += gr[a] * va.x - gi[a] * va.y;
+                    ygi += gr[a] * va.y + gi[a] * va.x;
+                }
+            }
+        }
+    }
+    if (active) {
+        if (x) yFpart[(int64_t)s * M + i] = make_double2(yfr, yfi);
+        if (v) yGpart[(int64_t)s * M + i] = make_double2(ygr, ygi);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+// FP64 correction for the deferred pairs of the mixed product.
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(128)
+matvec_correct_kernel(const int2 *__restrict__ defer, const unsigned int *__restrict__ defer_count,
+                      unsigned int defer_cap, const double *__restrict__ rec, int stride,
+                      int nidx_off, const double *__restrict__ phi, int qmax, RuleInfo ri,
+                      const double2 *__restrict__ x, const double2 *__restrict__ v,
+                      const double *__restrict__ tgt, double kre, double kim,
+                      double2 *__restrict__ yFn, double2 *__restrict__ yGn,
+                      unsigned long long *__restrict__ qpe_count) {
+    const unsigned int n = min(*defer_count, defer_cap);
+    unsigned long long nqpe = 0;
+    for (unsigned int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const int2 pr = defer[j];
+        const int64_t i = pr.x;
+        const double *r = rec + (size_t)pr.y * stride;
+        const double tx = tgt[3 * i], ty = tgt[3 * i + 1], tz = tgt[3 * i + 2];
+        const int c = dev::nearest_node<NP>(r, tx, ty, tz);
+        nqpe += ri.Q[c];
+        double fr[NP], fi[NP], gr[NP], gi[NP];
+        dev::element_fp64<NP, CPLX_K>(r + ri.off[c], ri.Q[c], phi + (size_t)c * qmax * NP, tx, ty,
+                                      tz, kre, kim, fr, fi, gr, gi);
+        const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
+        double yfr = 0, yfi = 0, ygr = 0, ygi = 0;
+#pragma unroll
+        for (int a = 0; a < NP; ++a) {
+            if (x) {
+                const double2 xa = x[nid[a]];
+                yfr += fr[a] * xa.x - fi[a] * xa.y;
+                yfi += fr[a] * xa.y + fi[a] * xa.x;
+            }
+            if (v) {
+                const double2 va = v[nid[a]];
+                ygr += gr[a] * va.x - gi[a] * va.y;
+                ygi += gr[a] * va.y + gi[a] * va.x;
+            }
+        }
+        if (x) {
+            atomicAdd(&yFn[i].x, yfr);
+            atomicAdd(&yFn[i].y, yfi);
+        }
+        if (v) {
+            atomicAdd(&yGn[i].x, ygr);
+            atomicAdd(&yGn[i].y, ygi);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+// y = sum_s part[s] (+ extra)
+__global__ void reduce_y_kernel(const double2 *__restrict__ part, int S,
+                                const double2 *__restrict__ extra, int64_t M,
+                                double2 *__restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M) return;
+    double re = 0, im = 0;
+    for (int s = 0; s < S; ++s) {
+        const double2 p = part[(int64_t)s * M + i];
+        re += p.x;
+        im += p.y;
+    }
+    if (extra) {
+        re += extra[i].x;
+        im += extra[i].y;
+    }
+    y[i] = make_double2(re, im);
+}
+
+template <int NP, bool CPLX>
+void run_mixed(Ctx &c, const MatvecArgs &a) {
+    const RecordLayout &L = c.lay;
+    const MixedLayout &X = c.mlay;
+    RuleInfo ri{}, ri64{}, rxi{};
+    int QT = 0;
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = ri64.Q[r] = rxi.Q[r] = L.Q[r];
+        ri.off[r] = X.rule_off[r];
+        ri64.off[r] = L.rule_off[r];
+        rxi.off[r] = QT;
+        QT += L.Q[r];
+    }
+    const int QTp = (QT + 1) & ~1;
+    const int64_t E = c.n_elements, M = a.M;
+    const bool doF = a.x != nullptr, doG = a.v != nullptr;
+
+    // scratch: xiF, xiG | yFpart, yGpart | defer list, counter, yFn, yGn
+    const int level = choose_slice_level(c, M, kThreads);
+    const int S = 1 << level;
+    const size_t xi_bytes = (size_t)E * QTp * sizeof(float2);
+    char *xb = static_cast<char *>(c.scratch(kScratchMatvecXi, 2 * xi_bytes));
+    float2 *xiF = doF ? reinterpret_cast<float2 *>(xb) : nullptr;
+    float2 *xiG = doG ? reinterpret_cast<float2 *>(xb + xi_bytes) : nullptr;
+    const size_t part_bytes = (size_t)S * M * sizeof(double2);
+    char *pb = static_cast<char *>(c.scratch(kScratchMatvecPart, 2 * part_bytes));
+    double2 *yFpart = reinterpret_cast<double2 *>(pb);
+    double2 *yGpart = reinterpret_cast<double2 *>(pb + part_bytes);
+    const unsigned int dcap = (unsigned int)std::min<int64_t>(M * 64 + 4096, (int64_t)1 << 30);
+    const size_t dbytes = (size_t)dcap * sizeof(int2);
+    char *db = static_cast<char *>(c.scratch(kScratchDefer, dbytes + 256 + 2 * (size_t)M * 16));
+    int2 *defer = reinterpret_cast<int2 *>(db);
+    unsigned int *dcount = reinterpret_cast<unsigned int *>(db + dbytes);
+    double2 *yFn = reinterpret_cast<double2 *>(db + dbytes + 256);
+    double2 *yGn = yFn + M;
+    BIE_CUDA(cudaMemsetAsync(db + dbytes, 0, 256 + 2 * (size_t)M * 16, c.stream));
+
+    const int64_t nslots = E * QT;
+    interp_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, c.stream>>>(
+        c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, L.NP, L.R, ri64, QT, QTp, E,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), xiF, xiG);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+
+    const size_t rec_bytes = (size_t)X.stride * sizeof(float);
+    const size_t per_el = rec_bytes + (size_t)(doF + doG) * QTp * sizeof(float2);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / per_el));
+    const size_t smem = (size_t)chunk * per_el;
+    auto kern = matvec_mixed_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((M + kThreads - 1) / kThreads), (unsigned)S);
+    cudaEvent_t t0 = c.timer_begin();
+    const Fp64Rec v64{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
+    kern<<<grid, kThreads, smem, c.stream>>>(c.d_mrecords, X.stride, E, S, ri, rxi, QTp, xiF, xiG,
+                                             a.targets, M, a.k_re, a.k_im, yFpart, yGpart, chunk,
+                                             defer, dcount, dcap, v64,
+                                             reinterpret_cast<const double2 *>(a.x),
+                                             reinterpret_cast<const double2 *>(a.v), c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    c.timer_end(t0);
+    ++c.kernel_launches;
+
+    matvec_correct_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+        defer, dcount, dcap, c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), a.targets,
+        a.k_re, a.k_im, yFn, yGn, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+    if (doF) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yFpart, S, yFn, M, reinterpret_cast<double2 *>(a.yF));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+    if (doG) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yGpart, S, yGn, M, reinterpret_cast<double2 *>(a.yG));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+}
+
+template <int NP, bool CPLX>
+void run_fp64(Ctx &c, const MatvecArgs &a) {
+    const RecordLayout &L = c.lay;
+    RuleInfo ri{};
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = L.Q[r];
+        ri.off[r] = L.rule_off[r];
+    }
+    const int64_t M = a.M;
+    const int level = choose_slice_level(c, M, kThreads);
+    const int S = 1 << level;
+    const size_t part_bytes = (size_t)S * M * sizeof(double2);
+    char *pb = static_cast<char *>(c.scratch(kScratchMatvecPart, 2 * part_bytes));
+    double2 *yFpart = reinterpret_cast<double2 *>(pb);
+    double2 *yGpart = reinterpret_cast<double2 *>(pb + part_bytes);
+    const size_t rec_bytes = (size_t)L.stride * sizeof(double);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (40u << 10) / rec_bytes));
+    const int nphi = L.R * L.qmax * L.NP;
+    const size_t smem = (size_t)((nphi + 1) & ~1) * sizeof(double) + (size_t)chunk * rec_bytes;
+    auto kern = matvec_fp64_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((M + kThreads - 1) / kThreads), (unsigned)S);
+    cudaEvent_t t0 = c.timer_begin();
+    kern<<<grid, kThreads, smem, c.stream>>>(
+        c.d_records, L.stride, L.nidx_off, c.n_elements, S, c.d_phi, nphi, L.qmax, ri,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), a.targets, M,
+        a.k_re, a.k_im, yFpart, yGpart, chunk, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    c.timer_end(t0);
+    ++c.kernel_launches;
+    if (a.x) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yFpart, S, nullptr, M, reinterpret_cast<double2 *>(a.yF));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+    if (a.v) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yGpart, S, nullptr, M, reinterpret_cast<double2 *>(a.yG));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+}
+
+}  // namespace
+
+void launch_matvec(Ctx &c, const MatvecArgs &a) {
+    if (!a.x && !a.v) return;
+    const bool cplx = a.k_im != 0.0;
+    if (a.precision == BIE_PREC_MIXED) {
+        if (c.lay.NP == 3) {
+            if (cplx) run_mixed<3, true>(c, a);
+            else run_mixed<3, false>(c, a);
+        } else {
+            if (cplx) run_mixed<6, true>(c, a);
+            else run_mixed<6, false>(c, a);
+        }
+    } else {
+        if (c.lay.NP == 3) {
+            if (cplx) run_fp64<3, true>(c, a);
+            else run_fp64<3, false>(c, a);
+        } else {
+            if (cplx) run_fp64<6, true>(c, a);
+            else run_fp64<6, false>(c, a);
+        }
+    }
+}
+
+}  // namespace bie

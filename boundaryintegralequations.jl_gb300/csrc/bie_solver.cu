@@ -1,0 +1,463 @@
+// K5: restarted GMRES on the device for  A x = b  with
+//     A x = s (K x) + d .* x,
+// K either a stored dense matrix (complex128 or complex64, column-major, the
+// output of the assembly) or the matrix-free double-layer operator F.
+// This replaces IterativeSolvers.gmres (v0.9) as called by the reference
+// (test/3d/assembly_test.jl:38, examples/3d_pulsating_sphere.jl:44-50):
+// same defaults (restart = min(20, N), reltol = sqrt(eps(Float64)), abstol 0,
+// maxiter = N, x0 = 0) and the same stopping test ||r|| <= max(reltol ||b||,
+// abstol) on the Arnoldi residual estimate.
+//
+// Arnoldi uses classical Gram-Schmidt with one reorthogonalisation pass
+// (CGS2, the same numerical role as IterativeSolvers' default DGKS
+// orthogonalisation); the small Hessenberg least-squares problem is solved on
+// the host with Givens rotations (FP64).  Mixed-precision iterative refinement
+// (opts->refine) runs the inner GMRES on the cheaper operator (complex64 dense
+// copy or mixed matrix-free product) and forms the outer residual b - A x with
+// the FP64 operator.
+#include "bie_internal.h"
+#include "bie_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+namespace bie {
+
+namespace {
+
+using cplx = std::complex<double>;
+constexpr int kT = 256;
+
+// y[i] = s * sum_j A[i + j*lda] x[j] for the column slice of blockIdx.y
+template <typename T2>
+__global__ void __launch_bounds__(kT)
+dense_gemv_kernel(const T2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
+                  double2 *__restrict__ part, int S) {
+    const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
+    const int s = blockIdx.y;
+    const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
+    __shared__ double2 xs[kT];
+    double re = 0, im = 0;
+    for (int64_t jb = j0; jb < j1; jb += kT) {
+        const int nb = (int)min((int64_t)kT, j1 - jb);
+        __syncthreads();
+        if (threadIdx.x < nb) xs[threadIdx.x] = x[jb + threadIdx.x];
+        __syncthreads();
+        if (i < n) {
+            const T2 *col = A + jb * n + i;
+#pragma unroll 4
+            for (int j = 0; j < nb; ++j) {
+                const T2 a = col[(int64_t)j * n];
+                const double ar = (double)a.x, ai = (double)a.y;
+                const double2 xv = xs[j];
+                re += ar * xv.x - ai * xv.y;
+                im += ar * xv.y + ai * xv.x;
+            }
+        }
+    }
+    if (i < n) part[(int64_t)s * n + i] = make_double2(re, im);
+}
+
+// y = s * sum_slices(part) + d .* x   (d may be null)
+__global__ void combine_kernel(const double2 *__restrict__ part, int S, int64_t n, double2 sc,
+                               const double2 *__restrict__ d, const double2 *__restrict__ x,
+                               double2 *__restrict__ y) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double re = 0, im = 0;
+    for (int s = 0; s < S; ++s) {
+        const double2 p = part[(int64_t)s * n + i];
+        re += p.x;
+        im += p.y;
+    }
+    double yr = sc.x * re - sc.y * im, yi = sc.x * im + sc.y * re;
+    if (d) {
+        const double2 dv = d[i], xv = x[i];
+        yr += dv.x * xv.x - dv.y * xv.y;
+        yi += dv.x * xv.y + dv.y * xv.x;
+    }
+    y[i] = make_double2(yr, yi);
+}
+
+// partial[col * nb + block] = sum over the block's rows of conj(V[:, col]) . w
+__global__ void __launch_bounds__(kT)
+multidot_kernel(const double2 *__restrict__ V, int64_t ldv, const double2 *__restrict__ w,
+                int64_t n, double2 *__restrict__ partial) {
+    const int col = blockIdx.y;
+    const double2 *v = V + (int64_t)col * ldv;
+    double re = 0, im = 0;
+    for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+        const double2 a = v[i], b = w[i];
+        re += a.x * b.x + a.y * b.y;
+        im += a.x * b.y - a.y * b.x;
+    }
+    __shared__ double sr[kT], si[kT];
+    sr[threadIdx.x] = re;
+    si[threadIdx.x] = im;
+    __syncthreads();
+    for (int o = kT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            sr[threadIdx.x] += sr[threadIdx.x + o];
+            si[threadIdx.x] += si[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(int64_t)col * gridDim.x + blockIdx.x] = make_double2(sr[0], si[0]);
+}
+
+__global__ void sum_partials_kernel(const double2 *__restrict__ partial, int nb, int ncol,
+                                    double2 *__restrict__ out) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= ncol) return;
+    double re = 0, im = 0;
+    for (int b = 0; b < nb; ++b) {
+        re += partial[(int64_t)col * nb + b].x;
+        im += partial[(int64_t)col * nb + b].y;
+    }
+    out[col] = make_double2(re, im);
+}
+
+// w -= V[:, 0..ncol) h
+__global__ void gs_update_kernel(const double2 *__restrict__ V, int64_t ldv, int ncol,
+                                 const double2 *__restrict__ h, double2 *__restrict__ w, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double re = w[i].x, im = w[i].y;
+    for (int c = 0; c < ncol; ++c) {
+        const double2 v = V[(int64_t)c * ldv + i], hc = h[c];
+        re -= v.x * hc.x - v.y * hc.y;
+        im -= v.x * hc.y + v.y * hc.x;
+    }
+    w[i] = make_double2(re, im);
+}
+
+// y = alpha * x (alpha real)
+__global__ void scale_kernel(const double2 *__restrict__ x, double alpha, double2 *__restrict__ y,
+                             int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = make_double2(alpha * x[i].x, alpha * x[i].y);
+}
+
+// y = a - b
+__global__ void sub_kernel(const double2 *__restrict__ a, const double2 *__restrict__ b,
+                           double2 *__restrict__ y, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = make_double2(a[i].x - b[i].x, a[i].y - b[i].y);
+}
+
+// x += sum_c V[:, c] yc  (yc in constant-size device array)
+__global__ void combo_add_kernel(const double2 *__restrict__ V, int64_t ldv, int ncol,
+                                 const double2 *__restrict__ yc, double2 *__restrict__ x, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double re = x[i].x, im = x[i].y;
+    for (int c = 0; c < ncol; ++c) {
+        const double2 v = V[(int64_t)c * ldv + i], y = yc[c];
+        re += v.x * y.x - v.y * y.y;
+        im += v.x * y.y + v.y * y.x;
+    }
+    x[i] = make_double2(re, im);
+}
+
+__global__ void round_c64_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------
+// Operator application and BLAS-1 helpers bound to a context
+// ---------------------------------------------------------------------------
+struct Solver {
+    Ctx &c;
+    int64_t n;
+    double2 *part = nullptr;      // gemv slices / multidot partials
+    int S = 1;
+    int nbdot = 1;
+    double2 *hdev = nullptr;      // device scratch for dot results (>= restart + 2)
+    std::vector<double2> hhost;
+
+    Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_) {
+        S = 1;
+        const int64_t row_tiles = (n + kT - 1) / kT;
+        while (row_tiles * S < 4LL * c.num_sms && S < 64) S *= 2;
+        nbdot = (int)std::min<int64_t>(std::max<int64_t>(1, (n + kT * 8 - 1) / (kT * 8)), 256);
+        const size_t part_bytes = (size_t)std::max<int64_t>(S * n, (int64_t)(restart + 2) * nbdot) * 16;
+        char *base = static_cast<char *>(c.scratch(kScratchSolverPart, part_bytes + (size_t)(restart + 2) * 16));
+        part = reinterpret_cast<double2 *>(base);
+        hdev = reinterpret_cast<double2 *>(base + part_bytes);
+        hhost.resize(restart + 2);
+    }
+
+    void launched() { ++c.kernel_launches; }
+
+    // y = s (K x) + d .* x
+    void apply(const bie_operator &op, int precision, const double2 *x, double2 *y) {
+        const double2 sc = make_double2(op.scale_re, op.scale_im);
+        const double2 *d = reinterpret_cast<const double2 *>(op.diag);
+        if (op.kind == BIE_OP_DENSE) {
+            dim3 grid(blocks(n, kT), (unsigned)S);
+            cudaEvent_t t0 = c.timer_begin();
+            if (precision == BIE_PREC_MIXED && op.A32)
+                dense_gemv_kernel<float2><<<grid, kT, 0, c.stream>>>(
+                    reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
+            else
+                dense_gemv_kernel<double2><<<grid, kT, 0, c.stream>>>(
+                    reinterpret_cast<const double2 *>(op.A), n, x, part, S);
+            BIE_CUDA(cudaGetLastError());
+            c.timer_end(t0);
+            launched();
+            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(part, S, n, sc, d, x, y);
+            BIE_CUDA(cudaGetLastError());
+            launched();
+        } else {
+            // matrix-free F x into y, then y = s y + d .* x
+            MatvecArgs m{op.k_re, op.k_im, c.d_sources, n, reinterpret_cast<const double *>(x),
+                         nullptr, reinterpret_cast<double *>(y), nullptr, precision};
+            launch_matvec(c, m);
+            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(y, 1, n, sc, d, x, y);
+            BIE_CUDA(cudaGetLastError());
+            launched();
+        }
+    }
+
+    // out[0..ncol) = V[:, 0..ncol)^H w  (copied to host)
+    void multidot(const double2 *V, int64_t ldv, int ncol, const double2 *w, std::vector<cplx> &out) {
+        dim3 grid((unsigned)nbdot, (unsigned)ncol);
+        multidot_kernel<<<grid, kT, 0, c.stream>>>(V, ldv, w, n, part);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+        sum_partials_kernel<<<blocks(ncol, 64), 64, 0, c.stream>>>(part, nbdot, ncol, hdev);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+        BIE_CUDA(cudaMemcpyAsync(hhost.data(), hdev, ncol * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+        out.resize(ncol);
+        for (int k = 0; k < ncol; ++k) out[k] = cplx(hhost[k].x, hhost[k].y);
+    }
+
+    double norm(const double2 *w) {
+        std::vector<cplx> o;
+        multidot(w, n, 1, w, o);
+        return std::sqrt(std::max(o[0].real(), 0.0));
+    }
+
+    void upload_coeffs(const std::vector<cplx> &h) {
+        for (size_t k = 0; k < h.size(); ++k) hhost[k] = make_double2(h[k].real(), h[k].imag());
+        BIE_CUDA(cudaMemcpyAsync(hdev, hhost.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice,
+                                 c.stream));
+    }
+
+    void gs_update(const double2 *V, int64_t ldv, int ncol, double2 *w, const std::vector<cplx> &h) {
+        upload_coeffs(h);
+        gs_update_kernel<<<blocks(n), 256, 0, c.stream>>>(V, ldv, ncol, hdev, w, n);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+    }
+
+    void combo_add(const double2 *V, int64_t ldv, int ncol, const std::vector<cplx> &y, double2 *x) {
+        upload_coeffs(y);
+        combo_add_kernel<<<blocks(n), 256, 0, c.stream>>>(V, ldv, ncol, hdev, x, n);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+    }
+
+    void scale(const double2 *x, double a, double2 *y) {
+        scale_kernel<<<blocks(n), 256, 0, c.stream>>>(x, a, y, n);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+    }
+
+    void sub(const double2 *a, const double2 *b, double2 *y) {
+        sub_kernel<<<blocks(n), 256, 0, c.stream>>>(a, b, y, n);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+    }
+};
+
+// Givens rotation zeroing b in (a, b): [c s; -conj(s) c] (a, b)^T = (r, 0)^T
+inline void givens(cplx a, cplx b, double &cs, cplx &sn, cplx &r) {
+    const double na = std::abs(a), nb = std::abs(b);
+    if (nb == 0.0) {
+        cs = 1.0;
+        sn = 0.0;
+        r = a;
+        return;
+    }
+    if (na == 0.0) {
+        cs = 0.0;
+        sn = std::conj(b) / nb;
+        r = nb;
+        return;
+    }
+    const double nrm = std::hypot(na, nb);
+    const cplx alpha = a / na;
+    cs = na / nrm;
+    sn = alpha * std::conj(b) / nrm;
+    r = alpha * nrm;
+}
+
+// One GMRES solve of A x = b from the initial x (device), operator precision
+// `prec`; returns the number of iterations; `tol` is an absolute tolerance on
+// the residual norm.  V: (restart + 1) x n workspace.
+int gmres_core(Solver &S, const bie_operator &op, int prec, const double2 *b, double2 *x,
+               bool x_zero, double2 *V, double2 *w, int restart, int maxiter, double tol,
+               double *res_out, int *restarts_out, int64_t *matvecs) {
+    const int64_t n = S.n;
+    int it = 0, restarts = 0;
+    double beta = 0.0;
+    std::vector<cplx> H((size_t)(restart + 1) * restart), g(restart + 1), sn(restart), h;
+    std::vector<double> cs(restart);
+    bool first = true;
+    while (true) {
+        // r = b - A x  (r = b for a zero start)
+        if (first && x_zero) {
+            BIE_CUDA(cudaMemcpyAsync(w, b, (size_t)n * 16, cudaMemcpyDeviceToDevice, S.c.stream));
+        } else {
+            S.apply(op, prec, x, w);
+            ++*matvecs;
+            S.sub(b, w, w);
+        }
+        first = false;
+        beta = S.norm(w);
+        if (beta <= tol || it >= maxiter) break;
+        S.scale(w, 1.0 / beta, V);
+        std::fill(g.begin(), g.end(), cplx(0.0));
+        g[0] = beta;
+        int j = 0;
+        double res = beta;
+        for (; j < restart && it < maxiter; ++j) {
+            double2 *vj = V + (int64_t)j * n;
+            double2 *vn = V + (int64_t)(j + 1) * n;
+            S.apply(op, prec, vj, w);
+            ++*matvecs;
+            ++it;
+            // CGS2
+            std::vector<cplx> h1, h2;
+            S.multidot(V, n, j + 1, w, h1);
+            S.gs_update(V, n, j + 1, w, h1);
+            S.multidot(V, n, j + 1, w, h2);
+            S.gs_update(V, n, j + 1, w, h2);
+            for (int k = 0; k <= j; ++k) H[(size_t)j * (restart + 1) + k] = h1[k] + h2[k];
+            const double hn = S.norm(w);
+            H[(size_t)j * (restart + 1) + j + 1] = hn;
+            if (hn > 0) S.scale(w, 1.0 / hn, vn);
+            // apply previous rotations to column j
+            cplx *col = &H[(size_t)j * (restart + 1)];
+            for (int k = 0; k < j; ++k) {
+                const cplx t = cs[k] * col[k] + sn[k] * col[k + 1];
+                col[k + 1] = -std::conj(sn[k]) * col[k] + cs[k] * col[k + 1];
+                col[k] = t;
+            }
+            cplx r;
+            givens(col[j], col[j + 1], cs[j], sn[j], r);
+            col[j] = r;
+            col[j + 1] = 0.0;
+            const cplx gt = cs[j] * g[j] + sn[j] * g[j + 1];
+            g[j + 1] = -std::conj(sn[j]) * g[j] + cs[j] * g[j + 1];
+            g[j] = gt;
+            res = std::abs(g[j + 1]);
+            if (res <= tol || hn == 0.0) {
+                ++j;
+                break;
+            }
+        }
+        // solve the triangular system and update x
+        std::vector<cplx> y(j);
+        for (int k = j - 1; k >= 0; --k) {
+            cplx s = g[k];
+            for (int l = k + 1; l < j; ++l) s -= H[(size_t)l * (restart + 1) + k] * y[l];
+            y[k] = s / H[(size_t)k * (restart + 1) + k];
+        }
+        if (j > 0) S.combo_add(V, n, j, y, x);
+        ++restarts;
+        if (res <= tol && j < restart) {
+            // converged inside the cycle: final true residual below
+        }
+        if (it >= maxiter) {
+            S.apply(op, prec, x, w);
+            ++*matvecs;
+            S.sub(b, w, w);
+            beta = S.norm(w);
+            break;
+        }
+    }
+    *res_out = beta;
+    *restarts_out = restarts;
+    return it;
+}
+
+}  // namespace
+
+void run_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, const bie_gmres_opts &o,
+               bie_gmres_info &info) {
+    const int64_t n = c.n_sources;
+    const int restart = (int)std::max<int64_t>(1, std::min<int64_t>(o.restart > 0 ? o.restart : 20, n));
+    const int maxiter = o.maxiter > 0 ? o.maxiter : (int)std::min<int64_t>(n, INT32_MAX);
+    const double reltol = o.reltol > 0 ? o.reltol : std::sqrt(2.220446049250313e-16);
+    const double abstol = std::max(0.0, o.abstol);
+    const double2 *b = reinterpret_cast<const double2 *>(b_);
+    double2 *x = reinterpret_cast<double2 *>(x_);
+
+    // workspace: V (restart + 1) x n, w, r, dx
+    char *ws = static_cast<char *>(c.scratch(kScratchSolver, (size_t)(restart + 4) * n * 16));
+    double2 *V = reinterpret_cast<double2 *>(ws);
+    double2 *w = V + (int64_t)(restart + 1) * n;
+    double2 *rr = w + n;
+    double2 *dx = rr + n;
+    Solver S(c, n, restart);
+    const double bnorm = S.norm(b);
+    const double tol = std::max(reltol * bnorm, abstol);
+    if (!o.initially_nonzero) BIE_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 16, c.stream));
+    int64_t matvecs = 0;
+    int iters = 0, restarts = 0;
+    double res = 0;
+    int outer = 0;
+    if (!o.refine) {
+        const int prec = o.precision;
+        iters = gmres_core(S, op, prec, b, x, !o.initially_nonzero, V, w, restart, maxiter, tol, &res,
+                           &restarts, &matvecs);
+    } else {
+        // iterative refinement: r = b - A x in FP64; inner solve A_low dx = r
+        const double inner_rel = o.inner_reltol > 0 ? o.inner_reltol : 1e-4;
+        const int max_outer = o.max_refine > 0 ? o.max_refine : 10;
+        bie_operator low = op;
+        for (outer = 0; outer < max_outer; ++outer) {
+            S.apply(op, BIE_PREC_FP64, x, w);
+            ++matvecs;
+            S.sub(b, w, rr);
+            res = S.norm(rr);
+            if (res <= tol || iters >= maxiter) break;
+            BIE_CUDA(cudaMemsetAsync(dx, 0, (size_t)n * 16, c.stream));
+            double ires = 0;
+            int irs = 0;
+            iters += gmres_core(S, low, BIE_PREC_MIXED, rr, dx, true, V, w, restart, maxiter - iters,
+                                std::max(inner_rel * res, tol * 0.5), &ires, &irs, &matvecs);
+            restarts += irs;
+            // x += dx
+            std::vector<cplx> one{cplx(1.0, 0.0)};
+            S.combo_add(dx, n, 1, one, x);
+        }
+    }
+    BIE_CUDA(cudaStreamSynchronize(c.stream));
+    info.iterations = iters;
+    info.restarts = restarts;
+    info.refinements = outer;
+    info.matvecs = matvecs;
+    info.residual_norm = res;
+    info.rhs_norm = bnorm;
+    info.converged = res <= tol ? 1 : 0;
+}
+
+void round_to_c64(Ctx &c, const double *in, float *out, int64_t n) {
+    round_c64_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 64LL * c.num_sms), 256, 0, c.stream>>>(
+        reinterpret_cast<const double2 *>(in), reinterpret_cast<float2 *>(out), n);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+}
+
+}  // namespace bie

@@ -180,6 +180,78 @@ BIE_API int bie_assemble_device(bie_ctx *ctx, double k_re, double k_im,
                         int flags, int precision,
                         double *d_F, double *d_G, double *d_C);
 
+/*
+ * Matrix-free operator application with HOST buffers:
+ *   yF = F x,  yG = G v
+ * with F, G exactly the matrices bie_assemble would return for the same
+ * targets (same rules, same arithmetic class), recomputed on the fly and never
+ * stored.  Either product may be skipped by passing NULL for its input and
+ * output.  targets: 3 x M (NULL = mesh sources; then M is ignored).
+ * Replaces the operator products fed to gmres: FMMFOperator / FMMGOperator
+ * `LinearMaps._unsafe_mul!` (src/3d/fast_multipole_method.jl:238-247, 392-404)
+ * and the field-point products `Fp*p + Gp*v` of examples/3d_pulsating_sphere.jl:60-63.
+ */
+BIE_API int bie_matvec(bie_ctx *ctx, double k_re, double k_im,
+                       const double *targets, int64_t n_targets,
+                       const double *x, const double *v, double *yF, double *yG,
+                       int precision);
+
+/* Same with DEVICE pointers; enqueued on the context stream, asynchronous. */
+BIE_API int bie_matvec_device(bie_ctx *ctx, double k_re, double k_im,
+                              const double *d_targets, int64_t n_targets,
+                              const double *d_x, const double *d_v, double *d_yF, double *d_yG,
+                              int precision);
+
+/* ---- linear systems A x = b,  A x = s (K x) + diag .* x ---------------- */
+#define BIE_OP_DENSE       0  /* K = stored dense N x N matrix (device)       */
+#define BIE_OP_MATRIX_FREE 1  /* K = F of the context at wavenumber k         */
+
+typedef struct bie_operator {
+    int32_t       kind;        /* BIE_OP_DENSE | BIE_OP_MATRIX_FREE                 */
+    const double *A;           /* dense: device N x N complex128, column-major      */
+    const float  *A32;         /* dense: optional complex64 copy for the mixed inner
+                                  iterations (NULL: the complex128 matrix is used)   */
+    double        k_re, k_im;  /* matrix-free: wavenumber                           */
+    double        scale_re, scale_im;   /* s                                         */
+    const double *diag;        /* device N complex, or NULL for zero                */
+} bie_operator;
+
+typedef struct bie_gmres_opts {
+    int32_t restart;           /* <= 0: min(20, N)                 (IterativeSolvers) */
+    int32_t maxiter;           /* <= 0: N                                             */
+    double  reltol;            /* <= 0: sqrt(eps(Float64))                            */
+    double  abstol;            /* >= 0, default 0                                     */
+    int32_t precision;         /* operator arithmetic without refinement (BIE_PREC_*) */
+    int32_t refine;            /* 1: mixed inner GMRES + FP64 residual refinement     */
+    double  inner_reltol;      /* refinement: inner relative tolerance (<= 0: 1e-4)   */
+    int32_t max_refine;        /* refinement: outer steps (<= 0: 10)                  */
+    int32_t initially_nonzero; /* 1: start from the given x instead of zero           */
+} bie_gmres_opts;
+
+typedef struct bie_gmres_info {
+    int32_t iterations;        /* Arnoldi steps (inner steps summed under refinement) */
+    int32_t restarts;
+    int32_t refinements;
+    int32_t converged;         /* ||b - A x|| <= max(reltol ||b||, abstol)            */
+    int64_t matvecs;
+    double  residual_norm;     /* final ||b - A x|| (FP64 operator under refinement)  */
+    double  rhs_norm;
+} bie_gmres_info;
+
+/*
+ * Restarted GMRES on the device (vectors of length N = n_sources, device
+ * pointers).  Replaces IterativeSolvers.gmres as used by the reference
+ * (test/3d/assembly_test.jl:38; examples/3d_pulsating_sphere.jl:44-50) with
+ * its defaults.  Returns BIE_ERR_NOT_CONVERGED (x still written, info filled)
+ * when maxiter is reached before the tolerance.
+ */
+BIE_API int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b,
+                             double *d_x, const bie_gmres_opts *opts, bie_gmres_info *info);
+
+/* out[i] = (complex64) in[i] for n complex entries (device), e.g. to build
+ * bie_operator.A32 from an assembled matrix. */
+BIE_API int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif
