@@ -39,11 +39,16 @@ def _is_torch(a) -> bool:
 class Diagonal:
     """Diagonal matrix (complex vector); the analogue of LinearAlgebra.Diagonal."""
 
+    __array_ufunc__ = None   # make numpy defer `ndarray + Diagonal` to __radd__
+
     def __init__(self, d):
         self.d = d
 
     def __sub__(self, other):
         return _as_affine(other).scaled(-1.0).plus_diag(self.d)
+
+    def __rsub__(self, other):
+        return _as_affine(other).plus_diag(-np.asarray(self.d))
 
     def __add__(self, other):
         return _as_affine(other).plus_diag(self.d)
@@ -53,6 +58,8 @@ class Diagonal:
 
 class UniformScaling:
     """lambda * I"""
+
+    __array_ufunc__ = None
 
     def __init__(self, lam: complex = 1.0):
         self.lam = complex(lam)
@@ -68,6 +75,8 @@ I = UniformScaling(1.0)  # noqa: E741
 
 class _Affine:
     """s * K + diag(d): K a matrix-free F (GPUFOperator) or a dense matrix."""
+
+    __array_ufunc__ = None
 
     def __init__(self, base, scale: complex = 1.0, diag=None):
         self.base = base

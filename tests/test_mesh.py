@@ -68,3 +68,21 @@ def test_comsol_reader(reference_meshes):
         assert m.sources.shape[1] == len(np.unique(m.physics_topology))
     C, T, ents = bm.read_comsol(reference_meshes / "sphere_1m")
     assert C.shape == (3, 1682) and T.shape == (6, 840)
+
+
+def test_operator_algebra_on_dense_matrices():
+    # the reference's compositions, on host matrices (no GPU involved)
+    from biegpu.operators import Diagonal, I, _Affine
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(5, 5)) + 1j * rng.normal(size=(5, 5))
+    d = rng.normal(size=5) + 0j
+    x = rng.normal(size=5) + 1j * rng.normal(size=5)
+    op = A + Diagonal(d)
+    assert isinstance(op, _Affine)
+    assert np.allclose(op @ x, A @ x + d * x)
+    op = Diagonal(d) - A
+    assert np.allclose(op @ x, d * x - A @ x)
+    op = A - Diagonal(d)
+    assert np.allclose(op @ x, A @ x - d * x)
+    op = _Affine(A) + 0.5 * I
+    assert np.allclose(op @ x, A @ x + 0.5 * x)
