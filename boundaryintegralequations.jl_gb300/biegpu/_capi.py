@@ -148,6 +148,7 @@ SIGNATURES = {
     "bie_assemble_device": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
     "bie_matvec": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
     "bie_matvec_device": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
+    "bie_matvec_device_noalloc": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P]),
     "bie_gmres_device": (_I, [_P, C.POINTER(Operator), _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
     "bie_round_c64_device": (_I, [_P, _P, _P, _I64]),
 }

@@ -245,6 +245,21 @@ int bie_matvec_device(bie_ctx *ctx, double k_re, double k_im, const double *d_ta
     });
 }
 
+int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im, const double *d_targets,
+                              int64_t n_targets, const double *d_x, const double *d_v,
+                              double *d_yF, double *d_yG) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        const int64_t M = d_targets ? n_targets : c.n_sources;
+        check_matvec_args(c, k_re, k_im, M, BIE_PREC_MIXED, d_x, d_v, d_yF, d_yG);
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie::MatvecArgs a{k_re, k_im, d_targets ? d_targets : c.d_sources, M, d_x, d_v, d_yF, d_yG,
+                          BIE_PREC_MIXED};
+        bie::launch_matvec_noalloc(c, a);
+    });
+}
+
 int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b, double *d_x,
                      const bie_gmres_opts *opts, bie_gmres_info *info) {
     int converged = 1;

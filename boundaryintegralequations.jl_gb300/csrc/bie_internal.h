@@ -185,6 +185,9 @@ struct MatvecArgs {
     int precision;
 };
 void launch_matvec(Ctx &c, const MatvecArgs &a);
+// Mixed-precision product whose temporaries live in a fixed static device array
+// (no device allocation by the library); rejects meshes that do not fit.
+void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a);
 
 // GMRES (bie_solver.cu); b, x device, N = n_sources
 void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,

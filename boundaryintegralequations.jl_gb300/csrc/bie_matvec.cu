@@ -488,7 +488,147 @@ void run_fp64(Ctx &c, const MatvecArgs &a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the mixed-precision product.
+//
+// Some callers cannot let a library call cudaMalloc: a Julia session whose
+// CUDA.jl memory pool (or a Python process whose PyTorch caching allocator)
+// has already reserved most of the device, real-time loops that must not
+// synchronise the device, or code that runs between the set-up and the
+// capture of a CUDA graph.  For them bie_matvec_device_noalloc keeps every
+// temporary of the product (interpolated densities, per-slice partial sums,
+// the list of pairs integrated in FP64) in one file-scope device array of
+// kNoAllocScratchBytes, which every GPU that loads the library holds until
+// the process exits.
+//
+// The array's host-side name is only a stand-in for the device symbol; its
+// device address is looked up with cudaGetSymbolAddress once per device, with
+// that device current, on the first call of the entry point on that device
+// (so that first call belongs before any stream capture).  All calls share
+// the array: the parts that must start at zero are cleared on every call, and
+// calls whose executions overlap on the GPU (different streams or contexts of
+// the same device) race on it.
+// ---------------------------------------------------------------------------
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;   // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (looked up once).
+char *noalloc_scratch(int device) {
+    if (device < 0 || device >= kMaxDevices) fail(BIE_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[device]) {
+        void *p = nullptr;
+        BIE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[device] = p;
+    }
+    return static_cast<char *>(g_noalloc_addr[device]);
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+template <int NP, bool CPLX>
+void run_mixed_noalloc(Ctx &c, const MatvecArgs &a) {
+    const RecordLayout &L = c.lay;
+    const MixedLayout &X = c.mlay;
+    RuleInfo ri{}, ri64{}, rxi{};
+    int QT = 0;
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = ri64.Q[r] = rxi.Q[r] = L.Q[r];
+        ri.off[r] = X.rule_off[r];
+        ri64.off[r] = L.rule_off[r];
+        rxi.off[r] = QT;
+        QT += L.Q[r];
+    }
+    const int QTp = (QT + 1) & ~1;
+    const int64_t E = c.n_elements, M = a.M;
+    const bool doF = a.x != nullptr, doG = a.v != nullptr;
+    const int level = choose_slice_level(c, M, kThreads);
+    const int S = 1 << level;
+
+    // carve the static array: xiF | xiG | yFpart | yGpart | defer list | counter | yFn, yGn
+    const size_t xi_bytes = align256((size_t)E * QTp * sizeof(float2));
+    const size_t part_bytes = align256((size_t)S * M * sizeof(double2));
+    const unsigned int dcap = (unsigned int)std::min<int64_t>(M * 16 + 1024, (int64_t)1 << 30);
+    const size_t dbytes = align256((size_t)dcap * sizeof(int2));
+    const size_t near_bytes = align256(256 + 2 * (size_t)M * sizeof(double2));
+    const size_t need = (doF ? xi_bytes : 0) + (doG ? xi_bytes : 0) + (doF ? part_bytes : 0) +
+                        (doG ? part_bytes : 0) + dbytes + near_bytes;
+    if (need > kNoAllocScratchBytes)
+        fail(BIE_ERR_INVALID, "bie_matvec_device_noalloc: this mesh needs " + std::to_string(need) +
+                                  " bytes of scratch, more than the fixed " +
+                                  std::to_string(kNoAllocScratchBytes) +
+                                  "; use bie_matvec_device");
+    char *base = noalloc_scratch(c.device);
+    size_t off = 0;
+    float2 *xiF = nullptr, *xiG = nullptr;
+    double2 *yFpart = nullptr, *yGpart = nullptr;
+    if (doF) { xiF = reinterpret_cast<float2 *>(base + off); off += xi_bytes; }
+    if (doG) { xiG = reinterpret_cast<float2 *>(base + off); off += xi_bytes; }
+    if (doF) { yFpart = reinterpret_cast<double2 *>(base + off); off += part_bytes; }
+    if (doG) { yGpart = reinterpret_cast<double2 *>(base + off); off += part_bytes; }
+    int2 *defer = reinterpret_cast<int2 *>(base + off);
+    off += dbytes;
+    unsigned int *dcount = reinterpret_cast<unsigned int *>(base + off);
+    double2 *yFn = reinterpret_cast<double2 *>(base + off + 256);
+    double2 *yGn = yFn + M;
+    // the counter and the FP64 correction sums start at zero on every call
+    BIE_CUDA(cudaMemsetAsync(base + off, 0, 256 + 2 * (size_t)M * sizeof(double2), c.stream));
+
+    const int64_t nslots = E * QT;
+    interp_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, c.stream>>>(
+        c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, L.NP, L.R, ri64, QT, QTp, E,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), xiF, xiG);
+    BIE_CUDA(cudaGetLastError());
+
+    const size_t rec_bytes = (size_t)X.stride * sizeof(float);
+    const size_t per_el = rec_bytes + (size_t)(doF + doG) * QTp * sizeof(float2);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / per_el));
+    const size_t smem = (size_t)chunk * per_el;
+    auto kern = matvec_mixed_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((M + kThreads - 1) / kThreads), (unsigned)S);
+    const Fp64Rec v64{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
+    kern<<<grid, kThreads, smem, c.stream>>>(c.d_mrecords, X.stride, E, S, ri, rxi, QTp, xiF, xiG,
+                                             a.targets, M, a.k_re, a.k_im, yFpart, yGpart, chunk,
+                                             defer, dcount, dcap, v64,
+                                             reinterpret_cast<const double2 *>(a.x),
+                                             reinterpret_cast<const double2 *>(a.v), c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    matvec_correct_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+        defer, dcount, dcap, c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), a.targets,
+        a.k_re, a.k_im, yFn, yGn, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    if (doF) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yFpart, S, yFn, M, reinterpret_cast<double2 *>(a.yF));
+        BIE_CUDA(cudaGetLastError());
+    }
+    if (doG) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yGpart, S, yGn, M, reinterpret_cast<double2 *>(a.yG));
+        BIE_CUDA(cudaGetLastError());
+    }
+    c.kernel_launches += 3 + (doF ? 1 : 0) + (doG ? 1 : 0);
+}
+
 }  // namespace
+
+void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a) {
+    if (!a.x && !a.v) return;
+    const bool cplx = a.k_im != 0.0;
+    if (c.lay.NP == 3) {
+        if (cplx) run_mixed_noalloc<3, true>(c, a);
+        else run_mixed_noalloc<3, false>(c, a);
+    } else {
+        if (cplx) run_mixed_noalloc<6, true>(c, a);
+        else run_mixed_noalloc<6, false>(c, a);
+    }
+}
 
 void launch_matvec(Ctx &c, const MatvecArgs &a) {
     if (!a.x && !a.v) return;

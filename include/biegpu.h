@@ -202,6 +202,28 @@ BIE_API int bie_matvec_device(bie_ctx *ctx, double k_re, double k_im,
                               const double *d_x, const double *d_v, double *d_yF, double *d_yG,
                               int precision);
 
+/*
+ * Allocation-free variant of bie_matvec_device (mixed precision only).
+ * This entry point has no counterpart in the reference; it exists for callers
+ * that must not have a library allocate device memory behind their back: a
+ * Julia session whose CUDA.jl pool (or a Python process whose PyTorch caching
+ * allocator) already holds most of the GPU, or a loop that may not
+ * synchronise the device.  Such a caller creates the context once at set-up,
+ * then calls this function as often as it likes; it performs no cudaMalloc or
+ * cudaFree.  All temporaries live in one fixed 32 MiB device array inside the
+ * library (held by every GPU that loads the library until the process exits);
+ * a mesh whose product needs more returns BIE_ERR_INVALID with the size in the
+ * message.  The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
+ * reuses the same array: calls whose executions overlap on the GPU race and
+ * must be serialised by the caller.  Inputs and outputs are device pointers as
+ * in bie_matvec_device; the call is asynchronous on the context stream.
+ */
+BIE_API int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im,
+                                      const double *d_targets, int64_t n_targets,
+                                      const double *d_x, const double *d_v,
+                                      double *d_yF, double *d_yG);
+
 /* ---- linear systems A x = b,  A x = s (K x) + diag .* x ---------------- */
 #define BIE_OP_DENSE       0  /* K = stored dense N x N matrix (device)       */
 #define BIE_OP_MATRIX_FREE 1  /* K = F of the context at wavenumber k         */
