@@ -25,10 +25,16 @@ SOURCES = [
     "bie_assemble_mixed.cu",
     "bie_matvec.cu",
     "bie_solver.cu",
+    "bie_nearfield.cpp",
+    "bie_nearfield.cu",
     "bie_peaks.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "-Xcompiler", "-fvisibility=hidden"]
+# Host code is compiled without FMA contraction so that the set-up arithmetic
+# (quadrature rules, subdivision decisions, element geometry) rounds the same
+# on x86-64 and aarch64 hosts; device code keeps nvcc's FMA contraction.
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
+          "-Xcompiler", "-fvisibility=hidden"]
 
 
 def nvcc() -> str:

@@ -149,6 +149,9 @@ SIGNATURES = {
     "bie_matvec": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
     "bie_matvec_device": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
     "bie_matvec_device_noalloc": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P]),
+    "bie_singular_rule": (_I, [_I, _D, _P, _P, _P, _I, C.POINTER(_I)]),
+    "bie_nearfield_pattern": (_I, [_P, _I, C.POINTER(_I64), _P, _P]),
+    "bie_nearfield_assemble": (_I, [_P, _D, _D, _I, _D, _I, _I, _I, _P, _P]),
     "bie_gmres_device": (_I, [_P, C.POINTER(Operator), _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
     "bie_round_c64_device": (_I, [_P, _P, _P, _I64]),
 }

@@ -122,6 +122,46 @@ class Context:
             _capi.ptr(F), _capi.ptr(G), _capi.ptr(Cv)))
 
 
+def nearfield_pattern(ctx: "Context", depth: int = 1):
+    """(row_ptr, cols) CSR pattern of the near field (0-based)."""
+    L = _capi.lib()
+    nnz = C.c_int64()
+    _capi.check(L.bie_nearfield_pattern(ctx.handle, int(depth), C.byref(nnz), None, None))
+    row_ptr = np.empty(ctx.n_sources + 1, dtype=np.int64)
+    cols = np.empty(nnz.value, dtype=np.int64)
+    _capi.check(L.bie_nearfield_pattern(ctx.handle, int(depth), C.byref(nnz), row_ptr.ctypes.data,
+                                        cols.ctypes.data))
+    return row_ptr, cols
+
+
+def nearfield_values(ctx: "Context", k, depth=1, offset=None, coarse=False, n_gauss=3, fOn=True, gOn=True):
+    """Near-field F, G values (complex, CSR order of nearfield_pattern)."""
+    k = complex(k)
+    row_ptr, cols = nearfield_pattern(ctx, depth)
+    nnz = len(cols)
+    F = np.empty(nnz, dtype=np.complex128) if fOn else None
+    G = np.empty(nnz, dtype=np.complex128) if gOn else None
+    flags = (_capi.BIE_F if fOn else 0) | (_capi.BIE_G if gOn else 0)
+    off = -1.0 if offset is None else float(offset)
+    _capi.check(_capi.lib().bie_nearfield_assemble(ctx.handle, k.real, k.imag, int(depth), off, flags,
+                                                   1 if coarse else 0, int(n_gauss), _capi.ptr(F),
+                                                   _capi.ptr(G)))
+    return row_ptr, cols, F, G
+
+
+def sparse_assemble_parallel(mesh: Mesh3d, k, fOn=True, gOn=True, depth=1, offset=None, device=0):
+    """GPU ``assemble_parallel!(mesh, k, mesh.sources; sparse=true)``
+    (sparse_assemble_parallel!, src/3d/assembly_collocation_losses.jl:200-405):
+    the near-field F and G with the adaptive singular rules, as scipy CSR
+    matrices (N x N)."""
+    import scipy.sparse as sp
+    ctx = get_context(mesh, device=device)
+    row_ptr, cols, F, G = nearfield_values(ctx, k, depth=depth, offset=offset, fOn=fOn, gOn=gOn)
+    N = mesh.n_sources
+    mk = lambda v: None if v is None else sp.csr_matrix((v, cols, row_ptr), shape=(N, N))  # noqa: E731
+    return mk(F), mk(G)
+
+
 _CTX_CACHE: "weakref.WeakKeyDictionary[Mesh3d, dict]" = weakref.WeakKeyDictionary()
 
 
@@ -145,7 +185,8 @@ def assemble_parallel(mesh: Mesh3d, k, sources=None, fOn=True, gOn=True, cOn=Tru
     is not part of this library yet and raises.
     """
     if sparse:
-        raise NotImplementedError("sparse (near-field) assembly is not provided by libbiegpu yet")
+        return sparse_assemble_parallel(mesh, k, fOn=fOn, gOn=gOn, depth=depth, offset=offset,
+                                        device=device)
     ctx = get_context(mesh, n=n, m=m, device=device)
     targets = None if sources is None or sources is mesh.sources else sources
     return ctx.assemble(k, targets=targets, fOn=fOn, gOn=gOn, cOn=cOn, precision=precision)

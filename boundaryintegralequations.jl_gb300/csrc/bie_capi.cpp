@@ -4,6 +4,7 @@
 // message, and never lets an exception cross the boundary.
 #include "bie_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <exception>
 #include <new>
@@ -257,6 +258,60 @@ int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im, const doub
         bie::MatvecArgs a{k_re, k_im, d_targets ? d_targets : c.d_sources, M, d_x, d_v, d_yF, d_yG,
                           BIE_PREC_MIXED};
         bie::launch_matvec_noalloc(c, a);
+    });
+}
+
+int bie_singular_rule(int node, double offset, double *u, double *v, double *w, int capacity,
+                      int *count) {
+    return guarded([&] {
+        if (!count) bie::fail(BIE_ERR_INVALID, "count must not be NULL");
+        if (!(offset >= 0.0) || offset > 1.0) bie::fail(BIE_ERR_INVALID, "offset must be in [0, 1]");
+        const bie::Rule r = bie::singular_rule(node, offset);
+        *count = r.size();
+        if (r.size() > capacity) bie::fail(BIE_ERR_INVALID, "capacity too small for the rule");
+        if (!u || !v || !w) bie::fail(BIE_ERR_INVALID, "u, v, w must not be NULL");
+        std::copy(r.u.begin(), r.u.end(), u);
+        std::copy(r.v.begin(), r.v.end(), v);
+        std::copy(r.w.begin(), r.w.end(), w);
+    });
+}
+
+int bie_nearfield_pattern(bie_ctx *ctx, int depth, int64_t *nnz, int64_t *row_ptr, int64_t *cols) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!nnz) bie::fail(BIE_ERR_INVALID, "nnz must not be NULL");
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        const bie::NearField &nf = bie::get_nearfield(c, depth, 0.0, 3);
+        *nnz = (int64_t)nf.cols.size();
+        if (row_ptr) std::copy(nf.row_ptr.begin(), nf.row_ptr.end(), row_ptr);
+        if (cols)
+            for (size_t j = 0; j < nf.cols.size(); ++j) cols[j] = nf.cols[j];
+    });
+}
+
+int bie_nearfield_assemble(bie_ctx *ctx, double k_re, double k_im, int depth, double offset,
+                           int flags, int coarse, int n_gauss, double *F, double *G) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!std::isfinite(k_re) || !std::isfinite(k_im)) bie::fail(BIE_ERR_INVALID, "k must be finite");
+        if (flags & ~(BIE_F | BIE_G)) bie::fail(BIE_ERR_INVALID, "flags: only BIE_F | BIE_G");
+        if ((flags & BIE_F) && !F) bie::fail(BIE_ERR_INVALID, "F requested but NULL");
+        if ((flags & BIE_G) && !G) bie::fail(BIE_ERR_INVALID, "G requested but NULL");
+        if (coarse) bie::triangle_gauss_rule(n_gauss);   // validates n_gauss
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        const double off = offset < 0 ? 0.0 : offset;
+        const bie::NearField &nf = bie::get_nearfield(c, depth, off, coarse ? n_gauss : 3);
+        const size_t bytes = nf.cols.size() * 16;
+        double *dF = (flags & BIE_F) ? static_cast<double *>(c.scratch(bie::kScratchF, bytes)) : nullptr;
+        double *dG = (flags & BIE_G) ? static_cast<double *>(c.scratch(bie::kScratchG, bytes)) : nullptr;
+        if (dF) BIE_CUDA(cudaMemsetAsync(dF, 0, bytes, c.stream));
+        if (dG) BIE_CUDA(cudaMemsetAsync(dG, 0, bytes, c.stream));
+        bie::launch_nearfield(c, nf, k_re, k_im, flags, coarse != 0, 1.0, dF, dG);
+        if (dF) BIE_CUDA(cudaMemcpyAsync(F, dF, bytes, cudaMemcpyDeviceToHost, c.stream));
+        if (dG) BIE_CUDA(cudaMemcpyAsync(G, dG, bytes, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
     });
 }
 

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -102,6 +103,31 @@ struct MixedLayout {
     int stride = 0;
 };
 
+// Near-field (sparse) structure for one (depth, offset, n_gauss): CSR pattern of
+// connected nodes per collocation node, the (row, element, CSR slots) pairs and
+// the rule tables (adaptive singular rules per element node + the coarse
+// Gauss rule).  Built on first use (bie_nearfield.cpp).
+struct NearField {
+    bool ready = false;
+    int depth = 1;
+    double offset = 0.0;
+    int n_gauss = 3;
+    std::vector<int64_t> row_ptr;        // N + 1
+    std::vector<int32_t> cols;           // nnz (0-based node indices)
+    std::vector<int32_t> pairs;          // npairs x pair_stride: row, element, slot[NP]
+    int pair_stride = 0;
+    int64_t npairs = 0;
+    std::vector<double> table;           // points x point_stride
+    int point_stride = 0;                // N[NS] dNu[NS] dNv[NS] Phi[NP] w
+    int nrules = 0;
+    int64_t rule_off[kMaxRules] = {};    // first point of rule r
+    int rule_q[kMaxRules] = {};
+    int64_t coarse_off = 0;
+    int coarse_q = 0;
+    int32_t *d_pairs = nullptr;
+    double *d_table = nullptr;
+};
+
 struct Ctx {
     std::mutex mu;
     int device = 0;
@@ -135,6 +161,9 @@ struct Ctx {
     MixedLayout mlay;
     float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)
+    double *d_coords = nullptr;          // 3 x Nc geometry nodes (near-field kernels)
+    int32_t *d_topo = nullptr;           // NS x E, 0-based
+    std::vector<std::unique_ptr<NearField>> nearfields;
 
     // grow-only device scratch, indexed by the kScratch* slots below
     void *d_scratch[kScratchCount] = {};
@@ -193,6 +222,15 @@ void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a);
 void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
                bie_gmres_info &info);
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
+
+// Near field (bie_nearfield.cpp / bie_nearfield.cu)
+Rule singular_rule(int node, double offset);
+NearField &get_nearfield(Ctx &c, int depth, double offset, int n_gauss);
+void free_nearfield(NearField &nf);
+// Fv, Gv: device, nnz complex each (may be null when the flag is off); values
+// are ADDED with sign `sign` (accurate rule) or computed with the coarse rule.
+void launch_nearfield(Ctx &c, const NearField &nf, double k_re, double k_im, int flags, bool coarse,
+                      double sign, double *Fv, double *Gv);
 
 // Mixed-precision assembly (bie_assemble_mixed.cu)
 // host: builds d_mrecords / d_mphi from the FP64 records (E x lay.stride) and uploads them

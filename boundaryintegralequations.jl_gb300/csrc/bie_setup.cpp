@@ -540,6 +540,12 @@ void destroy_context(Ctx &c) {
     cudaFree(c.d_mphi);
     c.d_mrecords = nullptr;
     c.d_mphi = nullptr;
+    for (auto &nf : c.nearfields) free_nearfield(*nf);
+    c.nearfields.clear();
+    cudaFree(c.d_coords);
+    cudaFree(c.d_topo);
+    c.d_coords = nullptr;
+    c.d_topo = nullptr;
     cudaFree(c.d_qpe);
     for (int i = 0; i < kScratchCount; ++i) cudaFree(c.d_scratch[i]);
     for (auto &p : c.ev_pending) {

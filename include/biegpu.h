@@ -224,6 +224,44 @@ BIE_API int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im,
                                       const double *d_x, const double *d_v,
                                       double *d_yF, double *d_yG);
 
+/* ---- near field (sparse) --------------------------------------------- */
+/*
+ * Adaptive singular rule towards element node `node` (1..6) with `offset`:
+ * singular_triangle_integration(shape, 3, source, Diagonal(ones(3)), 1e-6) as
+ * set up by sparse_assemble_parallel! (src/3d/adaptive_integration.jl:217-246,
+ * src/3d/assembly_collocation_losses.jl:208-220).  Host-only.  *count gets the
+ * rule size; at most `capacity` points are written.
+ */
+BIE_API int bie_singular_rule(int node, double offset, double *u, double *v, double *w,
+                              int capacity, int *count);
+
+/*
+ * CSR pattern of the near-field matrices: row i holds the physics nodes of
+ * the elements connected to collocation node i (depth 1: elements containing
+ * node i; depth 2: elements containing one of its neighbours), sorted.
+ * Replaces connected_sources (src/3d/assembly_collocation_losses.jl:98-132).
+ * Call with row_ptr = cols = NULL to get *nnz, then with row_ptr (N + 1
+ * entries) and cols (nnz entries); indices are 0-based.
+ */
+BIE_API int bie_nearfield_pattern(bie_ctx *ctx, int depth, int64_t *nnz, int64_t *row_ptr,
+                                  int64_t *cols);
+
+/*
+ * Near-field values of F and G in the CSR order of bie_nearfield_pattern
+ * (HOST buffers of nnz complex each; a buffer whose flag is off may be NULL).
+ * coarse == 0: the accurate adaptive-subdivision rules of
+ *   assemble_parallel!(mesh, k, mesh.sources; sparse=true, depth, offset)
+ *   = sparse_assemble_parallel! (src/3d/assembly_collocation_losses.jl:200-405,
+ *   src/3d/adaptive_integration.jl:172-246); offset < 0 means the reference's
+ *   default for continuous elements (0).
+ * coarse == 1: the n_gauss-point triangle rule of partial_assemble_parallel!
+ *   (src/3d/fast_multipole_method.jl:11-81), n_gauss in {1, 3, 4, 7, 12, 13}.
+ * FP64 arithmetic.  Blocks until the values are in the host buffers.
+ */
+BIE_API int bie_nearfield_assemble(bie_ctx *ctx, double k_re, double k_im, int depth,
+                                   double offset, int flags, int coarse, int n_gauss,
+                                   double *F, double *G);
+
 /* ---- linear systems A x = b,  A x = s (K x) + diag .* x ---------------- */
 #define BIE_OP_DENSE       0  /* K = stored dense N x N matrix (device)       */
 #define BIE_OP_MATRIX_FREE 1  /* K = F of the context at wavenumber k         */

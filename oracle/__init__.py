@@ -60,6 +60,10 @@ def lib():
             L.oracle_rule.argtypes = [I, I, I, P, P, P]
             L.oracle_total_weight.restype = D
             L.oracle_total_weight.argtypes = [P, P, I, I64, I, I]
+            L.oracle_singular_rule.restype = I
+            L.oracle_singular_rule.argtypes = [I, D, P, P, P, I]
+            L.oracle_nearfield.restype = I
+            L.oracle_nearfield.argtypes = [P, P, I, P, I, P, P, I64, I64, D, I, I, D, D, I, P, P, I]
             _lib = L
         return _lib
 
@@ -80,6 +84,72 @@ def total_weight(mesh, n: int = 2, m: int = 2) -> float:
     t = np.asfortranarray(mesh.topology, dtype=np.int64)
     return lib().oracle_total_weight(c.ctypes.data, t.ctypes.data, _KIND[mesh.shape_function],
                                      t.shape[1], n, m)
+
+
+def singular_rule(node: int, offset: float = 0.0):
+    """(u, v, w) of singular_triangle_integration towards element node ``node``."""
+    cap = 32768
+    u, v, w = (np.zeros(cap) for _ in range(3))
+    q = lib().oracle_singular_rule(node, float(offset), u.ctypes.data, v.ctypes.data, w.ctypes.data, cap)
+    return u[:q].copy(), v[:q].copy(), w[:q].copy()
+
+
+def connected_sources(mesh, depth: int = 1):
+    """connected_sources for continuous physics (src/3d/assembly_collocation_losses.jl:
+    98-132): per node, the sorted elements and physics nodes within ``depth``."""
+    T = mesh.physics_topology - 1
+    NP, E = T.shape
+    N = mesh.n_sources
+    econ = [[] for _ in range(N)]
+    scon = [[] for _ in range(N)]
+    for e in range(E):
+        for a in range(NP):
+            econ[T[a, e]].append(e)
+            scon[T[a, e]].extend(T[:, e].tolist())
+    if depth == 2:
+        e2 = [[] for _ in range(N)]
+        s2 = [[] for _ in range(N)]
+        for i in range(N):
+            for j in scon[i]:
+                e2[i].extend(econ[j])
+                s2[i].extend(scon[j])
+        econ, scon = e2, s2
+    return [sorted(set(x)) for x in econ], [sorted(set(x)) for x in scon]
+
+
+def nearfield(mesh, k, depth=1, offset=0.0, coarse=False, n_gauss=3, fOn=True, gOn=True, threads=0):
+    """Near-field F, G (CSR: row_ptr, cols, values) of sparse_assemble_parallel!
+    (coarse=False) or partial_assemble_parallel! (coarse=True)."""
+    k = complex(k)
+    econ, scon = connected_sources(mesh, depth)
+    N = mesh.n_sources
+    row_ptr = np.zeros(N + 1, dtype=np.int64)
+    for i in range(N):
+        row_ptr[i + 1] = row_ptr[i] + len(scon[i])
+    cols = np.concatenate([np.asarray(s, dtype=np.int64) for s in scon])
+    T = mesh.physics_topology - 1
+    NP = T.shape[0]
+    pairs = []
+    for i in range(N):
+        pos = {nd: row_ptr[i] + j for j, nd in enumerate(scon[i])}
+        for e in econ[i]:
+            pairs.append([i, e] + [pos[T[a, e]] for a in range(NP)])
+    pairs = np.ascontiguousarray(np.asarray(pairs, dtype=np.int64))
+    nnz = len(cols)
+    F = np.zeros(nnz, dtype=np.complex128)
+    G = np.zeros(nnz, dtype=np.complex128)
+    c = np.asfortranarray(mesh.coordinates, dtype=np.float64)
+    t = np.asfortranarray(mesh.topology, dtype=np.int64)
+    pt = np.asfortranarray(mesh.physics_topology, dtype=np.int64)
+    s = np.asfortranarray(mesh.sources, dtype=np.float64)
+    flags = (1 if fOn else 0) | (2 if gOn else 0)
+    st = lib().oracle_nearfield(c.ctypes.data, t.ctypes.data, _KIND[mesh.shape_function], pt.ctypes.data,
+                                _KIND[mesh.physics_function], s.ctypes.data, pairs.ctypes.data,
+                                len(pairs), nnz, float(offset), 1 if coarse else 0, int(n_gauss),
+                                k.real, k.imag, flags, F.ctypes.data, G.ctypes.data, int(threads))
+    if st != 0:
+        raise RuntimeError("oracle_nearfield failed")
+    return row_ptr, cols, F, G
 
 
 def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, threads=0):

@@ -359,3 +359,197 @@ int oracle_assemble(const double *coords, int64_t Nc, const int64_t *topo, int s
     }
     return 0;
 }
+
+/* ======================================================================== *
+ * Near field: sparse_assemble_parallel! (src/3d/assembly_collocation_losses.jl:
+ * 200-405), its adaptive rules (src/3d/adaptive_integration.jl:172-246) and the
+ * coarse partial_assemble_parallel! (src/3d/fast_multipole_method.jl:11-81).
+ * ======================================================================== */
+
+/* gauss_points_triangle (src/3d/adaptive_integration.jl:13-64) */
+static int gauss_triangle(int n, double *u, double *v, double *w) {
+    static const double t1[] = {1.0 / 3, 1.0 / 3, 0.5};
+    static const double t3[] = {1.0 / 6, 1.0 / 6, 1.0 / 6, 2.0 / 3, 1.0 / 6, 1.0 / 6, 1.0 / 6, 2.0 / 3, 1.0 / 6};
+    static const double t4[] = {1.0 / 3, 1.0 / 3, -9.0 / 32, 0.2, 0.6, 25.0 / 96, 0.2, 0.2, 25.0 / 96,
+                                0.6, 0.2, 25.0 / 96};
+    static const double t7[] = {1.0 / 3, 1.0 / 3, 0.1125,
+                                0.797426985353087, 0.101286507323456, 0.0629695902724135,
+                                0.101286507323456, 0.797426985353087, 0.0629695902724135,
+                                0.101286507323456, 0.101286507323456, 0.0629695902724135,
+                                0.059715871789770, 0.470142064105115, 0.066197076394253,
+                                0.470142064105115, 0.059715871789770, 0.066197076394253,
+                                0.470142064105115, 0.470142064105115, 0.066197076394253};
+    const double *t;
+    switch (n) {
+        case 1: t = t1; break;
+        case 3: t = t3; break;
+        case 4: t = t4; break;
+        case 7: t = t7; break;
+        default: return -1;
+    }
+    for (int i = 0; i < n; ++i) { u[i] = t[3 * i]; v[i] = t[3 * i + 1]; w[i] = t[3 * i + 2]; }
+    return n;
+}
+
+static double d3(const double *a, const double *b) {
+    double x = a[0] - b[0], y = a[1] - b[1], z = a[2] - b[2];
+    return sqrt((x * x + y * y) + z * z);
+}
+
+typedef struct { double *t; int n, cap; } tri_list;   /* 6 doubles per kept triangle */
+
+static void subdivide_triangle(const double *P1, const double *P2, const double *P3,
+                               const double *src, double esize, double tol, tri_list *out) {
+    double P12[2] = {(P1[0] + P2[0]) / 2, (P1[1] + P2[1]) / 2};
+    double P23[2] = {(P2[0] + P3[0]) / 2, (P2[1] + P3[1]) / 2};
+    double P31[2] = {(P3[0] + P1[0]) / 2, (P3[1] + P1[1]) / 2};
+    double C[2] = {(P1[0] + P2[0] + P3[0]) / 3.0, (P1[1] + P2[1] + P3[1]) / 3.0};
+    /* subelement = Diagonal(ones(3)) * N(u, v), N = [1-u-v, u, v] */
+    double c[3] = {(1.0 - C[0]) - C[1], C[0], C[1]};
+    double a[3] = {(1.0 - P1[0]) - P1[1], P1[0], P1[1]};
+    double b[3] = {(1.0 - P2[0]) - P2[1], P2[0], P2[1]};
+    double d[3] = {(1.0 - P3[0]) - P3[1], P3[0], P3[1]};
+    double dist = d3(c, src);
+    if (d3(a, src) < dist) dist = d3(a, src);
+    if (d3(b, src) < dist) dist = d3(b, src);
+    if (d3(d, src) < dist) dist = d3(d, src);
+    double size = d3(b, a);
+    if (d3(d, b) > size) size = d3(d, b);
+    if (d3(a, d) > size) size = d3(a, d);
+    if (size < esize * tol) size = 0;
+    if (size > dist / 4) {
+        subdivide_triangle(P1, P12, P31, src, esize, tol, out);
+        subdivide_triangle(P12, P2, P23, src, esize, tol, out);
+        subdivide_triangle(P31, P23, P3, src, esize, tol, out);
+        subdivide_triangle(P12, P23, P31, src, esize, tol, out);
+    } else {
+        if (out->n + 1 > out->cap) {
+            out->cap = out->cap ? 2 * out->cap : 1024;
+            out->t = realloc(out->t, (size_t)out->cap * 6 * sizeof(double));
+        }
+        double *t = out->t + 6 * (size_t)out->n;
+        t[0] = P1[0]; t[1] = P1[1]; t[2] = P2[0]; t[3] = P2[1]; t[4] = P3[0]; t[5] = P3[1];
+        out->n++;
+    }
+}
+
+/* singular_triangle_integration(shape, 3, source, I, 1e-6) for element node c
+ * (1..6) with offset `off`; returns the number of points (<= cap). */
+int oracle_singular_rule(int c, double off, double *U, double *V, double *W, int cap) {
+    double src[3];
+    switch (c) {
+        case 1: src[0] = 1.0; src[1] = off; src[2] = off; break;
+        case 2: src[0] = off; src[1] = 1.0; src[2] = off; break;
+        case 3: src[0] = off; src[1] = off; src[2] = 1.0; break;
+        case 4: src[0] = 0.5; src[1] = 0.5; src[2] = off; break;
+        case 5: src[0] = off; src[1] = 0.5; src[2] = 0.5; break;
+        default: src[0] = 0.5; src[1] = off; src[2] = 0.5; break;
+    }
+    const double e1[3] = {1, 0, 0}, e2[3] = {0, 1, 0}, e3[3] = {0, 0, 1};
+    double esize = d3(e2, e1);
+    if (d3(e3, e2) > esize) esize = d3(e3, e2);
+    if (d3(e1, e3) > esize) esize = d3(e1, e3);
+    tri_list L = {NULL, 0, 0};
+    const double A[2] = {0, 0}, B[2] = {1, 0}, Cc[2] = {0, 1};
+    subdivide_triangle(A, B, Cc, src, esize, 1e-6, &L);
+    double gu[3], gv[3], gw[3];
+    gauss_triangle(3, gu, gv, gw);
+    int q = 0;
+    for (int i = 0; i < L.n; ++i) {
+        const double *t = L.t + 6 * (size_t)i;
+        double s1 = sqrt((t[2] - t[0]) * (t[2] - t[0]) + (t[3] - t[1]) * (t[3] - t[1]));
+        double s2 = sqrt((t[4] - t[2]) * (t[4] - t[2]) + (t[5] - t[3]) * (t[5] - t[3]));
+        double s3 = sqrt((t[0] - t[4]) * (t[0] - t[4]) + (t[1] - t[5]) * (t[1] - t[5]));
+        double dim = s1 < s2 ? s1 : s2;
+        if (s3 < dim) dim = s3;
+        double cu = ((t[0] + t[2]) + t[4]) / 3, cv = ((t[1] + t[3]) + t[5]) / 3;
+        for (int g = 0; g < 3; ++g) {
+            if (q < cap) {
+                U[q] = (gu[g] - 1.0 / 3.0) * dim + cu;
+                V[q] = (gv[g] - 1.0 / 3.0) * dim + cv;
+                W[q] = gw[g] * (dim * dim);
+            }
+            ++q;
+        }
+    }
+    free(L.t);
+    return q;
+}
+
+/*
+ * Near-field F, G in CSR order.  pairs: npairs x (2 + NP) = (row, element,
+ * CSR slot of each physics node), built from connected_sources by the caller.
+ * coarse = 0: adaptive rules chosen by the nearest GEOMETRY node; 1: the
+ * n_gauss triangle rule.  F, G: nnz complex (zeroed here).
+ */
+int oracle_nearfield(const double *coords, const int64_t *topo, int skind, const int64_t *ptopo,
+                     int pkind, const double *sources, const int64_t *pairs, int64_t npairs,
+                     int64_t nnz, double offset, int coarse, int n_gauss, double kre, double kim,
+                     int flags, double *F, double *G, int nthreads) {
+    const int NS = nnodes(skind), NP = nnodes(pkind);
+    const int R = coarse ? 1 : NS;
+    int Q[6];
+    double *U[6], *V[6], *W[6];
+    for (int r = 0; r < R; ++r) {
+        int cap = 32768;
+        U[r] = malloc(cap * sizeof(double)); V[r] = malloc(cap * sizeof(double)); W[r] = malloc(cap * sizeof(double));
+        Q[r] = coarse ? gauss_triangle(n_gauss, U[r], V[r], W[r]) : oracle_singular_rule(r + 1, offset, U[r], V[r], W[r], cap);
+        if (Q[r] < 0 || Q[r] > cap) return -1;
+    }
+    if (flags & OR_F) memset(F, 0, (size_t)nnz * 16);
+    if (flags & OR_G) memset(G, 0, (size_t)nnz * 16);
+    const double complex k = kre + I * kim;
+    const int ps = 2 + NP;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    omp_lock_t lock;
+    omp_init_lock(&lock);
+#pragma omp parallel for schedule(dynamic, 16)
+#endif
+    for (int64_t p = 0; p < npairs; ++p) {
+        const int64_t *pr = pairs + p * ps;
+        const int64_t i = pr[0], e = pr[1];
+        const double *s = sources + 3 * i;
+        int r = 0;
+        if (!coarse) {   /* find_closest_corner on the element's geometry nodes */
+            double best = INFINITY;
+            for (int a = 0; a < NS; ++a) {
+                const double *X = coords + 3 * (topo[NS * e + a] - 1);
+                double dd = julia_hypot3(X[0] - s[0], X[1] - s[1], X[2] - s[2]);
+                if (dd < best) { best = dd; r = a; }
+            }
+        }
+        double *x = malloc((size_t)Q[r] * 3 * sizeof(double));
+        double *nr = malloc((size_t)Q[r] * 3 * sizeof(double));
+        double *jw = malloc((size_t)Q[r] * sizeof(double));
+        interpolate_element(skind, coords, topo, e, Q[r], U[r], V[r], W[r], x, nr, jw);
+        double complex fa[6] = {0}, ga[6] = {0};
+        for (int q = 0; q < Q[r]; ++q) {
+            double rr = julia_hypot3(x[3 * q] - s[0], x[3 * q + 1] - s[1], x[3 * q + 2] - s[2]);
+            double Nv[6];
+            basis(pkind, U[r][q], V[r][q], Nv);
+            double dn = nr[3 * q] * (x[3 * q] - s[0]) + nr[3 * q + 1] * (x[3 * q + 1] - s[1]) +
+                        nr[3 * q + 2] * (x[3 * q + 2] - s[2]);
+            double complex fv = cexp(I * k * rr) * (I * k * rr - 1.0) * dn / (4.0 * PI * rr * rr * rr) * jw[q];
+            double complex gv = cexp(I * k * rr) / (4.0 * PI * rr) * jw[q];
+            for (int a = 0; a < NP; ++a) { fa[a] += fv * Nv[a]; ga[a] += gv * Nv[a]; }
+        }
+        free(x); free(nr); free(jw);
+#ifdef _OPENMP
+        omp_set_lock(&lock);
+#endif
+        for (int a = 0; a < NP; ++a) {
+            const int64_t slot = pr[2 + a];
+            if (flags & OR_F) { F[2 * slot] += creal(fa[a]); F[2 * slot + 1] += cimag(fa[a]); }
+            if (flags & OR_G) { G[2 * slot] += creal(ga[a]); G[2 * slot + 1] += cimag(ga[a]); }
+        }
+#ifdef _OPENMP
+        omp_unset_lock(&lock);
+#endif
+    }
+#ifdef _OPENMP
+    omp_destroy_lock(&lock);
+#endif
+    for (int r = 0; r < R; ++r) { free(U[r]); free(V[r]); free(W[r]); }
+    return 0;
+}
