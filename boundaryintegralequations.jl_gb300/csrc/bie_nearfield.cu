@@ -74,6 +74,12 @@ nearfield_kernel(const int32_t *__restrict__ pairs, int pstride, int64_t npairs,
 #pragma unroll
         for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.0;
         for (int q = lane; q < Q; q += 32) {
+            // The subdivided rules put points within 1e-6 element sizes of the
+            // singular node, where x_q - t and n.(x_q - t) cancel: the geometry
+            // is therefore evaluated with separately rounded products and sums
+            // in the reference's order (interpolation, cross product, Julia
+            // hypot for the jacobian and the distance, IEEE division for the
+            // normal), so the result does not depend on FMA contraction.
             const double *P = table + (base + q) * tstride;
             double x[3] = {0, 0, 0}, tu[3] = {0, 0, 0}, tv[3] = {0, 0, 0};
 #pragma unroll
@@ -81,22 +87,20 @@ nearfield_kernel(const int32_t *__restrict__ pairs, int pstride, int64_t npairs,
                 const double Na = P[a], Ua = P[NS + a], Va = P[2 * NS + a];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    x[k] += X[3 * a + k] * Na;
-                    tu[k] += X[3 * a + k] * Ua;
-                    tv[k] += X[3 * a + k] * Va;
+                    x[k] = __dadd_rn(x[k], __dmul_rn(X[3 * a + k], Na));
+                    tu[k] = __dadd_rn(tu[k], __dmul_rn(X[3 * a + k], Ua));
+                    tv[k] = __dadd_rn(tv[k], __dmul_rn(X[3 * a + k], Va));
                 }
             }
-            const double n0 = tu[1] * tv[2] - tu[2] * tv[1];
-            const double n1 = tu[2] * tv[0] - tu[0] * tv[2];
-            const double n2 = tu[0] * tv[1] - tu[1] * tv[0];
-            const double jac = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
-            const double jw = jac * P[3 * NS + NP];
-            const double ijac = 1.0 / jac;
-            const double nx = -n0 * ijac, ny = -n1 * ijac, nz = -n2 * ijac;
-            const double dx = x[0] - tx, dy = x[1] - ty, dz = x[2] - tz;
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            const double rinv = rsqrt(r2);
-            const double rr = r2 * rinv;
+            const double n0 = __dsub_rn(__dmul_rn(tu[1], tv[2]), __dmul_rn(tu[2], tv[1]));
+            const double n1 = __dsub_rn(__dmul_rn(tu[2], tv[0]), __dmul_rn(tu[0], tv[2]));
+            const double n2 = __dsub_rn(__dmul_rn(tu[0], tv[1]), __dmul_rn(tu[1], tv[0]));
+            const double jac = dev::julia_hypot3(n0, n1, n2);
+            const double jw = __dmul_rn(jac, P[3 * NS + NP]);
+            const double nx = __ddiv_rn(-n0, jac), ny = __ddiv_rn(-n1, jac), nz = __ddiv_rn(-n2, jac);
+            const double dx = __dsub_rn(x[0], tx), dy = __dsub_rn(x[1], ty), dz = __dsub_rn(x[2], tz);
+            const double rr = dev::julia_hypot3(dx, dy, dz);
+            const double rinv = __ddiv_rn(1.0, rr);
             double sn, cs;
             sincos(kre * rr, &sn, &cs);
             if (CPLX_K) {
@@ -106,7 +110,7 @@ nearfield_kernel(const int32_t *__restrict__ pairs, int pstride, int64_t npairs,
             }
             const double wg = rinv * kInv4Pi * jw;
             const double Gr = cs * wg, Gi = sn * wg;
-            const double dn = nx * dx + ny * dy + nz * dz;
+            const double dn = __dadd_rn(__dadd_rn(__dmul_rn(nx, dx), __dmul_rn(ny, dy)), __dmul_rn(nz, dz));
             const double tq = dn * (rinv * rinv * rinv) * kInv4Pi * jw;
             const double ar = CPLX_K ? (-1.0 - kim * rr) : -1.0;
             const double ai = kre * rr;

@@ -28,8 +28,8 @@ def test_singular_rules_match_oracle(node, offset):
     u, v, w = product_rule(node, offset)
     uo, vo, wo = oracle.singular_rule(node, offset)
     assert len(u) == len(uo)
-    assert np.max(np.abs(u - uo)) <= 1e-15 and np.max(np.abs(v - vo)) <= 1e-15
-    assert np.max(np.abs(w - wo)) <= 1e-18
+    # same arithmetic in the same order (no FMA contraction on either side): bitwise equal
+    assert np.array_equal(u, uo) and np.array_equal(v, vo) and np.array_equal(w, wo)
     assert abs(w.sum() - 0.5) < 1e-13
     assert np.all(u >= -1e-15) and np.all(v >= -1e-15) and np.all(u + v <= 1 + 1e-15)
 
