@@ -11,5 +11,6 @@ from ._capi import BIEError, lib, library_path  # noqa: F401
 from .assembly import Context, assemble_parallel, get_context, quadrature_rule  # noqa: F401
 from .mesh import Mesh3d, ellipsoid, icosphere, load_comsol, read_comsol  # noqa: F401
 from .operators import Diagonal, GPUFOperator, GPUGOperator, I, UniformScaling, gmres  # noqa: F401
+from .sweep import sweep  # noqa: F401
 
 __version__ = "0.1.0"

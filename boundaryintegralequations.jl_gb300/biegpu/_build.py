@@ -27,6 +27,7 @@ SOURCES = [
     "bie_solver.cu",
     "bie_nearfield.cpp",
     "bie_nearfield.cu",
+    "bie_sweep.cu",
     "bie_peaks.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -125,6 +125,20 @@ class GmresInfo(C.Structure):
     ]
 
 
+class SweepOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("refine", C.c_int32), ("gmres", GmresOpts)]
+
+
+class SweepInfo(C.Structure):
+    _fields_ = [
+        ("solves", C.c_int64),
+        ("converged", C.c_int64),
+        ("iterations", C.c_int64),
+        ("assemble_ms", C.c_double),
+        ("solve_ms", C.c_double),
+    ]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -154,6 +168,8 @@ SIGNATURES = {
     "bie_nearfield_assemble": (_I, [_P, _D, _D, _I, _D, _I, _I, _I, _P, _P]),
     "bie_gmres_device": (_I, [_P, C.POINTER(Operator), _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
     "bie_round_c64_device": (_I, [_P, _P, _P, _I64]),
+    "bie_sweep": (_I, [C.POINTER(_P), _I, _P, _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(SweepOpts),
+                       C.POINTER(SweepInfo), _P]),
 }
 
 

@@ -346,6 +346,30 @@ int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b, do
     return st;
 }
 
+int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,
+              double *const *p, const bie_sweep_opts *opts, bie_sweep_info *info, int32_t *iters) {
+    return guarded([&] {
+        if (!ctxs || nmesh <= 0 || !ks || nk <= 0 || !w || !p)
+            bie::fail(BIE_ERR_INVALID, "ctxs, ks, w, p must be given with positive counts");
+        std::vector<bie::Ctx *> cs(nmesh);
+        for (int m = 0; m < nmesh; ++m) {
+            cs[m] = as_ctx(ctxs[m]);
+            if (!w[m] || !p[m]) bie::fail(BIE_ERR_INVALID, "w[m] and p[m] must not be NULL");
+        }
+        for (int j = 0; j < 2 * nk; ++j)
+            if (!std::isfinite(ks[j])) bie::fail(BIE_ERR_INVALID, "wavenumbers must be finite");
+        bie_sweep_opts o{};
+        o.precision = BIE_PREC_MIXED;
+        o.refine = 1;
+        if (opts) o = *opts;
+        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
+            bie::fail(BIE_ERR_INVALID, "unknown precision");
+        bie_sweep_info inf{};
+        bie::run_sweep(cs.data(), nmesh, ks, nk, w, p, o, inf, iters);
+        if (info) *info = inf;
+    });
+}
+
 int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n) {
     return guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);

@@ -222,6 +222,11 @@ void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a);
 void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
                bie_gmres_info &info);
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
+// Frequency sweep (bie_sweep.cu); locks each context while it runs.
+void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,
+               double *const *p, const bie_sweep_opts &o, bie_sweep_info &info, int32_t *iters);
+// y = s (K x) + diag .* x on the context stream (device vectors of length N)
+void apply_operator(Ctx &c, const bie_operator &op, int precision, const double *x, double *y);
 
 // Near field (bie_nearfield.cpp / bie_nearfield.cu)
 Rule singular_rule(int node, double offset);

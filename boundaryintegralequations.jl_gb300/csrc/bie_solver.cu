@@ -453,6 +453,11 @@ void run_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, con
     info.converged = res <= tol ? 1 : 0;
 }
 
+void apply_operator(Ctx &c, const bie_operator &op, int precision, const double *x, double *y) {
+    Solver S(c, c.n_sources, 1);
+    S.apply(op, precision, reinterpret_cast<const double2 *>(x), reinterpret_cast<double2 *>(y));
+}
+
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n) {
     round_c64_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 64LL * c.num_sms), 256, 0, c.stream>>>(
         reinterpret_cast<const double2 *>(in), reinterpret_cast<float2 *>(out), n);

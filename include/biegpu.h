@@ -308,6 +308,37 @@ typedef struct bie_gmres_info {
 BIE_API int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b,
                              double *d_x, const bie_gmres_opts *opts, bie_gmres_info *info);
 
+/* ---- frequency sweeps -------------------------------------------------- */
+typedef struct bie_sweep_opts {
+    int32_t precision;         /* assembly arithmetic: BIE_PREC_MIXED | BIE_PREC_FP64   */
+    int32_t refine;            /* mixed: complex64 inner GMRES + complex128 residual     */
+    bie_gmres_opts gmres;      /* restart, maxiter, reltol, abstol (zeros: defaults)     */
+} bie_sweep_opts;
+
+typedef struct bie_sweep_info {
+    int64_t solves;            /* (mesh, k) systems solved                                */
+    int64_t converged;         /* of which converged                                      */
+    int64_t iterations;        /* GMRES iterations summed                                 */
+    double  assemble_ms;       /* device time of the assemblies (CUDA events)            */
+    double  solve_ms;          /* device time of right-hand sides + GMRES                */
+} bie_sweep_info;
+
+/*
+ * Batched frequency sweep over meshes of uneven size: for every context m and
+ * wavenumber k_j, assemble F, G, C on the device, form
+ *     (F + Diagonal(1 - C)) p = G w_m
+ * (the reference's boundary integral equation, README.md:10-18, with the
+ * exterior collocation form of test/3d/assembly_test.jl:37) and solve it with
+ * GMRES, all on the device.  The reference has no batched form: users loop
+ * assemble_parallel! + gmres per frequency (examples/sweep_meta.jl:219-233,
+ * src/3d/rosebem.jl:235-262).  ks: nk complex (interleaved), w[m]: N_m complex
+ * host vectors, p[m]: nk x N_m complex host outputs (column j = k_j).
+ * iters (optional): nmesh x nk GMRES iteration counts.
+ */
+BIE_API int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk,
+                      const double *const *w, double *const *p, const bie_sweep_opts *opts,
+                      bie_sweep_info *info, int32_t *iters);
+
 /* out[i] = (complex64) in[i] for n complex entries (device), e.g. to build
  * bie_operator.A32 from an assembled matrix. */
 BIE_API int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n);

@@ -45,9 +45,10 @@ def test_nearfield_offset_and_coarse(offset):
 
 def test_sparse_assemble_parallel_api():
     mesh = bm.icosphere(3, geometry="quadratic")
+    # the dispatcher's default depth is 2 (src/3d/assembly_collocation.jl:259-260)
     F, G = biegpu.assemble_parallel(mesh, 2.0, mesh.sources, sparse=True)
     assert F.shape == (mesh.n_sources, mesh.n_sources)
-    rp, cols, Fo, Go = oracle.nearfield(mesh, 2.0)
+    rp, cols, Fo, Go = oracle.nearfield(mesh, 2.0, depth=2)
     assert rel(F.data, Fo) <= 1e-12
     # the diagonal (self) entries of G are the largest single-layer values
     assert np.all(np.abs(G.diagonal()) > 0)
