@@ -222,6 +222,52 @@ def timed_steps(ctx, stream, ks, F, G, Cv, flush, steps, warmup, precision, barr
     return dev_ms, wall, st
 
 
+def sweep_meshes():
+    """Sweep workload: sphere f=16 (2562 nodes), ellipsoid 3:2:1 f=28 (7842 nodes,
+    semi-axes 1, 2/3, 1/3), sphere f=45 (20252 nodes); linear triangles."""
+    from biegpu import mesh as bm
+    return [("sphere_2562", bm.icosphere(16)), ("ellipsoid_7842", bm.ellipsoid(28)),
+            ("sphere_20252", bm.icosphere(45))]
+
+
+def sweep_bench(args, rank, world, max_over_ranks):
+    """64 wavenumbers, ka uniform in [0.1, 10] (a = 1, the longest semi-axis),
+    boundary data seeded complex N(0,1) per node; every rank runs the whole
+    sweep on its own GPU (replicas).  Mixed assembly + refined GMRES is timed on
+    all 64 wavenumbers; the plain FP64 path on `sweep_fp64_k` of them, which
+    also give the relative surface-pressure error of the mixed path."""
+    import biegpu
+    named = sweep_meshes()
+    meshes = [m for _, m in named]
+    ks = np.linspace(0.1, 10.0, 64)
+    rng = np.random.default_rng(2026)
+    ws = [rng.normal(size=m.n_sources) + 1j * rng.normal(size=m.n_sources) for m in meshes]
+    biegpu.sweep(meshes, ks[:1], ws, precision="mixed", refine=True)      # warm-up (contexts, modules)
+    t0 = time.perf_counter()
+    pm, im = biegpu.sweep(meshes, ks, ws, precision="mixed", refine=True)
+    t_mixed = max_over_ranks(time.perf_counter() - t0)
+    sel = np.linspace(0, len(ks) - 1, max(1, args.sweep_fp64_k)).round().astype(int)
+    t0 = time.perf_counter()
+    p64, i64 = biegpu.sweep(meshes, ks[sel], ws, precision="fp64", refine=False)
+    t_fp64 = max_over_ranks(time.perf_counter() - t0)
+    errs = []
+    for a, b in zip(pm, p64):
+        for jj, j in enumerate(sel):
+            errs.append(float(np.linalg.norm(a[:, j] - b[:, jj]) / np.linalg.norm(b[:, jj])))
+    solves = im["solves"] * world
+    v_mixed = solves / t_mixed
+    v_fp64 = i64["solves"] * world / t_fp64
+    return {"metric": "sweep solves/s", "value": v_mixed, "unit": "solves/s",
+            "meshes": {n: m.n_sources for n, m in named}, "wavenumbers": len(ks), "solves": solves,
+            "seconds": t_mixed, "assemble_ms": im["assemble_ms"], "solve_ms": im["solve_ms"],
+            "converged": im["converged"], "gmres_iterations_mean": im["iterations"] / max(im["solves"], 1),
+            "plain_fp64": {"value": v_fp64, "unit": "solves/s", "solves": i64["solves"] * world,
+                           "seconds": t_fp64, "assemble_ms": i64["assemble_ms"], "solve_ms": i64["solve_ms"]},
+            "speedup_vs_plain_fp64": v_mixed / v_fp64,
+            "max_rel_err_vs_fp64": max(errs), "median_rel_err_vs_fp64": float(np.median(errs)),
+            "path": "mixed assembly + complex64 inner GMRES + complex128 residual (restart 20, reltol sqrt(eps))"}
+
+
 def roofline_entry(st, kernel, bound, peak_flops, workload_name, nphys):
     kernel_ms = st["timed_ms"] / max(st["timed_launches"], 1)
     flops = st["algorithmic_flops"] / max(st["timed_launches"], 1)
@@ -250,6 +296,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the frequency-sweep measurement")
+    ap.add_argument("--sweep-fp64-k", type=int, default=4,
+                    help="wavenumbers per mesh timed on the plain FP64 path (the error check set)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
@@ -352,6 +401,11 @@ def main():
                "h2d_bytes_per_step": int(tg.nbytes), "d2h_bytes_per_step": int(Fh.nbytes + Gh.nbytes + Ch.nbytes),
                "steps": n_e2e, "call": "bie_assemble (host buffers, pinned)"}
 
+    # ---- batched frequency sweep (configs[2]): sweep solves/s ---------------
+    sweep = None
+    if not args.no_sweep:
+        sweep = sweep_bench(args, rank, world, max_over_ranks)
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -370,7 +424,7 @@ def main():
         "dtype": "f32+f64" if args.precision == "mixed" else "f64",
         "precision": args.precision, "data": "synthetic",
         "config": dict(desc, l2="256 MB L2 flush between steps; each step writes 4.3 GB", parallelism=f"replicas{world}"),
-        "roofline": roofline, "plain_fp64": plain, "accuracy": accuracy,
+        "roofline": roofline, "plain_fp64": plain, "accuracy": accuracy, "sweep": sweep,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
         "clocks": clk.summary(), "gpu": torch.cuda.get_device_name(dev),
         "peaks": {"fp64_tflops": peaks["fp64_flops"] / 1e12, "fp32_tflops": peaks["fp32_flops"] / 1e12,
