@@ -242,9 +242,9 @@ def sweep_bench(args, rank, world, max_over_ranks):
     ks = np.linspace(0.1, 10.0, 64)
     rng = np.random.default_rng(2026)
     ws = [rng.normal(size=m.n_sources) + 1j * rng.normal(size=m.n_sources) for m in meshes]
-    biegpu.sweep(meshes, ks[:1], ws, precision="mixed", refine=True)      # warm-up (contexts, modules)
+    biegpu.sweep(meshes, ks[:1], ws, precision="mixed")      # warm-up (contexts, modules)
     t0 = time.perf_counter()
-    pm, im = biegpu.sweep(meshes, ks, ws, precision="mixed", refine=True)
+    pm, im = biegpu.sweep(meshes, ks, ws, precision="mixed")
     t_mixed = max_over_ranks(time.perf_counter() - t0)
     sel = np.linspace(0, len(ks) - 1, max(1, args.sweep_fp64_k)).round().astype(int)
     t0 = time.perf_counter()
@@ -265,7 +265,7 @@ def sweep_bench(args, rank, world, max_over_ranks):
                            "seconds": t_fp64, "assemble_ms": i64["assemble_ms"], "solve_ms": i64["solve_ms"]},
             "speedup_vs_plain_fp64": v_mixed / v_fp64,
             "max_rel_err_vs_fp64": max(errs), "median_rel_err_vs_fp64": float(np.median(errs)),
-            "path": "mixed assembly + complex64 inner GMRES + complex128 residual (restart 20, reltol sqrt(eps))"}
+            "path": "mixed assembly into complex64 matrices + GMRES with complex64 products and double-float sums (restart 20, reltol sqrt(eps))"}
 
 
 def roofline_entry(st, kernel, bound, peak_flops, workload_name, nphys):

@@ -189,13 +189,23 @@ __global__ void widen_kernel(const float4 *__restrict__ in, double2 *__restrict_
     }
 }
 
-// FP64 integration of the deferred pairs; results added with FP64 atomics.
-template <int NP, bool CPLX_K>
+__device__ __forceinline__ void add_entry(double2 *p, double re, double im) {
+    atomicAdd(&p->x, re);
+    atomicAdd(&p->y, im);
+}
+__device__ __forceinline__ void add_entry(float2 *p, double re, double im) {
+    atomicAdd(p, make_float2((float)re, (float)im));
+}
+
+// FP64 integration of the deferred pairs; results added atomically to the
+// complex128 output (or to the complex64 accumulators when the caller keeps
+// complex64 matrices).
+template <int NP, bool CPLX_K, typename T2>
 __global__ void __launch_bounds__(128)
 correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restrict__ defer_count,
                     unsigned int defer_cap, Fp64View v, const double *__restrict__ tgt, int64_t M,
-                    double kre, double kim, int flags, double2 *__restrict__ F,
-                    double2 *__restrict__ G, double *__restrict__ Cnear,
+                    double kre, double kim, int flags, T2 *__restrict__ F,
+                    T2 *__restrict__ G, double *__restrict__ Cnear,
                     unsigned long long *__restrict__ qpe_count) {
     const unsigned int n = min(*defer_count, defer_cap);
     const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
@@ -215,14 +225,8 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
 #pragma unroll
         for (int a = 0; a < NP; ++a) {
             const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
-            if (doF) {
-                atomicAdd(&F[off].x, fr[a]);
-                atomicAdd(&F[off].y, fi[a]);
-            }
-            if (doG) {
-                atomicAdd(&G[off].x, gr[a]);
-                atomicAdd(&G[off].y, gi[a]);
-            }
+            if (doF) add_entry(F + off, fr[a], fi[a]);
+            if (doG) add_entry(G + off, gr[a], gi[a]);
         }
         if (doC) atomicAdd(&Cnear[i], ce);
     }
@@ -262,6 +266,13 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
     const int64_t n2 = total / 2;
     const int tail = (int)(total & 1);
     const unsigned wgrid = (unsigned)std::min<int64_t>((n2 + 255) / 256, 8LL * c.num_sms * 8);
+    if (a.c64_out) {   // complex64 matrices requested: add the FP64 corrections in place
+        correct_fp64_kernel<NP, CPLX, float2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+            defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags, F32, G32, Cnear, c.d_qpe);
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+        return;
+    }
     if (a.flags & BIE_F) {
         widen_kernel<<<std::max(1u, wgrid), 256, 0, c.stream>>>(
             reinterpret_cast<const float4 *>(F32), reinterpret_cast<double2 *>(a.F), n2,
@@ -276,7 +287,7 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
         BIE_CUDA(cudaGetLastError());
         ++c.kernel_launches;
     }
-    correct_fp64_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+    correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
         defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
         reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe);
     BIE_CUDA(cudaGetLastError());
@@ -360,8 +371,14 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
     const int64_t N = c.n_sources;
     const size_t mat32 = (size_t)a.M * N * 8;
-    float2 *F32 = (a.flags & BIE_F) ? static_cast<float2 *>(c.scratch(kScratchF32, mat32)) : nullptr;
-    float2 *G32 = (a.flags & BIE_G) ? static_cast<float2 *>(c.scratch(kScratchG32, mat32)) : nullptr;
+    float2 *F32 = nullptr, *G32 = nullptr;
+    if (a.c64_out) {   // the caller's buffers are the complex64 accumulators
+        F32 = (a.flags & BIE_F) ? reinterpret_cast<float2 *>(a.F) : nullptr;
+        G32 = (a.flags & BIE_G) ? reinterpret_cast<float2 *>(a.G) : nullptr;
+    } else {
+        F32 = (a.flags & BIE_F) ? static_cast<float2 *>(c.scratch(kScratchF32, mat32)) : nullptr;
+        G32 = (a.flags & BIE_G) ? static_cast<float2 *>(c.scratch(kScratchG32, mat32)) : nullptr;
+    }
     if (F32) BIE_CUDA(cudaMemsetAsync(F32, 0, mat32, c.stream));
     if (G32) BIE_CUDA(cudaMemsetAsync(G32, 0, mat32, c.stream));
     if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;

@@ -197,6 +197,7 @@ struct AssembleArgs {
     int64_t M;
     int flags;
     double *F, *G, *C;       // device outputs (interleaved complex), may be null
+    bool c64_out = false;    // mixed only: F, G are complex64 (float2) buffers, not widened
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);

@@ -60,6 +60,109 @@ dense_gemv_kernel(const T2 *__restrict__ A, int64_t n, const double2 *__restrict
     if (i < n) part[(int64_t)s * n + i] = make_double2(re, im);
 }
 
+// Complex64 matrix times complex128 vector on the FP32 pipe, for the column
+// slice of blockIdx.y.  On GB300 the FP64 pipe cannot keep up with HBM even for
+// a matrix-vector product, so the products run in FP32 with the vector split
+// into double-float (x = hi + lo): a * hi is formed exactly (TwoProduct), a * lo
+// is added to its error term, and the sums are carried in double-float (TwoSum).
+// The result is the stored complex64 operator applied to x to ~1e-14 relative
+// — exact enough for GMRES to converge to sqrt(eps) on that operator.
+// Each thread handles two consecutive rows (one 16-byte load per column).
+__global__ void __launch_bounds__(kT)
+dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *__restrict__ x,
+                      double2 *__restrict__ part, int S) {
+    const int64_t r2 = (int64_t)blockIdx.x * kT + threadIdx.x;   // row pair index
+    const int64_t i0 = 2 * r2;
+    const int s = blockIdx.y;
+    const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
+    __shared__ float4 xs[kT];   // (re hi, re lo, im hi, im lo)
+    dev::df yr0 = {0.f, 0.f}, yi0 = {0.f, 0.f}, yr1 = {0.f, 0.f}, yi1 = {0.f, 0.f};
+    const int64_t ld2 = n / 2;  // float4 per column (n even)
+    for (int64_t jb = j0; jb < j1; jb += kT) {
+        const int nb = (int)min((int64_t)kT, j1 - jb);
+        __syncthreads();
+        if (threadIdx.x < nb) {
+            const double2 v = x[jb + threadIdx.x];
+            const dev::df re = dev::df_from_double(v.x), im = dev::df_from_double(v.y);
+            xs[threadIdx.x] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
+        __syncthreads();
+        if (i0 < n) {
+            const float4 *col = A2 + jb * ld2 + r2;
+#pragma unroll 4
+            for (int j = 0; j < nb; ++j) {
+                const float4 a = col[(int64_t)j * ld2];   // (re0, im0, re1, im1)
+                const float4 xv = xs[j];
+                // y += a x, real and imaginary parts, two rows
+                auto mac = [](dev::df &acc, float av, float xh, float xl) {
+                    const float p = av * xh;
+                    float e = __fmaf_rn(av, xh, -p);
+                    e = __fmaf_rn(av, xl, e);
+                    const dev::df t = dev::two_sum(acc.hi, p);
+                    acc = dev::fast_two_sum(t.hi, __fadd_rn(__fadd_rn(t.lo, e), acc.lo));
+                };
+                mac(yr0, a.x, xv.x, xv.y);
+                mac(yr0, -a.y, xv.z, xv.w);
+                mac(yi0, a.x, xv.z, xv.w);
+                mac(yi0, a.y, xv.x, xv.y);
+                mac(yr1, a.z, xv.x, xv.y);
+                mac(yr1, -a.w, xv.z, xv.w);
+                mac(yi1, a.z, xv.z, xv.w);
+                mac(yi1, a.w, xv.x, xv.y);
+            }
+        }
+    }
+    if (i0 < n) {
+        part[(int64_t)s * n + i0] = make_double2(dev::f2d(yr0.hi) + dev::f2d(yr0.lo),
+                                                 dev::f2d(yi0.hi) + dev::f2d(yi0.lo));
+        if (i0 + 1 < n)
+            part[(int64_t)s * n + i0 + 1] = make_double2(dev::f2d(yr1.hi) + dev::f2d(yr1.lo),
+                                                         dev::f2d(yi1.hi) + dev::f2d(yi1.lo));
+    }
+}
+
+// Same product for odd n: one row per thread, 8-byte loads.
+__global__ void __launch_bounds__(kT)
+dense_gemv_c64_rows_kernel(const float2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
+                           double2 *__restrict__ part, int S) {
+    const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
+    const int s = blockIdx.y;
+    const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
+    __shared__ float4 xs[kT];
+    dev::df yr = {0.f, 0.f}, yi = {0.f, 0.f};
+    for (int64_t jb = j0; jb < j1; jb += kT) {
+        const int nb = (int)min((int64_t)kT, j1 - jb);
+        __syncthreads();
+        if (threadIdx.x < nb) {
+            const double2 v = x[jb + threadIdx.x];
+            const dev::df re = dev::df_from_double(v.x), im = dev::df_from_double(v.y);
+            xs[threadIdx.x] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
+        __syncthreads();
+        if (i < n) {
+            const float2 *col = A + jb * n + i;
+            for (int j = 0; j < nb; ++j) {
+                const float2 a = col[(int64_t)j * n];
+                const float4 xv = xs[j];
+                auto mac = [](dev::df &acc, float av, float xh, float xl) {
+                    const float p = av * xh;
+                    float e = __fmaf_rn(av, xh, -p);
+                    e = __fmaf_rn(av, xl, e);
+                    const dev::df t = dev::two_sum(acc.hi, p);
+                    acc = dev::fast_two_sum(t.hi, __fadd_rn(__fadd_rn(t.lo, e), acc.lo));
+                };
+                mac(yr, a.x, xv.x, xv.y);
+                mac(yr, -a.y, xv.z, xv.w);
+                mac(yi, a.x, xv.z, xv.w);
+                mac(yi, a.y, xv.x, xv.y);
+            }
+        }
+    }
+    if (i < n)
+        part[(int64_t)s * n + i] = make_double2(dev::f2d(yr.hi) + dev::f2d(yr.lo),
+                                                dev::f2d(yi.hi) + dev::f2d(yi.lo));
+}
+
 // y = s * sum_slices(part) + d .* x   (d may be null)
 __global__ void combine_kernel(const double2 *__restrict__ part, int S, int64_t n, double2 sc,
                                const double2 *__restrict__ d, const double2 *__restrict__ x,
@@ -182,9 +285,10 @@ struct Solver {
     std::vector<double2> hhost;
 
     Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_) {
+        // column slices: ~8 blocks per SM for the two-rows-per-thread complex64 product
         S = 1;
-        const int64_t row_tiles = (n + kT - 1) / kT;
-        while (row_tiles * S < 4LL * c.num_sms && S < 64) S *= 2;
+        const int64_t row_tiles = (n / 2 + kT - 1) / kT;
+        while (row_tiles * S < 8LL * c.num_sms && S < 64) S *= 2;
         nbdot = (int)std::min<int64_t>(std::max<int64_t>(1, (n + kT * 8 - 1) / (kT * 8)), 256);
         const size_t part_bytes = (size_t)std::max<int64_t>(S * n, (int64_t)(restart + 2) * nbdot) * 16;
         char *base = static_cast<char *>(c.scratch(kScratchSolverPart, part_bytes + (size_t)(restart + 2) * 16));
@@ -200,14 +304,22 @@ struct Solver {
         const double2 sc = make_double2(op.scale_re, op.scale_im);
         const double2 *d = reinterpret_cast<const double2 *>(op.diag);
         if (op.kind == BIE_OP_DENSE) {
-            dim3 grid(blocks(n, kT), (unsigned)S);
             cudaEvent_t t0 = c.timer_begin();
-            if (precision == BIE_PREC_MIXED && op.A32)
-                dense_gemv_kernel<float2><<<grid, kT, 0, c.stream>>>(
-                    reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
-            else
+            if (op.A32 && (precision == BIE_PREC_MIXED || !op.A)) {
+                if (n % 2 == 0) {
+                    dim3 grid(blocks(n / 2, kT), (unsigned)S);
+                    dense_gemv_c64_kernel<<<grid, kT, 0, c.stream>>>(
+                        reinterpret_cast<const float4 *>(op.A32), n, x, part, S);
+                } else {
+                    dim3 grid(blocks(n, kT), (unsigned)S);
+                    dense_gemv_c64_rows_kernel<<<grid, kT, 0, c.stream>>>(
+                        reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
+                }
+            } else {
+                dim3 grid(blocks(n, kT), (unsigned)S);
                 dense_gemv_kernel<double2><<<grid, kT, 0, c.stream>>>(
                     reinterpret_cast<const double2 *>(op.A), n, x, part, S);
+            }
             BIE_CUDA(cudaGetLastError());
             c.timer_end(t0);
             launched();

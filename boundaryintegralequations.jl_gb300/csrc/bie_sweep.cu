@@ -3,9 +3,11 @@
 // Work queue: every (mesh, k) item runs on the mesh context's stream:
 //   1. dense assembly of F, G, C (mixed or FP64 kernels of this library),
 //   2. diag = 1 - C, b = G w (the library's dense product),
-//   3. GMRES on (F + Diagonal(1 - C)) p = b: with refinement, the inner
-//      iterations use a complex64 copy of F (half the HBM traffic per product)
-//      and the outer residual the complex128 F,
+//   3. GMRES on (F + Diagonal(1 - C)) p = b.  Mixed precision keeps F and G
+//      in complex64 end to end (the assembly's FP32 accumulators with the FP64
+//      near-pair corrections added in place; products with FP32 arithmetic and
+//      double-float sums, half the HBM bytes of complex128); FP64 uses
+//      complex128 matrices and FP64 products,
 //   4. p copied into the caller's host array (pinned or not).
 // Each mesh's device buffers are allocated once for its whole frequency list;
 // frequencies of a mesh reuse them (assemble -> solve -> overwrite), so a
@@ -46,11 +48,12 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
         std::lock_guard<std::mutex> lock(c.mu);
         BIE_CUDA(cudaSetDevice(c.device));
         const int64_t N = c.n_sources;
-        const size_t mat = (size_t)N * N * 16;
+        // mixed: complex64 matrices end to end (assembly accumulators with the FP64
+        // corrections added in place, complex64 products with double-float sums);
+        // FP64: complex128 matrices and FP64 products
+        const bool mixed = o.precision == BIE_PREC_MIXED;
+        const size_t mat = (size_t)N * N * (mixed ? 8 : 16);
         DevBuf F(mat), G(mat), vec(6 * (size_t)N * 16);
-        std::unique_ptr<DevBuf> A32;
-        const bool refine = o.refine && o.precision == BIE_PREC_MIXED;
-        if (refine) A32.reset(new DevBuf((size_t)N * N * 8));
         double2 *Cv = vec.as<double2>(), *dg = Cv + N, *b = dg + N, *x = b + N, *wd = x + N;
         BIE_CUDA(cudaMemcpyAsync(wd, w[m], (size_t)N * 16, cudaMemcpyHostToDevice, c.stream));
         cudaEvent_t e0, e1, e2;
@@ -62,7 +65,8 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
             BIE_CUDA(cudaEventRecord(e0, c.stream));
             AssembleArgs a{kr, ki, c.d_sources, N, BIE_F | BIE_G | BIE_C, F.as<double>(), G.as<double>(),
                            reinterpret_cast<double *>(Cv)};
-            if (o.precision == BIE_PREC_MIXED) launch_assemble_mixed(c, a);
+            a.c64_out = mixed;
+            if (mixed) launch_assemble_mixed(c, a);
             else launch_assemble_fp64(c, a);
             BIE_CUDA(cudaEventRecord(e1, c.stream));
             one_minus_kernel<<<(unsigned)((N + 255) / 256), 256, 0, c.stream>>>(Cv, dg, N);
@@ -71,23 +75,21 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
             // b = G w
             bie_operator gop{};
             gop.kind = BIE_OP_DENSE;
-            gop.A = G.as<double>();
+            if (mixed) gop.A32 = G.as<float>();
+            else gop.A = G.as<double>();
             gop.scale_re = 1.0;
-            apply_operator(c, gop, BIE_PREC_FP64, reinterpret_cast<const double *>(wd),
-                           reinterpret_cast<double *>(b));
+            apply_operator(c, gop, mixed ? BIE_PREC_MIXED : BIE_PREC_FP64,
+                           reinterpret_cast<const double *>(wd), reinterpret_cast<double *>(b));
             // (F + Diagonal(1 - C)) p = b
             bie_operator op{};
             op.kind = BIE_OP_DENSE;
-            op.A = F.as<double>();
+            if (mixed) op.A32 = F.as<float>();
+            else op.A = F.as<double>();
             op.scale_re = 1.0;
             op.diag = reinterpret_cast<const double *>(dg);
-            if (refine) {
-                round_to_c64(c, F.as<double>(), A32->as<float>(), (int64_t)N * N);
-                op.A32 = A32->as<float>();
-            }
             bie_gmres_opts go = o.gmres;
-            go.refine = refine ? 1 : 0;
-            go.precision = BIE_PREC_FP64;
+            go.refine = 0;
+            go.precision = mixed ? BIE_PREC_MIXED : BIE_PREC_FP64;
             go.initially_nonzero = 0;
             bie_gmres_info gi{};
             run_gmres(c, op, reinterpret_cast<const double *>(b), reinterpret_cast<double *>(x), go, gi);
