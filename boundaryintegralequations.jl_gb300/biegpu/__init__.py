@@ -12,5 +12,6 @@ from .assembly import Context, assemble_parallel, get_context, quadrature_rule  
 from .mesh import Mesh3d, ellipsoid, icosphere, load_comsol, read_comsol  # noqa: F401
 from .operators import Diagonal, GPUFOperator, GPUGOperator, I, UniformScaling, gmres  # noqa: F401
 from .sweep import sweep  # noqa: F401
+from .adjoint import farfield_objective  # noqa: F401
 
 __version__ = "0.1.0"

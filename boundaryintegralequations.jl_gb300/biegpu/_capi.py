@@ -139,6 +139,15 @@ class SweepInfo(C.Structure):
     ]
 
 
+class AdjointOpts(C.Structure):
+    _fields_ = [("rho_c", C.c_double), ("dir", C.c_double * 3), ("reltol", C.c_double)]
+
+
+class AdjointInfo(C.Structure):
+    _fields_ = [("forward_iterations", C.c_int32), ("forward_converged", C.c_int32),
+                ("adjoint_iterations", C.c_int32), ("adjoint_converged", C.c_int32)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -170,6 +179,8 @@ SIGNATURES = {
     "bie_round_c64_device": (_I, [_P, _P, _P, _I64]),
     "bie_sweep": (_I, [C.POINTER(_P), _I, _P, _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(SweepOpts),
                        C.POINTER(SweepInfo), _P]),
+    "bie_adjoint": (_I, [_P, _D, _D, _P, _P, _I64, C.POINTER(AdjointOpts), C.POINTER(_D), _P, _P, _P,
+                         C.POINTER(AdjointInfo)]),
 }
 
 

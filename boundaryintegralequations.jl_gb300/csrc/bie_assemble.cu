@@ -40,7 +40,8 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
                      const double *__restrict__ tgt, int64_t M, double kre, double kim,
                      int flags, double2 *__restrict__ F, double2 *__restrict__ G,
                      double *__restrict__ Cpart, int chunk,
-                     unsigned long long *__restrict__ qpe_count) {
+                     unsigned long long *__restrict__ qpe_count,
+                     const double2 *__restrict__ gweight) {
     extern __shared__ __align__(16) double smem[];
     double *s_phi = smem;                                   // nphi doubles (padded even)
     double *s_rec = smem + ((nphi + 1) & ~1);               // chunk * stride doubles
@@ -85,6 +86,15 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
             cacc += dev::element_fp64<NP, CPLX_K>(r + ri.off[c], Q, s_phi + (size_t)c * qmax * NP,
                                                   tx, ty, tz, kre, kim, fr, fi, gr, gi);
 
+            if (gweight && doG) {   // element factor on the single layer
+                const double2 wgt = gweight[cb + el];
+#pragma unroll
+                for (int a = 0; a < NP; ++a) {
+                    const double t = gr[a] * wgt.x - gi[a] * wgt.y;
+                    gi[a] = gr[a] * wgt.y + gi[a] * wgt.x;
+                    gr[a] = t;
+                }
+            }
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
             const uint32_t m = s_mask[el];
 #pragma unroll
@@ -140,7 +150,8 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int
         c.d_records, L.stride, L.nidx_off, c.n_elements, S,
         c.d_shared_mask + (size_t)level * c.n_elements, c.d_phi, L.R * L.qmax * L.NP, L.qmax,
         ri, a.targets, a.M, a.k_re, a.k_im, a.flags, reinterpret_cast<double2 *>(a.F),
-        reinterpret_cast<double2 *>(a.G), Cpart, chunk, c.d_qpe);
+        reinterpret_cast<double2 *>(a.G), Cpart, chunk, c.d_qpe,
+        reinterpret_cast<const double2 *>(a.g_weight));
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;

@@ -370,6 +370,39 @@ int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk, const d
     });
 }
 
+int bie_adjoint(bie_ctx *ctx, double k_re, double k_im, const double *Z, const double *field,
+                int64_t n_field, const bie_adjoint_opts *opts, double *J, double *pf, double *dX,
+                double *dZ, bie_adjoint_info *info) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!Z || !field || n_field <= 0 || !opts || !J)
+            bie::fail(BIE_ERR_INVALID, "Z, field, opts and J must be given (n_field > 0)");
+        if (!std::isfinite(k_re) || !std::isfinite(k_im) || !(opts->rho_c > 0))
+            bie::fail(BIE_ERR_INVALID, "k must be finite and rho_c positive");
+        const double dn = std::sqrt(opts->dir[0] * opts->dir[0] + opts->dir[1] * opts->dir[1] +
+                                    opts->dir[2] * opts->dir[2]);
+        if (!(std::fabs(dn - 1.0) < 1e-12)) bie::fail(BIE_ERR_INVALID, "dir must be a unit vector");
+        for (int64_t e = 0; e < 2 * c.n_elements; e += 2)
+            if (!std::isfinite(Z[e]) || !std::isfinite(Z[e + 1]) || (Z[e] == 0 && Z[e + 1] == 0))
+                bie::fail(BIE_ERR_INVALID, "impedances must be finite and non-zero");
+        for (int64_t i = 0; i < 3 * n_field; ++i)
+            if (!std::isfinite(field[i])) bie::fail(BIE_ERR_INVALID, "non-finite field point");
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie::AdjointArgs a{k_re, k_im, opts->rho_c, Z, {opts->dir[0], opts->dir[1], opts->dir[2]},
+                           field, n_field, opts->reltol, pf, dX, dZ};
+        bie::AdjointOut o;
+        bie::run_adjoint(c, a, o);
+        *J = o.J;
+        if (info) {
+            info->forward_iterations = o.forward_iterations;
+            info->forward_converged = o.forward_converged;
+            info->adjoint_iterations = o.adjoint_iterations;
+            info->adjoint_converged = o.adjoint_converged;
+        }
+    });
+}
+
 int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n) {
     return guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);

@@ -198,6 +198,8 @@ struct AssembleArgs {
     int flags;
     double *F, *G, *C;       // device outputs (interleaved complex), may be null
     bool c64_out = false;    // mixed only: F, G are complex64 (float2) buffers, not widened
+    const double *g_weight = nullptr;   // FP64 only: per-element complex factor on G
+                                        // (Morton record order), e.g. an element admittance
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
@@ -226,6 +228,25 @@ void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
 // Frequency sweep (bie_sweep.cu); locks each context while it runs.
 void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,
                double *const *p, const bie_sweep_opts &o, bie_sweep_info &info, int32_t *iters);
+// Adjoint shape / impedance gradient (bie_adjoint.cu); host pointers
+struct AdjointArgs {
+    double k_re, k_im, rho_c;
+    const double *Z;         // E complex element impedances (original element order)
+    double dir[3];           // incident direction (unit)
+    const double *field;     // 3 x n_field
+    int64_t n_field;
+    double reltol;           // GMRES tolerance of the forward and adjoint solves
+    double *pf;              // out: n_field complex field pressures (may be null)
+    double *dX;              // out: 3 x N vertex gradient (may be null)
+    double *dZ;              // out: E complex (dJ/dRe Z, dJ/dIm Z) (may be null)
+};
+struct AdjointOut {
+    double J = 0;
+    int forward_iterations = 0, forward_converged = 0;
+    int adjoint_iterations = 0, adjoint_converged = 0;
+};
+void run_adjoint(Ctx &c, const AdjointArgs &a, AdjointOut &out);
+
 // y = s (K x) + diag .* x on the context stream (device vectors of length N)
 void apply_operator(Ctx &c, const bie_operator &op, int precision, const double *x, double *y);
 

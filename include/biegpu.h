@@ -339,6 +339,37 @@ BIE_API int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk,
                       const double *const *w, double *const *p, const bie_sweep_opts *opts,
                       bie_sweep_info *info, int32_t *iters);
 
+/* ---- adjoint shape / impedance gradient ------------------------------- */
+typedef struct bie_adjoint_opts {
+    double rho_c;        /* characteristic impedance rho0 c of the fluid (e.g. 1.21 * 343) */
+    double dir[3];       /* incident plane-wave direction (unit vector)                  */
+    double reltol;       /* GMRES tolerance of the forward and adjoint solves (<= 0: 1e-13) */
+} bie_adjoint_opts;
+
+typedef struct bie_adjoint_info {
+    int32_t forward_iterations, forward_converged;
+    int32_t adjoint_iterations, adjoint_converged;
+} bie_adjoint_info;
+
+/*
+ * Far-field objective and its gradient (3-node triangles, nodal physics on the
+ * vertices, real k).  Forward model: (F + Diagonal(1 - C) - i rho c k G_Y) p =
+ * p_I with G_Y the single layer weighted by the element admittances 1 / Z_e
+ * (impedance condition v_n = p / Z on each element), p_I = exp(-i k dir.x)
+ * (incoming_wave, src/analytical/3d_scattering.jl:4-12); field pressures
+ * p_f = p_I + (-F_x + i rho c k G_{x,Y}) p at the M field points; J = sum |p_f|^2.
+ * The reference has no gradient code (its only prior art is finite differences
+ * in 2D, examples/2d_optimization.jl:187-219; nodal impedance form
+ * examples/3d_cube_wave_anechoic.jl:62-68).  Gradients by the adjoint method
+ * with a reverse pass that recomputes the quadrature (FP64):
+ *   dX: 3 x N_c, dJ/d(vertex coordinates);  dZ: E complex, dJ/dRe Z_e + i dJ/dIm Z_e.
+ * Z: E complex impedances in the element order of the mesh.  Outputs may be
+ * NULL (J alone costs one forward solve).  Host buffers; blocking.
+ */
+BIE_API int bie_adjoint(bie_ctx *ctx, double k_re, double k_im, const double *Z,
+                        const double *field, int64_t n_field, const bie_adjoint_opts *opts,
+                        double *J, double *pf, double *dX, double *dZ, bie_adjoint_info *info);
+
 /* out[i] = (complex64) in[i] for n complex entries (device), e.g. to build
  * bie_operator.A32 from an assembled matrix. */
 BIE_API int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n);

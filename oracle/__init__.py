@@ -60,6 +60,9 @@ def lib():
             L.oracle_rule.argtypes = [I, I, I, P, P, P]
             L.oracle_total_weight.restype = D
             L.oracle_total_weight.argtypes = [P, P, I, I64, I, I]
+            L.oracle_assemble_w.restype = I
+            L.oracle_assemble_w.argtypes = [P, I64, P, I, P, I, I64, P, I64, P, I64, I, I, D, D, I,
+                                             P, P, P, I, P]
             L.oracle_singular_rule.restype = I
             L.oracle_singular_rule.argtypes = [I, D, P, P, P, I]
             L.oracle_nearfield.restype = I
@@ -152,7 +155,25 @@ def nearfield(mesh, k, depth=1, offset=0.0, coarse=False, n_gauss=3, fOn=True, g
     return row_ptr, cols, F, G
 
 
-def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, threads=0):
+def farfield_objective(mesh, k, Z, field_points, rho_c=1.21 * 343.0, direction=(0.0, 0.0, 1.0), n=2, m=2):
+    """J = sum |p(x_f)|^2 of the impedance scattering model, by dense oracle
+    assembly and a direct solve:
+      (F + Diagonal(1 - C) - i rho c k G_Y) p = p_I,  p_f = p_I(x_f) + (-F_x + i rho c k G_xY) p,
+    G_Y = single layer with element factors 1 / Z_e, p_I = exp(-i k d.x)."""
+    d = np.asarray(direction, dtype=np.float64)
+    d = d / np.linalg.norm(d)
+    Y = np.ascontiguousarray(1.0 / np.asarray(Z, dtype=np.complex128))
+    F, G, Cv = assemble(mesh, k, n=n, m=m, g_weight=Y)
+    A = F + np.diag(1.0 - Cv) - 1j * rho_c * k * G
+    pI = np.exp(-1j * k * (d @ mesh.sources))
+    p = np.linalg.solve(A, pI)
+    X = np.asarray(field_points, dtype=np.float64)
+    Fx, Gx, _ = assemble(mesh, k, targets=X, n=n, m=m, cOn=False, g_weight=Y)
+    pf = np.exp(-1j * k * (d @ X)) + (-Fx + 1j * rho_c * k * Gx) @ p
+    return float(np.sum(np.abs(pf) ** 2)), pf
+
+
+def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, threads=0, g_weight=None):
     """Reference-algorithm (F, G, C) on the CPU; F, G are M x N Fortran-ordered."""
     k = complex(k)
     c = np.asfortranarray(mesh.coordinates, dtype=np.float64)
@@ -166,8 +187,9 @@ def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, thre
     Cv = np.zeros(M, dtype=np.complex128) if cOn else None
     flags = (1 if fOn else 0) | (2 if gOn else 0) | (4 if cOn else 0)
     addr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
-    lib().oracle_assemble(c.ctypes.data, c.shape[1], t.ctypes.data, _KIND[mesh.shape_function],
-                          pt.ctypes.data, _KIND[mesh.physics_function], t.shape[1], s.ctypes.data,
-                          N, tg.ctypes.data, M, n, m, k.real, k.imag, flags, addr(F), addr(G),
-                          addr(Cv), int(threads))
+    gw = None if g_weight is None else np.ascontiguousarray(g_weight, dtype=np.complex128)
+    lib().oracle_assemble_w(c.ctypes.data, c.shape[1], t.ctypes.data, _KIND[mesh.shape_function],
+                            pt.ctypes.data, _KIND[mesh.physics_function], t.shape[1], s.ctypes.data,
+                            N, tg.ctypes.data, M, n, m, k.real, k.imag, flags, addr(F), addr(G),
+                            addr(Cv), int(threads), addr(gw))
     return F, G, Cv

@@ -248,10 +248,25 @@ double oracle_total_weight(const double *coords, const int64_t *topo, int skind,
  * sources 3xN (mesh.sources: physics-node coordinates), targets 3xM.
  * F, G: M x N complex column-major (interleaved doubles), C: M complex.
  */
+int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int skind,
+                      const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
+                      const double *targets, int64_t M, int n, int m, double kre, double kim,
+                      int flags, double *F, double *G, double *C, int nthreads, const double *gw);
+
 int oracle_assemble(const double *coords, int64_t Nc, const int64_t *topo, int skind,
                     const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
                     const double *targets, int64_t M, int n, int m, double kre, double kim,
                     int flags, double *F, double *G, double *C, int nthreads) {
+    return oracle_assemble_w(coords, Nc, topo, skind, ptopo, pkind, E, sources, N, targets, M, n, m,
+                             kre, kim, flags, F, G, C, nthreads, NULL);
+}
+
+/* Same assembly with an optional per-element complex factor gw[e] (E complex)
+ * on the single-layer contributions (element admittance weighting). */
+int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int skind,
+                      const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
+                      const double *targets, int64_t M, int n, int m, double kre, double kim,
+                      int flags, double *F, double *G, double *C, int nthreads, const double *gw) {
     (void)Nc;
     const int NP = nnodes(pkind);
     const int R = (skind == OR_LINEAR) ? 3 : NP;
@@ -316,6 +331,7 @@ int oracle_assemble(const double *coords, int64_t Nc, const int64_t *topo, int s
                 for (int a = 0; a < NP; ++a) {                                      /* mygemm_vec! */
                     double complex acc = 0.0;
                     for (int q = 0; q < Qr; ++q) acc += integrand[q] * phi[q * NP + a];
+                    if (gw) acc *= gw[2 * e] + I * gw[2 * e + 1];
                     double *g = G + 2 * ((size_t)(pn[a] - 1) * M + i);
                     g[0] += creal(acc);
                     g[1] += cimag(acc);
