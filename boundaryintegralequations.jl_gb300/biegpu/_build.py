@@ -29,6 +29,7 @@ SOURCES = [
     "bie_nearfield.cu",
     "bie_sweep.cu",
     "bie_adjoint.cu",
+    "bie_lowp.cu",
     "bie_peaks.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -29,9 +29,14 @@ BIE_C = 4
 
 BIE_PREC_FP64 = 0
 BIE_PREC_MIXED = 1
+BIE_PREC_FP16 = 2
+BIE_PREC_BF16 = 3
+BIE_PREC_FP16_SPLIT = 4
+BIE_PREC_BF16_SPLIT = 5
 
 KIND = {"linear": BIE_TRI_LINEAR, "quadratic": BIE_TRI_QUADRATIC}
-PRECISION = {"fp64": BIE_PREC_FP64, "mixed": BIE_PREC_MIXED}
+PRECISION = {"fp64": BIE_PREC_FP64, "mixed": BIE_PREC_MIXED, "fp16": BIE_PREC_FP16, "bf16": BIE_PREC_BF16,
+             "fp16_split": BIE_PREC_FP16_SPLIT, "bf16_split": BIE_PREC_BF16_SPLIT}
 
 _ERRNAMES = {
     BIE_ERR_INVALID: "invalid argument",
@@ -172,6 +177,8 @@ SIGNATURES = {
     "bie_matvec": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
     "bie_matvec_device": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
     "bie_matvec_device_noalloc": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P]),
+    "bie_matvec_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
+    "bie_lowp_gemm_device": (_I, [_P, _I, _I64, _I64, _I64, _P, _P, _P]),
     "bie_singular_rule": (_I, [_I, _D, _P, _P, _P, _I, C.POINTER(_I)]),
     "bie_nearfield_pattern": (_I, [_P, _I, C.POINTER(_I64), _P, _P]),
     "bie_nearfield_assemble": (_I, [_P, _D, _D, _I, _D, _I, _I, _I, _P, _P]),

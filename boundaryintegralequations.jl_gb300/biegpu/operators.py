@@ -137,10 +137,14 @@ class _MatrixFreeOperator:
     which = "F"
 
     def __init__(self, mesh: Mesh3d, k, n: int = 2, m: int = 2, precision: str = "mixed",
-                 device: int = 0):
+                 device: int = 0, multi_precision: str | None = "fp16_split"):
         self.mesh = mesh
         self.k = complex(k)
         self.precision = precision
+        # arithmetic of products with a matrix of right-hand sides: a 16-bit
+        # tensor-core form ("fp16", "bf16", "fp16_split", "bf16_split") or None
+        # for one `precision` product per column
+        self.multi_precision = multi_precision
         self.ctx = get_context(mesh, n=n, m=m, device=device)
         N = mesh.n_sources
         self.shape = (N, N)
@@ -178,13 +182,31 @@ class _MatrixFreeOperator:
         _capi.check(L.bie_matvec(self.ctx.handle, self.k.real, self.k.imag, _capi.ptr(t), M, *args, prec))
         return y
 
+    def _apply_multi(self, X):
+        """Y = K X for an N x R matrix (bie_matvec_multi_device): the matrix form
+        of `_unsafe_mul!(Y, A, X::AbstractMatrix)` (src/3d/fast_multipole_method.jl:
+        249-287, 427-471)."""
+        torch = _torch()
+        on_device = _is_torch(X) and X.is_cuda
+        dev = X.device if on_device else torch.device(f"cuda:{self.ctx.device}")
+        Xd = torch.as_tensor(X, dtype=torch.complex128, device=dev) if not _is_torch(X) else \
+            X.to(device=dev, dtype=torch.complex128)
+        N, R = Xd.shape
+        Xd = Xd.T.contiguous().T   # column-major
+        Y = torch.empty((R, N), dtype=torch.complex128, device=dev).T
+        prec = self.multi_precision or self.precision
+        args = (Xd.data_ptr(), None, Y.data_ptr(), None) if self.which == "F" else \
+               (None, Xd.data_ptr(), None, Y.data_ptr())
+        torch.cuda.synchronize(dev)
+        _capi.check(_capi.lib().bie_matvec_multi_device(self.ctx.handle, self.k.real, self.k.imag, R, *args,
+                                                        _capi.PRECISION[prec], 0))
+        torch.cuda.synchronize(dev)
+        return Y if on_device else Y.cpu().numpy()
+
     def __matmul__(self, x):
         x = np.asarray(x) if not _is_torch(x) else x
         if x.ndim == 2:
-            cols = [self._apply(x[:, j]) for j in range(x.shape[1])]
-            if _is_torch(x):
-                return _torch().stack(cols, dim=1)
-            return np.stack(cols, axis=1)
+            return self._apply_multi(x)
         return self._apply(x)
 
     def evaluate_targets(self, x, targets):

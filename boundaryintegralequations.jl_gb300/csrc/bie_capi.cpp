@@ -261,6 +261,39 @@ int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im, const doub
     });
 }
 
+int bie_matvec_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *d_X,
+                            const double *d_V, double *d_YF, double *d_YG, int precision,
+                            int64_t scratch_bytes) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (!std::isfinite(k_re) || !std::isfinite(k_im)) bie::fail(BIE_ERR_INVALID, "k must be finite");
+        if (nrhs <= 0) bie::fail(BIE_ERR_INVALID, "nrhs must be positive");
+        if (precision < BIE_PREC_FP64 || precision > BIE_PREC_BF16_SPLIT)
+            bie::fail(BIE_ERR_INVALID, "unknown precision");
+        if (!d_X && !d_V) bie::fail(BIE_ERR_INVALID, "neither X nor V given");
+        if (d_X && !d_YF) bie::fail(BIE_ERR_INVALID, "X given without YF");
+        if (d_V && !d_YG) bie::fail(BIE_ERR_INVALID, "V given without YG");
+        if (scratch_bytes < 0) bie::fail(BIE_ERR_INVALID, "scratch_bytes must be >= 0");
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie::MultiArgs a{k_re, k_im, nrhs, d_X, d_V, d_YF, d_YG, precision, scratch_bytes};
+        bie::run_matvec_multi(c, a);
+    });
+}
+
+int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int64_t K, const float *d_A,
+                         const float *d_B, double *d_C) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (!d_A || !d_B || !d_C) bie::fail(BIE_ERR_INVALID, "A, B and C must not be NULL");
+        if (precision < BIE_PREC_FP16 || precision > BIE_PREC_BF16_SPLIT)
+            bie::fail(BIE_ERR_INVALID, "precision must be one of the 16-bit tensor-core forms");
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie::run_lowp_gemm(c, precision, M, N, K, d_A, d_B, d_C);
+    });
+}
+
 int bie_singular_rule(int node, double offset, double *u, double *v, double *w, int capacity,
                       int *count) {
     return guarded([&] {

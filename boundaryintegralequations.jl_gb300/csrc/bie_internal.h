@@ -86,7 +86,8 @@ enum ScratchSlot {
     kScratchMatvecPart = 9,// per-slice partial products
     kScratchSolver = 10,   // GMRES workspace
     kScratchSolverPart = 11,  // GMRES reduction partials and small coefficient vectors
-    kScratchCount = 12
+    kScratchLowp = 12,     // multi-RHS products: strips, 16-bit tiles, partial sums
+    kScratchCount = 13
 };
 
 // Mixed-precision element record (32-bit words, same element order as the FP64
@@ -246,6 +247,19 @@ struct AdjointOut {
     int adjoint_iterations = 0, adjoint_converged = 0;
 };
 void run_adjoint(Ctx &c, const AdjointArgs &a, AdjointOut &out);
+
+// K4: products with many right-hand sides (bie_lowp.cu)
+struct MultiArgs {
+    double k_re, k_im;
+    int64_t nrhs;
+    const double *X, *V;     // N x nrhs complex (device), null: skip that product
+    double *YF, *YG;         // N x nrhs complex outputs
+    int precision;           // BIE_PREC_*
+    int64_t scratch_bytes;   // cap of the strip scratch (<= 0: default)
+};
+void run_matvec_multi(Ctx &c, const MultiArgs &a);
+void run_lowp_gemm(Ctx &c, int precision, int64_t M, int64_t N, int64_t K, const float *A, const float *B,
+                   double *C);
 
 // y = s (K x) + diag .* x on the context stream (device vectors of length N)
 void apply_operator(Ctx &c, const bie_operator &op, int precision, const double *x, double *y);

@@ -58,6 +58,15 @@ extern "C" {
 /* ---- arithmetic of an assembly or operator application ---------------- */
 #define BIE_PREC_FP64  0  /* plain FP64 throughout (the reference's arithmetic) */
 #define BIE_PREC_MIXED 1  /* FP32 regular pairs, FP64 near-singular pairs and C  */
+/* Multi-right-hand-side products only (bie_matvec_multi_device): matrix tiles
+ * generated in mixed precision, then multiplied on the tensor cores with
+ * 16-bit operands scaled by powers of two per matrix row and per right-hand
+ * side, FP32 accumulation.  The _SPLIT forms carry every operand as hi + lo
+ * 16-bit parts and add three products (hi.hi + hi.lo + lo.hi).             */
+#define BIE_PREC_FP16       2   /* ~5e-4 relative product error */
+#define BIE_PREC_BF16       3   /* ~4e-3                        */
+#define BIE_PREC_FP16_SPLIT 4   /* ~1e-6                        */
+#define BIE_PREC_BF16_SPLIT 5   /* ~2e-5                        */
 
 typedef struct bie_ctx bie_ctx;
 
@@ -223,6 +232,37 @@ BIE_API int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im,
                                       const double *d_targets, int64_t n_targets,
                                       const double *d_x, const double *d_v,
                                       double *d_yF, double *d_yG);
+
+/*
+ * Products with many right-hand sides at the collocation nodes:
+ *     YF = F X,  YG = G V     (X, V, YF, YG: N x nrhs complex, column-major)
+ * the matrix form of the operator products (the reference's FMMFOperator /
+ * FMMGOperator `_unsafe_mul!` on a matrix, src/3d/fast_multipole_method.jl:
+ * 249-287, 427-471, which loop batches of 32 columns).  precision:
+ *   BIE_PREC_FP64 / BIE_PREC_MIXED: one matrix-free product per column
+ *     (exactly bie_matvec_device per column);
+ *   BIE_PREC_FP16 ... BIE_PREC_BF16_SPLIT: row strips of F and G are generated
+ *     in mixed precision into device scratch (complex64), quantised to 16-bit
+ *     tiles, and multiplied by all right-hand sides at once with tcgen05
+ *     tensor-core GEMMs; the matrices never exist whole.
+ * Either product may be skipped (NULL input and output).  Device pointers;
+ * asynchronous on the context stream.  `scratch_bytes` caps the strip scratch
+ * (0: 8 GiB); the right-hand-side operands and partial sums come on top.
+ */
+BIE_API int bie_matvec_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs,
+                                    const double *d_X, const double *d_V, double *d_YF,
+                                    double *d_YG, int precision, int64_t scratch_bytes);
+
+/*
+ * The tensor-core building block of bie_matvec_multi_device on its own
+ * (no reference counterpart): C = A B^T for real FP32 A (M x K) and B (N x K),
+ * both row-major, C (M x N, row-major) in FP64, through the same 16-bit
+ * quantisation (power-of-two scale per row of A and of B) and the same tcgen05
+ * GEMM kernel.  precision: BIE_PREC_FP16 ... BIE_PREC_BF16_SPLIT.  Device
+ * pointers; runs on the context stream.
+ */
+BIE_API int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int64_t K,
+                                 const float *d_A, const float *d_B, double *d_C);
 
 /* ---- near field (sparse) --------------------------------------------- */
 /*
