@@ -268,6 +268,141 @@ def sweep_bench(args, rank, world, max_over_ranks):
             "path": "mixed assembly into complex64 matrices + GMRES with complex64 products and double-float sums (restart 20, reltol sqrt(eps))"}
 
 
+def multi_rhs_bench(args, local, max_over_ranks):
+    """Multi-RHS workload: quadratic sphere f=32 (40962 nodes, 20480 tri6),
+    256 seeded complex N(0,1) right-hand sides, wavenumbers k, k_v, k_h of air
+    at 100 Hz (biegpu.lossy).  One step = F X and G X for all three wavenumbers
+    through bie_matvec_multi_device (strip generation in mixed precision +
+    tcgen05 FP16 split GEMM).  Compared with the mixed matrix-free product per
+    column (timed on a few columns and scaled to 256) and checked against the
+    FP64 matrix-free product on two columns per wavenumber."""
+    import torch
+    import biegpu
+    from biegpu import _capi
+    from biegpu import mesh as bm
+    from biegpu.lossy import boundary_layer_wavenumbers
+    mesh = bm.icosphere(32, geometry="quadratic")
+    N, R = mesh.n_sources, args.multi_rhs
+    ctx = biegpu.Context(mesh, n=2, m=2, device=local)
+    dev = torch.device(f"cuda:{local}")
+    g = torch.Generator(device="cpu").manual_seed(2026)
+    X = torch.complex(torch.randn(R, N, generator=g, dtype=torch.float64),
+                      torch.randn(R, N, generator=g, dtype=torch.float64)).to(dev).T   # column-major
+    YF = torch.empty((R, N), dtype=torch.complex128, device=dev).T
+    YG = torch.empty_like(YF)
+    ks = boundary_layer_wavenumbers(100.0)
+    L = _capi.lib()
+    prec = _capi.PRECISION[args.multi_precision]
+
+    def step():
+        for k in ks:
+            _capi.check(L.bie_matvec_multi_device(ctx.handle, k.real, k.imag, R, X.data_ptr(), X.data_ptr(),
+                                                  YF.data_ptr(), YG.data_ptr(), prec, 0))
+
+    step()   # warm-up (scratch, modules)
+    torch.cuda.synchronize(dev)
+    ctx.set_timing(True)
+    ctx.stats(reset=True)
+    steps = max(1, args.multi_steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize(dev)
+    t = max_over_ranks(time.perf_counter() - t0) / steps
+    st = ctx.stats(reset=True)
+    ctx.set_timing(False)
+    # accuracy against the FP64 matrix-free product, two columns per wavenumber
+    errs = []
+    for k in ks:
+        _capi.check(L.bie_matvec_multi_device(ctx.handle, k.real, k.imag, R, X.data_ptr(), X.data_ptr(),
+                                              YF.data_ptr(), YG.data_ptr(), prec, 0))
+        for c in (0, R - 1):
+            x = X[:, c].contiguous()
+            yF, yG = torch.empty_like(x), torch.empty_like(x)
+            _capi.check(L.bie_matvec_device(ctx.handle, k.real, k.imag, None, 0, x.data_ptr(), x.data_ptr(),
+                                            yF.data_ptr(), yG.data_ptr(), _capi.BIE_PREC_FP64))
+            torch.cuda.synchronize(dev)
+            errs.append(float(torch.linalg.norm(YF[:, c] - yF) / torch.linalg.norm(yF)))
+            errs.append(float(torch.linalg.norm(YG[:, c] - yG) / torch.linalg.norm(yG)))
+    # the matrix-free mixed product, one column at a time
+    ncol = 2
+    t0 = time.perf_counter()
+    for k in ks:
+        _capi.check(L.bie_matvec_multi_device(ctx.handle, k.real, k.imag, ncol, X.data_ptr(), X.data_ptr(),
+                                              YF.data_ptr(), YG.data_ptr(), _capi.BIE_PREC_MIXED, 0))
+    torch.cuda.synchronize(dev)
+    t_col = (time.perf_counter() - t0) / ncol
+    peaks = measured_peaks()
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    gemm_ms = st["tensor_ms"] / steps
+    executed_tf = st["tensor_flops_executed"] / max(st["tensor_ms"], 1e-9) / 1e9
+    algo_tf = st["tensor_flops"] / max(st["tensor_ms"], 1e-9) / 1e9
+    del X, YF, YG
+    ctx.close()
+    torch.cuda.empty_cache()
+    return {"metric": "multi-RHS operator products/s", "value": 2 * len(ks) * R / t, "unit": "rhs-products/s",
+            "workload": f"quadratic sphere f=32 ({N} nodes), {R} RHS, k={ks[0]:.4f}, k_v={ks[1]:.1f}, "
+                        f"k_h={ks[2]:.1f} (air, 100 Hz); F X and G X per wavenumber",
+            "precision": args.multi_precision, "ms_per_step": 1e3 * t,
+            "entries_per_s": 2 * len(ks) * float(N) * N / t,
+            "gemm": {"kernel": "lowp_gemm_kernel", "ms_per_step": gemm_ms, "launches_per_step": st["tensor_launches"] / steps,
+                     "roofline": {"bound": "tensor", "achieved": executed_tf, "peak": bf16, "unit": "TFLOP/s",
+                                  "frac": executed_tf / bf16, "algorithmic_tflops": algo_tf,
+                                  "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 burst) of measured",
+                                  "note": "executed = issued MMA flops incl. padding and the three split products"}},
+            "generation_ms_per_step": st["timed_ms"] / steps,
+            "max_rel_err_vs_fp64": max(errs), "median_rel_err_vs_fp64": float(np.median(errs)),
+            "per_column_mixed": {"ms_per_rhs_all_k": 1e3 * t_col, "speedup": t_col * R / t}}
+
+
+def adjoint_bench(args, max_over_ranks):
+    """Adjoint workload: ellipsoid 3:2:1 f=22 (4842 nodes, linear), ka=3, 32
+    seeded field points on the radius-10 sphere, seeded impedances |Z| = rho c.
+    One step = J and its gradient with respect to all vertex coordinates and
+    element impedances (forward solve, adjoint solve, reverse pass)."""
+    import biegpu
+    from biegpu import mesh as bm
+    rho_c = 1.21 * 343.0
+    P, T = bm.icosphere_arrays(22)
+    P = P * np.array([1.0, 2 / 3, 1 / 3])[:, None]
+    P = P + 2e-3 * np.random.default_rng(0).normal(size=P.shape) / 22
+    mesh = bm._finish(P, T + 1, "linear", "geometry")
+    rng = np.random.default_rng(1)
+    Z = rho_c * np.exp(1j * rng.uniform(-1.0, 1.0, mesh.n_elements))
+    Xf = rng.normal(size=(3, 32))
+    Xf *= 10.0 / np.linalg.norm(Xf, axis=0)
+    k = 3.0
+    biegpu.farfield_objective(mesh, k, Z, Xf, rho_c=rho_c)   # warm-up
+    steps = max(1, args.adjoint_steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        J, _, dX, dZ, info = biegpu.farfield_objective(mesh, k, Z, Xf, rho_c=rho_c)
+    t_grad = max_over_ranks(time.perf_counter() - t0) / steps
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        biegpu.farfield_objective(mesh, k, Z, Xf, rho_c=rho_c, gradient=False)
+    t_fwd = max_over_ranks(time.perf_counter() - t0) / steps
+    h = 1e-6
+    v, c = 1234, 2
+    Pp = mesh.coordinates.copy()
+    Pp[c, v] += h
+    Jp = biegpu.farfield_objective(bm._finish(Pp, mesh.topology, "linear", "geometry"), k, Z, Xf, rho_c=rho_c,
+                                   gradient=False)[0]
+    Pp[c, v] -= 2 * h
+    Jm = biegpu.farfield_objective(bm._finish(Pp, mesh.topology, "linear", "geometry"), k, Z, Xf, rho_c=rho_c,
+                                   gradient=False)[0]
+    fd = (Jp - Jm) / (2 * h)
+    n_params = 3 * mesh.coordinates.shape[1] + 2 * mesh.n_elements
+    return {"metric": "adjoint gradients/s", "value": 1.0 / t_grad, "unit": "gradients/s",
+            "workload": f"ellipsoid 3:2:1 f=22 ({mesh.n_sources} nodes, {mesh.n_elements} elements), ka=3, "
+                        "32 field points at radius 10",
+            "ms_per_gradient": 1e3 * t_grad, "ms_per_forward": 1e3 * t_fwd, "parameters": n_params,
+            "central_fd_equivalent_s": 2 * n_params * t_fwd,
+            "fd_check": {"component": f"dX[{c},{v}]", "adjoint": float(dX[c, v]), "central_fd_h1e-6": fd,
+                         "rel_to_max": abs(fd - dX[c, v]) / float(np.abs(dX).max())},
+            "gmres_iterations": [info["forward_iterations"], info["adjoint_iterations"]]}
+
+
 def roofline_entry(st, kernel, bound, peak_flops, workload_name, nphys):
     kernel_ms = st["timed_ms"] / max(st["timed_launches"], 1)
     flops = st["algorithmic_flops"] / max(st["timed_launches"], 1)
@@ -300,6 +435,13 @@ def main():
     ap.add_argument("--sweep-fp64-k", type=int, default=4,
                     help="wavenumbers per mesh timed on the plain FP64 path (the error check set)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-multi", action="store_true", help="skip the multi-RHS tensor-core measurement")
+    ap.add_argument("--multi-rhs", type=int, default=256)
+    ap.add_argument("--multi-steps", type=int, default=3)
+    ap.add_argument("--multi-precision", default="fp16_split",
+                    choices=["fp16", "bf16", "fp16_split", "bf16_split"])
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
+    ap.add_argument("--adjoint-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -406,6 +548,14 @@ def main():
     if not args.no_sweep:
         sweep = sweep_bench(args, rank, world, max_over_ranks)
 
+    # ---- multi-RHS tensor-core products and adjoint gradients ---------------
+    multi = None
+    if not args.no_multi:
+        multi = multi_rhs_bench(args, local, max_over_ranks)
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_bench(args, max_over_ranks)
+
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
@@ -425,6 +575,7 @@ def main():
         "precision": args.precision, "data": "synthetic",
         "config": dict(desc, l2="256 MB L2 flush between steps; each step writes 4.3 GB", parallelism=f"replicas{world}"),
         "roofline": roofline, "plain_fp64": plain, "accuracy": accuracy, "sweep": sweep,
+        "multi_rhs": multi, "adjoint": adjoint,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
         "clocks": clk.summary(), "gpu": torch.cuda.get_device_name(dev),
         "peaks": {"fp64_tflops": peaks["fp64_flops"] / 1e12, "fp32_tflops": peaks["fp32_flops"] / 1e12,

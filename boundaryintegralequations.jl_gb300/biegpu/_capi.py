@@ -84,6 +84,10 @@ class Stats(C.Structure):
         ("timed_ms", C.c_double),
         ("algorithmic_flops", C.c_double),
         ("quadrature_evals", C.c_int64),
+        ("tensor_launches", C.c_int64),
+        ("tensor_ms", C.c_double),
+        ("tensor_flops", C.c_double),
+        ("tensor_flops_executed", C.c_double),
     ]
 
 

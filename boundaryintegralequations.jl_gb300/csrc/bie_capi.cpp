@@ -159,10 +159,18 @@ int bie_ctx_stats(bie_ctx *ctx, bie_stats *out, int reset) {
         out->timed_ms = c.timed_ms;
         out->quadrature_evals = (int64_t)q;
         out->algorithmic_flops = (double)q * (32.0 + 8.0 * c.lay.NP);
+        out->tensor_launches = c.tensor_launches;
+        out->tensor_ms = c.tensor_ms;
+        out->tensor_flops = c.tensor_flops;
+        out->tensor_flops_executed = c.tensor_flops_executed;
         if (reset) {
             c.kernel_launches = 0;
             c.timed_launches = 0;
             c.timed_ms = 0.0;
+            c.tensor_launches = 0;
+            c.tensor_ms = 0.0;
+            c.tensor_flops = 0.0;
+            c.tensor_flops_executed = 0.0;
             BIE_CUDA(cudaMemset(c.d_qpe, 0, sizeof(unsigned long long)));
         }
     });

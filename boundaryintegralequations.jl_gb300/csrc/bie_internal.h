@@ -184,6 +184,12 @@ struct Ctx {
     // timer_end() after; both are no-ops while timing is off.
     cudaEvent_t timer_begin();
     void timer_end(cudaEvent_t a);
+    // Tensor-core GEMM launches of the multi-RHS products are timed on their
+    // own (tensor_*), with their algorithmic and executed flop counts.
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_tensor;
+    int64_t tensor_launches = 0;
+    double tensor_ms = 0.0, tensor_flops = 0.0, tensor_flops_executed = 0.0;
+    void tensor_timer_end(cudaEvent_t a, double flops, double flops_executed);
     void collect_timers();   // synchronises the stream
 };
 

@@ -580,7 +580,8 @@ void choose_split(const Ctx &c, int64_t mt, int64_t nt, int nkb, int &ksplit, in
 }
 
 void launch_gemm(Ctx &c, Format f, const uint8_t *Ahi, const uint8_t *Alo, const uint8_t *Bhi,
-                 const uint8_t *Blo, int64_t mt, int64_t nt, int nkb, int ksplit, int kb_per, float *P, int *err) {
+                 const uint8_t *Blo, int64_t mt, int64_t nt, int nkb, int ksplit, int kb_per, float *P, int *err,
+                 double algorithmic_flops) {
     GemmArgs g{};
     g.A[0] = Ahi;
     g.A[1] = Alo ? Alo : Ahi;
@@ -594,7 +595,9 @@ void launch_gemm(Ctx &c, Format f, const uint8_t *Ahi, const uint8_t *Alo, const
     g.err = err;
     if (mt > 0x7fffffff || nt > 65535 || ksplit > 65535) fail(BIE_ERR_INVALID, "GEMM grid too large");
     dim3 grid((unsigned)mt, (unsigned)nt, (unsigned)ksplit);
-    cudaEvent_t t0 = c.timer_begin();
+    const double executed = 2.0 * (double)(mt * kBM) * (double)(nt * kBN) * (double)nkb * kBK * (f.split ? 3 : 1);
+    cudaEvent_t t0 = c.timing ? c.take_event() : nullptr;
+    if (t0) BIE_CUDA(cudaEventRecord(t0, c.stream));
     if (f.bf16) {
         if (f.split) {
             set_gemm_attr<true, true>();
@@ -613,7 +616,7 @@ void launch_gemm(Ctx &c, Format f, const uint8_t *Ahi, const uint8_t *Alo, const
         }
     }
     BIE_CUDA(cudaGetLastError());
-    c.timer_end(t0);
+    c.tensor_timer_end(t0, algorithmic_flops, executed);
     ++c.kernel_launches;
 }
 
@@ -724,7 +727,7 @@ void run_lowp_gemm(Ctx &c, int precision, int64_t M, int64_t N, int64_t K, const
     c.kernel_launches += 2;
     pack_rowmajor_any(c, f, A, M, K, kBM, ra, nkb, mt * kBM, Ahi, Alo);
     pack_rowmajor_any(c, f, B, N, K, kBN, rb, nkb, nt * kBN, Bhi, Blo);
-    launch_gemm(c, f, Ahi, Alo, Bhi, Blo, mt, nt, nkb, ksplit, kb_per, P, err);
+    launch_gemm(c, f, Ahi, Alo, Bhi, Blo, mt, nt, nkb, ksplit, kb_per, P, err, 2.0 * (double)M * N * K);
     lowp_reduce_real_kernel<<<grid1(M * N), 256, 0, c.stream>>>(P, ksplit, mt * kBM, nt * kBN, M, N, ra, rb, C);
     BIE_CUDA(cudaGetLastError());
     ++c.kernel_launches;
@@ -819,7 +822,7 @@ void run_matvec_multi(Ctx &c, const MultiArgs &a) {
             ++c.kernel_launches;
             pack_strip_any(c, f, S, ms, ms, N, rmax, nkb, mt, Ahi, Alo);
             launch_gemm(c, f, Ahi, Alo, op == 0 ? BFh : BGh, op == 0 ? BFl : BGl, mt, nt, nkb, ksplit, kb_per, P,
-                        err);
+                        err, 8.0 * (double)ms * N * R);
             double2 *Y = reinterpret_cast<double2 *>(op == 0 ? a.YF : a.YG);
             lowp_reduce_complex_kernel<<<grid1(ms * R), 256, 0, c.stream>>>(P, ksplit, mt * kBM, nt * kBN, ms, R, Rp,
                                                                             rmax, cm, N, i0, Y);

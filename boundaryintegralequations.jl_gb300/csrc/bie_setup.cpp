@@ -315,6 +315,16 @@ void Ctx::timer_end(cudaEvent_t a) {
     ++timed_launches;
 }
 
+void Ctx::tensor_timer_end(cudaEvent_t a, double flops, double flops_executed) {
+    if (!timing || !a) return;
+    cudaEvent_t b = take_event();
+    BIE_CUDA(cudaEventRecord(b, stream));
+    ev_tensor.emplace_back(a, b);
+    ++tensor_launches;
+    tensor_flops += flops;
+    tensor_flops_executed += flops_executed;
+}
+
 void Ctx::collect_timers() {
     BIE_CUDA(cudaStreamSynchronize(stream));
     for (auto &p : ev_pending) {
@@ -325,6 +335,14 @@ void Ctx::collect_timers() {
         ev_free.push_back(p.second);
     }
     ev_pending.clear();
+    for (auto &p : ev_tensor) {
+        float ms = 0.f;
+        BIE_CUDA(cudaEventElapsedTime(&ms, p.first, p.second));
+        tensor_ms += ms;
+        ev_free.push_back(p.first);
+        ev_free.push_back(p.second);
+    }
+    ev_tensor.clear();
 }
 
 void build_context(Ctx &c, const bie_mesh_desc &d, int device) {
@@ -552,8 +570,13 @@ void destroy_context(Ctx &c) {
         cudaEventDestroy(p.first);
         cudaEventDestroy(p.second);
     }
+    for (auto &p : c.ev_tensor) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
     for (auto e : c.ev_free) cudaEventDestroy(e);
     c.ev_pending.clear();
+    c.ev_tensor.clear();
     c.ev_free.clear();
     c.d_qpe = nullptr;
     if (c.stream) cudaStreamDestroy(c.stream);

@@ -144,6 +144,12 @@ typedef struct bie_stats {
     double  algorithmic_flops;   /* flops of the timed launches, counted as
                                     32 + 8 n_phys per quadrature-point evaluation */
     int64_t quadrature_evals;    /* (target, quadrature point) evaluations */
+    /* tensor-core GEMM launches of bie_matvec_multi_device / bie_lowp_gemm_device,
+       timed on their own while timing is on */
+    int64_t tensor_launches;
+    double  tensor_ms;
+    double  tensor_flops;            /* algorithmic: 8 M N R per complex product, 2 M N K real */
+    double  tensor_flops_executed;   /* issued MMA flops (padding, 3 products when split)     */
 } bie_stats;
 
 /*

@@ -166,16 +166,8 @@ def test_multi_rhs_only_one_product():
 
 
 def _lossy_wavenumbers(freq=100.0):
-    """Acoustic and boundary-layer wavenumbers of air at 20 C (textbook values:
-    rho 1.204 kg/m^3, c 343.2 m/s, mu 1.81e-5 Pa s, thermal diffusivity
-    2.2e-5 m^2/s): k_v = sqrt(i omega rho / mu), k_h = sqrt(i omega / alpha),
-    the S = +1 convention of the reference's visco_thermal_constants (to
-    leading order).  Im/Re = 1 for both."""
-    w = 2 * np.pi * freq
-    k = w / 343.2
-    kv = np.sqrt(1j * w * 1.204 / 1.81e-5)
-    kh = np.sqrt(1j * w / 2.2e-5)
-    return [k, kv, kh]
+    from biegpu.lossy import boundary_layer_wavenumbers
+    return boundary_layer_wavenumbers(freq)
 
 
 def test_multi_rhs_lossy_sphere_40962():
