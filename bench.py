@@ -237,9 +237,9 @@ def sweep_bench(args, rank, world, max_over_ranks):
     all 64 wavenumbers; the plain FP64 path on `sweep_fp64_k` of them, which
     also give the relative surface-pressure error of the mixed path."""
     import biegpu
-    named = sweep_meshes()
+    named = sweep_meshes()[:max(1, args.sweep_meshes)]
     meshes = [m for _, m in named]
-    ks = np.linspace(0.1, 10.0, 64)
+    ks = np.linspace(0.1, 10.0, args.sweep_nk)
     rng = np.random.default_rng(2026)
     ws = [rng.normal(size=m.n_sources) + 1j * rng.normal(size=m.n_sources) for m in meshes]
     biegpu.sweep(meshes, ks[:1], ws, precision="mixed")      # warm-up (contexts, modules)
@@ -281,7 +281,7 @@ def multi_rhs_bench(args, local, max_over_ranks):
     from biegpu import _capi
     from biegpu import mesh as bm
     from biegpu.lossy import boundary_layer_wavenumbers
-    mesh = bm.icosphere(32, geometry="quadratic")
+    mesh = bm.icosphere(args.multi_f, geometry="quadratic")
     N, R = mesh.n_sources, args.multi_rhs
     ctx = biegpu.Context(mesh, n=2, m=2, device=local)
     dev = torch.device(f"cuda:{local}")
@@ -341,7 +341,7 @@ def multi_rhs_bench(args, local, max_over_ranks):
     ctx.close()
     torch.cuda.empty_cache()
     return {"metric": "multi-RHS operator products/s", "value": 2 * len(ks) * R / t, "unit": "rhs-products/s",
-            "workload": f"quadratic sphere f=32 ({N} nodes), {R} RHS, k={ks[0]:.4f}, k_v={ks[1]:.1f}, "
+            "workload": f"quadratic sphere f={args.multi_f} ({N} nodes), {R} RHS, k={ks[0]:.4f}, k_v={ks[1]:.1f}, "
                         f"k_h={ks[2]:.1f} (air, 100 Hz); F X and G X per wavenumber",
             "precision": args.multi_precision, "ms_per_step": 1e3 * t,
             "entries_per_s": 2 * len(ks) * float(N) * N / t,
@@ -435,8 +435,11 @@ def main():
     ap.add_argument("--sweep-fp64-k", type=int, default=4,
                     help="wavenumbers per mesh timed on the plain FP64 path (the error check set)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--sweep-nk", type=int, default=64, help="wavenumbers of the sweep")
+    ap.add_argument("--sweep-meshes", type=int, default=3, help="use the first n of the three sweep meshes")
     ap.add_argument("--no-multi", action="store_true", help="skip the multi-RHS tensor-core measurement")
     ap.add_argument("--multi-rhs", type=int, default=256)
+    ap.add_argument("--multi-f", type=int, default=32, help="sphere frequency of the multi-RHS mesh (32: 40962 nodes)")
     ap.add_argument("--multi-steps", type=int, default=3)
     ap.add_argument("--multi-precision", default="fp16_split",
                     choices=["fp16", "bf16", "fp16_split", "bf16_split"])

@@ -182,6 +182,7 @@ SIGNATURES = {
     "bie_matvec_device": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P, _I]),
     "bie_matvec_device_noalloc": (_I, [_P, _D, _D, _P, _I64, _P, _P, _P, _P]),
     "bie_matvec_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
+    "bie_matvec_multi": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_lowp_gemm_device": (_I, [_P, _I, _I64, _I64, _I64, _P, _P, _P]),
     "bie_singular_rule": (_I, [_I, _D, _P, _P, _P, _I, C.POINTER(_I)]),
     "bie_nearfield_pattern": (_I, [_P, _I, C.POINTER(_I64), _P, _P]),

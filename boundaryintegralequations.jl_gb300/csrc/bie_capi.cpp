@@ -289,6 +289,43 @@ int bie_matvec_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs
     });
 }
 
+int bie_matvec_multi(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *X, const double *V,
+                     double *YF, double *YG, int precision, int64_t scratch_bytes) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (nrhs <= 0) bie::fail(BIE_ERR_INVALID, "nrhs must be positive");
+        if (!X && !V) bie::fail(BIE_ERR_INVALID, "neither X nor V given");
+        if ((X && !YF) || (V && !YG)) bie::fail(BIE_ERR_INVALID, "an input is given without its output");
+        void *d = nullptr;
+        const size_t bytes = (size_t)c.n_sources * (size_t)nrhs * 16;
+        const int nbuf = (X ? 2 : 0) + (V ? 2 : 0);
+        {
+            std::lock_guard<std::mutex> lock(c.mu);
+            BIE_CUDA(cudaSetDevice(c.device));
+            BIE_CUDA(cudaMalloc(&d, bytes * nbuf));
+        }
+        struct Free {
+            void *p;
+            ~Free() { cudaFree(p); }
+        } guard{d};
+        double *dX = X ? static_cast<double *>(d) : nullptr;
+        double *dYF = X ? dX + 2 * c.n_sources * nrhs : nullptr;
+        double *dV = V ? static_cast<double *>(d) + (X ? 4 * c.n_sources * nrhs : 0) : nullptr;
+        double *dYG = V ? dV + 2 * c.n_sources * nrhs : nullptr;
+        {
+            std::lock_guard<std::mutex> lock(c.mu);
+            if (X) BIE_CUDA(cudaMemcpyAsync(dX, X, bytes, cudaMemcpyHostToDevice, c.stream));
+            if (V) BIE_CUDA(cudaMemcpyAsync(dV, V, bytes, cudaMemcpyHostToDevice, c.stream));
+        }
+        const int st = bie_matvec_multi_device(ctx, k_re, k_im, nrhs, dX, dV, dYF, dYG, precision, scratch_bytes);
+        if (st != BIE_OK) bie::fail(st, bie_last_error());
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (X) BIE_CUDA(cudaMemcpyAsync(YF, dYF, bytes, cudaMemcpyDeviceToHost, c.stream));
+        if (V) BIE_CUDA(cudaMemcpyAsync(YG, dYG, bytes, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
 int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int64_t K, const float *d_A,
                          const float *d_B, double *d_C) {
     return guarded([&] {

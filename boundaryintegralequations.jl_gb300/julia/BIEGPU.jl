@@ -18,7 +18,9 @@ the path of libbiegpu.so.
 module BIEGPU
 
 using LinearAlgebra
+using SparseArrays
 using LinearMaps
+import ChainRulesCore
 
 const libbiegpu = get(ENV, "BIEGPU_LIB", "libbiegpu.so")
 
@@ -180,8 +182,174 @@ function evaluate_targets(A::GPUOperator{W}, x, targets) where {W}
     return y
 end
 
+"""
+    LinearMaps._unsafe_mul!(Y, A::GPUOperator, X::AbstractMatrix)
+
+All columns at once through `bie_matvec_multi` (the matrix method of the FMM
+operators, src/3d/fast_multipole_method.jl:249-287, 427-471): matrix strips
+generated on the device and multiplied on the tensor cores (`multi_precision`,
+default FP16 hi + lo, ~1e-5 relative), or one product per column with
+`multi_precision=:none`.
+"""
+const MULTI_PRECISION = Dict(:fp16 => Cint(2), :bf16 => Cint(3), :fp16_split => Cint(4),
+                             :bf16_split => Cint(5))
+const multi_precision = Ref(:fp16_split)
+
+function LinearMaps._unsafe_mul!(Y::AbstractMatrix, A::GPUOperator{W}, X::AbstractMatrix) where {W}
+    Xm = Matrix{ComplexF64}(X)
+    Ym = Matrix{ComplexF64}(undef, size(Y))
+    prec = multi_precision[] === :none ? A.precision : MULTI_PRECISION[multi_precision[]]
+    GC.@preserve Xm Ym begin
+        px = pointer(Xm); py = pointer(Ym)
+        check(ccall((:bie_matvec_multi, libbiegpu), Cint,
+                    (Ptr{Cvoid}, Float64, Float64, Int64, Ptr{ComplexF64}, Ptr{ComplexF64},
+                     Ptr{ComplexF64}, Ptr{ComplexF64}, Cint, Int64),
+                    A.ctx.handle, real(A.k), imag(A.k), size(Xm, 2),
+                    W === :F ? px : C_NULL, W === :G ? px : C_NULL,
+                    W === :F ? py : C_NULL, W === :G ? py : C_NULL, prec, 0))
+    end
+    copyto!(Y, Ym)
+    return Y
+end
+
+# ---------------------------------------------------------------------------
+# Near field: sparse_assemble_parallel! (src/3d/assembly_collocation_losses.jl:200-405)
+# ---------------------------------------------------------------------------
+"""
+    sparse_assemble_parallel_gpu!(mesh, k; depth=1, offset=nothing, fOn=true, gOn=true)
+
+Accurate near-field F and G on the connected_sources pattern as
+`SparseMatrixCSC{ComplexF64}` (adaptive singular rules; offset = 0 unless given).
+"""
+function sparse_assemble_parallel_gpu!(mesh, k; depth=1, offset=nothing, fOn=true, gOn=true,
+                                       coarse=false, n_gauss=3, ctx=nothing)
+    c = ctx === nothing ? Context(mesh; n=2, m=2) : ctx
+    N = c.n_sources
+    nnz = Ref{Int64}(0)
+    check(ccall((:bie_nearfield_pattern, libbiegpu), Cint,
+                (Ptr{Cvoid}, Cint, Ref{Int64}, Ptr{Int64}, Ptr{Int64}), c.handle, depth, nnz, C_NULL, C_NULL))
+    rowptr = Vector{Int64}(undef, N + 1)
+    cols = Vector{Int64}(undef, nnz[])
+    check(ccall((:bie_nearfield_pattern, libbiegpu), Cint,
+                (Ptr{Cvoid}, Cint, Ref{Int64}, Ptr{Int64}, Ptr{Int64}), c.handle, depth, nnz, rowptr, cols))
+    kk = ComplexF64(k)
+    Fv = Vector{ComplexF64}(undef, fOn ? nnz[] : 0)
+    Gv = Vector{ComplexF64}(undef, gOn ? nnz[] : 0)
+    check(ccall((:bie_nearfield_assemble, libbiegpu), Cint,
+                (Ptr{Cvoid}, Float64, Float64, Cint, Float64, Cint, Cint, Cint,
+                 Ptr{ComplexF64}, Ptr{ComplexF64}),
+                c.handle, real(kk), imag(kk), depth, offset === nothing ? 0.0 : Float64(offset),
+                coarse ? 1 : 0, n_gauss, (fOn ? BIE_F : 0) | (gOn ? BIE_G : 0),
+                fOn ? pointer(Fv) : C_NULL, gOn ? pointer(Gv) : C_NULL))
+    # CSR rows -> CSC of the transpose, transposed back
+    I = Int[]; J = Int[]
+    for i in 1:N, p in rowptr[i]+1:rowptr[i+1]
+        push!(I, i); push!(J, cols[p] + 1)
+    end
+    F = fOn ? sparse(I, J, Fv, N, N) : spzeros(ComplexF64, N, N)
+    G = gOn ? sparse(I, J, Gv, N, N) : spzeros(ComplexF64, N, N)
+    return F, G
+end
+
+# ---------------------------------------------------------------------------
+# Frequency sweep (replaces the per-frequency loop of examples/sweep_meta.jl:219-233)
+# ---------------------------------------------------------------------------
+struct SweepOpts
+    precision::Int32
+    refine::Int32
+    restart::Int32; maxiter::Int32; reltol::Float64; abstol::Float64
+    gprecision::Int32; grefine::Int32; inner_reltol::Float64; max_refine::Int32
+    initially_nonzero::Int32
+end
+struct SweepInfo
+    solves::Int64; converged::Int64; iterations::Int64; assemble_ms::Float64; solve_ms::Float64
+end
+
+"""
+    sweep_gpu(meshes, ks, ws; precision=:mixed) -> Vector{Matrix{ComplexF64}}
+
+For every mesh m and wavenumber k_j: assemble F, G, C on the device and solve
+(F + Diagonal(1 .- C)) p = G w_m with GMRES; returns one N_m x length(ks)
+matrix per mesh.
+"""
+function sweep_gpu(meshes, ks, ws; precision=:mixed, refine=true, ctxs=nothing)
+    cs = ctxs === nothing ? [Context(m; n=2, m=2) for m in meshes] : ctxs
+    kv = ComplexF64.(ks)
+    wv = [Vector{ComplexF64}(w) for w in ws]
+    ps = [Matrix{ComplexF64}(undef, c.n_sources, length(kv)) for c in cs]
+    opts = Ref(SweepOpts(precision_code(precision), refine, 0, 0, 0.0, 0.0, 0, 0, 0.0, 0, 0))
+    info = Ref{SweepInfo}()
+    GC.@preserve cs kv wv ps begin
+        hs = [c.handle for c in cs]
+        wp = [pointer(w) for w in wv]
+        pp = [pointer(p) for p in ps]
+        check(ccall((:bie_sweep, libbiegpu), Cint,
+                    (Ptr{Ptr{Cvoid}}, Cint, Ptr{ComplexF64}, Cint, Ptr{Ptr{ComplexF64}},
+                     Ptr{Ptr{ComplexF64}}, Ref{SweepOpts}, Ref{SweepInfo}, Ptr{Int32}),
+                    hs, length(cs), kv, length(kv), wp, pp, opts, info, C_NULL))
+    end
+    return ps
+end
+
+# ---------------------------------------------------------------------------
+# Adjoint gradient (bie_adjoint) and its ChainRulesCore rule
+# ---------------------------------------------------------------------------
+struct AdjointOpts
+    rho_c::Float64
+    dir::NTuple{3,Float64}
+    reltol::Float64
+end
+struct AdjointInfo
+    forward_iterations::Int32; forward_converged::Int32
+    adjoint_iterations::Int32; adjoint_converged::Int32
+end
+
+"""
+    farfield_objective(coordinates, Z, mesh, k, field; rho_c=1.21*343, dir=(0,0,1), gradient=false)
+
+J = sum |p(x_f)|^2 of plane-wave scattering by the surface of `mesh` with its
+vertices moved to `coordinates` (3 x N_c) and element impedances `Z`; with
+`gradient=true` also dJ/dcoordinates (3 x N_c) and dJ/dZ (dJ/dRe Z + i dJ/dIm Z).
+"""
+function farfield_objective(coordinates, Z, mesh, k, field; rho_c=1.21 * 343.0, dir=(0.0, 0.0, 1.0),
+                            gradient=false, reltol=1e-13)
+    moved = (coordinates=Matrix{Float64}(coordinates), topology=mesh.topology,
+             physics_topology=mesh.physics_topology, sources=Matrix{Float64}(coordinates))
+    c = Context(moved; n=2, m=2)
+    Zv = Vector{ComplexF64}(Z)
+    X = Matrix{Float64}(field)
+    J = Ref{Float64}(0.0)
+    pf = Vector{ComplexF64}(undef, size(X, 2))
+    dX = gradient ? zeros(Float64, size(coordinates)) : Matrix{Float64}(undef, 0, 0)
+    dZ = gradient ? zeros(ComplexF64, length(Zv)) : Vector{ComplexF64}(undef, 0)
+    d = collect(Float64, dir); d ./= norm(d)
+    opts = Ref(AdjointOpts(rho_c, (d[1], d[2], d[3]), reltol))
+    info = Ref{AdjointInfo}()
+    GC.@preserve Zv X pf dX dZ begin
+        check(ccall((:bie_adjoint, libbiegpu), Cint,
+                    (Ptr{Cvoid}, Float64, Float64, Ptr{ComplexF64}, Ptr{Float64}, Int64, Ref{AdjointOpts},
+                     Ref{Float64}, Ptr{ComplexF64}, Ptr{Float64}, Ptr{ComplexF64}, Ref{AdjointInfo}),
+                    c.handle, Float64(real(k)), Float64(imag(k)), Zv, X, size(X, 2), opts, J, pf,
+                    gradient ? pointer(dX) : C_NULL, gradient ? pointer(dZ) : C_NULL, info))
+    end
+    return gradient ? (J[], dX, dZ) : J[]
+end
+
+# The pullback scales the adjoint gradients by the incoming cotangent of J; the
+# complex cotangent of Z follows ChainRules' convention (dJ/dRe Z + i dJ/dIm Z).
+function ChainRulesCore.rrule(::typeof(farfield_objective), coordinates, Z, mesh, k, field; kwargs...)
+    J, dX, dZ = farfield_objective(coordinates, Z, mesh, k, field; kwargs..., gradient=true)
+    function farfield_objective_pullback(dJ)
+        s = ChainRulesCore.unthunk(dJ)
+        return (ChainRulesCore.NoTangent(), s .* dX, s .* dZ, ChainRulesCore.NoTangent(),
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+    end
+    return J, farfield_objective_pullback
+end
+
 version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
-export Context, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets
+export Context, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
+       sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective
 
 end # module

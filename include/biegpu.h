@@ -259,6 +259,12 @@ BIE_API int bie_matvec_multi_device(bie_ctx *ctx, double k_re, double k_im, int6
                                     const double *d_X, const double *d_V, double *d_YF,
                                     double *d_YG, int precision, int64_t scratch_bytes);
 
+/* Same with HOST buffers (copied to and from the device inside the call;
+ * blocking), the form a Julia `Matrix{ComplexF64}` caller uses. */
+BIE_API int bie_matvec_multi(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs,
+                             const double *X, const double *V, double *YF, double *YG,
+                             int precision, int64_t scratch_bytes);
+
 /*
  * The tensor-core building block of bie_matvec_multi_device on its own
  * (no reference counterpart): C = A B^T for real FP32 A (M x K) and B (N x K),

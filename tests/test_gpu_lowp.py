@@ -215,3 +215,23 @@ def test_operator_matrix_product():
     assert np.linalg.norm(Y - F @ X) / np.linalg.norm(F @ X) <= MULTI_TOL["fp16_split"]
     Yg = GPUGOperator(mesh, k, multi_precision=None, precision="fp64") @ X
     assert np.linalg.norm(Yg - G @ X) / np.linalg.norm(G @ X) <= 1e-12
+
+
+def test_multi_rhs_host_entry_point():
+    """bie_matvec_multi (host buffers) equals the device entry point."""
+    import oracle
+    mesh = bm.icosphere(4, geometry="quadratic")
+    ctx = biegpu.Context(mesh, n=2, m=2, device=0)
+    N, R = mesh.n_sources, 11
+    k = 3.0 + 0.5j
+    F, G, _ = oracle.assemble(mesh, k, n=2, m=2, cOn=False)
+    rng = np.random.default_rng(12)
+    X = np.asfortranarray(rng.normal(size=(N, R)) + 1j * rng.normal(size=(N, R)))
+    V = np.asfortranarray(rng.normal(size=(N, R)) + 1j * rng.normal(size=(N, R)))
+    YF = np.empty((N, R), dtype=np.complex128, order="F")
+    YG = np.empty_like(YF)
+    for prec, tol in (("fp16_split", MULTI_TOL["fp16_split"]), ("fp64", 1e-12)):
+        _capi.check(_capi.lib().bie_matvec_multi(ctx.handle, k.real, k.imag, R, X.ctypes.data, V.ctypes.data,
+                                                 YF.ctypes.data, YG.ctypes.data, _capi.PRECISION[prec], 0))
+        assert np.linalg.norm(YF - F @ X) / np.linalg.norm(F @ X) <= tol
+        assert np.linalg.norm(YG - G @ V) / np.linalg.norm(G @ V) <= tol
