@@ -62,15 +62,28 @@ dense_gemv_kernel(const T2 *__restrict__ A, int64_t n, const double2 *__restrict
 
 // Complex64 matrix times complex128 vector on the FP32 pipe, for the column
 // slice of blockIdx.y.  On GB300 the FP64 pipe cannot keep up with HBM even for
-// a matrix-vector product, so the products run in FP32 with the vector split
-// into double-float (x = hi + lo): a * hi is formed exactly (TwoProduct), a * lo
-// is added to its error term, and the sums are carried in double-float (TwoSum).
-// The result is the stored complex64 operator applied to x to ~1e-14 relative
-// — exact enough for GMRES to converge to sqrt(eps) on that operator.
-// Each thread handles two consecutive rows (one 16-byte load per column).
+// a matrix-vector product, so the products run in FP32: the vector is rounded
+// to FP32, every block of kFold columns is summed with plain FP32 FMAs and the
+// block sums are carried in double-float (TwoSum).  The product then has a
+// relative error of a few FP32 roundings (~1e-7) — the size of the complex64
+// rounding of the stored matrix itself — at 8 FMAs per 16-byte load, which
+// keeps the kernel on the HBM roofline.  Each thread handles two consecutive
+// rows (one 16-byte load per column).
+constexpr int kFold = 16;
+
+__device__ __forceinline__ void df_fold(dev::df &acc, float s) {
+    const dev::df t = dev::two_sum(acc.hi, s);
+    acc = dev::fast_two_sum(t.hi, __fadd_rn(t.lo, acc.lo));
+}
+
+// The same product to ~1e-14 relative (the residuals of refinement and the
+// right-hand sides): the vector is split into double-float (x = hi + lo),
+// a * hi is formed exactly (TwoProduct), a * lo is added to its error term and
+// every sum is carried in double-float (TwoSum).  About 14 instructions per
+// real multiply-add, so issue-bound at roughly half the HBM rate.
 __global__ void __launch_bounds__(kT)
-dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *__restrict__ x,
-                      double2 *__restrict__ part, int S) {
+dense_gemv_c64_exact_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *__restrict__ x,
+                            double2 *__restrict__ part, int S) {
     const int64_t r2 = (int64_t)blockIdx.x * kT + threadIdx.x;   // row pair index
     const int64_t i0 = 2 * r2;
     const int s = blockIdx.y;
@@ -78,6 +91,13 @@ dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *_
     __shared__ float4 xs[kT];   // (re hi, re lo, im hi, im lo)
     dev::df yr0 = {0.f, 0.f}, yi0 = {0.f, 0.f}, yr1 = {0.f, 0.f}, yi1 = {0.f, 0.f};
     const int64_t ld2 = n / 2;  // float4 per column (n even)
+    auto mac = [](dev::df &acc, float av, float xh, float xl) {
+        const float p = av * xh;
+        float e = __fmaf_rn(av, xh, -p);
+        e = __fmaf_rn(av, xl, e);
+        const dev::df t = dev::two_sum(acc.hi, p);
+        acc = dev::fast_two_sum(t.hi, __fadd_rn(__fadd_rn(t.lo, e), acc.lo));
+    };
     for (int64_t jb = j0; jb < j1; jb += kT) {
         const int nb = (int)min((int64_t)kT, j1 - jb);
         __syncthreads();
@@ -93,14 +113,6 @@ dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *_
             for (int j = 0; j < nb; ++j) {
                 const float4 a = col[(int64_t)j * ld2];   // (re0, im0, re1, im1)
                 const float4 xv = xs[j];
-                // y += a x, real and imaginary parts, two rows
-                auto mac = [](dev::df &acc, float av, float xh, float xl) {
-                    const float p = av * xh;
-                    float e = __fmaf_rn(av, xh, -p);
-                    e = __fmaf_rn(av, xl, e);
-                    const dev::df t = dev::two_sum(acc.hi, p);
-                    acc = dev::fast_two_sum(t.hi, __fadd_rn(__fadd_rn(t.lo, e), acc.lo));
-                };
                 mac(yr0, a.x, xv.x, xv.y);
                 mac(yr0, -a.y, xv.z, xv.w);
                 mac(yi0, a.x, xv.z, xv.w);
@@ -121,15 +133,22 @@ dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *_
     }
 }
 
-// Same product for odd n: one row per thread, 8-byte loads.
+// Odd n, exact form: one row per thread, 8-byte loads.
 __global__ void __launch_bounds__(kT)
-dense_gemv_c64_rows_kernel(const float2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
-                           double2 *__restrict__ part, int S) {
+dense_gemv_c64_rows_exact_kernel(const float2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
+                                 double2 *__restrict__ part, int S) {
     const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
     const int s = blockIdx.y;
     const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
     __shared__ float4 xs[kT];
     dev::df yr = {0.f, 0.f}, yi = {0.f, 0.f};
+    auto mac = [](dev::df &acc, float av, float xh, float xl) {
+        const float p = av * xh;
+        float e = __fmaf_rn(av, xh, -p);
+        e = __fmaf_rn(av, xl, e);
+        const dev::df t = dev::two_sum(acc.hi, p);
+        acc = dev::fast_two_sum(t.hi, __fadd_rn(__fadd_rn(t.lo, e), acc.lo));
+    };
     for (int64_t jb = j0; jb < j1; jb += kT) {
         const int nb = (int)min((int64_t)kT, j1 - jb);
         __syncthreads();
@@ -144,17 +163,117 @@ dense_gemv_c64_rows_kernel(const float2 *__restrict__ A, int64_t n, const double
             for (int j = 0; j < nb; ++j) {
                 const float2 a = col[(int64_t)j * n];
                 const float4 xv = xs[j];
-                auto mac = [](dev::df &acc, float av, float xh, float xl) {
-                    const float p = av * xh;
-                    float e = __fmaf_rn(av, xh, -p);
-                    e = __fmaf_rn(av, xl, e);
-                    const dev::df t = dev::two_sum(acc.hi, p);
-                    acc = dev::fast_two_sum(t.hi, __fadd_rn(__fadd_rn(t.lo, e), acc.lo));
-                };
                 mac(yr, a.x, xv.x, xv.y);
                 mac(yr, -a.y, xv.z, xv.w);
                 mac(yi, a.x, xv.z, xv.w);
                 mac(yi, a.y, xv.x, xv.y);
+            }
+        }
+    }
+    if (i < n)
+        part[(int64_t)s * n + i] = make_double2(dev::f2d(yr.hi) + dev::f2d(yr.lo),
+                                                dev::f2d(yi.hi) + dev::f2d(yi.lo));
+}
+
+__global__ void __launch_bounds__(kT)
+dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *__restrict__ x,
+                      double2 *__restrict__ part, int S) {
+    const int64_t r2 = (int64_t)blockIdx.x * kT + threadIdx.x;   // row pair index
+    const int64_t i0 = 2 * r2;
+    const int s = blockIdx.y;
+    const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
+    __shared__ float2 xs[kT];
+    dev::df yr0 = {0.f, 0.f}, yi0 = {0.f, 0.f}, yr1 = {0.f, 0.f}, yi1 = {0.f, 0.f};
+    const int64_t ld2 = n / 2;  // float4 per column (n even)
+    for (int64_t jb = j0; jb < j1; jb += kT) {
+        const int nb = (int)min((int64_t)kT, j1 - jb);
+        __syncthreads();
+        if (threadIdx.x < nb) {
+            const double2 v = x[jb + threadIdx.x];
+            xs[threadIdx.x] = make_float2((float)v.x, (float)v.y);
+        }
+        __syncthreads();
+        if (i0 < n) {
+            const float4 *col = A2 + jb * ld2 + r2;
+            for (int jf = 0; jf < nb; jf += kFold) {
+                const int ne = min(kFold, nb - jf);
+                float sr0 = 0.f, si0 = 0.f, sr1 = 0.f, si1 = 0.f;
+                if (ne == kFold) {
+#pragma unroll
+                    for (int j = 0; j < kFold; ++j) {
+                        const float4 a = col[(int64_t)(jf + j) * ld2];   // (re0, im0, re1, im1)
+                        const float2 xv = xs[jf + j];
+                        sr0 = __fmaf_rn(a.x, xv.x, sr0);
+                        sr0 = __fmaf_rn(-a.y, xv.y, sr0);
+                        si0 = __fmaf_rn(a.x, xv.y, si0);
+                        si0 = __fmaf_rn(a.y, xv.x, si0);
+                        sr1 = __fmaf_rn(a.z, xv.x, sr1);
+                        sr1 = __fmaf_rn(-a.w, xv.y, sr1);
+                        si1 = __fmaf_rn(a.z, xv.y, si1);
+                        si1 = __fmaf_rn(a.w, xv.x, si1);
+                    }
+                } else {
+                    for (int j = 0; j < ne; ++j) {
+                        const float4 a = col[(int64_t)(jf + j) * ld2];
+                        const float2 xv = xs[jf + j];
+                        sr0 = __fmaf_rn(a.x, xv.x, sr0);
+                        sr0 = __fmaf_rn(-a.y, xv.y, sr0);
+                        si0 = __fmaf_rn(a.x, xv.y, si0);
+                        si0 = __fmaf_rn(a.y, xv.x, si0);
+                        sr1 = __fmaf_rn(a.z, xv.x, sr1);
+                        sr1 = __fmaf_rn(-a.w, xv.y, sr1);
+                        si1 = __fmaf_rn(a.z, xv.y, si1);
+                        si1 = __fmaf_rn(a.w, xv.x, si1);
+                    }
+                }
+                df_fold(yr0, sr0);
+                df_fold(yi0, si0);
+                df_fold(yr1, sr1);
+                df_fold(yi1, si1);
+            }
+        }
+    }
+    if (i0 < n) {
+        part[(int64_t)s * n + i0] = make_double2(dev::f2d(yr0.hi) + dev::f2d(yr0.lo),
+                                                 dev::f2d(yi0.hi) + dev::f2d(yi0.lo));
+        if (i0 + 1 < n)
+            part[(int64_t)s * n + i0 + 1] = make_double2(dev::f2d(yr1.hi) + dev::f2d(yr1.lo),
+                                                         dev::f2d(yi1.hi) + dev::f2d(yi1.lo));
+    }
+}
+
+// Same product for odd n: one row per thread, 8-byte loads.
+__global__ void __launch_bounds__(kT)
+dense_gemv_c64_rows_kernel(const float2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
+                           double2 *__restrict__ part, int S) {
+    const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
+    const int s = blockIdx.y;
+    const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
+    __shared__ float2 xs[kT];
+    dev::df yr = {0.f, 0.f}, yi = {0.f, 0.f};
+    for (int64_t jb = j0; jb < j1; jb += kT) {
+        const int nb = (int)min((int64_t)kT, j1 - jb);
+        __syncthreads();
+        if (threadIdx.x < nb) {
+            const double2 v = x[jb + threadIdx.x];
+            xs[threadIdx.x] = make_float2((float)v.x, (float)v.y);
+        }
+        __syncthreads();
+        if (i < n) {
+            const float2 *col = A + jb * n + i;
+            for (int jf = 0; jf < nb; jf += kFold) {
+                const int ne = min(kFold, nb - jf);
+                float sr = 0.f, si = 0.f;
+                for (int j = 0; j < ne; ++j) {
+                    const float2 a = col[(int64_t)(jf + j) * n];
+                    const float2 xv = xs[jf + j];
+                    sr = __fmaf_rn(a.x, xv.x, sr);
+                    sr = __fmaf_rn(-a.y, xv.y, sr);
+                    si = __fmaf_rn(a.x, xv.y, si);
+                    si = __fmaf_rn(a.y, xv.x, si);
+                }
+                df_fold(yr, sr);
+                df_fold(yi, si);
             }
         }
     }
@@ -306,14 +425,26 @@ struct Solver {
         if (op.kind == BIE_OP_DENSE) {
             cudaEvent_t t0 = c.timer_begin();
             if (op.A32 && (precision == BIE_PREC_MIXED || !op.A)) {
+                // complex64 operator: the fast product for mixed iterations, the
+                // exact one where FP64 arithmetic was asked for (residuals of
+                // refinement, right-hand sides) and no complex128 matrix exists
+                const bool exact = precision != BIE_PREC_MIXED;
                 if (n % 2 == 0) {
                     dim3 grid(blocks(n / 2, kT), (unsigned)S);
-                    dense_gemv_c64_kernel<<<grid, kT, 0, c.stream>>>(
-                        reinterpret_cast<const float4 *>(op.A32), n, x, part, S);
+                    if (exact)
+                        dense_gemv_c64_exact_kernel<<<grid, kT, 0, c.stream>>>(
+                            reinterpret_cast<const float4 *>(op.A32), n, x, part, S);
+                    else
+                        dense_gemv_c64_kernel<<<grid, kT, 0, c.stream>>>(
+                            reinterpret_cast<const float4 *>(op.A32), n, x, part, S);
                 } else {
                     dim3 grid(blocks(n, kT), (unsigned)S);
-                    dense_gemv_c64_rows_kernel<<<grid, kT, 0, c.stream>>>(
-                        reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
+                    if (exact)
+                        dense_gemv_c64_rows_exact_kernel<<<grid, kT, 0, c.stream>>>(
+                            reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
+                    else
+                        dense_gemv_c64_rows_kernel<<<grid, kT, 0, c.stream>>>(
+                            reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
                 }
             } else {
                 dim3 grid(blocks(n, kT), (unsigned)S);

@@ -5,9 +5,11 @@
 //   2. diag = 1 - C, b = G w (the library's dense product),
 //   3. GMRES on (F + Diagonal(1 - C)) p = b.  Mixed precision keeps F and G
 //      in complex64 end to end (the assembly's FP32 accumulators with the FP64
-//      near-pair corrections added in place; products with FP32 arithmetic and
-//      double-float sums, half the HBM bytes of complex128); FP64 uses
-//      complex128 matrices and FP64 products,
+//      near-pair corrections added in place; half the HBM bytes of
+//      complex128); with refinement the Arnoldi iterations use the fast FP32
+//      product (HBM-bound, ~1e-7) and the outer residuals and the right-hand
+//      side the exact one (double-float sums, ~1e-14); FP64 uses complex128
+//      matrices and FP64 products,
 //   4. p copied into the caller's host array (pinned or not).
 // Each mesh's device buffers are allocated once for its whole frequency list;
 // frequencies of a mesh reuse them (assemble -> solve -> overwrite), so a
@@ -78,8 +80,9 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
             if (mixed) gop.A32 = G.as<float>();
             else gop.A = G.as<double>();
             gop.scale_re = 1.0;
-            apply_operator(c, gop, mixed ? BIE_PREC_MIXED : BIE_PREC_FP64,
-                           reinterpret_cast<const double *>(wd), reinterpret_cast<double *>(b));
+            // (the exact complex64 product in the mixed path)
+            apply_operator(c, gop, BIE_PREC_FP64, reinterpret_cast<const double *>(wd),
+                           reinterpret_cast<double *>(b));
             // (F + Diagonal(1 - C)) p = b
             bie_operator op{};
             op.kind = BIE_OP_DENSE;
@@ -87,9 +90,14 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
             else op.A = F.as<double>();
             op.scale_re = 1.0;
             op.diag = reinterpret_cast<const double *>(dg);
+            // mixed + refine: iterations with the fast complex64 product (~1e-7),
+            // refined with residuals from the exact complex64 product; mixed
+            // without refine: the exact complex64 product throughout; plain:
+            // FP64 GMRES on complex128 matrices
             bie_gmres_opts go = o.gmres;
-            go.refine = 0;
-            go.precision = mixed ? BIE_PREC_MIXED : BIE_PREC_FP64;
+            go.refine = (mixed && o.refine) ? 1 : 0;
+            go.precision = go.refine ? BIE_PREC_MIXED : BIE_PREC_FP64;
+            if (go.refine && !(go.inner_reltol > 0)) go.inner_reltol = 1e-6;
             go.initially_nonzero = 0;
             bie_gmres_info gi{};
             run_gmres(c, op, reinterpret_cast<const double *>(b), reinterpret_cast<double *>(x), go, gi);
