@@ -10,7 +10,8 @@ reference's Julia API for the path:
 from ._capi import BIEError, lib, library_path  # noqa: F401
 from .assembly import Context, assemble_parallel, get_context, quadrature_rule  # noqa: F401
 from .mesh import Mesh3d, ellipsoid, icosphere, load_comsol, read_comsol  # noqa: F401
-from .operators import Diagonal, GPUFOperator, GPUGOperator, I, UniformScaling, gmres  # noqa: F401
+from .operators import (Diagonal, FMMFOperator, FMMGOperator, GPUFOperator, GPUGOperator, I,  # noqa: F401
+                        UniformScaling, gmres)
 from .sweep import sweep  # noqa: F401
 from .adjoint import farfield_objective  # noqa: F401
 

@@ -30,6 +30,7 @@ SOURCES = [
     "bie_sweep.cu",
     "bie_adjoint.cu",
     "bie_lowp.cu",
+    "bie_fastop.cu",
     "bie_peaks.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -63,9 +64,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OBJ_DIR.mkdir(parents=True, exist_ok=True)
     cc = nvcc()
 
+    # extra nvcc flags for tuning builds (e.g. "-DBIE_K2_MIN_BLOCKS=5")
+    extra = os.environ.get("BIE_NVCC_EXTRA", "").split()
+
     def compile_one(src: str) -> Path:
         obj = OBJ_DIR / (src + ".o")
-        cmd = [cc, *ARCH, *COMMON, "-I", str(PKG_ROOT.parent / "include"), "-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [cc, *ARCH, *COMMON, *extra, "-I", str(PKG_ROOT.parent / "include"), "-c", str(CSRC / src),
+               "-o", str(obj)]
         if verbose:
             print(" ".join(cmd))
         r = subprocess.run(cmd, capture_output=True, text=True)

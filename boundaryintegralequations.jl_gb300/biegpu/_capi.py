@@ -93,6 +93,7 @@ class Stats(C.Structure):
 
 BIE_OP_DENSE = 0
 BIE_OP_MATRIX_FREE = 1
+BIE_OP_FAST = 2
 
 
 class Operator(C.Structure):
@@ -105,6 +106,7 @@ class Operator(C.Structure):
         ("scale_re", C.c_double),
         ("scale_im", C.c_double),
         ("diag", C.c_void_p),
+        ("fast", C.c_void_p),
     ]
 
 
@@ -184,6 +186,11 @@ SIGNATURES = {
     "bie_matvec_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_matvec_multi": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_lowp_gemm_device": (_I, [_P, _I, _I64, _I64, _I64, _P, _P, _P]),
+    "bie_fastop_create": (_I, [_P, _D, _D, _I, _I, _I, _D, _I, C.POINTER(_P)]),
+    "bie_fastop_destroy": (_I, [_P]),
+    "bie_fastop_apply_device": (_I, [_P, _P, _P, _I]),
+    "bie_fastop_apply": (_I, [_P, _P, _P, _I]),
+    "bie_fastop_evaluate_targets": (_I, [_P, _P, _I64, _P, _P, _I]),
     "bie_singular_rule": (_I, [_I, _D, _P, _P, _P, _I, C.POINTER(_I)]),
     "bie_nearfield_pattern": (_I, [_P, _I, C.POINTER(_I64), _P, _P]),
     "bie_nearfield_assemble": (_I, [_P, _D, _D, _I, _D, _I, _I, _I, _P, _P]),

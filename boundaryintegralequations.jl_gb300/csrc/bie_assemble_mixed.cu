@@ -69,8 +69,57 @@ __device__ __noinline__ void pair_fp64_inplace(const Fp64View v, int64_t p, doub
     }
 }
 
+// Quadrature loop of one regular pair: per-node sums of F, G and the C term.
+// QN > 0: the rule size is known at compile time (4-point corner and 8-point
+// midpoint rules of n = m = 2), the loop is unrolled and the independent
+// points interleave; QN == 0: runtime size Q.
+template <int NP, bool CPLX_K, int QN>
+__device__ __forceinline__ void quad_loop(const float4 *g4, const float *phc, int Q, const mixed::PairSetup &P,
+                                          const mixed::Phase &ph, float kf, float kimf, float (&fr)[NP],
+                                          float (&fi)[NP], float (&gr)[NP], float (&gi)[NP], float &ce) {
+    constexpr int NPP = PhiPad<NP>::value;
+    const int nq = QN > 0 ? QN : Q;
+#pragma unroll
+    for (int q = 0; q < (QN > 0 ? QN : 1); ++q) {
+        if (QN == 0) break;
+        const mixed::QpeValues v = mixed::qpe<CPLX_K>(g4[2 * q], g4[2 * q + 1], P, ph, kf, kimf);
+        ce += v.tq;
+        float p[NPP];
+        *reinterpret_cast<float4 *>(p) = *reinterpret_cast<const float4 *>(phc + q * NPP);
+        if (NPP == 8) *reinterpret_cast<float4 *>(p + 4) = *reinterpret_cast<const float4 *>(phc + q * NPP + 4);
+#pragma unroll
+        for (int a = 0; a < NP; ++a) {
+            fr[a] = __fmaf_rn(v.Fr, p[a], fr[a]);
+            fi[a] = __fmaf_rn(v.Fi, p[a], fi[a]);
+            gr[a] = __fmaf_rn(v.Gr, p[a], gr[a]);
+            gi[a] = __fmaf_rn(v.Gi, p[a], gi[a]);
+        }
+    }
+    if (QN == 0) {
+        for (int q = 0; q < nq; ++q) {
+            const mixed::QpeValues v = mixed::qpe<CPLX_K>(g4[2 * q], g4[2 * q + 1], P, ph, kf, kimf);
+            ce += v.tq;
+            float p[NPP];
+            *reinterpret_cast<float4 *>(p) = *reinterpret_cast<const float4 *>(phc + q * NPP);
+            if (NPP == 8)
+                *reinterpret_cast<float4 *>(p + 4) = *reinterpret_cast<const float4 *>(phc + q * NPP + 4);
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                fr[a] = __fmaf_rn(v.Fr, p[a], fr[a]);
+                fi[a] = __fmaf_rn(v.Fi, p[a], fi[a]);
+                gr[a] = __fmaf_rn(v.Gr, p[a], gr[a]);
+                gi[a] = __fmaf_rn(v.Gi, p[a], gi[a]);
+            }
+        }
+    }
+}
+
+#ifndef BIE_K2_MIN_BLOCKS
+#define BIE_K2_MIN_BLOCKS 4   // resident 128-thread blocks per SM (register budget)
+#endif
+
 template <int NP, bool CPLX_K>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, BIE_K2_MIN_BLOCKS)
 assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
                       const float *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
                       const double *__restrict__ tgt, int64_t M, double kre, double kim, int flags,
@@ -140,21 +189,9 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                 const float *phc = s_phi + (size_t)c * qmax * NPP;
 #pragma unroll
                 for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.f;
-                for (int q = 0; q < Q; ++q) {
-                    const mixed::QpeValues v = mixed::qpe<CPLX_K>(g4[2 * q], g4[2 * q + 1], P, ph, kf, kimf);
-                    ce += v.tq;
-                    float p[NPP];
-                    *reinterpret_cast<float4 *>(p) = *reinterpret_cast<const float4 *>(phc + q * NPP);
-                    if (NPP == 8)
-                        *reinterpret_cast<float4 *>(p + 4) = *reinterpret_cast<const float4 *>(phc + q * NPP + 4);
-#pragma unroll
-                    for (int a = 0; a < NP; ++a) {
-                        fr[a] = __fmaf_rn(v.Fr, p[a], fr[a]);
-                        fi[a] = __fmaf_rn(v.Fi, p[a], fi[a]);
-                        gr[a] = __fmaf_rn(v.Gr, p[a], gr[a]);
-                        gi[a] = __fmaf_rn(v.Gi, p[a], gi[a]);
-                    }
-                }
+                if (Q == 4) quad_loop<NP, CPLX_K, 4>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
+                else if (Q == 8) quad_loop<NP, CPLX_K, 8>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
+                else quad_loop<NP, CPLX_K, 0>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
             }
             mixed::df_accum(cacc, -ce);   // C = -sum tq
             // F, G: vector FP32 reductions (fire-and-forget, no return value)

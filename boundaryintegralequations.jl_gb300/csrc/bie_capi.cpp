@@ -39,6 +39,16 @@ bie::Ctx *as_ctx(bie_ctx *p) {
     return reinterpret_cast<bie::Ctx *>(p);
 }
 
+bie::FastOp &as_fastop(bie_fastop *op) {
+    if (!op) bie::fail(BIE_ERR_INVALID, "operator is NULL");
+    return *reinterpret_cast<bie::FastOp *>(op);
+}
+
+void check_prec2(int precision) {
+    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED)
+        bie::fail(BIE_ERR_INVALID, "precision must be BIE_PREC_FP64 or BIE_PREC_MIXED");
+}
+
 void check_assemble_args(bie::Ctx &c, double kr, double ki, int64_t M, int flags, int precision,
                          const void *F, const void *G, const void *C) {
     if (!std::isfinite(kr) || !std::isfinite(ki)) bie::fail(BIE_ERR_INVALID, "k must be finite");
@@ -393,15 +403,100 @@ int bie_nearfield_assemble(bie_ctx *ctx, double k_re, double k_im, int depth, do
     });
 }
 
+int bie_fastop_create(bie_ctx *ctx, double k_re, double k_im, int which, int n_gauss, int nearfield,
+                      double offset, int depth, bie_fastop **out) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!out) bie::fail(BIE_ERR_INVALID, "out must not be NULL");
+        *out = nullptr;
+        if (!std::isfinite(k_re) || !std::isfinite(k_im)) bie::fail(BIE_ERR_INVALID, "k must be finite");
+        if (which != BIE_F && which != BIE_G) bie::fail(BIE_ERR_INVALID, "which must be BIE_F or BIE_G");
+        if (depth != 1 && depth != 2) bie::fail(BIE_ERR_INVALID, "depth must be 1 or 2");
+        if (!(offset >= 0.0) || offset > 1.0) bie::fail(BIE_ERR_INVALID, "offset must be in [0, 1]");
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        auto op = bie::create_fastop(c, k_re, k_im, which, n_gauss, nearfield != 0, offset, depth);
+        *out = reinterpret_cast<bie_fastop *>(op.release());
+    });
+}
+
+int bie_fastop_destroy(bie_fastop *op) {
+    return guarded([&] {
+        if (!op) return;
+        auto *f = reinterpret_cast<bie::FastOp *>(op);
+        std::lock_guard<std::mutex> lock(f->base->mu);
+        BIE_CUDA(cudaSetDevice(f->base->device));
+        BIE_CUDA(cudaStreamSynchronize(f->base->stream));
+        delete f;
+    });
+}
+
+int bie_fastop_apply_device(bie_fastop *op, const double *d_x, double *d_y, int precision) {
+    return guarded([&] {
+        bie::FastOp &f = as_fastop(op);
+        if (!d_x || !d_y) bie::fail(BIE_ERR_INVALID, "x and y must not be NULL");
+        check_prec2(precision);
+        std::lock_guard<std::mutex> lock(f.base->mu);
+        BIE_CUDA(cudaSetDevice(f.base->device));
+        bie::apply_fastop(f, d_x, d_y, precision, nullptr, 0);
+    });
+}
+
+int bie_fastop_apply(bie_fastop *op, const double *x, double *y, int precision) {
+    return guarded([&] {
+        bie::FastOp &f = as_fastop(op);
+        if (!x || !y) bie::fail(BIE_ERR_INVALID, "x and y must not be NULL");
+        check_prec2(precision);
+        std::lock_guard<std::mutex> lock(f.base->mu);
+        bie::Ctx &c = *f.base;
+        BIE_CUDA(cudaSetDevice(c.device));
+        const int64_t N = c.n_sources;
+        double *d = static_cast<double *>(c.scratch(bie::kScratchTargets, (size_t)N * 32 + 64));
+        BIE_CUDA(cudaMemcpyAsync(d, x, (size_t)N * 16, cudaMemcpyHostToDevice, c.stream));
+        bie::apply_fastop(f, d, d + 2 * N, precision, nullptr, 0);
+        BIE_CUDA(cudaMemcpyAsync(y, d + 2 * N, (size_t)N * 16, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int bie_fastop_evaluate_targets(bie_fastop *op, const double *targets, int64_t n_targets, const double *x,
+                                double *y, int precision) {
+    return guarded([&] {
+        bie::FastOp &f = as_fastop(op);
+        if (!targets || !x || !y) bie::fail(BIE_ERR_INVALID, "targets, x and y must not be NULL");
+        if (n_targets <= 0) bie::fail(BIE_ERR_INVALID, "n_targets must be positive");
+        check_prec2(precision);
+        for (int64_t i = 0; i < 3 * n_targets; ++i)
+            if (!std::isfinite(targets[i])) bie::fail(BIE_ERR_INVALID, "non-finite target");
+        std::lock_guard<std::mutex> lock(f.base->mu);
+        bie::Ctx &c = *f.base;
+        BIE_CUDA(cudaSetDevice(c.device));
+        const int64_t N = c.n_sources, M = n_targets;
+        const size_t tb = ((size_t)M * 24 + 15) & ~size_t(15);
+        char *buf = static_cast<char *>(c.scratch(bie::kScratchTargets, tb + (size_t)N * 16 + (size_t)M * 16 + 64));
+        double *dt = reinterpret_cast<double *>(buf);
+        double *dx = reinterpret_cast<double *>(buf + tb);
+        double *dy = dx + 2 * N;
+        BIE_CUDA(cudaMemcpyAsync(dt, targets, (size_t)M * 24, cudaMemcpyHostToDevice, c.stream));
+        BIE_CUDA(cudaMemcpyAsync(dx, x, (size_t)N * 16, cudaMemcpyHostToDevice, c.stream));
+        bie::apply_fastop(f, dx, dy, precision, dt, M);
+        BIE_CUDA(cudaMemcpyAsync(y, dy, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
 int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b, double *d_x,
                      const bie_gmres_opts *opts, bie_gmres_info *info) {
     int converged = 1;
     const int st = guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);
         if (!op || !d_b || !d_x) bie::fail(BIE_ERR_INVALID, "op, b and x must not be NULL");
-        if (op->kind != BIE_OP_DENSE && op->kind != BIE_OP_MATRIX_FREE)
+        if (op->kind != BIE_OP_DENSE && op->kind != BIE_OP_MATRIX_FREE && op->kind != BIE_OP_FAST)
             bie::fail(BIE_ERR_INVALID, "unknown operator kind");
         if (op->kind == BIE_OP_DENSE && !op->A) bie::fail(BIE_ERR_INVALID, "dense operator without A");
+        if (op->kind == BIE_OP_FAST &&
+            (!op->fast || reinterpret_cast<const bie::FastOp *>(op->fast)->base != &c))
+            bie::fail(BIE_ERR_INVALID, "fast operator missing or made from another context");
         if (!std::isfinite(op->k_re) || !std::isfinite(op->k_im) || !std::isfinite(op->scale_re) ||
             !std::isfinite(op->scale_im))
             bie::fail(BIE_ERR_INVALID, "k and scale must be finite");

@@ -133,6 +133,7 @@ struct Ctx {
     std::mutex mu;
     int device = 0;
     cudaStream_t stream = nullptr;
+    bool owns_stream = true;             // false: the stream belongs to another context
     int num_sms = 0;
 
     // mesh (host copies, 0-based)
@@ -194,7 +195,9 @@ struct Ctx {
 };
 
 // Host set-up (bie_setup.cpp)
-void build_context(Ctx &c, const bie_mesh_desc &d, int device);
+// gauss_rule > 0 replaces the clustered Duffy rules by the symmetric Gauss
+// rule of that many points (fast-operator far field).
+void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule = 0);
 void destroy_context(Ctx &c);
 
 // Kernel launchers (bie_assemble.cu)
@@ -266,6 +269,24 @@ struct MultiArgs {
 void run_matvec_multi(Ctx &c, const MultiArgs &a);
 void run_lowp_gemm(Ctx &c, int precision, int64_t M, int64_t N, int64_t K, const float *A, const float *B,
                    double *C);
+
+// Fast operators (bie_fastop.cu): Gauss-rule far field + near-field correction
+struct FastOp {
+    Ctx *base = nullptr;            // context the operator was made from (its stream)
+    std::unique_ptr<Ctx> g;         // same mesh, every rule the n_gauss Gauss rule
+    int which = BIE_F;              // BIE_F or BIE_G
+    double k_re = 0, k_im = 0;
+    int n_gauss = 3;
+    int64_t nnz = 0;                // near-field correction S - C_coarse (CSR, device)
+    int64_t *d_row_ptr = nullptr;
+    int32_t *d_cols = nullptr;
+    double2 *d_vals = nullptr;
+    ~FastOp();
+};
+std::unique_ptr<FastOp> create_fastop(Ctx &c, double k_re, double k_im, int which, int n_gauss, bool nearfield,
+                                      double offset, int depth);
+// y = K_gauss x (+ correction at the nodes); targets: device 3 x M or null
+void apply_fastop(FastOp &op, const double *x, double *y, int precision, const double *targets, int64_t M);
 
 // y = s (K x) + diag .* x on the context stream (device vectors of length N)
 void apply_operator(Ctx &c, const bie_operator &op, int precision, const double *x, double *y);

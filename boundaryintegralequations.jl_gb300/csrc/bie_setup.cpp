@@ -345,7 +345,7 @@ void Ctx::collect_timers() {
     ev_tensor.clear();
 }
 
-void build_context(Ctx &c, const bie_mesh_desc &d, int device) {
+void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule) {
     // ---- validation -------------------------------------------------------
     if (d.n_coordinates <= 0 || d.n_elements <= 0 || d.n_sources <= 0)
         fail(BIE_ERR_INVALID, "mesh sizes must be positive");
@@ -393,11 +393,17 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device) {
     // ---- clustered rules ---------------------------------------------------
     // Linear geometry: three rules clustered at the corners.  Quadratic geometry:
     // one rule per physics node (corners, then edge midpoints 4-6).
+    // gauss_rule > 0: every rule is the symmetric gauss_rule-point triangle rule
+    // (the far-field rule of the fast operators, setup_fast_operator,
+    // src/3d/fast_multipole_method.jl:163-170), whatever the nearest node.
     const int R = (d.shape_kind == BIE_TRI_LINEAR) ? 3 : NP;
     c.rules.clear();
-    for (int r = 0; r < R; ++r)
-        c.rules.push_back(r < 3 ? duffy_corner_rule(d.quad_n, d.quad_m, r + 1)
-                                : duffy_midpoint_rule(d.quad_n, d.quad_m, r + 1));
+    for (int r = 0; r < R; ++r) {
+        if (gauss_rule > 0) c.rules.push_back(triangle_gauss_rule(gauss_rule));
+        else
+            c.rules.push_back(r < 3 ? duffy_corner_rule(d.quad_n, d.quad_m, r + 1)
+                                    : duffy_midpoint_rule(d.quad_n, d.quad_m, r + 1));
+    }
     RecordLayout &L = c.lay;
     L = RecordLayout{};
     L.NP = NP;
@@ -579,7 +585,7 @@ void destroy_context(Ctx &c) {
     c.ev_tensor.clear();
     c.ev_free.clear();
     c.d_qpe = nullptr;
-    if (c.stream) cudaStreamDestroy(c.stream);
+    if (c.stream && c.owns_stream) cudaStreamDestroy(c.stream);
     c.d_records = nullptr;
     c.d_phi = nullptr;
     c.d_sources = nullptr;

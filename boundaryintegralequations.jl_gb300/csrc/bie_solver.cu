@@ -458,10 +458,16 @@ struct Solver {
             BIE_CUDA(cudaGetLastError());
             launched();
         } else {
-            // matrix-free F x into y, then y = s y + d .* x
-            MatvecArgs m{op.k_re, op.k_im, c.d_sources, n, reinterpret_cast<const double *>(x),
-                         nullptr, reinterpret_cast<double *>(y), nullptr, precision};
-            launch_matvec(c, m);
+            // matrix-free F x (or the fast operator) into y, then y = s y + d .* x
+            if (op.kind == BIE_OP_FAST) {
+                FastOp &f = *const_cast<FastOp *>(reinterpret_cast<const FastOp *>(op.fast));
+                apply_fastop(f, reinterpret_cast<const double *>(x), reinterpret_cast<double *>(y), precision,
+                             nullptr, 0);
+            } else {
+                MatvecArgs m{op.k_re, op.k_im, c.d_sources, n, reinterpret_cast<const double *>(x),
+                             nullptr, reinterpret_cast<double *>(y), nullptr, precision};
+                launch_matvec(c, m);
+            }
             combine_kernel<<<blocks(n), 256, 0, c.stream>>>(y, 1, n, sc, d, x, y);
             BIE_CUDA(cudaGetLastError());
             launched();

@@ -314,9 +314,40 @@ BIE_API int bie_nearfield_assemble(bie_ctx *ctx, double k_re, double k_im, int d
                                    double offset, int flags, int coarse, int n_gauss,
                                    double *F, double *G);
 
+/* ---- fast operators (FMMFOperator / FMMGOperator) ----------------------- */
+typedef struct bie_fastop bie_fastop;
+
+/*
+ * The operator of FMMFOperator(mesh, k; n_gauss, nearfield, offset, depth)
+ * (which = BIE_F) or FMMGOperator (which = BIE_G)
+ * (src/3d/fast_multipole_method.jl:163-194 setup_fast_operator, :306-324,
+ * :473-490): every element integrated with the symmetric n_gauss-point
+ * triangle rule for all collocation nodes, plus nearfield_correction = the
+ * accurate near field (adaptive rules, `offset`) minus its Gauss-rule part on
+ * the connected_sources(depth) pattern.  The reference sums the far field with
+ * FMM3D to `tol`; here the sum is exact (direct, on the GPU), so results agree
+ * with the reference to its FMM tolerance.  The correction is computed here,
+ * once, for the given k.  The operator keeps a pointer to `ctx` and runs on
+ * its stream; destroy it before the context.
+ */
+BIE_API int bie_fastop_create(bie_ctx *ctx, double k_re, double k_im, int which, int n_gauss, int nearfield,
+                              double offset, int depth, bie_fastop **out);
+BIE_API int bie_fastop_destroy(bie_fastop *op);
+/* y = A x at the collocation nodes (LinearMaps._unsafe_mul!, :238-247, :392-404).
+ * precision: BIE_PREC_FP64 (exact sum) or BIE_PREC_MIXED.  Device pointers,
+ * asynchronous on the context stream. */
+BIE_API int bie_fastop_apply_device(bie_fastop *op, const double *d_x, double *d_y, int precision);
+/* Same with host buffers (blocking). */
+BIE_API int bie_fastop_apply(bie_fastop *op, const double *x, double *y, int precision);
+/* The far-field sum at other points (evaluate_targets, :326-344, :497-519):
+ * no near-field correction, as in the reference.  Host buffers (blocking). */
+BIE_API int bie_fastop_evaluate_targets(bie_fastop *op, const double *targets, int64_t n_targets,
+                                        const double *x, double *y, int precision);
+
 /* ---- linear systems A x = b,  A x = s (K x) + diag .* x ---------------- */
 #define BIE_OP_DENSE       0  /* K = stored dense N x N matrix (device)       */
 #define BIE_OP_MATRIX_FREE 1  /* K = F of the context at wavenumber k         */
+#define BIE_OP_FAST        2  /* K = a fast operator (FMMFOperator algorithm)  */
 
 typedef struct bie_operator {
     int32_t       kind;        /* BIE_OP_DENSE | BIE_OP_MATRIX_FREE                 */
@@ -326,6 +357,8 @@ typedef struct bie_operator {
     double        k_re, k_im;  /* matrix-free: wavenumber                           */
     double        scale_re, scale_im;   /* s                                         */
     const double *diag;        /* device N complex, or NULL for zero                */
+    const struct bie_fastop *fast;      /* BIE_OP_FAST: a fast operator of the same
+                                           context (bie_fastop_create)              */
 } bie_operator;
 
 typedef struct bie_gmres_opts {

@@ -173,8 +173,28 @@ def farfield_objective(mesh, k, Z, field_points, rho_c=1.21 * 343.0, direction=(
     return float(np.sum(np.abs(pf) ** 2)), pf
 
 
+def fast_operator(mesh, k, which="F", n_gauss=3, nearfield=True, offset=0.2, depth=1):
+    """Dense matrix of FMMFOperator / FMMGOperator (src/3d/fast_multipole_method.jl:
+    163-194, 306-324, 473-490) with an exact far-field sum: every pair with the
+    n_gauss-point Gauss rule, plus nearfield_correction = accurate near field
+    (adaptive rules, offset) - its Gauss-rule part on the depth pattern."""
+    F, G, _ = assemble(mesh, k, n=-n_gauss, m=1, fOn=which == "F", gOn=which == "G", cOn=False)
+    A = np.array(F if which == "F" else G)
+    if nearfield:
+        near = globals()["nearfield"]   # the function (the argument shadows its name)
+        rp, cols, Fa, Ga = near(mesh, k, depth=depth, offset=offset, fOn=which == "F", gOn=which == "G")
+        _, _, Fc, Gc = near(mesh, k, depth=depth, coarse=True, n_gauss=n_gauss, fOn=which == "F",
+                            gOn=which == "G")
+        acc, coarse = (Fa, Fc) if which == "F" else (Ga, Gc)
+        for i in range(mesh.n_sources):
+            for p in range(rp[i], rp[i + 1]):
+                A[i, cols[p]] += acc[p] - coarse[p]
+    return A
+
+
 def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, threads=0, g_weight=None):
-    """Reference-algorithm (F, G, C) on the CPU; F, G are M x N Fortran-ordered."""
+    """Reference-algorithm (F, G, C) on the CPU; F, G are M x N Fortran-ordered.
+    n < 0 selects the symmetric (-n)-point Gauss rule for every pair."""
     k = complex(k)
     c = np.asfortranarray(mesh.coordinates, dtype=np.float64)
     t = np.asfortranarray(mesh.topology, dtype=np.int64)

@@ -261,13 +261,21 @@ int oracle_assemble(const double *coords, int64_t Nc, const int64_t *topo, int s
                              kre, kim, flags, F, G, C, nthreads, NULL);
 }
 
+static int gauss_triangle(int n, double *u, double *v, double *w);
+
 /* Same assembly with an optional per-element complex factor gw[e] (E complex)
- * on the single-layer contributions (element admittance weighting). */
+ * on the single-layer contributions (element admittance weighting).
+ * n < 0: every rule is the symmetric (-n)-point triangle rule (the far-field
+ * rule of setup_fast_operator, src/3d/fast_multipole_method.jl:163-170). */
 int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int skind,
                       const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
                       const double *targets, int64_t M, int n, int m, double kre, double kim,
                       int flags, double *F, double *G, double *C, int nthreads, const double *gw) {
     (void)Nc;
+    if (n < 0) {
+        double tu[16], tv[16], tw[16];
+        if (-n > 16 || gauss_triangle(-n, tu, tv, tw) <= 0) return -1;
+    }
     const int NP = nnodes(pkind);
     const int R = (skind == OR_LINEAR) ? 3 : NP;
     int Q[6];
@@ -277,7 +285,7 @@ int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int
         U[r] = malloc(4096 * sizeof(double));
         V[r] = malloc(4096 * sizeof(double));
         W[r] = malloc(4096 * sizeof(double));
-        Q[r] = oracle_rule(n, m, r + 1, U[r], V[r], W[r]);
+        Q[r] = n < 0 ? gauss_triangle(-n, U[r], V[r], W[r]) : oracle_rule(n, m, r + 1, U[r], V[r], W[r]);
         /* physics interpolation transposed: Q x NP */
         PHI[r] = malloc((size_t)Q[r] * NP * sizeof(double));
         for (int q = 0; q < Q[r]; ++q) {
