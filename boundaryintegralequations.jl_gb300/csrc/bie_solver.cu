@@ -34,7 +34,8 @@ constexpr int kT = 256;
 template <typename T2>
 __global__ void __launch_bounds__(kT)
 dense_gemv_kernel(const T2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
-                  double2 *__restrict__ part, int S) {
+                  double2 *__restrict__ part, int S, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
     const int s = blockIdx.y;
     const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
@@ -83,7 +84,8 @@ __device__ __forceinline__ void df_fold(dev::df &acc, float s) {
 // real multiply-add, so issue-bound at roughly half the HBM rate.
 __global__ void __launch_bounds__(kT)
 dense_gemv_c64_exact_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *__restrict__ x,
-                            double2 *__restrict__ part, int S) {
+                            double2 *__restrict__ part, int S, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t r2 = (int64_t)blockIdx.x * kT + threadIdx.x;   // row pair index
     const int64_t i0 = 2 * r2;
     const int s = blockIdx.y;
@@ -136,7 +138,8 @@ dense_gemv_c64_exact_kernel(const float4 *__restrict__ A2, int64_t n, const doub
 // Odd n, exact form: one row per thread, 8-byte loads.
 __global__ void __launch_bounds__(kT)
 dense_gemv_c64_rows_exact_kernel(const float2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
-                                 double2 *__restrict__ part, int S) {
+                                 double2 *__restrict__ part, int S, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
     const int s = blockIdx.y;
     const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
@@ -177,7 +180,8 @@ dense_gemv_c64_rows_exact_kernel(const float2 *__restrict__ A, int64_t n, const 
 
 __global__ void __launch_bounds__(kT)
 dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *__restrict__ x,
-                      double2 *__restrict__ part, int S) {
+                      double2 *__restrict__ part, int S, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t r2 = (int64_t)blockIdx.x * kT + threadIdx.x;   // row pair index
     const int64_t i0 = 2 * r2;
     const int s = blockIdx.y;
@@ -245,7 +249,8 @@ dense_gemv_c64_kernel(const float4 *__restrict__ A2, int64_t n, const double2 *_
 // Same product for odd n: one row per thread, 8-byte loads.
 __global__ void __launch_bounds__(kT)
 dense_gemv_c64_rows_kernel(const float2 *__restrict__ A, int64_t n, const double2 *__restrict__ x,
-                           double2 *__restrict__ part, int S) {
+                           double2 *__restrict__ part, int S, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x;
     const int s = blockIdx.y;
     const int64_t j0 = (int64_t)s * n / S, j1 = (int64_t)(s + 1) * n / S;
@@ -285,7 +290,8 @@ dense_gemv_c64_rows_kernel(const float2 *__restrict__ A, int64_t n, const double
 // y = s * sum_slices(part) + d .* x   (d may be null)
 __global__ void combine_kernel(const double2 *__restrict__ part, int S, int64_t n, double2 sc,
                                const double2 *__restrict__ d, const double2 *__restrict__ x,
-                               double2 *__restrict__ y) {
+                               double2 *__restrict__ y, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double re = 0, im = 0;
@@ -306,7 +312,8 @@ __global__ void combine_kernel(const double2 *__restrict__ part, int S, int64_t 
 // partial[col * nb + block] = sum over the block's rows of conj(V[:, col]) . w
 __global__ void __launch_bounds__(kT)
 multidot_kernel(const double2 *__restrict__ V, int64_t ldv, const double2 *__restrict__ w,
-                int64_t n, double2 *__restrict__ partial) {
+                int64_t n, double2 *__restrict__ partial, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int col = blockIdx.y;
     const double2 *v = V + (int64_t)col * ldv;
     double re = 0, im = 0;
@@ -330,7 +337,8 @@ multidot_kernel(const double2 *__restrict__ V, int64_t ldv, const double2 *__res
 }
 
 __global__ void sum_partials_kernel(const double2 *__restrict__ partial, int nb, int ncol,
-                                    double2 *__restrict__ out) {
+                                    double2 *__restrict__ out, const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int col = blockIdx.x * blockDim.x + threadIdx.x;
     if (col >= ncol) return;
     double re = 0, im = 0;
@@ -343,7 +351,9 @@ __global__ void sum_partials_kernel(const double2 *__restrict__ partial, int nb,
 
 // w -= V[:, 0..ncol) h
 __global__ void gs_update_kernel(const double2 *__restrict__ V, int64_t ldv, int ncol,
-                                 const double2 *__restrict__ h, double2 *__restrict__ w, int64_t n) {
+                                 const double2 *__restrict__ h, double2 *__restrict__ w, int64_t n,
+                                 const int *__restrict__ stop) {
+    if (stop && *stop) return;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double re = w[i].x, im = w[i].y;
@@ -353,13 +363,6 @@ __global__ void gs_update_kernel(const double2 *__restrict__ V, int64_t ldv, int
         im -= v.x * hc.y + v.y * hc.x;
     }
     w[i] = make_double2(re, im);
-}
-
-// y = alpha * x (alpha real)
-__global__ void scale_kernel(const double2 *__restrict__ x, double alpha, double2 *__restrict__ y,
-                             int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] = make_double2(alpha * x[i].x, alpha * x[i].y);
 }
 
 // y = a - b
@@ -383,6 +386,146 @@ __global__ void combo_add_kernel(const double2 *__restrict__ V, int64_t ldv, int
     x[i] = make_double2(re, im);
 }
 
+// ---- device-resident Arnoldi state (one GMRES cycle without host round trips)
+// Layout in one device block: H (m+1) x m, g (m+1), sn (m), h1 (m+1), h2 (m+1),
+// y (m) complex; cs (m) real; scalars.
+struct GmScalars {
+    double2 nrm2;      // output of the last norm reduction (|w|^2 in .x)
+    double beta;       // residual norm at the start of the cycle
+    double inv_beta;
+    double inv_hn;     // 1 / h_{j+1,j} of the last step
+    double res;        // |g_{j+1}| after the last step
+    double tol;
+    int done;          // 1: converged (or breakdown); later kernels of the cycle skip
+    int start_ok;      // 1: the starting residual already met the tolerance
+    int jdone;         // Arnoldi steps completed in this cycle
+    int pad;
+};
+struct GmState {
+    double2 *H, *g, *sn, *h1, *h2, *y;
+    double *cs;
+    GmScalars *s;
+    int m;
+};
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double cabs2(double2 a) { return hypot(a.x, a.y); }
+
+// start of a cycle: beta = |w|, g = (beta, 0, ...), done = beta <= tol
+__global__ void gm_init_kernel(GmState st, double tol) {
+    GmScalars &s = *st.s;
+    s.tol = tol;
+    const double beta = sqrt(fmax(s.nrm2.x, 0.0));
+    s.beta = beta;
+    s.res = beta;
+    s.jdone = 0;
+    s.start_ok = beta <= s.tol ? 1 : 0;
+    s.done = s.start_ok;
+    s.inv_beta = beta > 0.0 ? 1.0 / beta : 0.0;
+    for (int k = 0; k <= st.m; ++k) st.g[k] = make_double2(0.0, 0.0);
+    st.g[0] = make_double2(beta, 0.0);
+}
+
+// Arnoldi step j: column j of H from the two Gram-Schmidt passes and |w|,
+// previous rotations applied, new rotation, residual estimate, stop test.
+// The rotation follows the host form used before (cs real, sn complex).
+__global__ void gm_givens_kernel(GmState st, int j) {
+    GmScalars &s = *st.s;
+    if (s.done) return;
+    const int ld = st.m + 1;
+    double2 *col = st.H + (int64_t)j * ld;
+    for (int k = 0; k <= j; ++k) col[k] = make_double2(st.h1[k].x + st.h2[k].x, st.h1[k].y + st.h2[k].y);
+    const double hn = sqrt(fmax(s.nrm2.x, 0.0));
+    col[j + 1] = make_double2(hn, 0.0);
+    s.inv_hn = hn > 0.0 ? 1.0 / hn : 0.0;
+    for (int k = 0; k < j; ++k) {
+        const double c = st.cs[k];
+        const double2 sn = st.sn[k];
+        const double2 a = col[k], b = col[k + 1];
+        const double2 t = make_double2(c * a.x + cmul(sn, b).x, c * a.y + cmul(sn, b).y);
+        const double2 u = cmul(cconj(sn), a);
+        col[k + 1] = make_double2(-u.x + c * b.x, -u.y + c * b.y);
+        col[k] = t;
+    }
+    // rotation zeroing col[j + 1]
+    const double2 a = col[j], b = col[j + 1];
+    const double na = cabs2(a), nb = cabs2(b);
+    double c;
+    double2 sn, r;
+    if (nb == 0.0) {
+        c = 1.0;
+        sn = make_double2(0.0, 0.0);
+        r = a;
+    } else if (na == 0.0) {
+        c = 0.0;
+        sn = make_double2(b.x / nb, -b.y / nb);
+        r = make_double2(nb, 0.0);
+    } else {
+        const double nrm = hypot(na, nb);
+        const double2 alpha = make_double2(a.x / na, a.y / na);
+        c = na / nrm;
+        const double2 t = cmul(alpha, cconj(b));
+        sn = make_double2(t.x / nrm, t.y / nrm);
+        r = make_double2(alpha.x * nrm, alpha.y * nrm);
+    }
+    st.cs[j] = c;
+    st.sn[j] = sn;
+    col[j] = r;
+    col[j + 1] = make_double2(0.0, 0.0);
+    const double2 gj = st.g[j], gj1 = st.g[j + 1];
+    const double2 sg = cmul(sn, gj1);
+    const double2 ug = cmul(cconj(sn), gj);
+    st.g[j] = make_double2(c * gj.x + sg.x, c * gj.y + sg.y);
+    st.g[j + 1] = make_double2(-ug.x + c * gj1.x, -ug.y + c * gj1.y);
+    s.res = cabs2(st.g[j + 1]);
+    s.jdone = j + 1;
+    if (s.res <= s.tol || hn == 0.0) s.done = 1;
+}
+
+// y = R^{-1} g over the jdone columns (back substitution)
+__global__ void gm_trisolve_kernel(GmState st) {
+    const int j = st.s->jdone;
+    const int ld = st.m + 1;
+    for (int k = j - 1; k >= 0; --k) {
+        double2 acc = st.g[k];
+        for (int l = k + 1; l < j; ++l) {
+            const double2 t = cmul(st.H[(int64_t)l * ld + k], st.y[l]);
+            acc.x -= t.x;
+            acc.y -= t.y;
+        }
+        const double2 d = st.H[(int64_t)k * ld + k];
+        const double den = d.x * d.x + d.y * d.y;
+        st.y[k] = make_double2((acc.x * d.x + acc.y * d.y) / den, (acc.y * d.x - acc.x * d.y) / den);
+    }
+}
+
+// y = x * (*alpha) (alpha real, on the device)
+__global__ void scale_dev_kernel(const double2 *__restrict__ x, const double *__restrict__ alpha,
+                                 double2 *__restrict__ y, int64_t n, const int *__restrict__ stop) {
+    if (stop && *stop) return;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const double a = *alpha;
+    if (i < n) y[i] = make_double2(a * x[i].x, a * x[i].y);
+}
+
+// x += V[:, 0..*ncol) yc  (column count on the device)
+__global__ void combo_add_dev_kernel(const double2 *__restrict__ V, int64_t ldv, const int *__restrict__ ncol,
+                                     const double2 *__restrict__ yc, double2 *__restrict__ x, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int nc = *ncol;
+    double re = x[i].x, im = x[i].y;
+    for (int c = 0; c < nc; ++c) {
+        const double2 v = V[(int64_t)c * ldv + i], y = yc[c];
+        re += v.x * y.x - v.y * y.y;
+        im += v.x * y.y + v.y * y.x;
+    }
+    x[i] = make_double2(re, im);
+}
+
 __global__ void round_c64_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, int64_t n) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
@@ -397,28 +540,50 @@ inline unsigned blocks(int64_t n, int t = 256) { return (unsigned)((n + t - 1) /
 struct Solver {
     Ctx &c;
     int64_t n;
+    int m;                        // restart length
     double2 *part = nullptr;      // gemv slices / multidot partials
     int S = 1;
     int nbdot = 1;
     double2 *hdev = nullptr;      // device scratch for dot results (>= restart + 2)
     std::vector<double2> hhost;
+    GmState st{};                 // device-resident Arnoldi state
+    const int *stop = nullptr;    // device stop flag honoured by the launches below
 
-    Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_) {
+    Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_), m(restart) {
         // column slices: ~8 blocks per SM for the two-rows-per-thread complex64 product
         S = 1;
         const int64_t row_tiles = (n / 2 + kT - 1) / kT;
         while (row_tiles * S < 8LL * c.num_sms && S < 64) S *= 2;
         nbdot = (int)std::min<int64_t>(std::max<int64_t>(1, (n + kT * 8 - 1) / (kT * 8)), 256);
         const size_t part_bytes = (size_t)std::max<int64_t>(S * n, (int64_t)(restart + 2) * nbdot) * 16;
-        char *base = static_cast<char *>(c.scratch(kScratchSolverPart, part_bytes + (size_t)(restart + 2) * 16));
+        const size_t hbytes = (size_t)(restart + 2) * 16;
+        const size_t nc = (size_t)(restart + 1) * restart + 4 * (size_t)(restart + 1) + restart;
+        const size_t st_bytes = nc * 16 + (size_t)restart * 8 + sizeof(GmScalars) + 64;
+        char *base = static_cast<char *>(c.scratch(kScratchSolverPart, part_bytes + hbytes + st_bytes));
         part = reinterpret_cast<double2 *>(base);
         hdev = reinterpret_cast<double2 *>(base + part_bytes);
+        double2 *z = reinterpret_cast<double2 *>(base + part_bytes + hbytes);
+        st.m = restart;
+        st.H = z;
+        z += (size_t)(restart + 1) * restart;
+        st.g = z;
+        z += restart + 1;
+        st.sn = z;
+        z += restart;
+        st.h1 = z;
+        z += restart + 1;
+        st.h2 = z;
+        z += restart + 1;
+        st.y = z;
+        z += restart + 1;
+        st.cs = reinterpret_cast<double *>(z);
+        st.s = reinterpret_cast<GmScalars *>(reinterpret_cast<char *>(st.cs) + (((size_t)restart * 8 + 15) & ~size_t(15)));
         hhost.resize(restart + 2);
     }
 
     void launched() { ++c.kernel_launches; }
 
-    // y = s (K x) + d .* x
+    // y = s (K x) + d .* x   (dense kernels skip when *stop is set)
     void apply(const bie_operator &op, int precision, const double2 *x, double2 *y) {
         const double2 sc = make_double2(op.scale_re, op.scale_im);
         const double2 *d = reinterpret_cast<const double2 *>(op.diag);
@@ -433,56 +598,63 @@ struct Solver {
                     dim3 grid(blocks(n / 2, kT), (unsigned)S);
                     if (exact)
                         dense_gemv_c64_exact_kernel<<<grid, kT, 0, c.stream>>>(
-                            reinterpret_cast<const float4 *>(op.A32), n, x, part, S);
+                            reinterpret_cast<const float4 *>(op.A32), n, x, part, S, stop);
                     else
                         dense_gemv_c64_kernel<<<grid, kT, 0, c.stream>>>(
-                            reinterpret_cast<const float4 *>(op.A32), n, x, part, S);
+                            reinterpret_cast<const float4 *>(op.A32), n, x, part, S, stop);
                 } else {
                     dim3 grid(blocks(n, kT), (unsigned)S);
                     if (exact)
                         dense_gemv_c64_rows_exact_kernel<<<grid, kT, 0, c.stream>>>(
-                            reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
+                            reinterpret_cast<const float2 *>(op.A32), n, x, part, S, stop);
                     else
                         dense_gemv_c64_rows_kernel<<<grid, kT, 0, c.stream>>>(
-                            reinterpret_cast<const float2 *>(op.A32), n, x, part, S);
+                            reinterpret_cast<const float2 *>(op.A32), n, x, part, S, stop);
                 }
             } else {
                 dim3 grid(blocks(n, kT), (unsigned)S);
                 dense_gemv_kernel<double2><<<grid, kT, 0, c.stream>>>(
-                    reinterpret_cast<const double2 *>(op.A), n, x, part, S);
+                    reinterpret_cast<const double2 *>(op.A), n, x, part, S, stop);
             }
             BIE_CUDA(cudaGetLastError());
             c.timer_end(t0);
             launched();
-            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(part, S, n, sc, d, x, y);
+            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(part, S, n, sc, d, x, y, stop);
             BIE_CUDA(cudaGetLastError());
             launched();
         } else {
             // matrix-free F x (or the fast operator) into y, then y = s y + d .* x
+            // (these products do not look at the stop flag: the caller checks it
+            // on the host after every step)
             if (op.kind == BIE_OP_FAST) {
                 FastOp &f = *const_cast<FastOp *>(reinterpret_cast<const FastOp *>(op.fast));
                 apply_fastop(f, reinterpret_cast<const double *>(x), reinterpret_cast<double *>(y), precision,
                              nullptr, 0);
             } else {
-                MatvecArgs m{op.k_re, op.k_im, c.d_sources, n, reinterpret_cast<const double *>(x),
-                             nullptr, reinterpret_cast<double *>(y), nullptr, precision};
-                launch_matvec(c, m);
+                MatvecArgs mv{op.k_re, op.k_im, c.d_sources, n, reinterpret_cast<const double *>(x),
+                              nullptr, reinterpret_cast<double *>(y), nullptr, precision};
+                launch_matvec(c, mv);
             }
-            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(y, 1, n, sc, d, x, y);
+            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(y, 1, n, sc, d, x, y, stop);
             BIE_CUDA(cudaGetLastError());
             launched();
         }
     }
 
+    // out[0..ncol) = V[:, 0..ncol)^H w on the device (no host copy)
+    void multidot_dev(const double2 *V, int64_t ldv, int ncol, const double2 *w, double2 *out) {
+        dim3 grid((unsigned)nbdot, (unsigned)ncol);
+        multidot_kernel<<<grid, kT, 0, c.stream>>>(V, ldv, w, n, part, stop);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+        sum_partials_kernel<<<blocks(ncol, 64), 64, 0, c.stream>>>(part, nbdot, ncol, out, stop);
+        BIE_CUDA(cudaGetLastError());
+        launched();
+    }
+
     // out[0..ncol) = V[:, 0..ncol)^H w  (copied to host)
     void multidot(const double2 *V, int64_t ldv, int ncol, const double2 *w, std::vector<cplx> &out) {
-        dim3 grid((unsigned)nbdot, (unsigned)ncol);
-        multidot_kernel<<<grid, kT, 0, c.stream>>>(V, ldv, w, n, part);
-        BIE_CUDA(cudaGetLastError());
-        launched();
-        sum_partials_kernel<<<blocks(ncol, 64), 64, 0, c.stream>>>(part, nbdot, ncol, hdev);
-        BIE_CUDA(cudaGetLastError());
-        launched();
+        multidot_dev(V, ldv, ncol, w, hdev);
         BIE_CUDA(cudaMemcpyAsync(hhost.data(), hdev, ncol * sizeof(double2), cudaMemcpyDeviceToHost, c.stream));
         BIE_CUDA(cudaStreamSynchronize(c.stream));
         out.resize(ncol);
@@ -501,9 +673,9 @@ struct Solver {
                                  c.stream));
     }
 
-    void gs_update(const double2 *V, int64_t ldv, int ncol, double2 *w, const std::vector<cplx> &h) {
-        upload_coeffs(h);
-        gs_update_kernel<<<blocks(n), 256, 0, c.stream>>>(V, ldv, ncol, hdev, w, n);
+    // w -= V[:, 0..ncol) h  with h on the device
+    void gs_update_dev(const double2 *V, int64_t ldv, int ncol, double2 *w, const double2 *h) {
+        gs_update_kernel<<<blocks(n), 256, 0, c.stream>>>(V, ldv, ncol, h, w, n, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
     }
@@ -515,8 +687,8 @@ struct Solver {
         launched();
     }
 
-    void scale(const double2 *x, double a, double2 *y) {
-        scale_kernel<<<blocks(n), 256, 0, c.stream>>>(x, a, y, n);
+    void scale_dev(const double2 *x, const double *a, double2 *y) {
+        scale_dev_kernel<<<blocks(n), 256, 0, c.stream>>>(x, a, y, n, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
     }
@@ -528,112 +700,91 @@ struct Solver {
     }
 };
 
-// Givens rotation zeroing b in (a, b): [c s; -conj(s) c] (a, b)^T = (r, 0)^T
-inline void givens(cplx a, cplx b, double &cs, cplx &sn, cplx &r) {
-    const double na = std::abs(a), nb = std::abs(b);
-    if (nb == 0.0) {
-        cs = 1.0;
-        sn = 0.0;
-        r = a;
-        return;
-    }
-    if (na == 0.0) {
-        cs = 0.0;
-        sn = std::conj(b) / nb;
-        r = nb;
-        return;
-    }
-    const double nrm = std::hypot(na, nb);
-    const cplx alpha = a / na;
-    cs = na / nrm;
-    sn = alpha * std::conj(b) / nrm;
-    r = alpha * nrm;
-}
-
 // One GMRES solve of A x = b from the initial x (device), operator precision
 // `prec`; returns the number of iterations; `tol` is an absolute tolerance on
 // the residual norm.  V: (restart + 1) x n workspace.
+//
+// Each restart cycle runs on the device without host round trips: the
+// Gram-Schmidt coefficients, the Hessenberg column, the Givens rotations and
+// the residual estimate stay in device memory (GmState), a single-thread
+// kernel decides convergence and raises a stop flag, and every later kernel of
+// the cycle returns at once when it sees the flag.  The host reads the state
+// once per cycle (dense operators) or once per step (matrix-free and fast
+// operators, whose products do not look at the flag).
 int gmres_core(Solver &S, const bie_operator &op, int prec, const double2 *b, double2 *x,
                bool x_zero, double2 *V, double2 *w, int restart, int maxiter, double tol,
                double *res_out, int *restarts_out, int64_t *matvecs) {
     const int64_t n = S.n;
+    const bool dense = op.kind == BIE_OP_DENSE;
+    const GmState st = S.st;
+    const int *stop_flag = &st.s->done;
+    cudaStream_t stream = S.c.stream;
     int it = 0, restarts = 0;
     double beta = 0.0;
-    std::vector<cplx> H((size_t)(restart + 1) * restart), g(restart + 1), sn(restart), h;
-    std::vector<double> cs(restart);
     bool first = true;
+    GmScalars hs{};
     while (true) {
-        // r = b - A x  (r = b for a zero start)
+        // r = b - A x  (r = b for a zero start), beta = |r|
+        S.stop = nullptr;
         if (first && x_zero) {
-            BIE_CUDA(cudaMemcpyAsync(w, b, (size_t)n * 16, cudaMemcpyDeviceToDevice, S.c.stream));
+            BIE_CUDA(cudaMemcpyAsync(w, b, (size_t)n * 16, cudaMemcpyDeviceToDevice, stream));
         } else {
             S.apply(op, prec, x, w);
             ++*matvecs;
             S.sub(b, w, w);
         }
         first = false;
-        beta = S.norm(w);
-        if (beta <= tol || it >= maxiter) break;
-        S.scale(w, 1.0 / beta, V);
-        std::fill(g.begin(), g.end(), cplx(0.0));
-        g[0] = beta;
-        int j = 0;
-        double res = beta;
-        for (; j < restart && it < maxiter; ++j) {
-            double2 *vj = V + (int64_t)j * n;
-            double2 *vn = V + (int64_t)(j + 1) * n;
-            S.apply(op, prec, vj, w);
-            ++*matvecs;
-            ++it;
-            // CGS2
-            std::vector<cplx> h1, h2;
-            S.multidot(V, n, j + 1, w, h1);
-            S.gs_update(V, n, j + 1, w, h1);
-            S.multidot(V, n, j + 1, w, h2);
-            S.gs_update(V, n, j + 1, w, h2);
-            for (int k = 0; k <= j; ++k) H[(size_t)j * (restart + 1) + k] = h1[k] + h2[k];
-            const double hn = S.norm(w);
-            H[(size_t)j * (restart + 1) + j + 1] = hn;
-            if (hn > 0) S.scale(w, 1.0 / hn, vn);
-            // apply previous rotations to column j
-            cplx *col = &H[(size_t)j * (restart + 1)];
-            for (int k = 0; k < j; ++k) {
-                const cplx t = cs[k] * col[k] + sn[k] * col[k + 1];
-                col[k + 1] = -std::conj(sn[k]) * col[k] + cs[k] * col[k + 1];
-                col[k] = t;
-            }
-            cplx r;
-            givens(col[j], col[j + 1], cs[j], sn[j], r);
-            col[j] = r;
-            col[j + 1] = 0.0;
-            const cplx gt = cs[j] * g[j] + sn[j] * g[j + 1];
-            g[j + 1] = -std::conj(sn[j]) * g[j] + cs[j] * g[j + 1];
-            g[j] = gt;
-            res = std::abs(g[j + 1]);
-            if (res <= tol || hn == 0.0) {
-                ++j;
-                break;
-            }
-        }
-        // solve the triangular system and update x
-        std::vector<cplx> y(j);
-        for (int k = j - 1; k >= 0; --k) {
-            cplx s = g[k];
-            for (int l = k + 1; l < j; ++l) s -= H[(size_t)l * (restart + 1) + k] * y[l];
-            y[k] = s / H[(size_t)k * (restart + 1) + k];
-        }
-        if (j > 0) S.combo_add(V, n, j, y, x);
-        ++restarts;
-        if (res <= tol && j < restart) {
-            // converged inside the cycle: final true residual below
-        }
-        if (it >= maxiter) {
-            S.apply(op, prec, x, w);
-            ++*matvecs;
-            S.sub(b, w, w);
-            beta = S.norm(w);
+        S.multidot_dev(w, n, 1, w, &st.s->nrm2);
+        gm_init_kernel<<<1, 1, 0, stream>>>(st, tol);
+        BIE_CUDA(cudaGetLastError());
+        S.launched();
+        const int jmax = std::min(restart, std::max(0, maxiter - it));
+        BIE_CUDA(cudaMemcpyAsync(&hs, st.s, sizeof(GmScalars), cudaMemcpyDeviceToHost, stream));
+        BIE_CUDA(cudaStreamSynchronize(stream));
+        if (hs.start_ok || jmax == 0) {
+            beta = hs.beta;
             break;
         }
+        S.stop = stop_flag;
+        S.scale_dev(w, &st.s->inv_beta, V);
+        for (int j = 0; j < jmax; ++j) {
+            const double2 *vj = V + (int64_t)j * n;
+            double2 *vn = V + (int64_t)(j + 1) * n;
+            S.apply(op, prec, vj, w);
+            // CGS2
+            S.multidot_dev(V, n, j + 1, w, st.h1);
+            S.gs_update_dev(V, n, j + 1, w, st.h1);
+            S.multidot_dev(V, n, j + 1, w, st.h2);
+            S.gs_update_dev(V, n, j + 1, w, st.h2);
+            S.multidot_dev(w, n, 1, w, &st.s->nrm2);
+            gm_givens_kernel<<<1, 1, 0, stream>>>(st, j);
+            BIE_CUDA(cudaGetLastError());
+            S.launched();
+            S.scale_dev(w, &st.s->inv_hn, vn);
+            // the host looks at the stop flag after every step for operators whose
+            // products ignore it, every kCheck steps for dense ones (at most
+            // kCheck - 1 skipped steps are queued after convergence)
+            constexpr int kCheck = 4;
+            if (!dense || j % kCheck == kCheck - 1) {
+                int done = 0;
+                BIE_CUDA(cudaMemcpyAsync(&done, stop_flag, sizeof(int), cudaMemcpyDeviceToHost, stream));
+                BIE_CUDA(cudaStreamSynchronize(stream));
+                if (done) break;
+            }
+        }
+        // x += V y,  R y = g
+        S.stop = nullptr;
+        gm_trisolve_kernel<<<1, 1, 0, stream>>>(st);
+        BIE_CUDA(cudaGetLastError());
+        combo_add_dev_kernel<<<blocks(n), 256, 0, stream>>>(V, n, &st.s->jdone, st.y, x, n);
+        BIE_CUDA(cudaGetLastError());
+        S.launched();
+        S.launched();
+        BIE_CUDA(cudaMemcpyAsync(&hs, st.s, sizeof(GmScalars), cudaMemcpyDeviceToHost, stream));
+        BIE_CUDA(cudaStreamSynchronize(stream));
+        it += hs.jdone;
+        *matvecs += hs.jdone;
+        ++restarts;
     }
     *res_out = beta;
     *restarts_out = restarts;
