@@ -14,5 +14,6 @@ from .operators import (Diagonal, FMMFOperator, FMMGOperator, GPUFOperator, GPUG
                         UniformScaling, gmres)
 from .sweep import sweep  # noqa: F401
 from .adjoint import farfield_objective  # noqa: F401
+from .rosebem import apply_taylor_expansion, taylor_assemble  # noqa: F401
 
 __version__ = "0.1.0"

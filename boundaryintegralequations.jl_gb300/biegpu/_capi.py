@@ -186,6 +186,7 @@ SIGNATURES = {
     "bie_matvec_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_matvec_multi": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_lowp_gemm_device": (_I, [_P, _I, _I64, _I64, _I64, _P, _P, _P]),
+    "bie_taylor_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
     "bie_fastop_create": (_I, [_P, _D, _D, _I, _I, _I, _D, _I, C.POINTER(_P)]),
     "bie_fastop_destroy": (_I, [_P]),
     "bie_fastop_apply_device": (_I, [_P, _P, _P, _I]),

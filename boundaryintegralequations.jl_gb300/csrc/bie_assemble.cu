@@ -41,7 +41,7 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
                      int flags, double2 *__restrict__ F, double2 *__restrict__ G,
                      double *__restrict__ Cpart, int chunk,
                      unsigned long long *__restrict__ qpe_count,
-                     const double2 *__restrict__ gweight) {
+                     const double2 *__restrict__ gweight, int tm) {
     extern __shared__ __align__(16) double smem[];
     double *s_phi = smem;                                   // nphi doubles (padded even)
     double *s_rec = smem + ((nphi + 1) & ~1);               // chunk * stride doubles
@@ -79,12 +79,15 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
 
         for (int el = 0; el < n; ++el) {
             const double *r = s_rec + (size_t)el * stride;
-            const int c = dev::nearest_node<NP>(r, tx, ty, tz);
+            // k-derivative assembly uses the three corner rules only, nodes 4-6
+            // falling to the third (taylor_assemble!, src/3d/rosebem.jl:114-127)
+            const int cn = dev::nearest_node<NP>(r, tx, ty, tz);
+            const int c = (tm >= 0 && cn > 2) ? 2 : cn;
             const int Q = ri.Q[c];
             nqpe += Q;
             double fr[NP], fi[NP], gr[NP], gi[NP];
             cacc += dev::element_fp64<NP, CPLX_K>(r + ri.off[c], Q, s_phi + (size_t)c * qmax * NP,
-                                                  tx, ty, tz, kre, kim, fr, fi, gr, gi);
+                                                  tx, ty, tz, kre, kim, fr, fi, gr, gi, tm);
 
             if (gweight && doG) {   // element factor on the single layer
                 const double2 wgt = gweight[cb + el];
@@ -151,7 +154,7 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int
         c.d_shared_mask + (size_t)level * c.n_elements, c.d_phi, L.R * L.qmax * L.NP, L.qmax,
         ri, a.targets, a.M, a.k_re, a.k_im, a.flags, reinterpret_cast<double2 *>(a.F),
         reinterpret_cast<double2 *>(a.G), Cpart, chunk, c.d_qpe,
-        reinterpret_cast<const double2 *>(a.g_weight));
+        reinterpret_cast<const double2 *>(a.g_weight), a.taylor_m);
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;

@@ -216,6 +216,41 @@ int bie_assemble(bie_ctx *ctx, double k_re, double k_im, const double *targets, 
     });
 }
 
+int bie_taylor_assemble(bie_ctx *ctx, double k0_re, double k0_im, const double *targets, int64_t n_targets,
+                        int flags, int order, double *F, double *G, double *C) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        const int64_t M = targets ? n_targets : c.n_sources;
+        check_assemble_args(c, k0_re, k0_im, M, flags, BIE_PREC_FP64, F, G, C);
+        if (order < 0 || order > 64) bie::fail(BIE_ERR_INVALID, "order must be in 0..64");
+        BIE_CUDA(cudaSetDevice(c.device));
+        const double *d_t = c.d_sources;
+        if (targets) {
+            for (int64_t i = 0; i < 3 * M; ++i)
+                if (!std::isfinite(targets[i])) bie::fail(BIE_ERR_INVALID, "non-finite target");
+            double *dt = static_cast<double *>(c.scratch(bie::kScratchTargets, (size_t)M * 24));
+            BIE_CUDA(cudaMemcpyAsync(dt, targets, (size_t)M * 24, cudaMemcpyHostToDevice, c.stream));
+            d_t = dt;
+        }
+        const size_t mat = (size_t)M * (size_t)c.n_sources * 16;
+        const size_t ent = (size_t)M * (size_t)c.n_sources * 2;   // doubles per matrix
+        for (int m = 0; m <= order; ++m) {
+            const int fl = (flags & (BIE_F | BIE_G)) | (m == 0 ? (flags & BIE_C) : 0);
+            bie::AssembleArgs a{k0_re, k0_im, d_t, M, fl, nullptr, nullptr, nullptr};
+            a.taylor_m = m;
+            if (fl & BIE_F) a.F = static_cast<double *>(c.scratch(bie::kScratchF, mat));
+            if (fl & BIE_G) a.G = static_cast<double *>(c.scratch(bie::kScratchG, mat));
+            if (fl & BIE_C) a.C = static_cast<double *>(c.scratch(bie::kScratchC, (size_t)M * 16));
+            bie::launch_assemble_fp64(c, a);
+            if (fl & BIE_F) BIE_CUDA(cudaMemcpyAsync(F + m * ent, a.F, mat, cudaMemcpyDeviceToHost, c.stream));
+            if (fl & BIE_G) BIE_CUDA(cudaMemcpyAsync(G + m * ent, a.G, mat, cudaMemcpyDeviceToHost, c.stream));
+            if (fl & BIE_C) BIE_CUDA(cudaMemcpyAsync(C, a.C, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
+            BIE_CUDA(cudaStreamSynchronize(c.stream));
+        }
+    });
+}
+
 int bie_matvec(bie_ctx *ctx, double k_re, double k_im, const double *targets, int64_t n_targets,
                const double *x, const double *v, double *yF, double *yG, int precision) {
     return guarded([&] {

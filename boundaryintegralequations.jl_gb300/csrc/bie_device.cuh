@@ -73,7 +73,11 @@ __device__ __forceinline__ int nearest_node(const double *P, double tx, double t
 template <int NP, bool CPLX_K>
 __device__ __forceinline__ double element_fp64(const double *g, int Q, const double *ph, double tx,
                                                double ty, double tz, double kre, double kim,
-                                               double *fr, double *fi, double *gr, double *gi) {
+                                               double *fr, double *fi, double *gr, double *gi,
+                                               int tm = -1) {
+    // tm >= 0: tm-th derivative with respect to k (taylor_greens3d!,
+    // taylor_freens3d!, src/3d/kernels.jl:94-118): both kernels times (i r)^tm,
+    // and F's factor (i k r - 1) becomes (i k r - 1 + tm).
 #pragma unroll
     for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.0;
     double ce = 0.0;
@@ -95,14 +99,29 @@ __device__ __forceinline__ double element_fp64(const double *g, int Q, const dou
         }
         // G: e^{ikr} / (4 pi r) * jw
         const double wg = rinv * kInv4Pi * jw;
-        const double Gr = cs * wg, Gi = sn * wg;
+        double Gr = cs * wg, Gi = sn * wg;
         // C: -(x - y).n / (4 pi r^3) * jw ; F: e^{ikr} (ikr - 1) (x - y).n / (4 pi r^3) * jw
         const double tq = dn * (rinv * rinv * rinv) * kInv4Pi * jw;
         ce -= tq;
-        const double ar = CPLX_K ? (-1.0 - kim * rr) : -1.0;
+        double ar = CPLX_K ? (-1.0 - kim * rr) : -1.0;
         const double ai = kre * rr;
-        const double Fr = (cs * ar - sn * ai) * tq;
-        const double Fi = (cs * ai + sn * ar) * tq;
+        if (tm > 0) ar += (double)tm;
+        double Fr = (cs * ar - sn * ai) * tq;
+        double Fi = (cs * ai + sn * ar) * tq;
+        if (tm > 0) {
+            double rm = rr;
+            for (int t = 1; t < tm; ++t) rm *= rr;
+            // (i r)^tm = i^tm r^tm
+            const int q4 = tm & 3;
+            const double pr = q4 == 0 ? rm : (q4 == 2 ? -rm : 0.0);
+            const double pi = q4 == 1 ? rm : (q4 == 3 ? -rm : 0.0);
+            double t0 = Gr * pr - Gi * pi;
+            Gi = Gr * pi + Gi * pr;
+            Gr = t0;
+            t0 = Fr * pr - Fi * pi;
+            Fi = Fr * pi + Fi * pr;
+            Fr = t0;
+        }
         const double *pq = ph + q * NP;
 #pragma unroll
         for (int a = 0; a < NP; ++a) {

@@ -210,6 +210,8 @@ struct AssembleArgs {
     bool c64_out = false;    // mixed only: F, G are complex64 (float2) buffers, not widened
     const double *g_weight = nullptr;   // FP64 only: per-element complex factor on G
                                         // (Morton record order), e.g. an element admittance
+    int taylor_m = -1;                  // FP64 only: >= 0 assembles the taylor_m-th
+                                        // k-derivative (corner rules only)
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);

@@ -314,6 +314,24 @@ BIE_API int bie_nearfield_assemble(bie_ctx *ctx, double k_re, double k_im, int d
                                    double offset, int flags, int coarse, int n_gauss,
                                    double *F, double *G);
 
+/*
+ * Derivatives of F and G with respect to the wavenumber at k0, for Taylor
+ * expansions in k (ROSEBEM): taylor_assemble!(mesh, k0, targets,
+ * shape_function; M = order, fOn, gOn, cOn, n, m) with U = I
+ * (src/3d/rosebem.jl:56-157; kernels taylor_greens3d! / taylor_freens3d!,
+ * src/3d/kernels.jl:94-118):
+ *   G^(m) = (i r)^m e^{i k0 r} / (4 pi r),
+ *   F^(m) = e^{i k0 r} (i r)^m (1 - i k0 r - m) n.(x - y) / (4 pi r^3),
+ * integrated with the clustered corner rules of the context (physics nodes
+ * 4-6 of quadratic elements use the third corner rule, as the reference
+ * does).  F, G: M x N x (order + 1) complex column-major (matrix m at offset
+ * m M N), C: M complex (from the same rules).  FP64.  Host buffers, blocking.
+ * The expansion itself, sum_m (k - k0)^m / m! A^(m), is a host operation
+ * (apply_taylor_expansion, src/3d/rosebem.jl:164-176).
+ */
+BIE_API int bie_taylor_assemble(bie_ctx *ctx, double k0_re, double k0_im, const double *targets,
+                                int64_t n_targets, int flags, int order, double *F, double *G, double *C);
+
 /* ---- fast operators (FMMFOperator / FMMGOperator) ----------------------- */
 typedef struct bie_fastop bie_fastop;
 

@@ -63,6 +63,9 @@ def lib():
             L.oracle_assemble_w.restype = I
             L.oracle_assemble_w.argtypes = [P, I64, P, I, P, I, I64, P, I64, P, I64, I, I, D, D, I,
                                              P, P, P, I, P]
+            L.oracle_taylor_assemble.restype = I
+            L.oracle_taylor_assemble.argtypes = [P, I64, P, I, P, I, I64, P, I64, P, I64, I, I, D, D, I, I,
+                                                 P, P, P, I]
             L.oracle_singular_rule.restype = I
             L.oracle_singular_rule.argtypes = [I, D, P, P, P, I]
             L.oracle_nearfield.restype = I
@@ -171,6 +174,30 @@ def farfield_objective(mesh, k, Z, field_points, rho_c=1.21 * 343.0, direction=(
     Fx, Gx, _ = assemble(mesh, k, targets=X, n=n, m=m, cOn=False, g_weight=Y)
     pf = np.exp(-1j * k * (d @ X)) + (-Fx + 1j * rho_c * k * Gx) @ p
     return float(np.sum(np.abs(pf) ** 2)), pf
+
+
+def taylor_assemble(mesh, k0, order, targets=None, n=3, m=3, fOn=True, gOn=True, cOn=True, threads=0):
+    """taylor_assemble! (src/3d/rosebem.jl:56-157) with U = I: F, G of shape
+    (M, N, order + 1) (k-derivatives m = 0..order at k0) and C."""
+    k0 = complex(k0)
+    c = np.asfortranarray(mesh.coordinates, dtype=np.float64)
+    t = np.asfortranarray(mesh.topology, dtype=np.int64)
+    pt = np.asfortranarray(mesh.physics_topology, dtype=np.int64)
+    s = np.asfortranarray(mesh.sources, dtype=np.float64)
+    tg = s if targets is None else np.asfortranarray(targets, dtype=np.float64)
+    N, M = s.shape[1], tg.shape[1]
+    F = np.zeros((M, N, order + 1), dtype=np.complex128, order="F") if fOn else None
+    G = np.zeros((M, N, order + 1), dtype=np.complex128, order="F") if gOn else None
+    Cv = np.zeros(M, dtype=np.complex128) if cOn else None
+    flags = (1 if fOn else 0) | (2 if gOn else 0) | (4 if cOn else 0)
+    addr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+    st = lib().oracle_taylor_assemble(c.ctypes.data, c.shape[1], t.ctypes.data, _KIND[mesh.shape_function],
+                                      pt.ctypes.data, _KIND[mesh.physics_function], t.shape[1], s.ctypes.data,
+                                      N, tg.ctypes.data, M, n, m, k0.real, k0.imag, flags, int(order),
+                                      addr(F), addr(G), addr(Cv), int(threads))
+    if st != 0:
+        raise RuntimeError("oracle_taylor_assemble failed")
+    return F, G, Cv
 
 
 def fast_operator(mesh, k, which="F", n_gauss=3, nearfield=True, offset=0.2, depth=1):

@@ -267,10 +267,42 @@ static int gauss_triangle(int n, double *u, double *v, double *w);
  * on the single-layer contributions (element admittance weighting).
  * n < 0: every rule is the symmetric (-n)-point triangle rule (the far-field
  * rule of setup_fast_operator, src/3d/fast_multipole_method.jl:163-170). */
+static int assemble_impl(const double *coords, int64_t Nc, const int64_t *topo, int skind,
+                         const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
+                         const double *targets, int64_t M, int n, int m, double kre, double kim,
+                         int flags, double *F, double *G, double *C, int nthreads, const double *gw,
+                         int tm);
+
 int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int skind,
                       const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
                       const double *targets, int64_t M, int n, int m, double kre, double kim,
                       int flags, double *F, double *G, double *C, int nthreads, const double *gw) {
+    return assemble_impl(coords, Nc, topo, skind, ptopo, pkind, E, sources, N, targets, M, n, m, kre, kim,
+                         flags, F, G, C, nthreads, gw, -1);
+}
+
+/* taylor_assemble! (src/3d/rosebem.jl:56-157) with U = I: matrices m = 0..order
+ * of the k-derivatives (taylor_greens3d!, taylor_freens3d!, src/3d/kernels.jl:
+ * 94-118), F and G stacked as M x N x (order + 1); C from the same rules. */
+int oracle_taylor_assemble(const double *coords, int64_t Nc, const int64_t *topo, int skind,
+                           const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
+                           const double *targets, int64_t M, int n, int m, double kre, double kim,
+                           int flags, int order, double *F, double *G, double *C, int nthreads) {
+    for (int t = 0; t <= order; ++t) {
+        const int fl = (flags & (OR_F | OR_G)) | (t == 0 ? (flags & OR_C) : 0);
+        const int st = assemble_impl(coords, Nc, topo, skind, ptopo, pkind, E, sources, N, targets, M, n, m,
+                                     kre, kim, fl, F ? F + (size_t)2 * t * M * N : NULL,
+                                     G ? G + (size_t)2 * t * M * N : NULL, C, nthreads, NULL, t);
+        if (st) return st;
+    }
+    return 0;
+}
+
+static int assemble_impl(const double *coords, int64_t Nc, const int64_t *topo, int skind,
+                         const int64_t *ptopo, int pkind, int64_t E, const double *sources, int64_t N,
+                         const double *targets, int64_t M, int n, int m, double kre, double kim,
+                         int flags, double *F, double *G, double *C, int nthreads, const double *gw,
+                         int tm) {
     (void)Nc;
     if (n < 0) {
         double tu[16], tv[16], tw[16];
@@ -324,6 +356,9 @@ int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int
                 double d = julia_hypot3(P[0] - s[0], P[1] - s[1], P[2] - s[2]);
                 if (d < best) { best = d; c = a; }
             }
+            /* k-derivative assembly: corner rules only, nodes 4-6 -> rule 3
+             * (taylor_assemble!, src/3d/rosebem.jl:114-127) */
+            if (tm >= 0 && c > 2) c = 2;
             const int Qr = Q[c];
             const double *x = X[c] + (size_t)e * 3 * Qr;
             const double *nr = NR[c] + (size_t)e * 3 * Qr;
@@ -335,6 +370,8 @@ int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int
             if (flags & OR_G) {
                 for (int q = 0; q < Qr; ++q)
                     integrand[q] = cexp(I * k * rr[q]) / (4.0 * PI * rr[q]);      /* greens3d! */
+                if (tm >= 0)                                                        /* taylor_greens3d! */
+                    for (int q = 0; q < Qr; ++q) integrand[q] *= cpow(I * rr[q], tm);
                 for (int q = 0; q < Qr; ++q) integrand[q] = integrand[q] * jw[q];  /* integrand_mul! */
                 for (int a = 0; a < NP; ++a) {                                      /* mygemm_vec! */
                     double complex acc = 0.0;
@@ -359,8 +396,13 @@ int oracle_assemble_w(const double *coords, int64_t Nc, const int64_t *topo, int
                 for (int q = 0; q < Qr; ++q) {                                      /* freens3d! */
                     double dn = nr[3 * q] * (x[3 * q] - s[0]) + nr[3 * q + 1] * (x[3 * q + 1] - s[1]) +
                                 nr[3 * q + 2] * (x[3 * q + 2] - s[2]);
-                    integrand[q] = cexp(I * k * rr[q]) * (I * k * rr[q] - 1.0) * dn /
-                                   (4.0 * PI * rr[q] * rr[q] * rr[q]);
+                    if (tm >= 0)                                                    /* taylor_freens3d! */
+                        integrand[q] = cexp(I * k * rr[q]) * cpow(I * rr[q], tm) *
+                                       (1.0 - I * k * rr[q] - tm) * (-dn) /
+                                       (4.0 * PI * rr[q] * rr[q] * rr[q]);
+                    else
+                        integrand[q] = cexp(I * k * rr[q]) * (I * k * rr[q] - 1.0) * dn /
+                                       (4.0 * PI * rr[q] * rr[q] * rr[q]);
                     integrand[q] = integrand[q] * jw[q];
                 }
                 for (int a = 0; a < NP; ++a) {

@@ -78,3 +78,19 @@ def test_pulsating_sphere_quadratic():
     Fp, Gp, _ = oracle.assemble(mesh, k, targets=X, n=2, m=2)
     pa = an.pulsating_sphere_interior(k, 1.0, Z0, 1.0, z)
     assert np.linalg.norm(Fp @ p + Gp @ vs - pa) / np.linalg.norm(pa) < 5e-3
+
+
+def test_oracle_taylor_derivatives_match_finite_differences():
+    """The k-derivative restatement (taylor_assemble!) is consistent with the
+    plain assembly: order 0 equals it, order 1 matches a central difference in k."""
+    import oracle
+    from biegpu import mesh as bm
+    mesh = bm.icosphere(2)
+    k0, h = 2.0, 1e-5
+    F, G, C = oracle.taylor_assemble(mesh, k0, 2, n=2, m=2)
+    F0, G0, C0 = oracle.assemble(mesh, k0, n=2, m=2)
+    assert np.array_equal(F[:, :, 0], F0) and np.array_equal(G[:, :, 0], G0) and np.array_equal(C, C0)
+    Fp, Gp, _ = oracle.assemble(mesh, k0 + h, n=2, m=2)
+    Fm, Gm, _ = oracle.assemble(mesh, k0 - h, n=2, m=2)
+    assert np.linalg.norm((Fp - Fm) / (2 * h) - F[:, :, 1]) / np.linalg.norm(F[:, :, 1]) < 1e-8
+    assert np.linalg.norm((Gp - Gm) / (2 * h) - G[:, :, 1]) / np.linalg.norm(G[:, :, 1]) < 1e-8
