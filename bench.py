@@ -355,6 +355,56 @@ def multi_rhs_bench(args, local, max_over_ranks):
             "per_column_mixed": {"ms_per_rhs_all_k": 1e3 * t_col, "speedup": t_col * R / t}}
 
 
+def nearfield_bench(args, max_over_ranks):
+    """Near-field and fast-operator workload: pulsating-sphere mesh (f=32, 10242
+    nodes, linear), k = 2 pi 200 / 343.  Times (1) the accurate near field of F
+    and G on the depth-1 connected_sources pattern with the fast operators'
+    offset 0.2 (sparse_assemble_parallel!), (2) one product of the fast
+    operator (FMMFOperator algorithm: Gauss-rule far field summed exactly +
+    near-field correction) against (3) the matrix-free product of the exact
+    dense rows (GPUFOperator), FP64 and mixed."""
+    import biegpu
+    from biegpu import FMMFOperator, GPUFOperator
+    from biegpu import mesh as bm
+    from biegpu.assembly import nearfield_values
+    mesh = bm.icosphere(32)
+    k = 2 * np.pi * 200 / 343
+    ctx = biegpu.get_context(mesh, n=2, m=2)
+    reps = max(1, args.nearfield_steps)
+    rp, cols, _, _ = nearfield_values(ctx, k, depth=1, offset=0.2)   # builds pattern and rules
+    ctx.set_timing(True)
+    ctx.stats(reset=True)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        nearfield_values(ctx, k, depth=1, offset=0.2)
+    t_near = max_over_ranks(time.perf_counter() - t0) / reps
+    st = ctx.stats(reset=True)
+    ctx.set_timing(False)
+    x = np.random.default_rng(3).normal(size=mesh.n_sources) + 0j
+    out = {"workload": f"icosphere f=32 ({mesh.n_sources} nodes, {mesh.n_elements} linear elements), "
+                       "k = 2 pi 200/343, depth 1, offset 0.2",
+           "nnz": int(len(cols)), "near_field_ms": 1e3 * t_near,
+           "near_field_kernel_ms": st["timed_ms"] / max(st["timed_launches"], 1) if st["timed_launches"] else None}
+    t0 = time.perf_counter()
+    op = FMMFOperator(mesh, k, precision="fp64")
+    out["fast_operator_setup_ms"] = 1e3 * (time.perf_counter() - t0)
+    for prec in ("fp64", "mixed"):
+        op.precision = prec
+        dense = GPUFOperator(mesh, k, precision=prec)
+        op @ x
+        dense @ x
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            op @ x
+        t_fast = (time.perf_counter() - t0) / reps
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            dense @ x
+        t_dense = (time.perf_counter() - t0) / reps
+        out[f"product_ms_{prec}"] = {"fast_operator": 1e3 * t_fast, "exact_rows": 1e3 * t_dense}
+    return out
+
+
 def adjoint_bench(args, max_over_ranks):
     """Adjoint workload: ellipsoid 3:2:1 f=22 (4842 nodes, linear), ka=3, 32
     seeded field points on the radius-10 sphere, seeded impedances |Z| = rho c.
@@ -445,6 +495,8 @@ def main():
                     choices=["fp16", "bf16", "fp16_split", "bf16_split"])
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
     ap.add_argument("--adjoint-steps", type=int, default=3)
+    ap.add_argument("--no-nearfield", action="store_true", help="skip the near-field / fast-operator measurement")
+    ap.add_argument("--nearfield-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -558,6 +610,9 @@ def main():
     adjoint = None
     if not args.no_adjoint:
         adjoint = adjoint_bench(args, max_over_ranks)
+    nearfield = None
+    if not args.no_nearfield:
+        nearfield = nearfield_bench(args, max_over_ranks)
 
     if rank != 0:
         if dist is not None:
@@ -578,7 +633,7 @@ def main():
         "precision": args.precision, "data": "synthetic",
         "config": dict(desc, l2="256 MB L2 flush between steps; each step writes 4.3 GB", parallelism=f"replicas{world}"),
         "roofline": roofline, "plain_fp64": plain, "accuracy": accuracy, "sweep": sweep,
-        "multi_rhs": multi, "adjoint": adjoint,
+        "multi_rhs": multi, "adjoint": adjoint, "nearfield": nearfield,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
         "clocks": clk.summary(), "gpu": torch.cuda.get_device_name(dev),
         "peaks": {"fp64_tflops": peaks["fp64_flops"] / 1e12, "fp32_tflops": peaks["fp32_flops"] / 1e12,
