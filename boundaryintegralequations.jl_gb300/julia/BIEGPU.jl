@@ -347,9 +347,95 @@ function ChainRulesCore.rrule(::typeof(farfield_objective), coordinates, Z, mesh
     return J, farfield_objective_pullback
 end
 
+# ---------------------------------------------------------------------------
+# Fast operators: the FMMFOperator / FMMGOperator algorithm (Gauss-rule far
+# field summed exactly on the GPU + near-field correction),
+# src/3d/fast_multipole_method.jl:163-194, 306-324, 473-490
+# ---------------------------------------------------------------------------
+mutable struct GPUFastOperator{W} <: LinearMaps.LinearMap{ComplexF64}
+    ctx::Context
+    handle::Ptr{Cvoid}
+    precision::Cint
+end
+
+function GPUFastOperator{W}(mesh, k; tol=1e-6, n_gauss=3, nearfield=true, offset=0.2, depth=1,
+                            precision=:mixed, ctx=Context(mesh; n=2, m=2)) where {W}
+    kk = ComplexF64(k)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:bie_fastop_create, libbiegpu), Cint,
+                (Ptr{Cvoid}, Float64, Float64, Cint, Cint, Cint, Float64, Cint, Ref{Ptr{Cvoid}}),
+                ctx.handle, real(kk), imag(kk), W === :F ? BIE_F : BIE_G, n_gauss, nearfield ? 1 : 0,
+                offset, depth, h))
+    op = GPUFastOperator{W}(ctx, h[], precision_code(precision))
+    finalizer(o -> ccall((:bie_fastop_destroy, libbiegpu), Cint, (Ptr{Cvoid},), o.handle), op)
+    return op
+end
+
+"Drop-in for FMMFOperator(mesh, k; n_gauss, nearfield, offset, depth) (`tol` is accepted, the sum is exact)."
+const FastFOperator = GPUFastOperator{:F}
+"Drop-in for FMMGOperator(mesh, k; n_gauss, nearfield, offset, depth)."
+const FastGOperator = GPUFastOperator{:G}
+
+Base.size(A::GPUFastOperator) = (A.ctx.n_sources, A.ctx.n_sources)
+
+function LinearMaps._unsafe_mul!(y::AbstractVector, A::GPUFastOperator, x::AbstractVector)
+    xv = Vector{ComplexF64}(x)
+    yv = Vector{ComplexF64}(undef, length(y))
+    GC.@preserve xv yv check(ccall((:bie_fastop_apply, libbiegpu), Cint,
+                                   (Ptr{Cvoid}, Ptr{ComplexF64}, Ptr{ComplexF64}, Cint),
+                                   A.handle, xv, yv, A.precision))
+    copyto!(y, yv)
+    return y
+end
+
+function evaluate_targets(A::GPUFastOperator, x, targets)
+    xv = Vector{ComplexF64}(x)
+    tg = Matrix{Float64}(targets)
+    y = Vector{ComplexF64}(undef, size(tg, 2))
+    GC.@preserve xv tg y check(ccall((:bie_fastop_evaluate_targets, libbiegpu), Cint,
+                                     (Ptr{Cvoid}, Ptr{Float64}, Int64, Ptr{ComplexF64}, Ptr{ComplexF64}, Cint),
+                                     A.handle, tg, size(tg, 2), xv, y, A.precision))
+    return y
+end
+
+# ---------------------------------------------------------------------------
+# k-derivative assembly (taylor_assemble!, src/3d/rosebem.jl:56-157)
+# ---------------------------------------------------------------------------
+"""
+    taylor_assemble_gpu!(mesh, k0, sources; M=0, fOn=true, gOn=true, cOn=true, n=3, m=3, U=I)
+
+`(From, Grom, C)` with From[:, :, m+1] the m-th k-derivative of F at k0 (and G),
+projected on U as the reference does (From = U' F U).
+"""
+function taylor_assemble_gpu!(mesh, k0, sources; M=0, fOn=true, gOn=true, cOn=true, n=3, m=3, U=I,
+                              ctx=nothing)
+    c = ctx === nothing ? Context(mesh; n=n, m=m) : ctx
+    kk = ComplexF64(k0)
+    tg = Matrix{Float64}(sources)
+    Mt = size(tg, 2)
+    N = c.n_sources
+    F = fOn ? Array{ComplexF64}(undef, Mt, N, M + 1) : Array{ComplexF64}(undef, 0, 0, 0)
+    G = gOn ? Array{ComplexF64}(undef, Mt, N, M + 1) : Array{ComplexF64}(undef, 0, 0, 0)
+    C = cOn ? Vector{ComplexF64}(undef, Mt) : Vector{ComplexF64}(undef, 0)
+    flags = (fOn ? BIE_F : Cint(0)) | (gOn ? BIE_G : Cint(0)) | (cOn ? BIE_C : Cint(0))
+    same = sources === mesh.sources
+    GC.@preserve tg F G C check(ccall((:bie_taylor_assemble, libbiegpu), Cint,
+                                      (Ptr{Cvoid}, Float64, Float64, Ptr{Float64}, Int64, Cint, Cint,
+                                       Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                                      c.handle, real(kk), imag(kk), same ? C_NULL : pointer(tg), Mt, flags, M,
+                                      fOn ? pointer(F) : C_NULL, gOn ? pointer(G) : C_NULL,
+                                      cOn ? pointer(C) : C_NULL))
+    if !(U isa UniformScaling)
+        F = fOn ? cat([U' * F[:, :, j] * U for j in 1:M+1]...; dims=3) : F
+        G = gOn ? cat([U' * G[:, :, j] * U for j in 1:M+1]...; dims=3) : G
+    end
+    return F, G, C
+end
+
 version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
 export Context, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
-       sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective
+       sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective, FastFOperator, FastGOperator,
+       taylor_assemble_gpu!
 
 end # module
