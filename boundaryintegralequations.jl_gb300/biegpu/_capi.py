@@ -177,6 +177,7 @@ SIGNATURES = {
     "bie_ctx_stream": (_I, [_P, C.POINTER(_P)]),
     "bie_measure_peaks": (_I, [_I, C.POINTER(Peaks)]),
     "bie_ctx_set_timing": (_I, [_P, _I]),
+    "bie_ctx_set_autotune": (_I, [_P, _I]),
     "bie_ctx_stats": (_I, [_P, C.POINTER(Stats), _I]),
     "bie_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
     "bie_assemble_device": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),

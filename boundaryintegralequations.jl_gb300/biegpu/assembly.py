@@ -79,6 +79,11 @@ class Context:
     def set_timing(self, on: bool) -> None:
         _capi.check(_capi.lib().bie_ctx_set_timing(self._h, 1 if on else 0))
 
+    def set_autotune(self, on: bool) -> None:
+        """Time neighbouring element slicings on the first mixed assembly per
+        target count and keep the fastest (bie_ctx_set_autotune)."""
+        _capi.check(_capi.lib().bie_ctx_set_autotune(self._h, 1 if on else 0))
+
     def stats(self, reset: bool = False) -> dict:
         st = _capi.Stats()
         _capi.check(_capi.lib().bie_ctx_stats(self._h, C.byref(st), 1 if reset else 0))

@@ -429,23 +429,64 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     double *Cnear = reinterpret_cast<double *>(dbuf + dbytes + 256);
     BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
 
-    const int level = choose_slice_level(c, a.M, kThreads);
-    const int S = 1 << level;
     const int NPP = L.NP <= 4 ? 4 : 8;
     const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
     const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
     const size_t phi_f = (size_t)((L.R * L.qmax * NPP + 3) & ~3);
     const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes;
-    double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
     const bool cplx = a.k_im != 0.0;
-    if (L.NP == 3) {
-        if (cplx) launch_np<3, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        else launch_np<3, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-    } else {
-        if (cplx) launch_np<6, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        else launch_np<6, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+    auto run = [&](int level) {
+        const int S = 1 << level;
+        double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
+        if (L.NP == 3) {
+            if (cplx) launch_np<3, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+            else launch_np<3, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        } else {
+            if (cplx) launch_np<6, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+            else launch_np<6, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        }
+        if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
+    };
+    auto reset = [&] {   // fresh accumulators and deferred list
+        if (F32) BIE_CUDA(cudaMemsetAsync(F32, 0, mat32, c.stream));
+        if (G32) BIE_CUDA(cudaMemsetAsync(G32, 0, mat32, c.stream));
+        BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
+    };
+    int level = choose_slice_level(c, a.M, kThreads);
+    if (c.autotune) {
+        const auto it = c.tuned_mixed_level.find(a.M);
+        if (it != c.tuned_mixed_level.end()) {
+            level = it->second;
+        } else {
+            // time the neighbouring slicings once (each a complete assembly on
+            // fresh accumulators) and keep the fastest for this M
+            int best = level;
+            float best_ms = 3.4e38f;
+            cudaEvent_t e0, e1;
+            BIE_CUDA(cudaEventCreate(&e0));
+            BIE_CUDA(cudaEventCreate(&e1));
+            for (int l = level - 1; l <= level + 1; ++l) {
+                if (l < 0 || l >= kMaxLevels || (int64_t(1) << l) > c.n_elements) continue;
+                reset();
+                BIE_CUDA(cudaEventRecord(e0, c.stream));
+                run(l);
+                BIE_CUDA(cudaEventRecord(e1, c.stream));
+                BIE_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                BIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = l;
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            c.tuned_mixed_level[a.M] = best;
+            level = best;
+            reset();
+        }
     }
-    if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
+    run(level);
 }
 
 }  // namespace bie

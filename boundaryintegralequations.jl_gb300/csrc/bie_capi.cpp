@@ -155,6 +155,14 @@ int bie_ctx_set_timing(bie_ctx *ctx, int on) {
     });
 }
 
+int bie_ctx_set_autotune(bie_ctx *ctx, int on) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        c.autotune = on != 0;
+    });
+}
+
 int bie_ctx_stats(bie_ctx *ctx, bie_stats *out, int reset) {
     return guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <memory>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -173,6 +174,11 @@ struct Ctx {
     void *scratch(int slot, size_t bytes);
 
     // launch statistics (bie_ctx_stats)
+    // autotuning of the mixed assembly's element slicing: on the first call for
+    // a target count M the neighbouring slicing levels are timed and the
+    // fastest is kept (bie_ctx_set_autotune; bie_sweep turns it on)
+    bool autotune = false;
+    std::map<int64_t, int> tuned_mixed_level;
     bool timing = false;
     int64_t kernel_launches = 0;
     int64_t timed_launches = 0;

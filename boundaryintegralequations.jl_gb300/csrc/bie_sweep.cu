@@ -49,6 +49,7 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
         Ctx &c = *ctxs[m];
         std::lock_guard<std::mutex> lock(c.mu);
         BIE_CUDA(cudaSetDevice(c.device));
+        c.autotune = true;   // the first wavenumber of a mesh picks its slicing
         const int64_t N = c.n_sources;
         // mixed: complex64 matrices end to end (assembly accumulators with the FP64
         // corrections added in place, complex64 products with double-float sums);

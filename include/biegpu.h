@@ -164,6 +164,17 @@ typedef struct bie_peaks {
 BIE_API int bie_measure_peaks(int device, bie_peaks *out);
 
 BIE_API int bie_ctx_set_timing(bie_ctx *ctx, int on);
+
+/*
+ * Autotuning of the mixed-precision assembly (no reference counterpart: the
+ * reference has no GPU launch shapes).  While on, the first mixed assembly of
+ * the context for a given number of targets M times the element slicings next
+ * to the default one (each a complete assembly, so that first call costs about
+ * four assemblies) and keeps the fastest for later calls with that M.  Results
+ * of different slicings differ only by FP32 rounding order.  bie_sweep turns it
+ * on for the contexts it is given.
+ */
+BIE_API int bie_ctx_set_autotune(bie_ctx *ctx, int on);
 /* Synchronises the context stream, then fills *out; `reset` != 0 zeroes the counters. */
 BIE_API int bie_ctx_stats(bie_ctx *ctx, bie_stats *out, int reset);
 
