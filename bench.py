@@ -260,6 +260,7 @@ def sweep_bench(args, rank, world, max_over_ranks):
     return {"metric": "sweep solves/s", "value": v_mixed, "unit": "solves/s",
             "meshes": {n: m.n_sources for n, m in named}, "wavenumbers": len(ks), "solves": solves,
             "seconds": t_mixed, "assemble_ms": im["assemble_ms"], "solve_ms": im["solve_ms"],
+            "graph_record_ms": im["record_ms"], "graph_launches": im["graph_launches"],
             "converged": im["converged"], "gmres_iterations_mean": im["iterations"] / max(im["solves"], 1),
             "plain_fp64": {"value": v_fp64, "unit": "solves/s", "solves": i64["solves"] * world,
                            "seconds": t_fp64, "assemble_ms": i64["assemble_ms"], "solve_ms": i64["solve_ms"]},

@@ -137,7 +137,8 @@ class GmresInfo(C.Structure):
 
 
 class SweepOpts(C.Structure):
-    _fields_ = [("precision", C.c_int32), ("refine", C.c_int32), ("gmres", GmresOpts)]
+    _fields_ = [("precision", C.c_int32), ("refine", C.c_int32), ("gmres", GmresOpts),
+                ("eager", C.c_int32)]
 
 
 class SweepInfo(C.Structure):
@@ -147,6 +148,8 @@ class SweepInfo(C.Structure):
         ("iterations", C.c_int64),
         ("assemble_ms", C.c_double),
         ("solve_ms", C.c_double),
+        ("record_ms", C.c_double),
+        ("graph_launches", C.c_int64),
     ]
 
 

@@ -18,13 +18,15 @@ from .assembly import get_context
 
 def sweep(meshes, ks, ws, precision: str = "mixed", refine: bool = True, n: int = 2, m: int = 2,
           reltol: float = math.sqrt(np.finfo(np.float64).eps), restart: int = 0, maxiter: int = 0,
-          device: int = 0):
+          device: int = 0, eager: bool = False):
     """Solve the frequency sweep; returns (list of N_m x nk complex arrays, info dict).
 
     ``ks``: wavenumbers (real or complex), ``ws``: per-mesh boundary data
     (length N_m complex).  ``precision="mixed"`` with ``refine=True`` is the
     fast path (mixed assembly, complex64 inner GMRES, complex128 residual);
-    ``precision="fp64", refine=False`` is the plain FP64 path.
+    ``precision="fp64", refine=False`` is the plain FP64 path.  By default the
+    wavenumbers after the first of each mesh solve by replaying one recorded
+    CUDA graph of the GMRES solve; ``eager=True`` drives GMRES from the host.
     """
     ctxs = [get_context(mesh, n=n, m=m, device=device) for mesh in meshes]
     ks = np.asarray(ks, dtype=np.complex128)
@@ -42,7 +44,8 @@ def sweep(meshes, ks, ws, precision: str = "mixed", refine: bool = True, n: int 
     g = _capi.GmresOpts(restart=int(restart), maxiter=int(maxiter), reltol=float(reltol), abstol=0.0,
                         precision=_capi.BIE_PREC_FP64, refine=0, inner_reltol=0.0, max_refine=0,
                         initially_nonzero=0)
-    opts = _capi.SweepOpts(precision=_capi.PRECISION[precision], refine=1 if refine else 0, gmres=g)
+    opts = _capi.SweepOpts(precision=_capi.PRECISION[precision], refine=1 if refine else 0, gmres=g,
+                           eager=1 if eager else 0)
     info = _capi.SweepInfo()
     iters = np.zeros((nm, nk), dtype=np.int32)
     _capi.check(_capi.lib().bie_sweep(carr, nm, kbuf.ctypes.data, nk, warr, parr, C.byref(opts),

@@ -457,7 +457,7 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
         const auto it = c.tuned_mixed_level.find(a.M);
         if (it != c.tuned_mixed_level.end()) {
             level = it->second;
-        } else {
+        } else if (!c.capturing) {   // (timing needs host synchronisation)
             // time the neighbouring slicings once (each a complete assembly on
             // fresh accumulators) and keep the fastest for this M
             int best = level;

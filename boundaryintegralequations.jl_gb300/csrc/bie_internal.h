@@ -172,12 +172,16 @@ struct Ctx {
     void *d_scratch[kScratchCount] = {};
     size_t scratch_bytes[kScratchCount] = {};
     void *scratch(int slot, size_t bytes);
+    // set while the context stream records a CUDA graph: scratch must not grow
+    // then (a reallocation would leave the graph pointing at freed memory)
+    bool capturing = false;
 
-    // launch statistics (bie_ctx_stats)
     // autotuning of the mixed assembly's element slicing: on the first call for
     // a target count M the neighbouring slicing levels are timed and the
     // fastest is kept (bie_ctx_set_autotune; bie_sweep turns it on)
     bool autotune = false;
+
+    // launch statistics (bie_ctx_stats)
     std::map<int64_t, int> tuned_mixed_level;
     bool timing = false;
     int64_t kernel_launches = 0;
@@ -242,6 +246,15 @@ void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a);
 // GMRES (bie_solver.cu); b, x device, N = n_sources
 void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
                bie_gmres_info &info);
+// The same solve (dense operator, x = 0 start) recorded into the graph being
+// captured on c.stream: the refinement, restart and Arnoldi loops become
+// conditional WHILE nodes and the step index a SWITCH node, all driven by
+// device-side state, so a replay needs no host round trip.  body[0..3]: four
+// idle streams for the nested body captures.  *d_info (device) receives the
+// solve's statistics when the graph runs.
+constexpr int kGraphMaxRestart = 64;
+void capture_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
+                   bie_gmres_info *d_info, const cudaStream_t *body);
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
 // Frequency sweep (bie_sweep.cu); locks each context while it runs.
 void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,

@@ -280,6 +280,7 @@ static uint32_t spread10(uint32_t x) {
 void *Ctx::scratch(int slot, size_t bytes) {
     if (bytes == 0) bytes = 16;
     if (scratch_bytes[slot] < bytes) {
+        if (capturing) fail(BIE_ERR_INVALID, "device scratch would grow while a CUDA graph is recorded");
         if (d_scratch[slot]) BIE_CUDA(cudaFree(d_scratch[slot]));
         d_scratch[slot] = nullptr;
         scratch_bytes[slot] = 0;

@@ -526,6 +526,148 @@ __global__ void combo_add_dev_kernel(const double2 *__restrict__ V, int64_t ldv,
     x[i] = make_double2(re, im);
 }
 
+// ---- graph form: the whole (refined) solve as conditional graph nodes --------
+// Control flow lives in device memory (RfState) and in conditional handles that
+// single-thread kernels set; every loop has a counter bound, so each WHILE node
+// ends even for NaN residuals.
+struct RfState {
+    double bnorm, tol;     // |b| and the absolute tolerance max(reltol |b|, abstol)
+    double res;            // last outer residual |b - A x| (exact product)
+    double inner_tol;      // absolute tolerance of the current inner solve
+    double last_beta;      // residual norm at the start of the last cycle
+    long long matvecs;
+    int iters, restarts, refinements;
+    int outer_zero;        // x == 0: the outer residual is b (its product skipped)
+    int inner_zero;        // dx == 0: the cycle residual is the right-hand side
+    int jmax;              // Arnoldi steps allowed in the current cycle
+    int steps, cycles;     // loop counters (bounds of the WHILE nodes)
+    int pad;
+};
+
+// out = *zero ? r : r - w   (out may be w)
+__global__ void resid_flag_kernel(const double2 *__restrict__ r, const double2 *w, double2 *out, int64_t n,
+                                  const int *__restrict__ zero) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 a = r[i];
+    if (*zero) {
+        out[i] = a;
+    } else {
+        const double2 b = w[i];
+        out[i] = make_double2(a.x - b.x, a.y - b.y);
+    }
+}
+
+// x += d
+__global__ void axpy1_kernel(const double2 *__restrict__ d, double2 *__restrict__ x, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = make_double2(x[i].x + d[i].x, x[i].y + d[i].y);
+}
+
+// |b| from the norm reduction, tolerance, counters; enter the outer loop
+__global__ void rf_start_kernel(GmState st, RfState *rf, double reltol, double abstol,
+                                cudaGraphConditionalHandle h_outer) {
+    RfState &r = *rf;
+    const double bn = sqrt(fmax(st.s->nrm2.x, 0.0));
+    r = RfState{};
+    r.bnorm = bn;
+    r.tol = fmax(reltol * bn, abstol);
+    r.res = bn;
+    r.last_beta = bn;
+    r.outer_zero = 1;
+    cudaGraphSetConditional(h_outer, 1u);
+}
+
+// Top of an outer pass.  Refinement: the outer residual |b - A x| decides
+// whether another inner solve runs (the host loop of run_gmres); plain GMRES:
+// one pass whose inner solve is the whole solve.
+__global__ void rf_check_kernel(GmState st, RfState *rf, int refine, int maxiter, int max_outer,
+                                double inner_rel, cudaGraphConditionalHandle h_outer,
+                                cudaGraphConditionalHandle h_cycle) {
+    RfState &r = *rf;
+    if (refine) {
+        if (!r.outer_zero) r.matvecs += 1;
+        r.outer_zero = 0;
+        const double res = sqrt(fmax(st.s->nrm2.x, 0.0));
+        r.res = res;
+        if (res <= r.tol || r.iters >= maxiter || r.refinements >= max_outer) {
+            cudaGraphSetConditional(h_outer, 0u);
+            cudaGraphSetConditional(h_cycle, 0u);
+            return;
+        }
+        r.refinements += 1;
+        r.inner_tol = fmax(inner_rel * res, r.tol * 0.5);
+    } else {
+        r.inner_tol = r.tol;
+        cudaGraphSetConditional(h_outer, 0u);
+    }
+    r.inner_zero = 1;
+    r.cycles = 0;
+    cudaGraphSetConditional(h_cycle, 1u);
+}
+
+// Start of a restart cycle (gm_init_kernel with the inner tolerance read from
+// the device); opens the Arnoldi loop unless the true residual already meets it.
+__global__ void gm_cycle_init_kernel(GmState st, RfState *rf, int maxiter, int restart,
+                                     cudaGraphConditionalHandle h_step, cudaGraphConditionalHandle h_sel) {
+    GmScalars &s = *st.s;
+    RfState &r = *rf;
+    s.tol = r.inner_tol;
+    const double beta = sqrt(fmax(s.nrm2.x, 0.0));
+    s.beta = beta;
+    s.res = beta;
+    s.jdone = 0;
+    s.start_ok = beta <= s.tol ? 1 : 0;
+    s.done = s.start_ok;
+    s.inv_beta = beta > 0.0 ? 1.0 / beta : 0.0;
+    for (int k = 0; k <= st.m; ++k) st.g[k] = make_double2(0.0, 0.0);
+    st.g[0] = make_double2(beta, 0.0);
+    if (!r.inner_zero) r.matvecs += 1;
+    r.inner_zero = 0;
+    r.last_beta = beta;
+    r.jmax = min(restart, max(0, maxiter - r.iters));
+    r.steps = 0;
+    cudaGraphSetConditional(h_step, (!s.start_ok && r.jmax > 0) ? 1u : 0u);
+    cudaGraphSetConditional(h_sel, 0u);
+}
+
+// After each Arnoldi step: the next step index, and whether it runs (not
+// converged, steps left in the cycle; at most `restart` passes)
+__global__ void gm_step_guard_kernel(GmState st, RfState *rf, int restart, cudaGraphConditionalHandle h_step,
+                                     cudaGraphConditionalHandle h_sel) {
+    const GmScalars &s = *st.s;
+    RfState &r = *rf;
+    r.steps += 1;
+    const int jd = s.jdone;
+    cudaGraphSetConditional(h_step, (!s.done && jd < r.jmax && r.steps < restart) ? 1u : 0u);
+    cudaGraphSetConditional(h_sel, (unsigned)jd);
+}
+
+// End of a cycle: tallies; another cycle (whose first action re-checks the true
+// residual) follows any cycle that took steps
+__global__ void gm_cycle_end_kernel(GmState st, RfState *rf, int maxiter, cudaGraphConditionalHandle h_cycle) {
+    RfState &r = *rf;
+    const int jd = st.s->jdone;
+    r.iters += jd;
+    r.matvecs += jd;
+    if (jd > 0) r.restarts += 1;
+    r.cycles += 1;
+    cudaGraphSetConditional(h_cycle, (jd > 0 && r.cycles <= maxiter) ? 1u : 0u);
+}
+
+__global__ void rf_final_kernel(const RfState *rf, int refine, bie_gmres_info *out) {
+    const RfState &r = *rf;
+    bie_gmres_info o{};
+    o.iterations = r.iters;
+    o.restarts = r.restarts;
+    o.refinements = refine ? r.refinements : 0;
+    o.matvecs = r.matvecs;
+    o.residual_norm = refine ? r.res : r.last_beta;
+    o.rhs_norm = r.bnorm;
+    o.converged = o.residual_norm <= r.tol ? 1 : 0;
+    *out = o;
+}
+
 __global__ void round_c64_kernel(const double2 *__restrict__ in, float2 *__restrict__ out, int64_t n) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
@@ -547,9 +689,11 @@ struct Solver {
     double2 *hdev = nullptr;      // device scratch for dot results (>= restart + 2)
     std::vector<double2> hhost;
     GmState st{};                 // device-resident Arnoldi state
+    RfState *rf = nullptr;        // device-resident refinement state (graph form)
     const int *stop = nullptr;    // device stop flag honoured by the launches below
+    cudaStream_t stream;          // launch stream (a capture stream while recording a graph)
 
-    Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_), m(restart) {
+    Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_), m(restart), stream(ctx.stream) {
         // column slices: ~8 blocks per SM for the two-rows-per-thread complex64 product
         S = 1;
         const int64_t row_tiles = (n / 2 + kT - 1) / kT;
@@ -558,7 +702,7 @@ struct Solver {
         const size_t part_bytes = (size_t)std::max<int64_t>(S * n, (int64_t)(restart + 2) * nbdot) * 16;
         const size_t hbytes = (size_t)(restart + 2) * 16;
         const size_t nc = (size_t)(restart + 1) * restart + 4 * (size_t)(restart + 1) + restart;
-        const size_t st_bytes = nc * 16 + (size_t)restart * 8 + sizeof(GmScalars) + 64;
+        const size_t st_bytes = nc * 16 + (size_t)restart * 8 + sizeof(GmScalars) + sizeof(RfState) + 96;
         char *base = static_cast<char *>(c.scratch(kScratchSolverPart, part_bytes + hbytes + st_bytes));
         part = reinterpret_cast<double2 *>(base);
         hdev = reinterpret_cast<double2 *>(base + part_bytes);
@@ -578,6 +722,7 @@ struct Solver {
         z += restart + 1;
         st.cs = reinterpret_cast<double *>(z);
         st.s = reinterpret_cast<GmScalars *>(reinterpret_cast<char *>(st.cs) + (((size_t)restart * 8 + 15) & ~size_t(15)));
+        rf = reinterpret_cast<RfState *>(reinterpret_cast<char *>(st.s) + ((sizeof(GmScalars) + 15) & ~size_t(15)));
         hhost.resize(restart + 2);
     }
 
@@ -597,29 +742,29 @@ struct Solver {
                 if (n % 2 == 0) {
                     dim3 grid(blocks(n / 2, kT), (unsigned)S);
                     if (exact)
-                        dense_gemv_c64_exact_kernel<<<grid, kT, 0, c.stream>>>(
+                        dense_gemv_c64_exact_kernel<<<grid, kT, 0, stream>>>(
                             reinterpret_cast<const float4 *>(op.A32), n, x, part, S, stop);
                     else
-                        dense_gemv_c64_kernel<<<grid, kT, 0, c.stream>>>(
+                        dense_gemv_c64_kernel<<<grid, kT, 0, stream>>>(
                             reinterpret_cast<const float4 *>(op.A32), n, x, part, S, stop);
                 } else {
                     dim3 grid(blocks(n, kT), (unsigned)S);
                     if (exact)
-                        dense_gemv_c64_rows_exact_kernel<<<grid, kT, 0, c.stream>>>(
+                        dense_gemv_c64_rows_exact_kernel<<<grid, kT, 0, stream>>>(
                             reinterpret_cast<const float2 *>(op.A32), n, x, part, S, stop);
                     else
-                        dense_gemv_c64_rows_kernel<<<grid, kT, 0, c.stream>>>(
+                        dense_gemv_c64_rows_kernel<<<grid, kT, 0, stream>>>(
                             reinterpret_cast<const float2 *>(op.A32), n, x, part, S, stop);
                 }
             } else {
                 dim3 grid(blocks(n, kT), (unsigned)S);
-                dense_gemv_kernel<double2><<<grid, kT, 0, c.stream>>>(
+                dense_gemv_kernel<double2><<<grid, kT, 0, stream>>>(
                     reinterpret_cast<const double2 *>(op.A), n, x, part, S, stop);
             }
             BIE_CUDA(cudaGetLastError());
             c.timer_end(t0);
             launched();
-            combine_kernel<<<blocks(n), 256, 0, c.stream>>>(part, S, n, sc, d, x, y, stop);
+            combine_kernel<<<blocks(n), 256, 0, stream>>>(part, S, n, sc, d, x, y, stop);
             BIE_CUDA(cudaGetLastError());
             launched();
         } else {
@@ -644,10 +789,10 @@ struct Solver {
     // out[0..ncol) = V[:, 0..ncol)^H w on the device (no host copy)
     void multidot_dev(const double2 *V, int64_t ldv, int ncol, const double2 *w, double2 *out) {
         dim3 grid((unsigned)nbdot, (unsigned)ncol);
-        multidot_kernel<<<grid, kT, 0, c.stream>>>(V, ldv, w, n, part, stop);
+        multidot_kernel<<<grid, kT, 0, stream>>>(V, ldv, w, n, part, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
-        sum_partials_kernel<<<blocks(ncol, 64), 64, 0, c.stream>>>(part, nbdot, ncol, out, stop);
+        sum_partials_kernel<<<blocks(ncol, 64), 64, 0, stream>>>(part, nbdot, ncol, out, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
     }
@@ -675,7 +820,7 @@ struct Solver {
 
     // w -= V[:, 0..ncol) h  with h on the device
     void gs_update_dev(const double2 *V, int64_t ldv, int ncol, double2 *w, const double2 *h) {
-        gs_update_kernel<<<blocks(n), 256, 0, c.stream>>>(V, ldv, ncol, h, w, n, stop);
+        gs_update_kernel<<<blocks(n), 256, 0, stream>>>(V, ldv, ncol, h, w, n, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
     }
@@ -688,13 +833,13 @@ struct Solver {
     }
 
     void scale_dev(const double2 *x, const double *a, double2 *y) {
-        scale_dev_kernel<<<blocks(n), 256, 0, c.stream>>>(x, a, y, n, stop);
+        scale_dev_kernel<<<blocks(n), 256, 0, stream>>>(x, a, y, n, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
     }
 
     void sub(const double2 *a, const double2 *b, double2 *y) {
-        sub_kernel<<<blocks(n), 256, 0, c.stream>>>(a, b, y, n);
+        sub_kernel<<<blocks(n), 256, 0, stream>>>(a, b, y, n);
         BIE_CUDA(cudaGetLastError());
         launched();
     }
@@ -718,7 +863,7 @@ int gmres_core(Solver &S, const bie_operator &op, int prec, const double2 *b, do
     const bool dense = op.kind == BIE_OP_DENSE;
     const GmState st = S.st;
     const int *stop_flag = &st.s->done;
-    cudaStream_t stream = S.c.stream;
+    cudaStream_t stream = S.stream;
     int it = 0, restarts = 0;
     double beta = 0.0;
     bool first = true;
@@ -791,7 +936,197 @@ int gmres_core(Solver &S, const bie_operator &op, int prec, const double2 *b, do
     return it;
 }
 
+// A conditional handle of the graph being captured on `s`.
+cudaGraphConditionalHandle new_handle(cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    BIE_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+    if (cs != cudaStreamCaptureStatusActive) fail(BIE_ERR_INVALID, "graph GMRES: the stream is not capturing");
+    cudaGraphConditionalHandle h;
+    BIE_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    return h;
+}
+
+// Appends a conditional node after the capture's current dependencies; its body
+// graphs are returned for capture on other streams.
+void add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                     unsigned size, cudaGraph_t *bodies) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    BIE_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &nd));
+    if (cs != cudaStreamCaptureStatusActive) fail(BIE_ERR_INVALID, "graph GMRES: the stream is not capturing");
+    cudaGraphNodeParams p{};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = type;
+    p.conditional.size = size;
+    cudaGraphNode_t node;
+    BIE_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    BIE_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    for (unsigned i = 0; i < size; ++i) bodies[i] = p.conditional.phGraph_out[i];
+}
+
+// Records onto stream `s` into the body graph `g` until end() (or destruction,
+// which ends an unfinished capture after an error).
+struct BodyCapture {
+    cudaStream_t s;
+    bool on = false;
+    BodyCapture(cudaStream_t s_, cudaGraph_t g) : s(s_) {
+        BIE_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+        on = true;
+    }
+    void end() {
+        on = false;
+        cudaGraph_t out = nullptr;
+        BIE_CUDA(cudaStreamEndCapture(s, &out));
+    }
+    ~BodyCapture() {
+        if (on) {
+            cudaGraph_t out = nullptr;
+            cudaStreamEndCapture(s, &out);
+        }
+    }
+    BodyCapture(const BodyCapture &) = delete;
+    BodyCapture &operator=(const BodyCapture &) = delete;
+};
+
 }  // namespace
+
+void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, const bie_gmres_opts &o,
+                   bie_gmres_info *d_info, const cudaStream_t *body) {
+    if (op.kind != BIE_OP_DENSE) fail(BIE_ERR_UNSUPPORTED, "graph GMRES needs a dense operator");
+    if (o.initially_nonzero) fail(BIE_ERR_UNSUPPORTED, "graph GMRES starts from x = 0");
+    const int64_t n = c.n_sources;
+    const int restart = (int)std::max<int64_t>(1, std::min<int64_t>(o.restart > 0 ? o.restart : 20, n));
+    if (restart > kGraphMaxRestart) fail(BIE_ERR_UNSUPPORTED, "graph GMRES: restart above 64");
+    const int maxiter = o.maxiter > 0 ? o.maxiter : (int)std::min<int64_t>(n, INT32_MAX);
+    const double reltol = o.reltol > 0 ? o.reltol : std::sqrt(2.220446049250313e-16);
+    const double abstol = std::max(0.0, o.abstol);
+    const bool refine = o.refine != 0;
+    const int prec = refine ? BIE_PREC_MIXED : o.precision;
+    const double inner_rel = o.inner_reltol > 0 ? o.inner_reltol : 1e-4;
+    const int max_outer = o.max_refine > 0 ? o.max_refine : 10;
+    const double2 *b = reinterpret_cast<const double2 *>(b_);
+    double2 *x = reinterpret_cast<double2 *>(x_);
+
+    char *ws = static_cast<char *>(c.scratch(kScratchSolver, (size_t)(restart + 4) * n * 16));
+    double2 *V = reinterpret_cast<double2 *>(ws);
+    double2 *w = V + (int64_t)(restart + 1) * n;
+    double2 *rr = w + n;
+    double2 *dx = rr + n;
+    Solver S(c, n, restart);
+    const GmState st = S.st;
+    RfState *rf = S.rf;
+    cudaStream_t s0 = c.stream;
+
+    BIE_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 16, s0));
+    S.multidot_dev(b, n, 1, b, &st.s->nrm2);
+    const cudaGraphConditionalHandle h_outer = new_handle(s0);
+    rf_start_kernel<<<1, 1, 0, s0>>>(st, rf, reltol, abstol, h_outer);
+    BIE_CUDA(cudaGetLastError());
+    S.launched();
+    cudaGraph_t g_outer;
+    add_conditional(s0, h_outer, cudaGraphCondTypeWhile, 1, &g_outer);
+    {
+        // outer pass: refinement residual rr = b - A x (exact product), then the
+        // inner restarted GMRES on A dx = rr
+        BodyCapture bc1(body[0], g_outer);
+        S.stream = body[0];
+        if (refine) {
+            S.stop = &rf->outer_zero;
+            S.apply(op, BIE_PREC_FP64, x, w);
+            S.stop = nullptr;
+            resid_flag_kernel<<<blocks(n), 256, 0, S.stream>>>(b, w, rr, n, &rf->outer_zero);
+            BIE_CUDA(cudaGetLastError());
+            S.launched();
+            S.multidot_dev(rr, n, 1, rr, &st.s->nrm2);
+            BIE_CUDA(cudaMemsetAsync(dx, 0, (size_t)n * 16, S.stream));
+        }
+        const double2 *rhs = refine ? rr : b;
+        double2 *sol = refine ? dx : x;
+        const cudaGraphConditionalHandle h_cycle = new_handle(S.stream);
+        rf_check_kernel<<<1, 1, 0, S.stream>>>(st, rf, refine ? 1 : 0, maxiter, max_outer, inner_rel, h_outer,
+                                                h_cycle);
+        BIE_CUDA(cudaGetLastError());
+        S.launched();
+        cudaGraph_t g_cycle;
+        add_conditional(S.stream, h_cycle, cudaGraphCondTypeWhile, 1, &g_cycle);
+        {
+            // restart cycle: w = rhs - A sol (rhs itself on the first cycle), beta,
+            // then up to `restart` Arnoldi steps
+            BodyCapture bc2(body[1], g_cycle);
+            S.stream = body[1];
+            S.stop = &rf->inner_zero;
+            S.apply(op, prec, sol, w);
+            S.stop = nullptr;
+            resid_flag_kernel<<<blocks(n), 256, 0, S.stream>>>(rhs, w, w, n, &rf->inner_zero);
+            BIE_CUDA(cudaGetLastError());
+            S.launched();
+            S.multidot_dev(w, n, 1, w, &st.s->nrm2);
+            const cudaGraphConditionalHandle h_step = new_handle(S.stream);
+            const cudaGraphConditionalHandle h_sel = new_handle(S.stream);
+            gm_cycle_init_kernel<<<1, 1, 0, S.stream>>>(st, rf, maxiter, restart, h_step, h_sel);
+            BIE_CUDA(cudaGetLastError());
+            S.launched();
+            S.scale_dev(w, &st.s->inv_beta, V);
+            cudaGraph_t g_step;
+            add_conditional(S.stream, h_step, cudaGraphCondTypeWhile, 1, &g_step);
+            {
+                // one Arnoldi step per pass: a switch over the step index j runs
+                // the body recorded for that j (CGS2 over j + 1 basis vectors)
+                BodyCapture bc3(body[2], g_step);
+                S.stream = body[2];
+                std::vector<cudaGraph_t> branch(restart);
+                add_conditional(S.stream, h_sel, cudaGraphCondTypeSwitch, (unsigned)restart, branch.data());
+                gm_step_guard_kernel<<<1, 1, 0, S.stream>>>(st, rf, restart, h_step, h_sel);
+                BIE_CUDA(cudaGetLastError());
+                S.launched();
+                for (int j = 0; j < restart; ++j) {
+                    BodyCapture bc4(body[3], branch[j]);
+                    S.stream = body[3];
+                    const double2 *vj = V + (int64_t)j * n;
+                    double2 *vn = V + (int64_t)(j + 1) * n;
+                    S.apply(op, prec, vj, w);
+                    S.multidot_dev(V, n, j + 1, w, st.h1);
+                    S.gs_update_dev(V, n, j + 1, w, st.h1);
+                    S.multidot_dev(V, n, j + 1, w, st.h2);
+                    S.gs_update_dev(V, n, j + 1, w, st.h2);
+                    S.multidot_dev(w, n, 1, w, &st.s->nrm2);
+                    gm_givens_kernel<<<1, 1, 0, S.stream>>>(st, j);
+                    BIE_CUDA(cudaGetLastError());
+                    S.launched();
+                    S.scale_dev(w, &st.s->inv_hn, vn);
+                    bc4.end();
+                }
+                bc3.end();
+            }
+            S.stream = body[1];
+            gm_trisolve_kernel<<<1, 1, 0, S.stream>>>(st);
+            BIE_CUDA(cudaGetLastError());
+            combo_add_dev_kernel<<<blocks(n), 256, 0, S.stream>>>(V, n, &st.s->jdone, st.y, sol, n);
+            BIE_CUDA(cudaGetLastError());
+            gm_cycle_end_kernel<<<1, 1, 0, S.stream>>>(st, rf, maxiter, h_cycle);
+            BIE_CUDA(cudaGetLastError());
+            S.launched();
+            S.launched();
+            S.launched();
+            bc2.end();
+        }
+        S.stream = body[0];
+        if (refine) {
+            axpy1_kernel<<<blocks(n), 256, 0, S.stream>>>(dx, x, n);
+            BIE_CUDA(cudaGetLastError());
+            S.launched();
+        }
+        bc1.end();
+    }
+    S.stream = s0;
+    rf_final_kernel<<<1, 1, 0, s0>>>(rf, refine ? 1 : 0, d_info);
+    BIE_CUDA(cudaGetLastError());
+    S.launched();
+}
 
 void run_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, const bie_gmres_opts &o,
                bie_gmres_info &info) {

@@ -260,9 +260,11 @@ struct SweepOpts
     restart::Int32; maxiter::Int32; reltol::Float64; abstol::Float64
     gprecision::Int32; grefine::Int32; inner_reltol::Float64; max_refine::Int32
     initially_nonzero::Int32
+    eager::Int32                 # 0: the sweep of each mesh replays one CUDA graph
 end
 struct SweepInfo
     solves::Int64; converged::Int64; iterations::Int64; assemble_ms::Float64; solve_ms::Float64
+    record_ms::Float64; graph_launches::Int64
 end
 
 """
@@ -277,7 +279,7 @@ function sweep_gpu(meshes, ks, ws; precision=:mixed, refine=true, ctxs=nothing)
     kv = ComplexF64.(ks)
     wv = [Vector{ComplexF64}(w) for w in ws]
     ps = [Matrix{ComplexF64}(undef, c.n_sources, length(kv)) for c in cs]
-    opts = Ref(SweepOpts(precision_code(precision), refine, 0, 0, 0.0, 0.0, 0, 0, 0.0, 0, 0))
+    opts = Ref(SweepOpts(precision_code(precision), refine, 0, 0, 0.0, 0.0, 0, 0, 0.0, 0, 0, 0))
     info = Ref{SweepInfo}()
     GC.@preserve cs kv wv ps begin
         hs = [c.handle for c in cs]

@@ -427,6 +427,10 @@ typedef struct bie_sweep_opts {
     int32_t precision;         /* assembly arithmetic: BIE_PREC_MIXED | BIE_PREC_FP64   */
     int32_t refine;            /* mixed: complex64 inner GMRES + complex128 residual     */
     bie_gmres_opts gmres;      /* restart, maxiter, reltol, abstol (zeros: defaults)     */
+    int32_t eager;             /* 0 (default): after the first wavenumber of a mesh, its
+                                  GMRES solve is recorded as one CUDA graph and replayed
+                                  for the other wavenumbers; 1: host-driven GMRES for
+                                  every wavenumber                                       */
 } bie_sweep_opts;
 
 typedef struct bie_sweep_info {
@@ -435,6 +439,8 @@ typedef struct bie_sweep_info {
     int64_t iterations;        /* GMRES iterations summed                                 */
     double  assemble_ms;       /* device time of the assemblies (CUDA events)            */
     double  solve_ms;          /* device time of right-hand sides + GMRES                */
+    double  record_ms;         /* host time spent recording + instantiating graphs       */
+    int64_t graph_launches;    /* CUDA graph launches (nk - 1 per mesh unless eager)     */
 } bie_sweep_info;
 
 /*
@@ -448,6 +454,13 @@ typedef struct bie_sweep_info {
  * src/3d/rosebem.jl:235-262).  ks: nk complex (interleaved), w[m]: N_m complex
  * host vectors, p[m]: nk x N_m complex host outputs (column j = k_j).
  * iters (optional): nmesh x nk GMRES iteration counts.
+ * Unless opts->eager is set, the first wavenumber of each mesh runs launch by
+ * launch (it sizes the device scratch and, through the autotuner, picks the
+ * assembly's slicing); then the mesh's GMRES solve is recorded once as a CUDA
+ * graph whose loops are conditional nodes driven by device state (restart <=
+ * 64) and each later wavenumber is its assembly plus one launch of that graph,
+ * all enqueued without a host round trip.  Both forms give the same results
+ * up to the rounding order of the assemblies' atomic sums.
  */
 BIE_API int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk,
                       const double *const *w, double *const *p, const bie_sweep_opts *opts,

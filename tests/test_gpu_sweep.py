@@ -41,3 +41,52 @@ def test_sweep_mixed_matches_fp64():
     for a, b in zip(pmx, p64):
         for j in range(len(ks)):
             assert rel(a[:, j], b[:, j]) <= 1e-5
+
+
+@pytest.mark.parametrize("precision,refine", [("mixed", True), ("fp64", False), ("mixed", False)])
+def test_sweep_graph_replay_matches_eager(precision, refine):
+    """The recorded CUDA graph (conditional WHILE/SWITCH nodes for the GMRES
+    loops) gives the solutions and iteration counts of the host-driven sweep.
+    The assemblies add element contributions with atomics, so two runs differ
+    by rounding order: ~1e-16 per entry in FP64, ~1e-7 in the FP32 accumulators
+    of the mixed form; the solutions are compared at 1e-10 and 1e-6, the
+    iteration counts to within two steps."""
+    meshes = [bm.icosphere(5), bm.ellipsoid(6)]
+    ks = [0.3, 2.5, 5.0 + 0.1j, 7.5]
+    rng = np.random.default_rng(11)
+    ws = [rng.normal(size=mm.n_sources) + 1j * rng.normal(size=mm.n_sources) for mm in meshes]
+    pe, ie = biegpu.sweep(meshes, ks, ws, precision=precision, refine=refine, eager=True)
+    pg, ig = biegpu.sweep(meshes, ks, ws, precision=precision, refine=refine)
+    assert ie["graph_launches"] == 0 and ig["graph_launches"] == 2 * (len(ks) - 1)
+    assert ig["converged"] == ig["solves"] == 8
+    d_it = np.abs(ig["iterations_per_solve"] - ie["iterations_per_solve"])
+    assert d_it.max() <= 2
+    tol = 1e-10 if precision == "fp64" else 1e-6
+    for a, b in zip(pg, pe):
+        for j in range(len(ks)):
+            assert rel(a[:, j], b[:, j]) <= tol
+
+
+def test_sweep_graph_small_restart_and_maxiter():
+    """restart 3 (many passes through the restart WHILE node) and a maxiter that
+    stops the solve early: the replay ends and agrees with the eager sweep
+    (FP64 assembly, so the runs differ only by the order of FP64 atomics)."""
+    mesh = bm.icosphere(5)
+    ks = [1.0, 3.0, 6.0]
+    w = np.random.default_rng(3).normal(size=mesh.n_sources) + 0j
+    for maxiter in (0, 7):
+        kw = dict(precision="fp64", refine=False, restart=3, maxiter=maxiter)
+        pe, ie = biegpu.sweep([mesh], ks, [w], eager=True, **kw)
+        pg, ig = biegpu.sweep([mesh], ks, [w], **kw)
+        np.testing.assert_array_equal(ig["iterations_per_solve"], ie["iterations_per_solve"])
+        assert ig["converged"] == ie["converged"]
+        if maxiter:
+            assert (ig["iterations_per_solve"] == 7).all() and ig["converged"] == 0
+        for j in range(len(ks)):
+            assert rel(pg[0][:, j], pe[0][:, j]) <= 1e-10
+    # the refined mixed path through the same small restart
+    pe, ie = biegpu.sweep([mesh], ks, [w], precision="mixed", restart=3, eager=True)
+    pg, ig = biegpu.sweep([mesh], ks, [w], precision="mixed", restart=3)
+    assert ig["converged"] == ie["converged"] == 3
+    for j in range(len(ks)):
+        assert rel(pg[0][:, j], pe[0][:, j]) <= 1e-6
