@@ -15,5 +15,7 @@ from .operators import (Diagonal, FMMFOperator, FMMGOperator, GPUFOperator, GPUG
 from .sweep import sweep  # noqa: F401
 from .adjoint import farfield_objective  # noqa: F401
 from .rosebem import apply_taylor_expansion, taylor_assemble  # noqa: F401
+from .lossy import (LossyGlobalOuter, ambient_to_properties, tangential_derivatives,  # noqa: F401
+                    visco_thermal_constants)
 
 __version__ = "0.1.0"

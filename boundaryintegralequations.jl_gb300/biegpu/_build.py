@@ -32,6 +32,8 @@ SOURCES = [
     "bie_lowp.cu",
     "bie_fastop.cu",
     "bie_peaks.cu",
+    "bie_lossy.cpp",
+    "bie_lossy.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code is compiled without FMA contraction so that the set-up arithmetic

@@ -162,6 +162,27 @@ class AdjointInfo(C.Structure):
                 ("adjoint_iterations", C.c_int32), ("adjoint_converged", C.c_int32)]
 
 
+_C2 = C.c_double * 2
+
+
+class LossyConstants(C.Structure):
+    _fields_ = [("rho", C.c_double), ("c", C.c_double), ("kp", C.c_double),
+                ("ka", _C2), ("kh", _C2), ("kv", _C2), ("tau_a", _C2), ("tau_h", _C2),
+                ("phi_a", _C2), ("phi_h", _C2), ("eta", C.c_double), ("mu", C.c_double),
+                ("mu_a", _C2), ("mu_h", _C2)]
+
+
+class LossyOpts(C.Structure):
+    _fields_ = [("S", C.c_double), ("custom_air", C.c_int32), ("pa", C.c_double), ("t", C.c_double),
+                ("Hr", C.c_double), ("depth", C.c_int32), ("interior", C.c_int32), ("fmm_on", C.c_int32),
+                ("n_gauss", C.c_int32), ("fmm_offset", C.c_double), ("normals", C.c_void_p),
+                ("solve", GmresOpts)]
+
+
+BIE_LOSSY_BLOCKS = {"outer": 0, "Ha": 1, "Ga": 2, "Hh": 3, "Gh": 4, "Hv": 5, "Gv": 6, "Dc": 7, "Dr": 8,
+                    "Nd": 9, "NdT": 10, "inner": 11}
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -205,6 +226,17 @@ SIGNATURES = {
                        C.POINTER(SweepInfo), _P]),
     "bie_adjoint": (_I, [_P, _D, _D, _P, _P, _I64, C.POINTER(AdjointOpts), C.POINTER(_D), _P, _P, _P,
                          C.POINTER(AdjointInfo)]),
+    "bie_ambient_to_properties": (_I, [_D, _D, _D, _D, _P]),
+    "bie_visco_thermal_constants": (_I, [_D, _D, _D, _D, _D, C.POINTER(LossyConstants)]),
+    "bie_tangential_derivatives": (_I, [C.POINTER(MeshDesc), C.POINTER(_I64), _P, _P, _P, _P, _P]),
+    "bie_lossy_create": (_I, [_P, _D, C.POINTER(LossyOpts), C.POINTER(_P)]),
+    "bie_lossy_destroy": (_I, [_P]),
+    "bie_lossy_constants_of": (_I, [_P, C.POINTER(LossyConstants)]),
+    "bie_lossy_apply_device": (_I, [_P, _I, _P, _P]),
+    "bie_lossy_solve_device": (_I, [_P, _I, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
+    "bie_lossy_apply": (_I, [_P, _I, _P, _P]),
+    "bie_lossy_solve": (_I, [_P, _I, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
+    "bie_lossy_stats": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64), _I]),
 }
 
 

@@ -81,6 +81,19 @@ void run_assemble(bie::Ctx &c, const bie::AssembleArgs &a, int precision) {
     else bie::launch_assemble_fp64(c, a);
 }
 
+bie::LossyOp &as_lossy(bie_lossy *L) {
+    if (!L) bie::fail(BIE_ERR_INVALID, "lossy system is NULL");
+    return *reinterpret_cast<bie::LossyOp *>(L);
+}
+
+void check_block(int block) {
+    if (block < BIE_LOSSY_OUTER || block > BIE_LOSSY_INNER) bie::fail(BIE_ERR_INVALID, "unknown lossy block");
+}
+
+void check_solve_opts(const bie_gmres_opts &o) {
+    if (!(o.reltol >= 0) || !(o.abstol >= 0)) bie::fail(BIE_ERR_INVALID, "tolerances must be >= 0");
+}
+
 }  // namespace
 
 extern "C" {
@@ -641,6 +654,206 @@ int bie_assemble_device(bie_ctx *ctx, double k_re, double k_im, const double *d_
         bie::AssembleArgs a{k_re, k_im, d_targets ? d_targets : c.d_sources, M, flags,
                             d_F, d_G, d_C};
         run_assemble(c, a, precision);
+    });
+}
+
+// ---- visco-thermal system ----------------------------------------------------
+int bie_ambient_to_properties(double f, double ps, double t, double H, double out[10]) {
+    return guarded([&] {
+        if (!out) bie::fail(BIE_ERR_INVALID, "out must not be NULL");
+        if (!std::isfinite(f) || !std::isfinite(ps) || !std::isfinite(t) || !std::isfinite(H) || !(ps > 0) ||
+            !(t > -273.15) || H < 0)
+            bie::fail(BIE_ERR_INVALID, "need finite f, ps > 0, t > -273.15 C, H >= 0");
+        bie::ambient_to_properties(f, ps, t, H, out);
+    });
+}
+
+int bie_visco_thermal_constants(double freq, double S, double pa, double t, double Hr, bie_lossy_constants *out) {
+    return guarded([&] {
+        if (!out) bie::fail(BIE_ERR_INVALID, "out must not be NULL");
+        if (!(freq > 0) || !std::isfinite(freq) || !std::isfinite(S) || S == 0.0)
+            bie::fail(BIE_ERR_INVALID, "need freq > 0 and a nonzero finite S");
+        if (!std::isfinite(pa) || !(pa > 0) || !std::isfinite(t) || !(t > -273.15) || !std::isfinite(Hr) || Hr < 0)
+            bie::fail(BIE_ERR_INVALID, "need pa > 0, t > -273.15 C, Hr >= 0");
+        *out = bie::visco_thermal_constants(freq, S, pa, t, Hr);
+    });
+}
+
+int bie_tangential_derivatives(const bie_mesh_desc *d, int64_t *nnz, int64_t *row_ptr, int64_t *cols, double *Dx,
+                               double *Dy, double *Dz) {
+    return guarded([&] {
+        if (!d || !nnz) bie::fail(BIE_ERR_INVALID, "mesh and nnz must not be NULL");
+        if (d->n_coordinates <= 0 || d->n_elements <= 0 || d->n_sources <= 0 || !d->coordinates || !d->topology ||
+            !d->physics_topology)
+            bie::fail(BIE_ERR_INVALID, "mesh sizes must be positive and its arrays given");
+        if (d->n_coordinates > INT32_MAX || d->n_sources > INT32_MAX || d->n_elements > INT32_MAX)
+            bie::fail(BIE_ERR_INVALID, "mesh too large for 32-bit node indices");
+        const int NS = bie::n_nodes_of_kind(d->shape_kind), NP = bie::n_nodes_of_kind(d->physics_kind);
+        const int64_t E = d->n_elements, N = d->n_sources;
+        std::vector<int32_t> topo((size_t)NS * E), ptopo((size_t)NP * E);
+        for (int64_t i = 0; i < NS * E; ++i) {
+            const int64_t v = d->topology[i];
+            if (v < 1 || v > d->n_coordinates) bie::fail(BIE_ERR_INVALID, "topology index out of range");
+            topo[(size_t)i] = (int32_t)(v - 1);
+        }
+        for (int64_t i = 0; i < NP * E; ++i) {
+            const int64_t v = d->physics_topology[i];
+            if (v < 1 || v > N) bie::fail(BIE_ERR_INVALID, "physics_topology index out of range");
+            ptopo[(size_t)i] = (int32_t)(v - 1);
+        }
+        for (int64_t i = 0; i < 3 * d->n_coordinates; ++i)
+            if (!std::isfinite(d->coordinates[i])) bie::fail(BIE_ERR_INVALID, "non-finite coordinate");
+        std::vector<int64_t> rp;
+        std::vector<int32_t> cl;
+        std::vector<double> dx, dy, dz;
+        bie::tangential_derivatives(d->shape_kind, d->physics_kind, d->coordinates, E, topo.data(), ptopo.data(), N,
+                                    rp, cl, dx, dy, dz);
+        *nnz = (int64_t)cl.size();
+        if (!row_ptr) return;
+        if (!cols || !Dx || !Dy || !Dz) bie::fail(BIE_ERR_INVALID, "cols, Dx, Dy, Dz must not be NULL");
+        std::copy(rp.begin(), rp.end(), row_ptr);
+        std::copy(cl.begin(), cl.end(), cols);
+        std::copy(dx.begin(), dx.end(), Dx);
+        std::copy(dy.begin(), dy.end(), Dy);
+        std::copy(dz.begin(), dz.end(), Dz);
+    });
+}
+
+int bie_lossy_create(bie_ctx *ctx, double freq, const bie_lossy_opts *opts, bie_lossy **out) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!opts || !out) bie::fail(BIE_ERR_INVALID, "opts and out must not be NULL");
+        *out = nullptr;
+        const bie_lossy_opts &o = *opts;
+        if (!(freq > 0) || !std::isfinite(freq)) bie::fail(BIE_ERR_INVALID, "freq must be positive");
+        if (!o.normals) bie::fail(BIE_ERR_INVALID, "normals (3 x N) must be given");
+        if (!std::isfinite(o.S)) bie::fail(BIE_ERR_INVALID, "S must be finite");
+        if (o.custom_air && (!(o.pa > 0) || !std::isfinite(o.pa) || !(o.t > -273.15) || !std::isfinite(o.t) ||
+                             !(o.Hr >= 0) || !std::isfinite(o.Hr)))
+            bie::fail(BIE_ERR_INVALID, "need pa > 0, t > -273.15 C, Hr >= 0");
+        if (o.depth != 0 && o.depth != 1 && o.depth != 2) bie::fail(BIE_ERR_INVALID, "depth must be 1 or 2");
+        if (o.fmm_on && o.fmm_offset > 1.0) bie::fail(BIE_ERR_INVALID, "fmm_offset must be <= 1");
+        check_solve_opts(o.solve);
+        for (int64_t i = 0; i < 3 * c.n_sources; ++i)
+            if (!std::isfinite(o.normals[i])) bie::fail(BIE_ERR_INVALID, "non-finite normal");
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        *out = reinterpret_cast<bie_lossy *>(bie::create_lossy(c, freq, o));
+    });
+}
+
+int bie_lossy_destroy(bie_lossy *L) {
+    return guarded([&] {
+        if (!L) return;
+        bie::LossyOp *p = reinterpret_cast<bie::LossyOp *>(L);
+        bie::Ctx &c = bie::lossy_context(*p);
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+        bie::destroy_lossy(p);
+    });
+}
+
+int bie_lossy_constants_of(const bie_lossy *L, bie_lossy_constants *out) {
+    return guarded([&] {
+        if (!out) bie::fail(BIE_ERR_INVALID, "out must not be NULL");
+        *out = bie::lossy_constants(as_lossy(const_cast<bie_lossy *>(L)));
+    });
+}
+
+int bie_lossy_apply_device(bie_lossy *L, int block, const double *d_x, double *d_y) {
+    return guarded([&] {
+        bie::LossyOp &op = as_lossy(L);
+        check_block(block);
+        if (!d_x || !d_y) bie::fail(BIE_ERR_INVALID, "x and y must not be NULL");
+        if (d_x == d_y) bie::fail(BIE_ERR_INVALID, "x and y must not alias");
+        bie::Ctx &c = bie::lossy_context(op);
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie::lossy_apply(op, block, d_x, d_y);
+    });
+}
+
+int bie_lossy_solve_device(bie_lossy *L, int block, const double *d_b, double *d_x, const bie_gmres_opts *opts,
+                           bie_gmres_info *info) {
+    int converged = 1;
+    const int st = guarded([&] {
+        bie::LossyOp &op = as_lossy(L);
+        check_block(block);
+        if (!d_b || !d_x) bie::fail(BIE_ERR_INVALID, "b and x must not be NULL");
+        if (d_b == d_x) bie::fail(BIE_ERR_INVALID, "b and x must not alias");
+        bie_gmres_opts o{};
+        if (opts) o = *opts;
+        check_solve_opts(o);
+        bie::Ctx &c = bie::lossy_context(op);
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie_gmres_info inf{};
+        bie::lossy_solve(op, block, d_b, d_x, o, inf);
+        if (info) *info = inf;
+        converged = inf.converged;
+    });
+    if (st == BIE_OK && !converged) {
+        g_last_error = "GMRES reached maxiter before the tolerance";
+        return BIE_ERR_NOT_CONVERGED;
+    }
+    return st;
+}
+
+int bie_lossy_apply(bie_lossy *L, int block, const double *x, double *y) {
+    return guarded([&] {
+        bie::LossyOp &op = as_lossy(L);
+        check_block(block);
+        if (!x || !y) bie::fail(BIE_ERR_INVALID, "x and y must not be NULL");
+        bie::Ctx &c = bie::lossy_context(op);
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        const int64_t N = c.n_sources;
+        const int64_t ni = bie::lossy_block_len(block, true, N), no = bie::lossy_block_len(block, false, N);
+        double *d = static_cast<double *>(c.scratch(bie::kScratchTargets, (size_t)(ni + no) * 16));
+        BIE_CUDA(cudaMemcpyAsync(d, x, (size_t)ni * 16, cudaMemcpyHostToDevice, c.stream));
+        bie::lossy_apply(op, block, d, d + 2 * ni);
+        BIE_CUDA(cudaMemcpyAsync(y, d + 2 * ni, (size_t)no * 16, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int bie_lossy_solve(bie_lossy *L, int block, const double *b, double *x, const bie_gmres_opts *opts,
+                    bie_gmres_info *info) {
+    int converged = 1;
+    const int st = guarded([&] {
+        bie::LossyOp &op = as_lossy(L);
+        check_block(block);
+        if (!b || !x) bie::fail(BIE_ERR_INVALID, "b and x must not be NULL");
+        bie_gmres_opts o{};
+        if (opts) o = *opts;
+        check_solve_opts(o);
+        bie::Ctx &c = bie::lossy_context(op);
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        const int64_t n = bie::lossy_block_len(block, true, c.n_sources);
+        double *d = static_cast<double *>(c.scratch(bie::kScratchTargets, (size_t)n * 32));
+        BIE_CUDA(cudaMemcpyAsync(d, b, (size_t)n * 16, cudaMemcpyHostToDevice, c.stream));
+        bie_gmres_info inf{};
+        bie::lossy_solve(op, block, d, d + 2 * n, o, inf);
+        BIE_CUDA(cudaMemcpyAsync(x, d + 2 * n, (size_t)n * 16, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+        if (info) *info = inf;
+        converged = inf.converged;
+    });
+    if (st == BIE_OK && !converged) {
+        g_last_error = "GMRES reached maxiter before the tolerance";
+        return BIE_ERR_NOT_CONVERGED;
+    }
+    return st;
+}
+
+int bie_lossy_stats(bie_lossy *L, int64_t *nested_solves, int64_t *nested_iterations, int reset) {
+    return guarded([&] {
+        bie::LossyOp &op = as_lossy(L);
+        bie::Ctx &c = bie::lossy_context(op);
+        std::lock_guard<std::mutex> lock(c.mu);
+        bie::lossy_stats(op, nested_solves, nested_iterations, reset != 0);
     });
 }
 

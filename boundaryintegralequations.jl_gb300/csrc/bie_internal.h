@@ -88,7 +88,9 @@ enum ScratchSlot {
     kScratchSolver = 10,   // GMRES workspace
     kScratchSolverPart = 11,  // GMRES reduction partials and small coefficient vectors
     kScratchLowp = 12,     // multi-RHS products: strips, 16-bit tiles, partial sums
-    kScratchCount = 13
+    kScratchSolverNested = 13,  // GMRES workspace + partials of nested solves, two slots
+                                // per level 1, 2 (solves inside another solve's product)
+    kScratchCount = 17
 };
 
 // Mixed-precision element record (32-bit words, same element order as the FP64
@@ -253,6 +255,46 @@ void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const
 // idle streams for the nested body captures.  *d_info (device) receives the
 // solve's statistics when the graph runs.
 constexpr int kGraphMaxRestart = 64;
+
+// Visco-thermal system, host part (bie_lossy.cpp)
+void ambient_to_properties(double f, double ps, double t, double H, double out[10]);
+bie_lossy_constants visco_thermal_constants(double freq, double S, double pa, double t, double Hr);
+// per node the sorted physics nodes of its elements (connected_sources, depth 1)
+void node_pattern(int64_t N, int64_t E, int NP, const int32_t *ptopo, std::vector<int64_t> &row_ptr,
+                  std::vector<int32_t> &cols);
+// Dx, Dy, Dz on node_pattern; topo NS x E, ptopo NP x E, 0-based
+void tangential_derivatives(int shape_kind, int physics_kind, const double *coords, int64_t E,
+                            const int32_t *topo, const int32_t *ptopo, int64_t N, std::vector<int64_t> &row_ptr,
+                            std::vector<int32_t> &cols, std::vector<double> &Dx, std::vector<double> &Dy,
+                            std::vector<double> &Dz);
+
+// Visco-thermal system, device part (bie_lossy.cu); calls hold the context mutex
+struct LossyOp;
+LossyOp *create_lossy(Ctx &c, double freq, const bie_lossy_opts &o);
+void destroy_lossy(LossyOp *L);
+Ctx &lossy_context(const LossyOp &L);
+const bie_lossy_constants &lossy_constants(const LossyOp &L);
+int64_t lossy_block_len(int block, bool input, int64_t N);   // vector lengths of a block
+void lossy_apply(LossyOp &L, int block, const double *x, double *y);   // device vectors
+void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gmres_opts &o,
+                 bie_gmres_info &info);
+void lossy_stats(LossyOp &L, int64_t *solves, int64_t *iterations, bool reset);
+
+// An operator that the library's GMRES applies through a virtual call (the
+// visco-thermal composite and its sparse blocks).  apply: y = A x on the
+// context stream; operators whose kernels return at once while *stop is set
+// say so (honours_stop), so GMRES may queue several steps between host checks.
+struct DevOp {
+    virtual ~DevOp() = default;
+    virtual int64_t size() const = 0;
+    virtual void apply(const double2 *x, double2 *y, const int *stop) = 0;
+    virtual bool honours_stop() const { return false; }
+};
+// run_gmres on a DevOp of size n; `level` 0, 1 or 2 selects the workspace, so a
+// solve may run inside the product of a solve one level up.
+constexpr int kMaxSolveLevel = 2;
+void run_gmres_devop(Ctx &c, DevOp &op, const double *b, double *x, const bie_gmres_opts &o,
+                     bie_gmres_info &info, int level);
 void capture_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
                    bie_gmres_info *d_info, const cudaStream_t *body);
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);

@@ -692,8 +692,12 @@ struct Solver {
     RfState *rf = nullptr;        // device-resident refinement state (graph form)
     const int *stop = nullptr;    // device stop flag honoured by the launches below
     cudaStream_t stream;          // launch stream (a capture stream while recording a graph)
+    DevOp *devop = nullptr;       // operator applied through DevOp::apply (else bie_operator)
 
-    Solver(Ctx &ctx, int64_t n_, int restart) : c(ctx), n(n_), m(restart), stream(ctx.stream) {
+    // level > 0: the workspace of a solve nested inside another solve's product
+    Solver(Ctx &ctx, int64_t n_, int restart, int level = 0)
+        : c(ctx), n(n_), m(restart), stream(ctx.stream) {
+        const int part_slot = level == 0 ? kScratchSolverPart : kScratchSolverNested + 2 * (level - 1) + 1;
         // column slices: ~8 blocks per SM for the two-rows-per-thread complex64 product
         S = 1;
         const int64_t row_tiles = (n / 2 + kT - 1) / kT;
@@ -703,7 +707,7 @@ struct Solver {
         const size_t hbytes = (size_t)(restart + 2) * 16;
         const size_t nc = (size_t)(restart + 1) * restart + 4 * (size_t)(restart + 1) + restart;
         const size_t st_bytes = nc * 16 + (size_t)restart * 8 + sizeof(GmScalars) + sizeof(RfState) + 96;
-        char *base = static_cast<char *>(c.scratch(kScratchSolverPart, part_bytes + hbytes + st_bytes));
+        char *base = static_cast<char *>(c.scratch(part_slot, part_bytes + hbytes + st_bytes));
         part = reinterpret_cast<double2 *>(base);
         hdev = reinterpret_cast<double2 *>(base + part_bytes);
         double2 *z = reinterpret_cast<double2 *>(base + part_bytes + hbytes);
@@ -730,6 +734,10 @@ struct Solver {
 
     // y = s (K x) + d .* x   (dense kernels skip when *stop is set)
     void apply(const bie_operator &op, int precision, const double2 *x, double2 *y) {
+        if (devop) {
+            devop->apply(x, y, stop);
+            return;
+        }
         const double2 sc = make_double2(op.scale_re, op.scale_im);
         const double2 *d = reinterpret_cast<const double2 *>(op.diag);
         if (op.kind == BIE_OP_DENSE) {
@@ -860,7 +868,7 @@ int gmres_core(Solver &S, const bie_operator &op, int prec, const double2 *b, do
                bool x_zero, double2 *V, double2 *w, int restart, int maxiter, double tol,
                double *res_out, int *restarts_out, int64_t *matvecs) {
     const int64_t n = S.n;
-    const bool dense = op.kind == BIE_OP_DENSE;
+    const bool dense = S.devop ? S.devop->honours_stop() : op.kind == BIE_OP_DENSE;
     const GmState st = S.st;
     const int *stop_flag = &st.s->done;
     cudaStream_t stream = S.stream;
@@ -1128,9 +1136,12 @@ void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_,
     S.launched();
 }
 
-void run_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, const bie_gmres_opts &o,
-               bie_gmres_info &info) {
-    const int64_t n = c.n_sources;
+namespace {
+
+// The restarted (optionally refined) GMRES behind run_gmres and run_gmres_devop.
+void gmres_solve(Ctx &c, const bie_operator &op, DevOp *devop, int64_t n, int level, const double *b_,
+                 double *x_, const bie_gmres_opts &o, bie_gmres_info &info) {
+    if (level < 0 || level > kMaxSolveLevel) fail(BIE_ERR_INVALID, "GMRES nesting deeper than two levels");
     const int restart = (int)std::max<int64_t>(1, std::min<int64_t>(o.restart > 0 ? o.restart : 20, n));
     const int maxiter = o.maxiter > 0 ? o.maxiter : (int)std::min<int64_t>(n, INT32_MAX);
     const double reltol = o.reltol > 0 ? o.reltol : std::sqrt(2.220446049250313e-16);
@@ -1139,12 +1150,14 @@ void run_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, con
     double2 *x = reinterpret_cast<double2 *>(x_);
 
     // workspace: V (restart + 1) x n, w, r, dx
-    char *ws = static_cast<char *>(c.scratch(kScratchSolver, (size_t)(restart + 4) * n * 16));
+    const int ws_slot = level == 0 ? kScratchSolver : kScratchSolverNested + 2 * (level - 1);
+    char *ws = static_cast<char *>(c.scratch(ws_slot, (size_t)(restart + 4) * n * 16));
     double2 *V = reinterpret_cast<double2 *>(ws);
     double2 *w = V + (int64_t)(restart + 1) * n;
     double2 *rr = w + n;
     double2 *dx = rr + n;
-    Solver S(c, n, restart);
+    Solver S(c, n, restart, level);
+    S.devop = devop;
     const double bnorm = S.norm(b);
     const double tol = std::max(reltol * bnorm, abstol);
     if (!o.initially_nonzero) BIE_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 16, c.stream));
@@ -1186,6 +1199,22 @@ void run_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, con
     info.residual_norm = res;
     info.rhs_norm = bnorm;
     info.converged = res <= tol ? 1 : 0;
+}
+
+}  // namespace
+
+void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
+               bie_gmres_info &info) {
+    gmres_solve(c, op, nullptr, c.n_sources, 0, b, x, o, info);
+}
+
+void run_gmres_devop(Ctx &c, DevOp &op, const double *b, double *x, const bie_gmres_opts &o,
+                     bie_gmres_info &info, int level) {
+    bie_gmres_opts plain = o;
+    plain.refine = 0;   // one arithmetic: the operator's own
+    bie_operator none{};
+    none.kind = -1;
+    gmres_solve(c, none, &op, op.size(), level, b, x, plain, info);
 }
 
 void apply_operator(Ctx &c, const bie_operator &op, int precision, const double *x, double *y) {

@@ -501,6 +501,97 @@ BIE_API int bie_adjoint(bie_ctx *ctx, double k_re, double k_im, const double *Z,
  * bie_operator.A32 from an assembled matrix. */
 BIE_API int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n);
 
+/* ---- visco-thermal ("lossy") system ------------------------------------ */
+/* Physical properties of air (Rasmussen 1997, annex A), as
+ * ambient_to_properties(f, ps, t, H) of src/utils/ambient_to_properties.jl:1-134:
+ * out = rho, c0, cf, CpCv, eta, alfa, Cp, Cv, landa, beta.  Host only. */
+BIE_API int bie_ambient_to_properties(double f, double ps, double t, double H, double out[10]);
+
+typedef struct bie_lossy_constants {
+    double rho, c, kp;           /* density, zero-frequency speed of sound, 2 pi f / c      */
+    double ka[2], kh[2], kv[2];  /* acoustic, thermal, viscous wavenumbers (re, im)         */
+    double tau_a[2], tau_h[2];   /* isothermal-condition constants                         */
+    double phi_a[2], phi_h[2];   /* no-slip-condition constants                            */
+    double eta, mu;              /* bulk (0.6 mu) and shear viscosity                       */
+    double mu_a[2], mu_h[2];     /* phi_a - tau_a phi_h / tau_h  and  tau_a phi_h / tau_h   */
+} bie_lossy_constants;
+
+/* visco_thermal_constants(; freq, S, pa, t, Hr) of src/utils/lossy_constants.jl:1-34
+ * (the reference's defaults: S = -1, pa = 101325, t = 20, Hr = 50; LossyGlobalOuter
+ * uses S = 1).  Host only. */
+BIE_API int bie_visco_thermal_constants(double freq, double S, double pa, double t, double Hr,
+                                        bie_lossy_constants *out);
+
+/* Tangential derivative matrices Dx, Dy, Dz of the physics interpolation,
+ * interpolation_function_derivatives(mesh) of
+ * src/3d/interpolation_function_derivatives.jl:36-118: at every node, the
+ * surface gradient of each element's basis functions, averaged over the
+ * elements of the node.  CSR on the depth-1 node pattern (0-based, sorted
+ * columns).  Call with row_ptr == NULL to get *nnz; then row_ptr[N + 1],
+ * cols[nnz], Dx/Dy/Dz[nnz].  Host only (no context, no GPU). */
+BIE_API int bie_tangential_derivatives(const bie_mesh_desc *mesh, int64_t *nnz, int64_t *row_ptr,
+                                       int64_t *cols, double *Dx, double *Dy, double *Dz);
+
+typedef struct bie_lossy_opts {
+    double  S;              /* sign convention of the constants (0: 1, as LossyGlobalOuter)    */
+    int32_t custom_air;     /* 0: 101325 Pa, 20 C, 50 % humidity; 1: pa, t, Hr below          */
+    double  pa, t, Hr;      /* ambient pressure (Pa), temperature (Celsius), humidity (%)      */
+    int32_t depth;          /* near-field pattern of the thermal and viscous operators (1, 2)  */
+    int32_t interior;       /* 0: exterior problem (default); 1: interior                      */
+    int32_t fmm_on;         /* 1: acoustic H, G by the fast-operator algorithm                 */
+    int32_t n_gauss;        /* fast operators: Gauss rule (<= 0: 3)                            */
+    double  fmm_offset;     /* fast operators: near-field offset (< 0: 0.2)                    */
+    const double *normals;  /* 3 x N nodal normals (mesh.normals), host, required              */
+    bie_gmres_opts solve;   /* the nested gmres calls (zeros: IterativeSolvers defaults)       */
+} bie_lossy_opts;
+
+/* Blocks of the system (x, y lengths: N, or 3N where stated) */
+#define BIE_LOSSY_OUTER  0  /* LossyGlobalOuter product (N -> N)                         */
+#define BIE_LOSSY_HA     1  /* acoustic H with its integral-free term (N -> N)           */
+#define BIE_LOSSY_GA     2  /* acoustic G (N -> N)                                       */
+#define BIE_LOSSY_HH     3  /* thermal H, near field + integral-free term (N -> N)       */
+#define BIE_LOSSY_GH     4  /* thermal G, near field (N -> N)                            */
+#define BIE_LOSSY_HV     5  /* blockdiag(Av, Av, Av), viscous H (3N -> 3N)               */
+#define BIE_LOSSY_GV     6  /* blockdiag(Bv, Bv, Bv), viscous G (3N -> 3N)               */
+#define BIE_LOSSY_DC     7  /* [Dx; Dy; Dz] (N -> 3N)                                    */
+#define BIE_LOSSY_DR     8  /* [Dx Dy Dz] (3N -> N)                                      */
+#define BIE_LOSSY_ND     9  /* Nd = -[diag(nx); diag(ny); diag(nz)] (N -> 3N)            */
+#define BIE_LOSSY_NDT   10  /* Nd' (3N -> N)                                             */
+#define BIE_LOSSY_INNER 11  /* LossyGlobalInner: Dr Nd z - Nd' gmres(Gv, Hv Nd z) (N)    */
+
+typedef struct bie_lossy bie_lossy;
+
+/*
+ * LossyGlobalOuter(mesh, freq; depth, exterior, fmm_on, n = quadrature of the
+ * context) of src/3d/LossyGlobalMatrix.jl:76-172, resident on the device:
+ * acoustic H, G (dense complex128 from this library's FP64 assembly, or fast
+ * operators), thermal and viscous H, G as near-field CSR matrices (the
+ * library's adaptive near-field rules, sparse_assemble_parallel!), Dx, Dy, Dz
+ * and the normals.  The reference's LossyGlobalOuter passes n = m = 3 to the
+ * acoustic assembly: create the context with quad_n = quad_m = 3 for the same
+ * matrices.  The product (LossyGlobalMatrix.jl:179-197)
+ *     y = -phi_a Ha x + Ga (mu_h gmres(Gh, Hh x)
+ *                          + mu_a gmres(inner, Dr Dc x - Nd' gmres(Gv, Hv Dc x)))
+ * runs its nested GMRES solves on the device (two levels deep inside the
+ * inner operator), each as the reference's gmres call with opts->solve.
+ */
+BIE_API int bie_lossy_create(bie_ctx *ctx, double freq, const bie_lossy_opts *opts, bie_lossy **out);
+BIE_API int bie_lossy_destroy(bie_lossy *L);
+BIE_API int bie_lossy_constants_of(const bie_lossy *L, bie_lossy_constants *out);
+/* y = block x (device vectors, complex interleaved); blocking */
+BIE_API int bie_lossy_apply_device(bie_lossy *L, int block, const double *d_x, double *d_y);
+/* x = gmres(block, b) from x = 0 for the square blocks OUTER, HA, GA, HH, GH,
+ * HV, GV, INNER (device vectors); info optional; BIE_ERR_NOT_CONVERGED with
+ * x written when maxiter is reached. */
+BIE_API int bie_lossy_solve_device(bie_lossy *L, int block, const double *d_b, double *d_x,
+                                   const bie_gmres_opts *opts, bie_gmres_info *info);
+/* The same with host vectors. */
+BIE_API int bie_lossy_apply(bie_lossy *L, int block, const double *x, double *y);
+BIE_API int bie_lossy_solve(bie_lossy *L, int block, const double *b, double *x,
+                            const bie_gmres_opts *opts, bie_gmres_info *info);
+/* Nested GMRES solves and their iterations since creation (or the last reset). */
+BIE_API int bie_lossy_stats(bie_lossy *L, int64_t *nested_solves, int64_t *nested_iterations, int reset);
+
 #ifdef __cplusplus
 }
 #endif
