@@ -406,6 +406,45 @@ def nearfield_bench(args, max_over_ranks):
     return out
 
 
+def lossy_bench(args, max_over_ranks):
+    """Visco-thermal workload: LossyGlobalOuter on a sphere f=16 (2562 nodes,
+    linear, radius 1) at 100 Hz, depth 1, n = m = 3 (the reference's
+    defaults), dense acoustic blocks.  Times the device set-up (FP64 acoustic
+    assembly, thermal / viscous near field, derivative matrices), the product
+    L x (with its nested gmres calls) and the solve of the reference test's
+    system (test/3d/losses_test.jl:30-35: v0 = 0.01 normal velocity)."""
+    import biegpu
+    from biegpu import mesh as bm
+    mesh = bm.icosphere(16)
+    N = mesh.n_sources
+    t0 = time.perf_counter()
+    L = biegpu.LossyGlobalOuter(mesh, 100.0, depth=1, n=3)
+    t_setup = time.perf_counter() - t0
+    x = np.random.default_rng(4).normal(size=N) + 1j * np.random.default_rng(5).normal(size=N)
+    L @ x
+    L.stats(reset=True)
+    reps = max(1, args.lossy_steps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        L @ x
+    t_prod = max_over_ranks(time.perf_counter() - t0) / reps
+    st = L.stats(reset=True)
+    v0 = np.concatenate([0.01 * np.ones(N), np.zeros(2 * N)])
+    t0 = time.perf_counter()
+    rhs = L.rhs(v0)
+    pa, info = L.solve(rhs, return_info=True)
+    t_solve = max_over_ranks(time.perf_counter() - t0)
+    st2 = L.stats(reset=True)
+    res = float(np.linalg.norm(L @ pa - rhs) / np.linalg.norm(rhs))
+    return {"workload": f"icosphere f=16 ({N} nodes, linear), 100 Hz, depth 1, n = m = 3, dense acoustic blocks",
+            "setup_s": t_setup, "product_ms": 1e3 * t_prod,
+            "nested_solves_per_product": st["nested_solves"] / reps,
+            "nested_iterations_per_product": st["nested_iterations"] / reps,
+            "solve_s": t_solve, "outer_iterations": info["iterations"], "converged": info["converged"],
+            "solve_nested_iterations": st2["nested_iterations"], "relative_residual": res,
+            "timing": "host wall clock (the nested solves synchronise with the host)"}
+
+
 def adjoint_bench(args, max_over_ranks):
     """Adjoint workload: ellipsoid 3:2:1 f=22 (4842 nodes, linear), ka=3, 32
     seeded field points on the radius-10 sphere, seeded impedances |Z| = rho c.
@@ -498,6 +537,8 @@ def main():
     ap.add_argument("--adjoint-steps", type=int, default=3)
     ap.add_argument("--no-nearfield", action="store_true", help="skip the near-field / fast-operator measurement")
     ap.add_argument("--nearfield-steps", type=int, default=3)
+    ap.add_argument("--no-lossy", action="store_true", help="skip the visco-thermal system measurement")
+    ap.add_argument("--lossy-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -614,6 +655,9 @@ def main():
     nearfield = None
     if not args.no_nearfield:
         nearfield = nearfield_bench(args, max_over_ranks)
+    lossy = None
+    if not args.no_lossy:
+        lossy = lossy_bench(args, max_over_ranks)
 
     if rank != 0:
         if dist is not None:
@@ -634,7 +678,7 @@ def main():
         "precision": args.precision, "data": "synthetic",
         "config": dict(desc, l2="256 MB L2 flush between steps; each step writes 4.3 GB", parallelism=f"replicas{world}"),
         "roofline": roofline, "plain_fp64": plain, "accuracy": accuracy, "sweep": sweep,
-        "multi_rhs": multi, "adjoint": adjoint, "nearfield": nearfield,
+        "multi_rhs": multi, "adjoint": adjoint, "nearfield": nearfield, "lossy": lossy,
         "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
         "clocks": clk.summary(), "gpu": torch.cuda.get_device_name(dev),
         "peaks": {"fp64_tflops": peaks["fp64_flops"] / 1e12, "fp32_tflops": peaks["fp32_flops"] / 1e12,

@@ -434,10 +434,134 @@ function taylor_assemble_gpu!(mesh, k0, sources; M=0, fOn=true, gOn=true, cOn=tr
     return F, G, C
 end
 
+# ---------------------------------------------------------------------------
+# Visco-thermal system (LossyGlobalOuter, src/3d/LossyGlobalMatrix.jl:76-197)
+# ---------------------------------------------------------------------------
+struct GmresOptsC
+    restart::Int32; maxiter::Int32; reltol::Float64; abstol::Float64
+    precision::Int32; refine::Int32; inner_reltol::Float64; max_refine::Int32; initially_nonzero::Int32
+end
+GmresOptsC(; reltol=0.0, restart=0, maxiter=0) = GmresOptsC(restart, maxiter, reltol, 0.0, 0, 0, 0.0, 0, 0)
+
+struct GmresInfoC
+    iterations::Int32; restarts::Int32; refinements::Int32; converged::Int32
+    matvecs::Int64; residual_norm::Float64; rhs_norm::Float64
+end
+
+struct LossyOpts
+    S::Float64; custom_air::Int32; pa::Float64; t::Float64; Hr::Float64
+    depth::Int32; interior::Int32; fmm_on::Int32; n_gauss::Int32; fmm_offset::Float64
+    normals::Ptr{Float64}; solve::GmresOptsC
+end
+
+const LOSSY_BLOCKS = (outer=0, Ha=1, Ga=2, Hh=3, Gh=4, Hv=5, Gv=6, Dc=7, Dr=8, Nd=9, NdT=10, inner=11)
+
+"A block of the device-resident lossy system as a `LinearMap` (products on the GPU)."
+struct GPULossyBlock <: LinearMaps.LinearMap{ComplexF64}
+    owner::Any
+    code::Cint
+    dims::Tuple{Int,Int}
+end
+Base.size(A::GPULossyBlock) = A.dims
+
+function LinearMaps._unsafe_mul!(y::AbstractVector, A::GPULossyBlock, x::AbstractVector)
+    xv = Vector{ComplexF64}(x)
+    yv = Vector{ComplexF64}(undef, size(A, 1))
+    GC.@preserve xv yv check(ccall((:bie_lossy_apply, libbiegpu), Cint,
+                                   (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                                   A.owner.handle, A.code, xv, yv))
+    copyto!(y, yv)
+    return y
+end
+
+"""
+    gmres_gpu(A::GPULossyBlock, b; reltol=0, restart=0, maxiter=0)
+
+`gmres(A, b)` with the device GMRES of the library (IterativeSolvers defaults
+for zeros); square blocks only.
+"""
+function gmres_gpu(A::GPULossyBlock, b; reltol=0.0, restart=0, maxiter=0)
+    bv = Vector{ComplexF64}(b)
+    x = similar(bv)
+    opts = Ref(GmresOptsC(; reltol=reltol, restart=restart, maxiter=maxiter))
+    info = Ref{GmresInfoC}()
+    st = GC.@preserve bv x ccall((:bie_lossy_solve, libbiegpu), Cint,
+                                 (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Ptr{ComplexF64}, Ref{GmresOptsC},
+                                  Ref{GmresInfoC}), A.owner.handle, A.code, bv, x, opts, info)
+    st == Cint(-3) || check(st)   # not converged: x is still returned, as gmres does
+    return x
+end
+
+"""
+    GPULossyGlobalOuter(mesh, freq; depth=1, n=3, exterior=true, fmm_on=false, S=1)
+
+Drop-in for `LossyGlobalOuter(mesh, freq; depth, n, exterior, fmm_on)`: the
+acoustic, thermal and viscous BEM blocks, the tangential derivatives and the
+normals live on the device and the product (with its nested gmres calls) runs
+there.  The fields `Ha, Ga, Hh, Gh, Hv, Gv, Dc, Dr, Nd, inner` are
+`GPULossyBlock`s (`Nd'` is `NdT`), and `phi_a, phi_h, tau_a, tau_h, mu_a,
+mu_h` the constants, as in the reference's struct.
+"""
+mutable struct GPULossyGlobalOuter <: LinearMaps.LinearMap{ComplexF64}
+    ctx::Context
+    handle::Ptr{Cvoid}
+    n::Int
+    normals::Matrix{Float64}
+    Ha::GPULossyBlock; Ga::GPULossyBlock; Hh::GPULossyBlock; Gh::GPULossyBlock
+    Hv::GPULossyBlock; Gv::GPULossyBlock; Dc::GPULossyBlock; Dr::GPULossyBlock
+    Nd::GPULossyBlock; NdT::GPULossyBlock; inner::GPULossyBlock
+    phi_a::ComplexF64; phi_h::ComplexF64; tau_a::ComplexF64; tau_h::ComplexF64
+    mu_a::ComplexF64; mu_h::ComplexF64
+    GPULossyGlobalOuter() = new()
+end
+
+function GPULossyGlobalOuter(mesh, freq; depth=1, n=3, exterior=true, fmm_on=false, S=1.0, fmm_offset=0.2,
+                             reltol=0.0, restart=0, maxiter=0, ctx=Context(mesh; n=n, m=n))
+    L = GPULossyGlobalOuter()
+    L.ctx = ctx
+    N = ctx.n_sources
+    L.n = N
+    L.normals = Matrix{Float64}(mesh.normals)
+    opts = Ref(LossyOpts(S, 0, 0.0, 0.0, 0.0, depth, exterior ? 0 : 1, fmm_on ? 1 : 0, n, fmm_offset,
+                         pointer(L.normals), GmresOptsC(; reltol=reltol, restart=restart, maxiter=maxiter)))
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve L check(ccall((:bie_lossy_create, libbiegpu), Cint,
+                               (Ptr{Cvoid}, Float64, Ref{LossyOpts}, Ref{Ptr{Cvoid}}), ctx.handle, freq, opts, h))
+    L.handle = h[]
+    finalizer(o -> ccall((:bie_lossy_destroy, libbiegpu), Cint, (Ptr{Cvoid},), o.handle), L)
+    k = Ref{NTuple{23,Float64}}()
+    check(ccall((:bie_lossy_constants_of, libbiegpu), Cint, (Ptr{Cvoid}, Ref{NTuple{23,Float64}}), L.handle, k))
+    v = k[]
+    cx(i) = complex(v[i], v[i+1])
+    L.tau_a, L.tau_h, L.phi_a, L.phi_h = cx(10), cx(12), cx(14), cx(16)
+    L.mu_a, L.mu_h = cx(20), cx(22)
+    blk(name, d) = GPULossyBlock(L, Cint(LOSSY_BLOCKS[name]), d)
+    L.Ha, L.Ga, L.Hh, L.Gh = blk(:Ha, (N, N)), blk(:Ga, (N, N)), blk(:Hh, (N, N)), blk(:Gh, (N, N))
+    L.Hv, L.Gv = blk(:Hv, (3N, 3N)), blk(:Gv, (3N, 3N))
+    L.Dc, L.Dr = blk(:Dc, (3N, N)), blk(:Dr, (N, 3N))
+    L.Nd, L.NdT, L.inner = blk(:Nd, (3N, N)), blk(:NdT, (N, 3N)), blk(:inner, (N, N))
+    return L
+end
+
+Base.size(L::GPULossyGlobalOuter) = (L.n, L.n)
+
+function LinearMaps._unsafe_mul!(y::AbstractVector, L::GPULossyGlobalOuter, x::AbstractVector)
+    xv = Vector{ComplexF64}(x)
+    yv = Vector{ComplexF64}(undef, L.n)
+    GC.@preserve xv yv check(ccall((:bie_lossy_apply, libbiegpu), Cint,
+                                   (Ptr{Cvoid}, Cint, Ptr{ComplexF64}, Ptr{ComplexF64}),
+                                   L.handle, Cint(LOSSY_BLOCKS.outer), xv, yv))
+    copyto!(y, yv)
+    return y
+end
+
+"`gmres(L, b)` for the whole lossy system with the library's device GMRES."
+gmres_gpu(L::GPULossyGlobalOuter, b; kwargs...) = gmres_gpu(GPULossyBlock(L, Cint(0), (L.n, L.n)), b; kwargs...)
+
 version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
 export Context, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
        sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective, FastFOperator, FastGOperator,
-       taylor_assemble_gpu!
+       taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu
 
 end # module
