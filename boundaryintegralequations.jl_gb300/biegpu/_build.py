@@ -34,6 +34,7 @@ SOURCES = [
     "bie_peaks.cu",
     "bie_lossy.cpp",
     "bie_lossy.cu",
+    "bie_mesh_io.cpp",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code is compiled without FMA contraction so that the set-up arithmetic

@@ -226,6 +226,8 @@ SIGNATURES = {
                        C.POINTER(SweepInfo), _P]),
     "bie_adjoint": (_I, [_P, _D, _D, _P, _P, _I64, C.POINTER(AdjointOpts), C.POINTER(_D), _P, _P, _P,
                          C.POINTER(AdjointInfo)]),
+    "bie_read_comsol": (_I, [C.c_char_p, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(C.c_int32),
+                             C.POINTER(_I64), _P, _P, _P]),
     "bie_ambient_to_properties": (_I, [_D, _D, _D, _D, _P]),
     "bie_visco_thermal_constants": (_I, [_D, _D, _D, _D, _D, C.POINTER(LossyConstants)]),
     "bie_tangential_derivatives": (_I, [C.POINTER(MeshDesc), C.POINTER(_I64), _P, _P, _P, _P, _P]),

@@ -288,6 +288,24 @@ def read_comsol(path: str | Path):
     return C, T, np.array(ents, dtype=np.int64)
 
 
+def read_comsol_native(path: str | Path):
+    """:func:`read_comsol` through libbiegpu's C reader (bie_read_comsol)."""
+    import ctypes as C
+
+    from . import _capi
+    L = _capi.lib()
+    nc, ne, ni = C.c_int64(), C.c_int64(), C.c_int64()
+    npe = C.c_int32()
+    p = str(path).encode()
+    _capi.check(L.bie_read_comsol(p, C.byref(nc), C.byref(ne), C.byref(npe), C.byref(ni), None, None, None))
+    coords = np.empty((3, nc.value), dtype=np.float64, order="F")
+    topo = np.empty((npe.value, ne.value), dtype=np.int64, order="F")
+    ents = np.empty(ni.value, dtype=np.int64)
+    _capi.check(L.bie_read_comsol(p, C.byref(nc), C.byref(ne), C.byref(npe), C.byref(ni), coords.ctypes.data,
+                                  topo.ctypes.data, ents.ctypes.data))
+    return np.ascontiguousarray(coords), np.ascontiguousarray(topo), ents
+
+
 def _remove_unused_nodes(topology: np.ndarray) -> np.ndarray:
     used = np.unique(topology)
     remap = np.zeros(int(used.max()) + 1, dtype=np.int64)
@@ -295,9 +313,13 @@ def _remove_unused_nodes(topology: np.ndarray) -> np.ndarray:
     return remap[topology]
 
 
-def load_comsol(path: str | Path, geometry_order: str = "quadratic", physics_order: str = "geometry") -> Mesh3d:
-    """load3dTriangularComsolMesh for physics 'geometry' or 'linear'."""
-    C0, T0, ents = read_comsol(path)
+def load_comsol(path: str | Path, geometry_order: str = "quadratic", physics_order: str = "geometry",
+                reader: str = "native") -> Mesh3d:
+    """load3dTriangularComsolMesh for physics 'geometry' or 'linear'; ``reader``
+    "native" parses the file with libbiegpu's C reader, "python" in Python."""
+    if reader not in ("native", "python"):
+        raise ValueError("reader must be 'native' or 'python'")
+    C0, T0, ents = read_comsol_native(path) if reader == "native" else read_comsol(path)
     if geometry_order == "linear":
         T0 = T0[:3, :]
     elif geometry_order != "quadratic":

@@ -657,6 +657,28 @@ int bie_assemble_device(bie_ctx *ctx, double k_re, double k_im, const double *d_
     });
 }
 
+// ---- mesh input ------------------------------------------------------------------
+int bie_read_comsol(const char *path, int64_t *n_coordinates, int64_t *n_elements, int32_t *nodes_per_element,
+                    int64_t *n_entities, double *coordinates, int64_t *topology, int64_t *entities) {
+    return guarded([&] {
+        if (!path || !n_coordinates || !n_elements || !nodes_per_element || !n_entities)
+            bie::fail(BIE_ERR_INVALID, "path and the size outputs must not be NULL");
+        std::vector<double> co;
+        std::vector<int64_t> to, en;
+        int npe = 0;
+        bie::read_comsol(path, co, to, npe, en);
+        *n_coordinates = (int64_t)co.size() / 3;
+        *nodes_per_element = npe;
+        *n_elements = (int64_t)to.size() / npe;
+        *n_entities = (int64_t)en.size();
+        if (!coordinates) return;
+        if (!topology) bie::fail(BIE_ERR_INVALID, "topology must not be NULL");
+        std::copy(co.begin(), co.end(), coordinates);
+        std::copy(to.begin(), to.end(), topology);
+        if (entities) std::copy(en.begin(), en.end(), entities);
+    });
+}
+
 // ---- visco-thermal system ----------------------------------------------------
 int bie_ambient_to_properties(double f, double ps, double t, double H, double out[10]) {
     return guarded([&] {

@@ -256,6 +256,10 @@ void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const
 // solve's statistics when the graph runs.
 constexpr int kGraphMaxRestart = 64;
 
+// COMSOL text mesh (bie_mesh_io.cpp): coords 3 x Nc, topo npe x E (1-based)
+void read_comsol(const std::string &path, std::vector<double> &coords, std::vector<int64_t> &topo, int &npe,
+                 std::vector<int64_t> &entities);
+
 // Visco-thermal system, host part (bie_lossy.cpp)
 void ambient_to_properties(double f, double ps, double t, double H, double out[10]);
 bie_lossy_constants visco_thermal_constants(double freq, double S, double pa, double t, double Hr);

@@ -501,6 +501,18 @@ BIE_API int bie_adjoint(bie_ctx *ctx, double k_re, double k_im, const double *Z,
  * bie_operator.A32 from an assembled matrix. */
 BIE_API int bie_round_c64_device(bie_ctx *ctx, const double *d_in, float *d_out, int64_t n);
 
+/* ---- mesh input ----------------------------------------------------------- */
+/* COMSOL text mesh, read_comsol_mesh(mesh_file) of src/3d/read_comsol.jl:9-54:
+ * the vertex coordinates (3 x Nc, column-major), the triangles (npe x E with
+ * npe = 3 or 6, 1-based, rows 5 and 6 of 6-node triangles swapped into the
+ * library's node order) and the geometric entity indices.  ".mphtxt" is
+ * appended to `path` when missing.  Call with coordinates == NULL to get the
+ * sizes, then again with coordinates[3 Nc], topology[npe E], entities[n_ent]
+ * (entities may be NULL).  Host only. */
+BIE_API int bie_read_comsol(const char *path, int64_t *n_coordinates, int64_t *n_elements,
+                            int32_t *nodes_per_element, int64_t *n_entities, double *coordinates,
+                            int64_t *topology, int64_t *entities);
+
 /* ---- visco-thermal ("lossy") system ------------------------------------ */
 /* Physical properties of air (Rasmussen 1997, annex A), as
  * ambient_to_properties(f, ps, t, H) of src/utils/ambient_to_properties.jl:1-134:

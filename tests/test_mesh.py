@@ -70,6 +70,62 @@ def test_comsol_reader(reference_meshes):
     assert C.shape == (3, 1682) and T.shape == (6, 840)
 
 
+def test_comsol_native_reader_matches_python(reference_meshes):
+    # the C reader (bie_read_comsol) and the Python reader agree on every
+    # triangle fixture the reference ships
+    n = 0
+    for f in sorted(reference_meshes.glob("*.mphtxt")):
+        Cp, Tp, Ep = bm.read_comsol(f)
+        if Tp.shape[0] not in (3, 6):
+            continue   # quadrilateral meshes
+        Cn, Tn, En = bm.read_comsol_native(f)
+        assert np.array_equal(Cn, Cp) and np.array_equal(Tn, Tp) and np.array_equal(En, Ep), f.name
+        n += 1
+    assert n >= 5
+    a = bm.load_comsol(reference_meshes / "sphere_1m", "quadratic", "geometry", reader="native")
+    b = bm.load_comsol(reference_meshes / "sphere_1m", "quadratic", "geometry", reader="python")
+    assert np.array_equal(a.topology, b.topology) and np.array_equal(a.sources, b.sources)
+
+
+MPHTXT = """# Created by hand
+0 1
+# Mesh vertex coordinates
+0 0 0
+1 0 0
+0 1 0
+0.5 0 0
+0.5 0.5 0
+0 0.5 0
+
+3 # number of vertices per element
+# Elements
+{elements}
+
+# Geometric entity indices
+{entities}
+
+"""
+
+
+def test_comsol_native_reader_small_files(tmp_path):
+    from biegpu import BIEError
+    p = tmp_path / "tri6.mphtxt"
+    p.write_text(MPHTXT.format(elements="0 1 2 3 4 5 ", entities="1"))
+    C, T, E = bm.read_comsol_native(tmp_path / "tri6")          # ".mphtxt" appended
+    assert C.shape == (3, 6) and T.tolist() == [[1], [2], [3], [4], [6], [5]] and E.tolist() == [1]
+    Cp, Tp, Ep = bm.read_comsol(p)
+    assert np.array_equal(C, Cp) and np.array_equal(T, Tp) and np.array_equal(E, Ep)
+    p.write_text(MPHTXT.format(elements="0 1 2\n3 4 5", entities="1\n2"))
+    C, T, E = bm.read_comsol_native(p)
+    assert T.tolist() == [[1, 4], [2, 5], [3, 6]] and E.tolist() == [1, 2]
+    for bad in ["0 1 2\n3 4", "0 1 9", "0 1 x", "0 1 2 3"]:
+        p.write_text(MPHTXT.format(elements=bad, entities="1"))
+        with pytest.raises(BIEError):
+            bm.read_comsol_native(p)
+    with pytest.raises(BIEError):
+        bm.read_comsol_native(tmp_path / "missing.mphtxt")
+
+
 def test_operator_algebra_on_dense_matrices():
     # the reference's compositions, on host matrices (no GPU involved)
     from biegpu.operators import Diagonal, I, _Affine
