@@ -223,16 +223,81 @@ int bie_assemble(bie_ctx *ctx, double k_re, double k_im, const double *targets, 
             BIE_CUDA(cudaMemcpyAsync(dt, targets, (size_t)M * 24, cudaMemcpyHostToDevice, c.stream));
             d_t = dt;
         }
-        const size_t mat = (size_t)M * (size_t)c.n_sources * 16;
-        bie::AssembleArgs a{k_re, k_im, d_t, M, flags, nullptr, nullptr, nullptr};
-        if (flags & BIE_F) a.F = static_cast<double *>(c.scratch(bie::kScratchF, mat));
-        if (flags & BIE_G) a.G = static_cast<double *>(c.scratch(bie::kScratchG, mat));
-        if (flags & BIE_C) a.C = static_cast<double *>(c.scratch(bie::kScratchC, (size_t)M * 16));
-        run_assemble(c, a, precision);
-        if (flags & BIE_F) BIE_CUDA(cudaMemcpyAsync(F, a.F, mat, cudaMemcpyDeviceToHost, c.stream));
-        if (flags & BIE_G) BIE_CUDA(cudaMemcpyAsync(G, a.G, mat, cudaMemcpyDeviceToHost, c.stream));
-        if (flags & BIE_C)
-            BIE_CUDA(cudaMemcpyAsync(C, a.C, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
+        const int64_t N = c.n_sources;
+        const size_t mat = (size_t)M * (size_t)N * 16;
+        const int nmat = ((flags & BIE_F) ? 1 : 0) + ((flags & BIE_G) ? 1 : 0);
+        // Outputs of 256 MB and more: row blocks assembled on the context stream
+        // while the previous block is copied to the host on a second stream, so
+        // the assembly hides behind the device-to-host transfer (which bounds
+        // this call).  Each block is its own assembly over targets [i0, i1); a
+        // block's rows are a strided 2D copy whose row segments are kept >= 45 KB
+        // (narrower segments slow the copy engines: measured 193 GB/s at 46 KB,
+        // 171 GB/s at 20 KB on GB300), so nb <= 8 and M >= 2 * 2880.
+        const int nb = (mat * nmat >= (size_t(256) << 20)) ? (int)std::min<int64_t>(8, M * 16 / 46080) : 1;
+        if (nb < 2) {
+            bie::AssembleArgs a{k_re, k_im, d_t, M, flags, nullptr, nullptr, nullptr};
+            if (flags & BIE_F) a.F = static_cast<double *>(c.scratch(bie::kScratchF, mat));
+            if (flags & BIE_G) a.G = static_cast<double *>(c.scratch(bie::kScratchG, mat));
+            if (flags & BIE_C) a.C = static_cast<double *>(c.scratch(bie::kScratchC, (size_t)M * 16));
+            run_assemble(c, a, precision);
+            if (flags & BIE_F) BIE_CUDA(cudaMemcpyAsync(F, a.F, mat, cudaMemcpyDeviceToHost, c.stream));
+            if (flags & BIE_G) BIE_CUDA(cudaMemcpyAsync(G, a.G, mat, cudaMemcpyDeviceToHost, c.stream));
+            if (flags & BIE_C)
+                BIE_CUDA(cudaMemcpyAsync(C, a.C, (size_t)M * 16, cudaMemcpyDeviceToHost, c.stream));
+            BIE_CUDA(cudaStreamSynchronize(c.stream));
+            return;
+        }
+        const int64_t mb = (M + nb - 1) / nb;   // rows per block
+        const size_t blk = (size_t)mb * (size_t)N * 16;
+        double *dF = (flags & BIE_F) ? static_cast<double *>(c.scratch(bie::kScratchF, 2 * blk)) : nullptr;
+        double *dG = (flags & BIE_G) ? static_cast<double *>(c.scratch(bie::kScratchG, 2 * blk)) : nullptr;
+        double *dC = (flags & BIE_C) ? static_cast<double *>(c.scratch(bie::kScratchC, 2 * (size_t)mb * 16)) : nullptr;
+        if (!c.copy_stream) BIE_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+        struct Events {
+            cudaStream_t s0, s1;
+            cudaEvent_t e[4] = {};
+            ~Events() {   // (also on an error: no copy into the caller's arrays outlives the call)
+                cudaStreamSynchronize(s1);
+                cudaStreamSynchronize(s0);
+                for (auto x : e)
+                    if (x) cudaEventDestroy(x);
+            }
+        } ev{c.stream, c.copy_stream};   // ready[2] (block assembled), copied[2] (slot free again)
+        for (auto &x : ev.e) BIE_CUDA(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+        const int nblocks = (int)((M + mb - 1) / mb);
+        auto compute = [&](int b) {
+            const int slot = b & 1;
+            const int64_t i0 = (int64_t)b * mb, m = std::min<int64_t>(mb, M - i0);
+            if (b >= 2) BIE_CUDA(cudaStreamWaitEvent(c.stream, ev.e[2 + slot], 0));
+            bie::AssembleArgs a{k_re, k_im, d_t + 3 * i0, m, flags,
+                                dF ? dF + slot * (blk / 8) : nullptr, dG ? dG + slot * (blk / 8) : nullptr,
+                                dC ? dC + slot * 2 * mb : nullptr};
+            run_assemble(c, a, precision);
+            BIE_CUDA(cudaEventRecord(ev.e[slot], c.stream));
+        };
+        auto copy = [&](int b) {
+            const int slot = b & 1;
+            const int64_t i0 = (int64_t)b * mb, m = std::min<int64_t>(mb, M - i0);
+            cudaStream_t s = c.copy_stream;
+            BIE_CUDA(cudaStreamWaitEvent(s, ev.e[slot], 0));
+            if (dF)
+                BIE_CUDA(cudaMemcpy2DAsync(F + 2 * i0, (size_t)M * 16, dF + slot * (blk / 8), (size_t)m * 16,
+                                           (size_t)m * 16, (size_t)N, cudaMemcpyDeviceToHost, s));
+            if (dG)
+                BIE_CUDA(cudaMemcpy2DAsync(G + 2 * i0, (size_t)M * 16, dG + slot * (blk / 8), (size_t)m * 16,
+                                           (size_t)m * 16, (size_t)N, cudaMemcpyDeviceToHost, s));
+            if (dC)
+                BIE_CUDA(cudaMemcpyAsync(C + 2 * i0, dC + slot * 2 * mb, (size_t)m * 16, cudaMemcpyDeviceToHost, s));
+            BIE_CUDA(cudaEventRecord(ev.e[2 + slot], s));
+        };
+        // the next block is enqueued before this block's copy, so that the
+        // assembly overlaps the copy even when a pageable host copy blocks
+        compute(0);
+        for (int b = 0; b < nblocks; ++b) {
+            if (b + 1 < nblocks) compute(b + 1);
+            copy(b);
+        }
+        BIE_CUDA(cudaStreamSynchronize(c.copy_stream));
         BIE_CUDA(cudaStreamSynchronize(c.stream));
     });
 }

@@ -137,6 +137,8 @@ struct Ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool owns_stream = true;             // false: the stream belongs to another context
+    cudaStream_t copy_stream = nullptr;  // device-to-host copies overlapped with the assembly
+                                         // (bie_assemble with host buffers), made on first use
     int num_sms = 0;
 
     // mesh (host copies, 0-based)

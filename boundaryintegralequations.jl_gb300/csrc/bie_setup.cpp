@@ -586,6 +586,11 @@ void destroy_context(Ctx &c) {
     c.ev_tensor.clear();
     c.ev_free.clear();
     c.d_qpe = nullptr;
+    if (c.copy_stream) {
+        cudaStreamSynchronize(c.copy_stream);
+        cudaStreamDestroy(c.copy_stream);
+        c.copy_stream = nullptr;
+    }
     if (c.stream && c.owns_stream) cudaStreamDestroy(c.stream);
     c.d_records = nullptr;
     c.d_phi = nullptr;
