@@ -17,5 +17,6 @@ from .adjoint import farfield_objective  # noqa: F401
 from .rosebem import apply_taylor_expansion, taylor_assemble  # noqa: F401
 from .lossy import (LossyGlobalOuter, ambient_to_properties, tangential_derivatives,  # noqa: F401
                     visco_thermal_constants)
+from .distributed import sharded_sweep  # noqa: F401
 
 __version__ = "0.1.0"
