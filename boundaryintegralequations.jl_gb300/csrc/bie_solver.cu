@@ -712,7 +712,9 @@ struct Solver {
     Solver(Ctx &ctx, int64_t n_, int restart, int level = 0)
         : c(ctx), n(n_), m(restart), stream(ctx.stream) {
         const int part_slot = level == 0 ? kScratchSolverPart : kScratchSolverNested + 2 * (level - 1) + 1;
-        nbdot = (int)std::min<int64_t>(std::max<int64_t>(1, (n + kT * 8 - 1) / (kT * 8)), 256);
+        // dot-product blocks per column; vectors up to 4096 entries take one
+        // block per column, which writes its result directly (no second launch)
+        nbdot = n <= 4096 ? 1 : (int)std::min<int64_t>(std::max<int64_t>(1, (n + kT * 8 - 1) / (kT * 8)), 256);
         const size_t part_bytes = (size_t)std::max<int64_t>(kMaxSlices * n, (int64_t)(restart + 2) * nbdot) * 16;
         const size_t hbytes = (size_t)(restart + 2) * 16;
         const size_t nc = (size_t)(restart + 1) * restart + 4 * (size_t)(restart + 1) + restart;
@@ -812,9 +814,10 @@ struct Solver {
     // out[0..ncol) = V[:, 0..ncol)^H w on the device (no host copy)
     void multidot_dev(const double2 *V, int64_t ldv, int ncol, const double2 *w, double2 *out) {
         dim3 grid((unsigned)nbdot, (unsigned)ncol);
-        multidot_kernel<<<grid, kT, 0, stream>>>(V, ldv, w, n, part, stop);
+        multidot_kernel<<<grid, kT, 0, stream>>>(V, ldv, w, n, nbdot == 1 ? out : part, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
+        if (nbdot == 1) return;   // partial[col] is the sum already
         sum_partials_kernel<<<blocks(ncol, 64), 64, 0, stream>>>(part, nbdot, ncol, out, stop);
         BIE_CUDA(cudaGetLastError());
         launched();
