@@ -24,9 +24,10 @@ def sweep(meshes, ks, ws, precision: str = "mixed", refine: bool = True, n: int 
     ``ks``: wavenumbers (real or complex), ``ws``: per-mesh boundary data
     (length N_m complex).  ``precision="mixed"`` with ``refine=True`` is the
     fast path (mixed assembly, complex64 inner GMRES, complex128 residual);
-    ``precision="fp64", refine=False`` is the plain FP64 path.  By default the
-    wavenumbers after the first of each mesh solve by replaying one recorded
-    CUDA graph of the GMRES solve; ``eager=True`` drives GMRES from the host.
+    ``precision="fp64", refine=False`` is the plain FP64 path.  By default
+    everything after each mesh's first wavenumber is one launch of a recorded
+    CUDA graph (device-side loops over wavenumbers and GMRES iterations);
+    ``eager=True`` launches kernel by kernel from the host.
     """
     ctxs = [get_context(mesh, n=n, m=m, device=device) for mesh in meshes]
     ks = np.asarray(ks, dtype=np.complex128)

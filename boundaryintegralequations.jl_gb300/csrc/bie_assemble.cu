@@ -41,7 +41,11 @@ assemble_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off,
                      int flags, double2 *__restrict__ F, double2 *__restrict__ G,
                      double *__restrict__ Cpart, int chunk,
                      unsigned long long *__restrict__ qpe_count,
-                     const double2 *__restrict__ gweight, int tm) {
+                     const double2 *__restrict__ gweight, int tm, const double *__restrict__ kdev) {
+    if (kdev) {   // wavenumber read from device memory (recorded sweeps)
+        kre = kdev[0];
+        kim = kdev[1];
+    }
     extern __shared__ __align__(16) double smem[];
     double *s_phi = smem;                                   // nphi doubles (padded even)
     double *s_rec = smem + ((nphi + 1) & ~1);               // chunk * stride doubles
@@ -154,7 +158,7 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int
         c.d_shared_mask + (size_t)level * c.n_elements, c.d_phi, L.R * L.qmax * L.NP, L.qmax,
         ri, a.targets, a.M, a.k_re, a.k_im, a.flags, reinterpret_cast<double2 *>(a.F),
         reinterpret_cast<double2 *>(a.G), Cpart, chunk, c.d_qpe,
-        reinterpret_cast<const double2 *>(a.g_weight), a.taylor_m);
+        reinterpret_cast<const double2 *>(a.g_weight), a.taylor_m, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;

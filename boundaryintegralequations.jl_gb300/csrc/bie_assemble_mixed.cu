@@ -126,7 +126,11 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                       float2 *__restrict__ F32, float2 *__restrict__ G32,
                       double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
                       unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
-                      unsigned long long *__restrict__ qpe_count) {
+                      unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
+    if (kdev) {   // wavenumber read from device memory (recorded sweeps)
+        kre = kdev[0];
+        kim = kdev[1];
+    }
     constexpr int NPP = PhiPad<NP>::value;
     extern __shared__ __align__(16) float smemf[];
     float *s_phi = smemf;                                   // nphi floats (padded to 4)
@@ -243,7 +247,11 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
                     unsigned int defer_cap, Fp64View v, const double *__restrict__ tgt, int64_t M,
                     double kre, double kim, int flags, T2 *__restrict__ F,
                     T2 *__restrict__ G, double *__restrict__ Cnear,
-                    unsigned long long *__restrict__ qpe_count) {
+                    unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
+    if (kdev) {
+        kre = kdev[0];
+        kim = kdev[1];
+    }
     const unsigned int n = min(*defer_count, defer_cap);
     const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
     unsigned long long nqpe = 0;
@@ -293,7 +301,7 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
     kern<<<grid, kThreads, smem, c.stream>>>(
         c.d_mrecords, X.stride, X.nidx_off, c.n_elements, S, c.d_mphi,
         L.R * L.qmax * PhiPad<NP>::value, L.qmax, ri, a.targets, a.M, a.k_re, a.k_im, a.flags,
-        F32, G32, Cpart, chunk, defer, dcount, dcap, v, c.d_qpe);
+        F32, G32, Cpart, chunk, defer, dcount, dcap, v, c.d_qpe, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;
@@ -305,7 +313,7 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
     const unsigned wgrid = (unsigned)std::min<int64_t>((n2 + 255) / 256, 8LL * c.num_sms * 8);
     if (a.c64_out) {   // complex64 matrices requested: add the FP64 corrections in place
         correct_fp64_kernel<NP, CPLX, float2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
-            defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags, F32, G32, Cnear, c.d_qpe);
+            defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags, F32, G32, Cnear, c.d_qpe, a.k_dev);
         BIE_CUDA(cudaGetLastError());
         ++c.kernel_launches;
         return;
@@ -326,7 +334,7 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
     }
     correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
         defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
-        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe);
+        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     ++c.kernel_launches;
 }

@@ -226,6 +226,9 @@ struct AssembleArgs {
                                         // (Morton record order), e.g. an element admittance
     int taylor_m = -1;                  // FP64 only: >= 0 assembles the taylor_m-th
                                         // k-derivative (corner rules only)
+    const double *k_dev = nullptr;      // device (re, im): the kernels read k here instead
+                                        // of k_re, k_im (which then only select the real-
+                                        // or complex-k code path: k_im != 0)
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
@@ -257,6 +260,36 @@ void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const
 // idle streams for the nested body captures.  *d_info (device) receives the
 // solve's statistics when the graph runs.
 constexpr int kGraphMaxRestart = 64;
+// Stream-capture helpers for conditional graph nodes (bie_solver.cu): a handle
+// of the graph being captured on `s`; a conditional node appended after the
+// capture's current dependencies, its body graphs returned.
+cudaGraphConditionalHandle graph_new_handle(cudaStream_t s);
+void graph_add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                           unsigned size, cudaGraph_t *bodies);
+// Records onto stream `s` into the body graph `g` until end() (or destruction,
+// which ends an unfinished capture after an error).
+struct BodyCapture {
+    cudaStream_t s;
+    bool on = false;
+    BodyCapture(cudaStream_t s_, cudaGraph_t g) : s(s_) {
+        cuda_check(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+                   "cudaStreamBeginCaptureToGraph");
+        on = true;
+    }
+    void end() {
+        on = false;
+        cudaGraph_t out = nullptr;
+        cuda_check(cudaStreamEndCapture(s, &out), "cudaStreamEndCapture");
+    }
+    ~BodyCapture() {
+        if (on) {
+            cudaGraph_t out = nullptr;
+            cudaStreamEndCapture(s, &out);
+        }
+    }
+    BodyCapture(const BodyCapture &) = delete;
+    BodyCapture &operator=(const BodyCapture &) = delete;
+};
 
 // COMSOL text mesh (bie_mesh_io.cpp): coords 3 x Nc, topo npe x E (1-based)
 void read_comsol(const std::string &path, std::vector<double> &coords, std::vector<int64_t> &topo, int &npe,

@@ -962,8 +962,10 @@ int gmres_core(Solver &S, const bie_operator &op, int prec, const double2 *b, do
     return it;
 }
 
+}  // namespace
+
 // A conditional handle of the graph being captured on `s`.
-cudaGraphConditionalHandle new_handle(cudaStream_t s) {
+cudaGraphConditionalHandle graph_new_handle(cudaStream_t s) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
     BIE_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
@@ -975,8 +977,8 @@ cudaGraphConditionalHandle new_handle(cudaStream_t s) {
 
 // Appends a conditional node after the capture's current dependencies; its body
 // graphs are returned for capture on other streams.
-void add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
-                     unsigned size, cudaGraph_t *bodies) {
+void graph_add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                           unsigned size, cudaGraph_t *bodies) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t *deps = nullptr;
@@ -993,32 +995,6 @@ void add_conditional(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraphCond
     BIE_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
     for (unsigned i = 0; i < size; ++i) bodies[i] = p.conditional.phGraph_out[i];
 }
-
-// Records onto stream `s` into the body graph `g` until end() (or destruction,
-// which ends an unfinished capture after an error).
-struct BodyCapture {
-    cudaStream_t s;
-    bool on = false;
-    BodyCapture(cudaStream_t s_, cudaGraph_t g) : s(s_) {
-        BIE_CUDA(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-        on = true;
-    }
-    void end() {
-        on = false;
-        cudaGraph_t out = nullptr;
-        BIE_CUDA(cudaStreamEndCapture(s, &out));
-    }
-    ~BodyCapture() {
-        if (on) {
-            cudaGraph_t out = nullptr;
-            cudaStreamEndCapture(s, &out);
-        }
-    }
-    BodyCapture(const BodyCapture &) = delete;
-    BodyCapture &operator=(const BodyCapture &) = delete;
-};
-
-}  // namespace
 
 void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_, const bie_gmres_opts &o,
                    bie_gmres_info *d_info, const cudaStream_t *body) {
@@ -1049,12 +1025,12 @@ void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_,
 
     BIE_CUDA(cudaMemsetAsync(x, 0, (size_t)n * 16, s0));
     S.multidot_dev(b, n, 1, b, &st.s->nrm2);
-    const cudaGraphConditionalHandle h_outer = new_handle(s0);
+    const cudaGraphConditionalHandle h_outer = graph_new_handle(s0);
     rf_start_kernel<<<1, 1, 0, s0>>>(st, rf, reltol, abstol, h_outer);
     BIE_CUDA(cudaGetLastError());
     S.launched();
     cudaGraph_t g_outer;
-    add_conditional(s0, h_outer, cudaGraphCondTypeWhile, 1, &g_outer);
+    graph_add_conditional(s0, h_outer, cudaGraphCondTypeWhile, 1, &g_outer);
     {
         // outer pass: refinement residual rr = b - A x (exact product), then the
         // inner restarted GMRES on A dx = rr
@@ -1072,13 +1048,13 @@ void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_,
         }
         const double2 *rhs = refine ? rr : b;
         double2 *sol = refine ? dx : x;
-        const cudaGraphConditionalHandle h_cycle = new_handle(S.stream);
+        const cudaGraphConditionalHandle h_cycle = graph_new_handle(S.stream);
         rf_check_kernel<<<1, 1, 0, S.stream>>>(st, rf, refine ? 1 : 0, maxiter, max_outer, inner_rel, h_outer,
                                                 h_cycle);
         BIE_CUDA(cudaGetLastError());
         S.launched();
         cudaGraph_t g_cycle;
-        add_conditional(S.stream, h_cycle, cudaGraphCondTypeWhile, 1, &g_cycle);
+        graph_add_conditional(S.stream, h_cycle, cudaGraphCondTypeWhile, 1, &g_cycle);
         {
             // restart cycle: w = rhs - A sol (rhs itself on the first cycle), beta,
             // then up to `restart` Arnoldi steps
@@ -1091,21 +1067,21 @@ void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_,
             BIE_CUDA(cudaGetLastError());
             S.launched();
             S.multidot_dev(w, n, 1, w, &st.s->nrm2);
-            const cudaGraphConditionalHandle h_step = new_handle(S.stream);
-            const cudaGraphConditionalHandle h_sel = new_handle(S.stream);
+            const cudaGraphConditionalHandle h_step = graph_new_handle(S.stream);
+            const cudaGraphConditionalHandle h_sel = graph_new_handle(S.stream);
             gm_cycle_init_kernel<<<1, 1, 0, S.stream>>>(st, rf, maxiter, restart, h_step, h_sel);
             BIE_CUDA(cudaGetLastError());
             S.launched();
             S.scale_dev(w, &st.s->inv_beta, V);
             cudaGraph_t g_step;
-            add_conditional(S.stream, h_step, cudaGraphCondTypeWhile, 1, &g_step);
+            graph_add_conditional(S.stream, h_step, cudaGraphCondTypeWhile, 1, &g_step);
             {
                 // one Arnoldi step per pass: a switch over the step index j runs
                 // the body recorded for that j (CGS2 over j + 1 basis vectors)
                 BodyCapture bc3(body[2], g_step);
                 S.stream = body[2];
                 std::vector<cudaGraph_t> branch(restart);
-                add_conditional(S.stream, h_sel, cudaGraphCondTypeSwitch, (unsigned)restart, branch.data());
+                graph_add_conditional(S.stream, h_sel, cudaGraphCondTypeSwitch, (unsigned)restart, branch.data());
                 gm_step_guard_kernel<<<1, 1, 0, S.stream>>>(st, rf, restart, h_step, h_sel);
                 BIE_CUDA(cudaGetLastError());
                 S.launched();

@@ -427,10 +427,10 @@ typedef struct bie_sweep_opts {
     int32_t precision;         /* assembly arithmetic: BIE_PREC_MIXED | BIE_PREC_FP64   */
     int32_t refine;            /* mixed: complex64 inner GMRES + complex128 residual     */
     bie_gmres_opts gmres;      /* restart, maxiter, reltol, abstol (zeros: defaults)     */
-    int32_t eager;             /* 0 (default): after the first wavenumber of a mesh, its
-                                  GMRES solve is recorded as one CUDA graph and replayed
-                                  for the other wavenumbers; 1: host-driven GMRES for
-                                  every wavenumber                                       */
+    int32_t eager;             /* 0 (default): after the first wavenumber of each mesh,
+                                  the rest of the sweep is one launch of a recorded CUDA
+                                  graph (every mesh's matrices resident at once);
+                                  1: launch by launch, one mesh's matrices at a time     */
 } bie_sweep_opts;
 
 typedef struct bie_sweep_info {
@@ -440,7 +440,7 @@ typedef struct bie_sweep_info {
     double  assemble_ms;       /* device time of the assemblies (CUDA events)            */
     double  solve_ms;          /* device time of right-hand sides + GMRES                */
     double  record_ms;         /* host time spent recording + instantiating graphs       */
-    int64_t graph_launches;    /* CUDA graph launches (nk - 1 per mesh unless eager)     */
+    int64_t graph_launches;    /* CUDA graph launches (1 per sweep unless eager)         */
 } bie_sweep_info;
 
 /*
@@ -456,11 +456,12 @@ typedef struct bie_sweep_info {
  * iters (optional): nmesh x nk GMRES iteration counts.
  * Unless opts->eager is set, the first wavenumber of each mesh runs launch by
  * launch (it sizes the device scratch and, through the autotuner, picks the
- * assembly's slicing); then the mesh's GMRES solve is recorded once as a CUDA
- * graph whose loops are conditional nodes driven by device state (restart <=
- * 64) and each later wavenumber is its assembly plus one launch of that graph,
- * all enqueued without a host round trip.  Both forms give the same results
- * up to the rounding order of the assemblies' atomic sums.
+ * assembly's slicing); then everything else is ONE launch of a recorded CUDA
+ * graph: per mesh a loop over the wavenumbers (k read from device memory)
+ * whose GMRES refinement, restart and Arnoldi loops are nested conditional
+ * nodes driven by device state (restart <= 64; contexts on one device).  Both
+ * forms give the same results up to the rounding order of the assemblies'
+ * atomic sums.
  */
 BIE_API int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk,
                       const double *const *w, double *const *p, const bie_sweep_opts *opts,
