@@ -589,6 +589,7 @@ typedef struct bie_lossy bie_lossy;
  * inner operator), each as the reference's gmres call with opts->solve.
  */
 BIE_API int bie_lossy_create(bie_ctx *ctx, double freq, const bie_lossy_opts *opts, bie_lossy **out);
+/* Frees the system's device memory; call it before bie_ctx_destroy of its context. */
 BIE_API int bie_lossy_destroy(bie_lossy *L);
 BIE_API int bie_lossy_constants_of(const bie_lossy *L, bie_lossy_constants *out);
 /* y = block x (device vectors, complex interleaved); blocking */
