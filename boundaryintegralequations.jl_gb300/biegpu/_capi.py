@@ -73,6 +73,15 @@ class MeshDesc(C.Structure):
     ]
 
 
+class RuleTable(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_int64),
+        ("u", C.POINTER(C.c_double)),
+        ("v", C.POINTER(C.c_double)),
+        ("w", C.POINTER(C.c_double)),
+    ]
+
+
 class Peaks(C.Structure):
     _fields_ = [("fp64_flops", C.c_double), ("fp32_flops", C.c_double)]
 
@@ -197,6 +206,7 @@ SIGNATURES = {
     "bie_last_error": (C.c_char_p, []),
     "bie_quadrature_rule": (_I, [_I, _I, _I, _P, _P, _P, _I, C.POINTER(_I)]),
     "bie_ctx_create": (_I, [C.POINTER(_P), C.POINTER(MeshDesc), _I]),
+    "bie_ctx_create_rules": (_I, [C.POINTER(_P), C.POINTER(MeshDesc), C.POINTER(RuleTable), _I, _I]),
     "bie_ctx_destroy": (_I, [_P]),
     "bie_ctx_stream": (_I, [_P, C.POINTER(_P)]),
     "bie_measure_peaks": (_I, [_I, C.POINTER(Peaks)]),

@@ -31,9 +31,16 @@ def quadrature_rule(n: int, m: int, node: int):
 
 
 class Context:
-    """A libbiegpu context: one mesh, one quadrature order (n, m), one device."""
+    """A libbiegpu context: one mesh, one quadrature order (n, m), one device.
 
-    def __init__(self, mesh: Mesh3d, n: int = 4, m: int = 4, device: int = 0):
+    ``rules``, when given, replaces the rules built from (n, m): a sequence of
+    (u, v, w) arrays, one per element node that can be the nearest to a
+    collocation point (3 for linear geometry, 3 or 6 physics nodes for
+    quadratic geometry), e.g. the ``gauss_u``, ``gauss_v``, ``weights`` of the
+    shape functions ``create_rotated_element`` returns
+    (src/3d/assembly_collocation.jl:122-136) - bie_ctx_create_rules."""
+
+    def __init__(self, mesh: Mesh3d, n: int = 4, m: int = 4, device: int = 0, rules=None):
         L = _capi.lib()
         self.mesh = mesh
         self.n, self.m, self.device = int(n), int(m), int(device)
@@ -56,7 +63,19 @@ class Context:
             quad_m=self.m,
         )
         h = C.c_void_p()
-        _capi.check(L.bie_ctx_create(C.byref(h), C.byref(desc), self.device))
+        if rules is None:
+            _capi.check(L.bie_ctx_create(C.byref(h), C.byref(desc), self.device))
+        else:
+            self.n = self.m = 0
+            keep = [tuple(np.ascontiguousarray(a, dtype=np.float64) for a in r) for r in rules]
+            if any(len({a.shape for a in r}) != 1 or r[0].ndim != 1 for r in keep):
+                raise ValueError("every rule is three 1-D arrays (u, v, w) of one length")
+            tabs = (_capi.RuleTable * len(keep))(*[
+                _capi.RuleTable(n_points=r[0].size,
+                                u=r[0].ctypes.data_as(C.POINTER(C.c_double)),
+                                v=r[1].ctypes.data_as(C.POINTER(C.c_double)),
+                                w=r[2].ctypes.data_as(C.POINTER(C.c_double))) for r in keep])
+            _capi.check(L.bie_ctx_create_rules(C.byref(h), C.byref(desc), tabs, len(keep), self.device))
         self._h = h
         self._finalizer = weakref.finalize(self, L.bie_ctx_destroy, h)
 

@@ -136,6 +136,36 @@ int bie_ctx_create(bie_ctx **out, const bie_mesh_desc *desc, int device) {
     });
 }
 
+int bie_ctx_create_rules(bie_ctx **out, const bie_mesh_desc *desc, const bie_rule_table *rules, int n_rules,
+                         int device) {
+    return guarded([&] {
+        if (!out || !desc || !rules) bie::fail(BIE_ERR_INVALID, "out, desc and rules must not be NULL");
+        *out = nullptr;
+        if (n_rules < 1 || n_rules > 6) bie::fail(BIE_ERR_INVALID, "n_rules must be in 1..6");
+        std::vector<bie::Rule> tables((size_t)n_rules);
+        for (int r = 0; r < n_rules; ++r) {
+            const bie_rule_table &t = rules[r];
+            if (t.n_points < 1 || t.n_points > bie::kMaxQ)
+                bie::fail(BIE_ERR_INVALID, "rule table " + std::to_string(r) + " must hold 1.." +
+                                               std::to_string(bie::kMaxQ) + " points");
+            if (!t.u || !t.v || !t.w)
+                bie::fail(BIE_ERR_INVALID, "rule table " + std::to_string(r) + " has a NULL array");
+            tables[r].u.assign(t.u, t.u + t.n_points);
+            tables[r].v.assign(t.v, t.v + t.n_points);
+            tables[r].w.assign(t.w, t.w + t.n_points);
+        }
+        auto *c = new bie::Ctx();
+        try {
+            bie::build_context(*c, *desc, device, 0, &tables);
+        } catch (...) {
+            bie::destroy_context(*c);
+            delete c;
+            throw;
+        }
+        *out = reinterpret_cast<bie_ctx *>(c);
+    });
+}
+
 int bie_ctx_destroy(bie_ctx *ctx) {
     return guarded([&] {
         if (!ctx) return;

@@ -210,8 +210,10 @@ struct Ctx {
 
 // Host set-up (bie_setup.cpp)
 // gauss_rule > 0 replaces the clustered Duffy rules by the symmetric Gauss
-// rule of that many points (fast-operator far field).
-void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule = 0);
+// rule of that many points (fast-operator far field); explicit_rules != NULL
+// replaces them by the caller's tables (one per nearest element node).
+void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule = 0,
+                   const std::vector<Rule> *explicit_rules = nullptr);
 void destroy_context(Ctx &c);
 
 // Kernel launchers (bie_assemble.cu)

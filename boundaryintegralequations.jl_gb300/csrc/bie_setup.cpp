@@ -346,7 +346,8 @@ void Ctx::collect_timers() {
     ev_tensor.clear();
 }
 
-void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule) {
+void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
+                   const std::vector<Rule> *explicit_rules) {
     // ---- validation -------------------------------------------------------
     if (d.n_coordinates <= 0 || d.n_elements <= 0 || d.n_sources <= 0)
         fail(BIE_ERR_INVALID, "mesh sizes must be positive");
@@ -358,16 +359,37 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule) {
     const int NP = n_nodes_of_kind(d.physics_kind);
     if (d.shape_kind == BIE_TRI_LINEAR && d.physics_kind == BIE_TRI_QUADRATIC)
         fail(BIE_ERR_UNSUPPORTED, "quadratic physics on linear geometry is not supported");
-    if (d.quad_n < 1 || d.quad_m < 1 || d.quad_n > 32 || d.quad_m > 32)
+    const bool own_rules = gauss_rule <= 0 && !explicit_rules;
+    if (own_rules && (d.quad_n < 1 || d.quad_m < 1 || d.quad_n > 32 || d.quad_m > 32))
         fail(BIE_ERR_INVALID, "quad_n and quad_m must be in 1..32");
+    const int R = (d.shape_kind == BIE_TRI_LINEAR) ? 3 : NP;
+    if (explicit_rules) {
+        if ((int)explicit_rules->size() != R)
+            fail(BIE_ERR_INVALID, "expected " + std::to_string(R) + " rule tables for this element kind, got " +
+                                      std::to_string(explicit_rules->size()));
+        for (int r = 0; r < R; ++r) {
+            const Rule &t = (*explicit_rules)[r];
+            if (t.size() < 1 || t.size() > kMaxQ || (int)t.u.size() != t.size() || (int)t.v.size() != t.size())
+                fail(BIE_ERR_INVALID, "rule table " + std::to_string(r) + " must hold 1.." +
+                                          std::to_string(kMaxQ) + " points");
+            for (int q = 0; q < t.size(); ++q) {
+                const double u = t.u[q], v = t.v[q], w = t.w[q];
+                if (!std::isfinite(u) || !std::isfinite(v) || !std::isfinite(w))
+                    fail(BIE_ERR_INVALID, "non-finite value in rule table " + std::to_string(r));
+                if (u < 0.0 || v < 0.0 || u + v > 1.0 + 1e-12)
+                    fail(BIE_ERR_INVALID, "rule table " + std::to_string(r) + " point " + std::to_string(q) +
+                                              " lies outside the reference triangle");
+            }
+        }
+    }
     c.shape_kind = d.shape_kind;
     c.physics_kind = d.physics_kind;
     c.n_coords = d.n_coordinates;
     c.n_elements = d.n_elements;
     c.n_sources = d.n_sources;
     c.NS = NS;
-    c.quad_n = d.quad_n;
-    c.quad_m = d.quad_m;
+    c.quad_n = own_rules ? d.quad_n : 0;   // 0: the rules did not come from (n, m)
+    c.quad_m = own_rules ? d.quad_m : 0;
     const int64_t E = d.n_elements;
 
     c.coords.assign(d.coordinates, d.coordinates + 3 * d.n_coordinates);
@@ -397,10 +419,10 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule) {
     // gauss_rule > 0: every rule is the symmetric gauss_rule-point triangle rule
     // (the far-field rule of the fast operators, setup_fast_operator,
     // src/3d/fast_multipole_method.jl:163-170), whatever the nearest node.
-    const int R = (d.shape_kind == BIE_TRI_LINEAR) ? 3 : NP;
     c.rules.clear();
     for (int r = 0; r < R; ++r) {
-        if (gauss_rule > 0) c.rules.push_back(triangle_gauss_rule(gauss_rule));
+        if (explicit_rules) c.rules.push_back((*explicit_rules)[r]);
+        else if (gauss_rule > 0) c.rules.push_back(triangle_gauss_rule(gauss_rule));
         else
             c.rules.push_back(r < 3 ? duffy_corner_rule(d.quad_n, d.quad_m, r + 1)
                                     : duffy_midpoint_rule(d.quad_n, d.quad_m, r + 1));

@@ -64,16 +64,29 @@ element_kind(n_nodes::Integer) = n_nodes == 3 ? BIE_TRI_LINEAR :
                                  n_nodes == 6 ? BIE_TRI_QUADRATIC :
                                  throw(ArgumentError("only 3- and 6-node triangles are supported"))
 
+# bie_rule_table (include/biegpu.h)
+struct RuleTable
+    n_points::Int64
+    u::Ptr{Float64}
+    v::Ptr{Float64}
+    w::Ptr{Float64}
+end
+
 """
-    Context(mesh; n=4, m=4, device=0)
+    Context(mesh; n=4, m=4, device=0, rules=nothing)
 
 Uploads the mesh (coordinates, topology, sources, physics topology) and builds
 the clustered quadrature rules on the device.  One context per (mesh, n, m).
+`rules`, when given, is a vector of `(u, v, w)` tuples, one per element node
+that can be the nearest to a collocation point (3 for linear geometry, the
+physics nodes per element for quadratic geometry); they replace the rules
+built from (n, m) (`bie_ctx_create_rules`).  `reference_rules` collects them
+from the shape functions of the reference's own `create_rotated_element`.
 """
 mutable struct Context
     handle::Ptr{Cvoid}
     n_sources::Int
-    function Context(mesh; n=4, m=4, device=0)
+    function Context(mesh; n=4, m=4, device=0, rules=nothing)
         coords = Matrix{Float64}(mesh.coordinates)
         topo = Matrix{Int64}(mesh.topology)
         ptopo = Matrix{Int64}(mesh.physics_topology)
@@ -84,12 +97,45 @@ mutable struct Context
                                 element_kind(size(topo, 1)), element_kind(size(ptopo, 1)),
                                 pointer(topo), pointer(ptopo), size(src, 2), pointer(src),
                                 Int32(n), Int32(m)))
-            check(ccall((:bie_ctx_create, libbiegpu), Cint,
-                        (Ref{Ptr{Cvoid}}, Ref{MeshDesc}, Cint), h, desc, device))
+            if rules === nothing
+                check(ccall((:bie_ctx_create, libbiegpu), Cint,
+                            (Ref{Ptr{Cvoid}}, Ref{MeshDesc}, Cint), h, desc, device))
+            else
+                keep = [(Vector{Float64}(u), Vector{Float64}(v), Vector{Float64}(w)) for (u, v, w) in rules]
+                GC.@preserve keep begin
+                    tabs = [RuleTable(length(t[3]), pointer(t[1]), pointer(t[2]), pointer(t[3])) for t in keep]
+                    check(ccall((:bie_ctx_create_rules, libbiegpu), Cint,
+                                (Ref{Ptr{Cvoid}}, Ref{MeshDesc}, Ptr{RuleTable}, Cint, Cint),
+                                h, desc, tabs, length(tabs), device))
+                end
+            end
         end
         ctx = new(h[], size(src, 2))
         finalizer(c -> ccall((:bie_ctx_destroy, libbiegpu), Cint, (Ptr{Cvoid},), c.handle), ctx)
         return ctx
+    end
+end
+
+"""
+    reference_rules(create_rotated_element, rotated_midpoint_triangular_quadpoints,
+                    shape_function, n, m, n_rules)
+
+The reference's own clustered rules as `(u, v, w)` tuples for
+`Context(mesh; rules=...)`: `create_rotated_element(shape_function, n, m, node)`
+for the corners (src/3d/assembly_collocation.jl:122-136, 287-289, 372-374) and
+`rotated_midpoint_triangular_quadpoints(n, m, node)` for the edge midpoints
+4-6 of quadratic elements (:385-387).  Pass the reference's functions.
+"""
+function reference_rules(create_rotated_element, rotated_midpoint_triangular_quadpoints,
+                         shape_function, n, m, n_rules)
+    map(1:n_rules) do r
+        if r <= 3
+            e = create_rotated_element(shape_function, n, m, r)
+            (copy(e.gauss_u), copy(e.gauss_v), copy(e.weights))
+        else
+            x, y, w = rotated_midpoint_triangular_quadpoints(n, m, r)
+            (Vector{Float64}(x), Vector{Float64}(y), Vector{Float64}(w))
+        end
     end
 end
 
@@ -560,7 +606,7 @@ gmres_gpu(L::GPULossyGlobalOuter, b; kwargs...) = gmres_gpu(GPULossyBlock(L, Cin
 
 version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
-export Context, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
+export Context, reference_rules, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
        sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective, FastFOperator, FastGOperator,
        taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu
 

@@ -122,6 +122,30 @@ BIE_API int bie_quadrature_rule(int n, int m, int node, double *u, double *v, do
  */
 BIE_API int bie_ctx_create(bie_ctx **out, const bie_mesh_desc *desc, int device);
 
+/* One clustered quadrature rule on the reference triangle: `n_points` points
+ * (u, v) with weights w (a full-triangle rule has weights summing to 1/2). */
+typedef struct bie_rule_table {
+    int64_t       n_points;           /* 1..64                                  */
+    const double *u;                  /* n_points                               */
+    const double *v;                  /* n_points                               */
+    const double *w;                  /* n_points                               */
+} bie_rule_table;
+
+/*
+ * bie_ctx_create with the caller's own rule tables instead of the rules built
+ * from (quad_n, quad_m), which are then ignored: `rules[r]` is the rule used
+ * when element node r+1 is the nearest physics node to the collocation point
+ * (n_rules = 3 for linear geometry, = the physics nodes per element, 3 or 6,
+ * for quadratic geometry), points summed in table order.  Passing the
+ * `gauss_u`, `gauss_v`, `weights` of the shape functions that
+ * create_rotated_element returns (src/3d/assembly_collocation.jl:122-136,
+ * 284-305, 369-413) reproduces the reference's quadrature bit for bit.
+ * Every point must satisfy u >= 0, v >= 0, u + v <= 1 and all values must be
+ * finite; the tables are copied.
+ */
+BIE_API int bie_ctx_create_rules(bie_ctx **out, const bie_mesh_desc *desc,
+                                 const bie_rule_table *rules, int n_rules, int device);
+
 /* Release every device and host resource of a context. NULL is a no-op. */
 BIE_API int bie_ctx_destroy(bie_ctx *ctx);
 

@@ -102,3 +102,39 @@ def test_null_context_is_rejected():
     assert st == _capi.BIE_ERR_INVALID
     assert b"NULL" in L.bie_last_error()
     assert L.bie_ctx_destroy(None) == _capi.BIE_OK
+
+
+def _tables(rules):
+    keep = [tuple(np.ascontiguousarray(a, dtype=np.float64) for a in r) for r in rules]
+    tabs = (_capi.RuleTable * max(len(keep), 1))(*[
+        _capi.RuleTable(r[0].size, r[0].ctypes.data_as(C.POINTER(C.c_double)),
+                        r[1].ctypes.data_as(C.POINTER(C.c_double)),
+                        r[2].ctypes.data_as(C.POINTER(C.c_double))) for r in keep])
+    return tabs, keep
+
+
+@pytest.mark.parametrize("case", ["count", "outside", "nan", "empty", "too_many", "null"])
+def test_ctx_create_rules_rejects_invalid_tables(case):
+    """bie_ctx_create_rules validates the caller's rule tables on the host
+    before any device call (so these need no GPU)."""
+    mesh = biegpu.icosphere(2)
+    rules = [biegpu.quadrature_rule(2, 2, r) for r in (1, 2, 3)]
+    if case == "count":
+        rules = rules[:2]
+    elif case == "outside":
+        u, v, w = (a.copy() for a in rules[1]); u[0] = 0.9; v[0] = 0.2; rules[1] = (u, v, w)
+    elif case == "nan":
+        u, v, w = (a.copy() for a in rules[2]); w[3] = np.nan; rules[2] = (u, v, w)
+    elif case == "empty":
+        rules[0] = (np.zeros(0), np.zeros(0), np.zeros(0))
+    elif case == "too_many":
+        rules[0] = (np.full(65, 0.1), np.full(65, 0.1), np.full(65, 0.5 / 65))
+    tabs, keep = _tables(rules)
+    if case == "null":
+        tabs[1].v = C.POINTER(C.c_double)()
+    d, keep_mesh = _desc(mesh, n=0, m=0)      # (n, m) are ignored with explicit tables
+    h = C.c_void_p()
+    st = _capi.lib().bie_ctx_create_rules(C.byref(h), C.byref(d), tabs, len(rules), 0)
+    assert st == _capi.BIE_ERR_INVALID
+    assert h.value is None
+    assert len(_capi.lib().bie_last_error()) > 0
