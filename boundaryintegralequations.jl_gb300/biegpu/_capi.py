@@ -231,6 +231,7 @@ SIGNATURES = {
     "bie_nearfield_pattern": (_I, [_P, _I, C.POINTER(_I64), _P, _P]),
     "bie_nearfield_assemble": (_I, [_P, _D, _D, _I, _D, _I, _I, _I, _P, _P]),
     "bie_gmres_device": (_I, [_P, C.POINTER(Operator), _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
+    "bie_gmres": (_I, [_P, C.POINTER(Operator), _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
     "bie_round_c64_device": (_I, [_P, _P, _P, _I64]),
     "bie_sweep": (_I, [C.POINTER(_P), _I, _P, _I, C.POINTER(_P), C.POINTER(_P), C.POINTER(SweepOpts),
                        C.POINTER(SweepInfo), _P]),

@@ -358,67 +358,87 @@ def gmres(A, b, restart: int | None = None, maxiter: int | None = None,
     ``GPUFOperator``.  ``precision`` selects the operator arithmetic;
     ``refine=True`` runs mixed inner iterations (on ``A32``, a complex64 copy
     of a dense matrix, or the mixed matrix-free operator) with an FP64 outer
-    residual.  Returns x (same array kind as b), or (x, GmresResult) when
-    ``log`` is true.
+    residual.  Host (numpy) inputs go through ``bie_gmres`` (the library
+    copies them to the device and x back); CUDA tensors through
+    ``bie_gmres_device``.  Returns x (same array kind as b), or
+    (x, GmresResult) when ``log`` is true.
     """
-    torch = _torch()
     aff = _as_affine(A)
     base = aff.base
     op = _capi.Operator()
     op.scale_re, op.scale_im = aff.scale.real, aff.scale.imag
     keep = []
+    dense = not isinstance(base, (_MatrixFreeOperator, _FastOperator))
+    on_host = not any(_is_torch(t) for t in (b, x0, aff.diag, A32, base if dense else None))
     if isinstance(base, _MatrixFreeOperator):
         if base.which != "F":
             raise ValueError("only the double-layer operator F can be inverted matrix-free")
         ctx = base.ctx
-        dev = torch.device(f"cuda:{ctx.device}")
         op.kind = _capi.BIE_OP_MATRIX_FREE
         op.k_re, op.k_im = base.k.real, base.k.imag
     elif isinstance(base, _FastOperator):
         ctx = base.ctx
-        dev = torch.device(f"cuda:{ctx.device}")
         op.kind = _capi.BIE_OP_FAST
         op.fast = base._h.value
         keep.append(base)
+    elif ctx is None:
+        raise ValueError("dense gmres needs the context of the mesh (ctx=...)")
     else:
-        if ctx is None:
-            raise ValueError("dense gmres needs the context of the mesh (ctx=...)")
-        dev = torch.device(f"cuda:{ctx.device}")
-        if _is_torch(base):
-            Ad = base
-        else:
-            # column-major N x N numpy -> device memory of the same layout
-            Ad = torch.as_tensor(np.asfortranarray(base, dtype=np.complex128).T.copy(), device=dev)
-        keep.append(Ad)
         op.kind = _capi.BIE_OP_DENSE
-        op.A = Ad.data_ptr()
-        if A32 is not None:
-            keep.append(A32)
-            op.A32 = A32.data_ptr()
-        elif refine or precision == "mixed":
-            A32 = torch.empty(Ad.shape, dtype=torch.complex64, device=dev)
-            _capi.check(_capi.lib().bie_round_c64_device(ctx.handle, Ad.data_ptr(), A32.data_ptr(), Ad.numel()))
-            keep.append(A32)
-            op.A32 = A32.data_ptr()
-    if aff.diag is not None:
-        dg = _device_complex(aff.diag, dev)
-        keep.append(dg)
-        op.diag = dg.data_ptr()
-    bd = _device_complex(b, dev)
-    if x0 is not None:
-        xd = _device_complex(x0, dev).clone()
-    else:
-        xd = torch.zeros_like(bd)
     opts = _capi.GmresOpts(restart=int(restart or 0), maxiter=int(maxiter or 0), reltol=float(reltol),
                            abstol=float(abstol), precision=_capi.PRECISION[precision],
                            refine=1 if refine else 0, inner_reltol=0.0, max_refine=0,
                            initially_nonzero=1 if x0 is not None else 0)
     info = _capi.GmresInfo()
-    torch.cuda.synchronize(dev)
-    st = _capi.lib().bie_gmres_device(ctx.handle, C.byref(op), bd.data_ptr(), xd.data_ptr(),
-                                      C.byref(opts), C.byref(info))
+    if on_host:
+        # column-major N x N matrices and vectors stay on the host; bie_gmres copies them
+        if dense:
+            Ah = np.asfortranarray(base, dtype=np.complex128)
+            keep.append(Ah)
+            op.A = Ah.ctypes.data
+            if A32 is not None:
+                A32h = np.asfortranarray(A32, dtype=np.complex64)
+                keep.append(A32h)
+                op.A32 = A32h.ctypes.data
+        if aff.diag is not None:
+            dg = np.ascontiguousarray(aff.diag, dtype=np.complex128)
+            keep.append(dg)
+            op.diag = dg.ctypes.data
+        bh = np.ascontiguousarray(b, dtype=np.complex128)
+        x = np.array(x0, dtype=np.complex128) if x0 is not None else np.zeros_like(bh)
+        st = _capi.lib().bie_gmres(ctx.handle, C.byref(op), bh.ctypes.data, x.ctypes.data,
+                                   C.byref(opts), C.byref(info))
+    else:
+        torch = _torch()
+        dev = torch.device(f"cuda:{ctx.device}")
+        if dense:
+            if _is_torch(base):
+                Ad = base
+            else:
+                # column-major N x N numpy -> device memory of the same layout
+                Ad = torch.as_tensor(np.asfortranarray(base, dtype=np.complex128).T.copy(), device=dev)
+            keep.append(Ad)
+            op.A = Ad.data_ptr()
+            if A32 is not None:
+                keep.append(A32)
+                op.A32 = A32.data_ptr()
+            elif refine or precision == "mixed":
+                A32 = torch.empty(Ad.shape, dtype=torch.complex64, device=dev)
+                _capi.check(_capi.lib().bie_round_c64_device(ctx.handle, Ad.data_ptr(), A32.data_ptr(),
+                                                             Ad.numel()))
+                keep.append(A32)
+                op.A32 = A32.data_ptr()
+        if aff.diag is not None:
+            dg = _device_complex(aff.diag, dev)
+            keep.append(dg)
+            op.diag = dg.data_ptr()
+        bd = _device_complex(b, dev)
+        xd = _device_complex(x0, dev).clone() if x0 is not None else torch.zeros_like(bd)
+        torch.cuda.synchronize(dev)
+        st = _capi.lib().bie_gmres_device(ctx.handle, C.byref(op), bd.data_ptr(), xd.data_ptr(),
+                                          C.byref(opts), C.byref(info))
+        x = xd if _is_torch(b) else xd.cpu().numpy()
     if st not in (_capi.BIE_OK, _capi.BIE_ERR_NOT_CONVERGED):
         _capi.check(st)
-    x = xd if _is_torch(b) else xd.cpu().numpy()
     res = GmresResult(x, info)
     return (x, res) if log else x

@@ -670,6 +670,76 @@ int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b, do
     return st;
 }
 
+int bie_gmres(bie_ctx *ctx, const bie_operator *op, const double *b, double *x, const bie_gmres_opts *opts,
+              bie_gmres_info *info) {
+    int converged = 1;
+    const int st = guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (!op || !b || !x) bie::fail(BIE_ERR_INVALID, "op, b and x must not be NULL");
+        if (op->kind != BIE_OP_DENSE && op->kind != BIE_OP_MATRIX_FREE && op->kind != BIE_OP_FAST)
+            bie::fail(BIE_ERR_INVALID, "unknown operator kind");
+        if (op->kind == BIE_OP_DENSE && !op->A) bie::fail(BIE_ERR_INVALID, "dense operator without A");
+        if (op->kind == BIE_OP_FAST &&
+            (!op->fast || reinterpret_cast<const bie::FastOp *>(op->fast)->base != &c))
+            bie::fail(BIE_ERR_INVALID, "fast operator missing or made from another context");
+        if (!std::isfinite(op->k_re) || !std::isfinite(op->k_im) || !std::isfinite(op->scale_re) ||
+            !std::isfinite(op->scale_im))
+            bie::fail(BIE_ERR_INVALID, "k and scale must be finite");
+        bie_gmres_opts o{};
+        if (opts) o = *opts;
+        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
+            bie::fail(BIE_ERR_INVALID, "unknown precision");
+        if (!(o.reltol >= 0) || !(o.abstol >= 0)) bie::fail(BIE_ERR_INVALID, "tolerances must be >= 0");
+        // one device block: [A (16 N^2)] [A32 (8 N^2)] [diag (16 N)] b (16 N) x (16 N)
+        const size_t N = (size_t)c.n_sources;
+        const bool dense = op->kind == BIE_OP_DENSE;
+        const bool low = dense && (op->A32 || o.refine || o.precision == BIE_PREC_MIXED);
+        const size_t a_bytes = dense ? 16 * N * N : 0, a32_bytes = low ? 8 * N * N : 0;
+        const size_t d_bytes = op->diag ? 16 * N : 0, v_bytes = 16 * N;
+        std::lock_guard<std::mutex> lock(c.mu);
+        BIE_CUDA(cudaSetDevice(c.device));
+        char *d = nullptr;
+        BIE_CUDA(cudaMalloc(&d, a_bytes + a32_bytes + d_bytes + 2 * v_bytes));
+        struct Free {
+            void *p;
+            ~Free() { cudaFree(p); }
+        } guard{d};
+        double *dA = dense ? reinterpret_cast<double *>(d) : nullptr;
+        float *dA32 = low ? reinterpret_cast<float *>(d + a_bytes) : nullptr;
+        double *ddiag = op->diag ? reinterpret_cast<double *>(d + a_bytes + a32_bytes) : nullptr;
+        double *db = reinterpret_cast<double *>(d + a_bytes + a32_bytes + d_bytes);
+        double *dx = db + 2 * N;
+        if (dense) BIE_CUDA(cudaMemcpyAsync(dA, op->A, a_bytes, cudaMemcpyHostToDevice, c.stream));
+        if (low) {
+            if (op->A32)
+                BIE_CUDA(cudaMemcpyAsync(dA32, op->A32, a32_bytes, cudaMemcpyHostToDevice, c.stream));
+            else
+                bie::round_to_c64(c, dA, dA32, (int64_t)(N * N));
+        }
+        if (ddiag) BIE_CUDA(cudaMemcpyAsync(ddiag, op->diag, d_bytes, cudaMemcpyHostToDevice, c.stream));
+        BIE_CUDA(cudaMemcpyAsync(db, b, v_bytes, cudaMemcpyHostToDevice, c.stream));
+        if (o.initially_nonzero)
+            BIE_CUDA(cudaMemcpyAsync(dx, x, v_bytes, cudaMemcpyHostToDevice, c.stream));
+        else
+            BIE_CUDA(cudaMemsetAsync(dx, 0, v_bytes, c.stream));
+        bie_operator dop = *op;
+        dop.A = dA;
+        dop.A32 = dA32;
+        dop.diag = ddiag;
+        bie_gmres_info inf{};
+        bie::run_gmres(c, dop, db, dx, o, inf);
+        BIE_CUDA(cudaMemcpyAsync(x, dx, v_bytes, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+        if (info) *info = inf;
+        converged = inf.converged;
+    });
+    if (st == BIE_OK && !converged) {
+        g_last_error = "GMRES reached maxiter before the tolerance";
+        return BIE_ERR_NOT_CONVERGED;
+    }
+    return st;
+}
+
 int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,
               double *const *p, const bie_sweep_opts *opts, bie_sweep_info *info, int32_t *iters) {
     return guarded([&] {

@@ -494,6 +494,70 @@ struct GmresInfoC
     matvecs::Int64; residual_norm::Float64; rhs_norm::Float64
 end
 
+# bie_operator (include/biegpu.h)
+struct OperatorC
+    kind::Int32
+    A::Ptr{ComplexF64}
+    A32::Ptr{ComplexF32}
+    k_re::Float64; k_im::Float64
+    scale_re::Float64; scale_im::Float64
+    diag::Ptr{ComplexF64}
+    fast::Ptr{Cvoid}
+end
+
+function _gmres_host(ctx::Context, op::OperatorC, b, reltol, restart, maxiter, precision, refine)
+    bv = Vector{ComplexF64}(b)
+    x = zeros(ComplexF64, length(bv))
+    opts = GmresOptsC(restart, maxiter, reltol, 0.0, precision_code(precision), refine ? 1 : 0, 0.0, 0, 0)
+    info = Ref{GmresInfoC}()
+    st = GC.@preserve bv x ccall((:bie_gmres, libbiegpu), Cint,
+                                 (Ptr{Cvoid}, Ref{OperatorC}, Ptr{ComplexF64}, Ptr{ComplexF64},
+                                  Ref{GmresOptsC}, Ref{GmresInfoC}), ctx.handle, op, bv, x, opts, info)
+    st == Cint(-3) || check(st)   # not converged: x is still returned, as gmres does
+    return x
+end
+
+"""
+    gmres_gpu(ctx, H::AbstractMatrix, b; diag=nothing, scale=1, refine=false,
+              precision=:fp64, reltol=0, restart=0, maxiter=0)
+
+`gmres(scale * H + Diagonal(diag), b)` for a dense matrix on the host (e.g.
+`gmres(Fp + Diagonal(1 .- Cp), pI)`, test/3d/assembly_test.jl:37-38 →
+`gmres_gpu(ctx, Fp, pI; diag=1 .- Cp)`), solved by the library's device GMRES
+(`bie_gmres`; IterativeSolvers defaults for zero arguments).  `refine=true`
+runs complex64 inner iterations with FP64 residual refinement.
+"""
+function gmres_gpu(ctx::Context, H::AbstractMatrix, b; diag=nothing, scale=1.0, refine=false,
+                   precision=:fp64, reltol=0.0, restart=0, maxiter=0)
+    Hm = Matrix{ComplexF64}(H)
+    dv = diag === nothing ? ComplexF64[] : Vector{ComplexF64}(diag)
+    s = ComplexF64(scale)
+    GC.@preserve Hm dv begin
+        op = OperatorC(0, pointer(Hm), C_NULL, 0.0, 0.0, real(s), imag(s),
+                       diag === nothing ? C_NULL : pointer(dv), C_NULL)
+        return _gmres_host(ctx, op, b, reltol, restart, maxiter, precision, refine)
+    end
+end
+
+"""
+    gmres_gpu(Ff::GPUFOperator, b; diag=nothing, scale=1, ...)
+
+`gmres(scale * Ff + Diagonal(diag), b)` matrix-free (the F rows generated on
+the fly in every product), e.g. `gmres(Diagonal(1 .- C) - Ff, Gf * vs)`
+(examples/3d_pulsating_sphere.jl:46-50) → `gmres_gpu(Ff, Gf * vs; diag=1 .- C, scale=-1)`.
+"""
+function gmres_gpu(Ff::GPUOperator{:F}, b; diag=nothing, scale=1.0, refine=false, reltol=0.0,
+                   restart=0, maxiter=0)
+    dv = diag === nothing ? ComplexF64[] : Vector{ComplexF64}(diag)
+    s = ComplexF64(scale)
+    prec = Ff.precision == BIE_PREC_MIXED ? :mixed : :fp64
+    GC.@preserve dv begin
+        op = OperatorC(1, C_NULL, C_NULL, real(Ff.k), imag(Ff.k), real(s), imag(s),
+                       diag === nothing ? C_NULL : pointer(dv), C_NULL)
+        return _gmres_host(Ff.ctx, op, b, reltol, restart, maxiter, prec, refine)
+    end
+end
+
 struct LossyOpts
     S::Float64; custom_air::Int32; pa::Float64; t::Float64; Hr::Float64
     depth::Int32; interior::Int32; fmm_on::Int32; n_gauss::Int32; fmm_offset::Float64

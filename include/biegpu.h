@@ -446,6 +446,18 @@ typedef struct bie_gmres_info {
 BIE_API int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b,
                              double *d_x, const bie_gmres_opts *opts, bie_gmres_info *info);
 
+/*
+ * bie_gmres_device with host buffers (blocking): b, x (N complex128) and the
+ * operator's A (N x N complex128, column-major), A32 and diag are host arrays,
+ * copied to temporary device memory; x is written back.  With a dense operator
+ * and `refine` or BIE_PREC_MIXED, a NULL A32 is formed on the device by
+ * rounding A to complex64.  The call `gmres(H, b)` of the reference on a
+ * matrix returned by bie_assemble (test/3d/assembly_test.jl:37-38;
+ * examples/3d_pulsating_sphere.jl:44) becomes one call here.
+ */
+BIE_API int bie_gmres(bie_ctx *ctx, const bie_operator *op, const double *b, double *x,
+                      const bie_gmres_opts *opts, bie_gmres_info *info);
+
 /* ---- frequency sweeps -------------------------------------------------- */
 typedef struct bie_sweep_opts {
     int32_t precision;         /* assembly arithmetic: BIE_PREC_MIXED | BIE_PREC_FP64   */

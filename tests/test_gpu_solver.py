@@ -124,3 +124,63 @@ def test_pulsating_sphere_full_size_matrix_free():
     pf = Ff.evaluate_targets(p, X) + Gf.evaluate_targets(vs, X)
     pa = an.pulsating_sphere_interior(k, 1.0, Z0, 1.0, z)
     assert rel(pf, pa) <= 0.1    # flat-facet geometry error, O(h) (0.14 at f=20 with the oracle)
+
+
+def _torch_dev():
+    import torch
+    return torch, torch.device("cuda:0")
+
+
+@pytest.mark.parametrize("refine,prec", [(False, "fp64"), (True, "fp64"), (False, "mixed")])
+def test_gmres_host_entry_matches_device_entry_dense(refine, prec):
+    """bie_gmres (host buffers: numpy in, numpy out) against bie_gmres_device
+    (CUDA tensors) on the same dense system: same iterate sequence, so the
+    solutions agree to rounding and the iteration counts match."""
+    torch, dev = _torch_dev()
+    mesh = bm.icosphere(5, geometry="quadratic")
+    Fp, _, Cp = biegpu.assemble_parallel(mesh, 2.5, mesh.sources, n=2, m=2, gOn=False)
+    b = rand_c(mesh.n_sources, 8)
+    ctx = biegpu.get_context(mesh, n=2, m=2)
+    xh, rh = gmres(Fp + Diagonal(1.0 - Cp), b, ctx=ctx, refine=refine, precision=prec, log=True)
+    Ad = torch.as_tensor(np.asfortranarray(Fp).T.copy(), device=dev)
+    xd, rd = gmres(Ad + Diagonal(torch.as_tensor(1.0 - Cp, device=dev)), torch.as_tensor(b, device=dev),
+                   ctx=ctx, refine=refine, precision=prec, log=True)
+    assert isinstance(xh, np.ndarray)
+    assert rh.converged and rd.converged
+    assert abs(rh.iterations - rd.iterations) <= 1
+    assert rel(xh, xd.cpu().numpy()) <= (1e-12 if prec == "fp64" and not refine else 1e-6)
+    assert rel(xh, np.linalg.solve(Fp + np.diag(1.0 - Cp), b)) <= 1e-6
+
+
+def test_gmres_host_entry_given_a32_and_start():
+    """A caller-supplied complex64 matrix and a non-zero start vector through
+    the host entry: a start at the solution converges in no more than one
+    Arnoldi step."""
+    mesh = bm.icosphere(4, geometry="quadratic")
+    Fp, _, Cp = biegpu.assemble_parallel(mesh, 1.5, mesh.sources, n=2, m=2, gOn=False)
+    A = Fp + np.diag(1.0 - Cp)
+    b = rand_c(mesh.n_sources, 9)
+    ctx = biegpu.get_context(mesh, n=2, m=2)
+    x, res = gmres(Fp + Diagonal(1.0 - Cp), b, ctx=ctx, refine=True, A32=np.asfortranarray(Fp, np.complex64),
+                   log=True)
+    assert res.converged and rel(x, np.linalg.solve(A, b)) <= 1e-6
+    xs = np.linalg.solve(A, b)
+    x2, res2 = gmres(Fp + Diagonal(1.0 - Cp), b, ctx=ctx, x0=xs, log=True)
+    assert res2.converged and res2.iterations <= 1
+    assert rel(x2, xs) <= 1e-12
+
+
+def test_gmres_host_entry_matrix_free_and_not_converged():
+    mesh = bm.icosphere(5, geometry="quadratic")
+    k = 1.0
+    _, _, C = oracle.assemble(mesh, k, n=2, m=2, fOn=False, gOn=False)
+    Ff = GPUFOperator(mesh, k, precision="fp64")
+    b = rand_c(mesh.n_sources, 10)
+    x, res = gmres(Diagonal(1.0 - C) - Ff, b, log=True)
+    torch, dev = _torch_dev()
+    xd, rd = gmres(Diagonal(torch.as_tensor(1.0 - C, device=dev)) - Ff, torch.as_tensor(b, device=dev), log=True)
+    assert res.converged and abs(res.iterations - rd.iterations) <= 1
+    assert rel(x, xd.cpu().numpy()) <= 1e-12
+    # maxiter reached: x is still returned with the info filled, as gmres does
+    x3, r3 = gmres(Diagonal(1.0 - C) - Ff, b, maxiter=2, log=True)
+    assert not r3.converged and r3.iterations == 2 and np.all(np.isfinite(x3))
