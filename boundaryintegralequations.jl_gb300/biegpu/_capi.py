@@ -34,7 +34,12 @@ BIE_PREC_BF16 = 3
 BIE_PREC_FP16_SPLIT = 4
 BIE_PREC_BF16_SPLIT = 5
 
-KIND = {"linear": BIE_TRI_LINEAR, "quadratic": BIE_TRI_QUADRATIC}
+BIE_TRI_DISC_CONSTANT = 3
+BIE_TRI_DISC_LINEAR = 4
+BIE_TRI_DISC_QUADRATIC = 5
+
+KIND = {"linear": BIE_TRI_LINEAR, "quadratic": BIE_TRI_QUADRATIC, "disctriconstant": BIE_TRI_DISC_CONSTANT,
+        "disctrilinear": BIE_TRI_DISC_LINEAR, "disctriquadratic": BIE_TRI_DISC_QUADRATIC}
 PRECISION = {"fp64": BIE_PREC_FP64, "mixed": BIE_PREC_MIXED, "fp16": BIE_PREC_FP16, "bf16": BIE_PREC_BF16,
              "fp16_split": BIE_PREC_FP16_SPLIT, "bf16_split": BIE_PREC_BF16_SPLIT}
 
@@ -70,6 +75,7 @@ class MeshDesc(C.Structure):
         ("sources", C.POINTER(C.c_double)),
         ("quad_n", C.c_int32),
         ("quad_m", C.c_int32),
+        ("physics_beta", C.c_double),
     ]
 
 

@@ -61,6 +61,7 @@ class Context:
             sources=self._src.ctypes.data_as(C.POINTER(C.c_double)),
             quad_n=self.n,
             quad_m=self.m,
+            physics_beta=float(getattr(mesh, "physics_beta", 0.0)),
         )
         h = C.c_void_p()
         if rules is None:

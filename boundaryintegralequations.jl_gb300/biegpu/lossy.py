@@ -74,7 +74,8 @@ def _mesh_desc(mesh: Mesh3d):
         n_elements=keep[1].shape[1], shape_kind=_capi.KIND[mesh.shape_function],
         physics_kind=_capi.KIND[mesh.physics_function], topology=keep[1].ctypes.data_as(C.POINTER(C.c_int64)),
         physics_topology=keep[2].ctypes.data_as(C.POINTER(C.c_int64)), n_sources=keep[3].shape[1],
-        sources=keep[3].ctypes.data_as(C.POINTER(C.c_double)), quad_n=1, quad_m=1)
+        sources=keep[3].ctypes.data_as(C.POINTER(C.c_double)), quad_n=1, quad_m=1,
+        physics_beta=float(getattr(mesh, "physics_beta", 0.0)))
     return d, keep
 
 

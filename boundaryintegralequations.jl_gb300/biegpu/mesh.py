@@ -6,7 +6,11 @@ n_shape x E and ``physics_topology`` n_phys x E (both 1-based), plus nodal
 ``normals``/``tangents``/``sangents`` and the element kinds.  Here the same
 arrays are numpy arrays of those shapes; the element kinds are the strings
 ``"linear"`` (3-node triangle) and ``"quadratic"`` (6-node triangle, nodes
-1 2 3 corners, 4 on edge 1-2, 5 on edge 2-3, 6 on edge 3-1).
+1 2 3 corners, 4 on edge 1-2, 5 on edge 2-3, 6 on edge 3-1), and for the
+physics also the discontinuous triangles ``"disctriconstant"``,
+``"disctrilinear"``, ``"disctriquadratic"`` (nodes inside each element, offset
+``physics_beta`` from the edges; src/3d/SurfaceFunction.jl:81-105, 430-439,
+src/3d/surface_functions.jl:236-318).
 
 Builders:
   * :func:`icosphere` - geodesic sphere, each icosahedron face split f x f
@@ -15,7 +19,8 @@ Builders:
     onto the sphere;
   * :func:`ellipsoid` - a sphere mesh scaled to semi-axes (a, b, c);
   * :func:`load_comsol` - COMSOL ``.mphtxt`` reader for triangle meshes
-    (src/3d/read_comsol.jl:9-119) with physics ``"geometry"`` or ``"linear"``.
+    (src/3d/read_comsol.jl:9-119) with physics ``"geometry"``, ``"linear"`` or
+    a discontinuous kind.
 """
 from __future__ import annotations
 
@@ -24,7 +29,8 @@ from pathlib import Path
 
 import numpy as np
 
-KIND_NODES = {"linear": 3, "quadratic": 6}
+KIND_NODES = {"linear": 3, "quadratic": 6, "disctriconstant": 1, "disctrilinear": 3, "disctriquadratic": 6}
+DISCONTINUOUS = ("disctriconstant", "disctrilinear", "disctriquadratic")
 
 
 @dataclass(eq=False)   # identity hash: contexts are cached per mesh object
@@ -36,9 +42,10 @@ class Mesh3d:
     tangents: np.ndarray           # 3 x N
     sangents: np.ndarray           # 3 x N
     shape_function: str            # "linear" | "quadratic"
-    physics_function: str          # "linear" | "quadratic"
+    physics_function: str          # "linear" | "quadratic" | "disctri*"
     physics_topology: np.ndarray   # NP x E  1-based into sources
     entities: np.ndarray = field(default_factory=lambda: np.zeros(0, dtype=np.int64))
+    physics_beta: float = 0.0      # node offset of discontinuous physics (0 otherwise)
 
     @property
     def n_elements(self) -> int:
@@ -75,6 +82,66 @@ def _shape_derivatives(kind: str, u: np.ndarray, v: np.ndarray):
     du = np.stack([d1, 4 * u - 1, np.zeros_like(u), 4 * l - 4 * u, 4 * v, -4 * v])
     dv = np.stack([d1, np.zeros_like(u), 4 * v - 1, -4 * u, 4 * u, 4 * l - 4 * v])
     return du, dv
+
+
+def _shape_values(kind: str, u: np.ndarray, v: np.ndarray) -> np.ndarray:
+    """N(u, v) as an (n_shape, len(u)) array (src/3d/surface_functions.jl:191-236)."""
+    if kind == "linear":
+        return np.stack([(1.0 - u) - v, u, v])
+    l = (1.0 - v) - u
+    return np.stack([l * ((1.0 - 2.0 * v) - 2.0 * u), u * (2.0 * u - 1.0), v * (2.0 * v - 1.0),
+                     4.0 * u * l, 4.0 * u * v, 4.0 * v * l])
+
+
+def discontinuous_beta(kind: str, beta_type="legendre") -> float:
+    """Node offset of a discontinuous triangle (set_physics_element /
+    get_beta_tri_* of src/3d/mesh.jl:156-214): half the quadrilateral value,
+    which is 1 + the first Gauss-Legendre node of 2 (linear) or 3 (quadratic)
+    points for "legendre", 1/2 or 1/3 for "equidistant", or the number given."""
+    if kind == "disctriconstant":
+        return 0.0
+    quad = kind == "disctriquadratic"
+    if isinstance(beta_type, (int, float)) and not isinstance(beta_type, bool):
+        b = float(beta_type)
+    elif beta_type == "legendre":
+        b = 1.0 + np.polynomial.legendre.leggauss(3 if quad else 2)[0][0]
+    elif beta_type == "equidistant":
+        b = 1.0 / 3.0 if quad else 0.5
+    else:
+        raise ValueError(f"unknown beta_type {beta_type!r}")
+    return b / 2
+
+
+def discontinuous_nodes(kind: str, beta: float):
+    """(u, v) of the nodes of a discontinuous triangle (src/3d/SurfaceFunction.jl:430-439)."""
+    b = float(beta)
+    if kind == "disctriconstant":
+        return np.array([1 / 3]), np.array([1 / 3])
+    if kind == "disctrilinear":
+        return np.array([b, 1 - 2 * b, b]), np.array([b, b, 1 - 2 * b])
+    if kind == "disctriquadratic":
+        return (np.array([b, 1 - 2 * b, b, (1 - b) / 2, (1 - b) / 2, b]),
+                np.array([b, b, 1 - 2 * b, b, (1 - b) / 2, (1 - b) / 2]))
+    raise ValueError(f"not a discontinuous kind: {kind!r}")
+
+
+def compute_sources(shape: str, kind: str, beta: float, coordinates: np.ndarray, topology: np.ndarray):
+    """Collocation nodes, their normals and the physics topology of
+    discontinuous physics (compute_sources, src/3d/mesh.jl:115-145): the nodes
+    of element e are sources e*NP+1 .. e*NP+NP, placed by the geometry's
+    shape functions, with the negated unit normal of the geometry there."""
+    u, v = discontinuous_nodes(kind, beta)
+    NP, E = len(u), topology.shape[1]
+    N = _shape_values(shape, u, v)                      # NS x NP
+    du, dv = _shape_derivatives(shape, u, v)
+    X = coordinates[:, topology - 1]                    # 3 x NS x E
+    src = np.einsum("kae,ab->kbe", X, N)                # 3 x NP x E
+    t1 = np.einsum("kae,ab->kbe", X, du)
+    t2 = np.einsum("kae,ab->kbe", X, dv)
+    n = np.cross(t1, t2, axis=0)
+    n = -n / np.sqrt(np.sum(n**2, axis=0, keepdims=True))
+    ptopo = np.arange(1, NP * E + 1, dtype=np.int64).reshape(NP, E, order="F")
+    return src.reshape(3, NP * E, order="F").copy(), n.reshape(3, NP * E, order="F").copy(), ptopo
 
 
 def element_normals(kind: str, coordinates: np.ndarray, topology: np.ndarray) -> np.ndarray:
@@ -115,10 +182,16 @@ def tangents(normals: np.ndarray):
     return t1.T.copy(), t2.T.copy()
 
 
-def _finish(coordinates, topology, shape, physics) -> Mesh3d:
-    """Build the Mesh3d for physics 'geometry' (same nodes) or 'linear' (corners only),
-    following load3dTriangularComsolMesh (src/3d/read_comsol.jl:61-119)."""
-    if physics in ("geometry", shape):
+def _finish(coordinates, topology, shape, physics, beta_type="legendre") -> Mesh3d:
+    """Build the Mesh3d for physics 'geometry' (same nodes), 'linear' (corners
+    only) or a discontinuous kind, following load3dTriangularComsolMesh
+    (src/3d/read_comsol.jl:61-119)."""
+    beta = 0.0
+    if physics in DISCONTINUOUS:
+        beta = discontinuous_beta(physics, beta_type)
+        sources, normals, ptopo = compute_sources(shape, physics, beta, coordinates, topology)
+        pkind = physics
+    elif physics in ("geometry", shape):
         normals = element_normals(shape, coordinates, topology)
         sources = coordinates[:, np.unique(topology) - 1]
         ptopo = topology
@@ -137,7 +210,7 @@ def _finish(coordinates, topology, shape, physics) -> Mesh3d:
     t1, t2 = tangents(normals)
     return Mesh3d(sources=sources, coordinates=coordinates, topology=topology, normals=normals,
                   tangents=t1, sangents=t2, shape_function=shape, physics_function=pkind,
-                  physics_topology=ptopo.copy())
+                  physics_topology=ptopo.copy(), physics_beta=beta)
 
 
 # ---------------------------------------------------------------------------
@@ -234,7 +307,7 @@ def promote_quadratic_arrays(coords: np.ndarray, tris: np.ndarray, radius: float
 
 
 def icosphere(f: int, radius: float = 1.0, geometry: str = "linear", physics: str = "geometry",
-              axes: tuple[float, float, float] | None = None) -> Mesh3d:
+              axes: tuple[float, float, float] | None = None, beta_type="legendre") -> Mesh3d:
     """Geodesic sphere (optionally scaled to an ellipsoid with semi-axes ``axes``)."""
     P, T = icosphere_arrays(f, radius)
     if geometry == "quadratic":
@@ -243,7 +316,7 @@ def icosphere(f: int, radius: float = 1.0, geometry: str = "linear", physics: st
         raise ValueError("geometry must be 'linear' or 'quadratic'")
     if axes is not None:
         P = P * (np.asarray(axes, dtype=np.float64)[:, None] / radius)
-    return _finish(P, T + 1, geometry, physics)
+    return _finish(P, T + 1, geometry, physics, beta_type)
 
 
 def ellipsoid(f: int, axes=(1.0, 2.0 / 3.0, 1.0 / 3.0), geometry: str = "linear",
@@ -314,9 +387,10 @@ def _remove_unused_nodes(topology: np.ndarray) -> np.ndarray:
 
 
 def load_comsol(path: str | Path, geometry_order: str = "quadratic", physics_order: str = "geometry",
-                reader: str = "native") -> Mesh3d:
-    """load3dTriangularComsolMesh for physics 'geometry' or 'linear'; ``reader``
-    "native" parses the file with libbiegpu's C reader, "python" in Python."""
+                reader: str = "native", beta_type="legendre") -> Mesh3d:
+    """load3dTriangularComsolMesh for physics 'geometry', 'linear' or a
+    discontinuous kind; ``reader`` "native" parses the file with libbiegpu's C
+    reader, "python" in Python."""
     if reader not in ("native", "python"):
         raise ValueError("reader must be 'native' or 'python'")
     C0, T0, ents = read_comsol_native(path) if reader == "native" else read_comsol(path)
@@ -327,6 +401,6 @@ def load_comsol(path: str | Path, geometry_order: str = "quadratic", physics_ord
     used = np.unique(T0)
     T = _remove_unused_nodes(T0)
     C = C0[:, used - 1]
-    m = _finish(C, T, geometry_order, physics_order)
+    m = _finish(C, T, geometry_order, physics_order, beta_type)
     m.entities = ents
     return m

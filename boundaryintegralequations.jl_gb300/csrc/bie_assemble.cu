@@ -197,7 +197,10 @@ void launch_assemble_fp64(Ctx &c, const AssembleArgs &a) {
 
     double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
     const bool cplx = a.k_im != 0.0;
-    if (L.NP == 3) {
+    if (L.NP == 1) {
+        if (cplx) launch_np<1, true>(c, a, S, level, smem, chunk, Cpart);
+        else launch_np<1, false>(c, a, S, level, smem, chunk, Cpart);
+    } else if (L.NP == 3) {
         if (cplx) launch_np<3, true>(c, a, S, level, smem, chunk, Cpart);
         else launch_np<3, false>(c, a, S, level, smem, chunk, Cpart);
     } else {

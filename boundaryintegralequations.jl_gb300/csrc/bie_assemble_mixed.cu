@@ -446,7 +446,10 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     auto run = [&](int level) {
         const int S = 1 << level;
         double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
-        if (L.NP == 3) {
+        if (L.NP == 1) {
+            if (cplx) launch_np<1, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+            else launch_np<1, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
+        } else if (L.NP == 3) {
             if (cplx) launch_np<3, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
             else launch_np<3, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
         } else {

@@ -690,25 +690,30 @@ int bie_gmres(bie_ctx *ctx, const bie_operator *op, const double *b, double *x, 
         if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
             bie::fail(BIE_ERR_INVALID, "unknown precision");
         if (!(o.reltol >= 0) || !(o.abstol >= 0)) bie::fail(BIE_ERR_INVALID, "tolerances must be >= 0");
-        // one device block: [A (16 N^2)] [A32 (8 N^2)] [diag (16 N)] b (16 N) x (16 N)
+        // one device block: [A (16 N^2)] [A32 (8 N^2)] [diag (16 N)] b (16 N) x (16 N),
+        // every part starting on a 256-byte boundary (8 N^2 is not a multiple
+        // of 16 for odd N)
         const size_t N = (size_t)c.n_sources;
         const bool dense = op->kind == BIE_OP_DENSE;
         const bool low = dense && (op->A32 || o.refine || o.precision == BIE_PREC_MIXED);
+        auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
         const size_t a_bytes = dense ? 16 * N * N : 0, a32_bytes = low ? 8 * N * N : 0;
         const size_t d_bytes = op->diag ? 16 * N : 0, v_bytes = 16 * N;
+        const size_t o_a32 = up(a_bytes), o_diag = o_a32 + up(a32_bytes), o_b = o_diag + up(d_bytes);
+        const size_t o_x = o_b + up(v_bytes);
         std::lock_guard<std::mutex> lock(c.mu);
         BIE_CUDA(cudaSetDevice(c.device));
         char *d = nullptr;
-        BIE_CUDA(cudaMalloc(&d, a_bytes + a32_bytes + d_bytes + 2 * v_bytes));
+        BIE_CUDA(cudaMalloc(&d, o_x + up(v_bytes)));
         struct Free {
             void *p;
             ~Free() { cudaFree(p); }
         } guard{d};
         double *dA = dense ? reinterpret_cast<double *>(d) : nullptr;
-        float *dA32 = low ? reinterpret_cast<float *>(d + a_bytes) : nullptr;
-        double *ddiag = op->diag ? reinterpret_cast<double *>(d + a_bytes + a32_bytes) : nullptr;
-        double *db = reinterpret_cast<double *>(d + a_bytes + a32_bytes + d_bytes);
-        double *dx = db + 2 * N;
+        float *dA32 = low ? reinterpret_cast<float *>(d + o_a32) : nullptr;
+        double *ddiag = op->diag ? reinterpret_cast<double *>(d + o_diag) : nullptr;
+        double *db = reinterpret_cast<double *>(d + o_b);
+        double *dx = reinterpret_cast<double *>(d + o_x);
         if (dense) BIE_CUDA(cudaMemcpyAsync(dA, op->A, a_bytes, cudaMemcpyHostToDevice, c.stream));
         if (low) {
             if (op->A32)

@@ -52,6 +52,8 @@ FastOp::~FastOp() {
 
 std::unique_ptr<FastOp> create_fastop(Ctx &c, double k_re, double k_im, int which, int n_gauss, bool nearfield,
                                       double offset, int depth) {
+    if (is_discontinuous(c.physics_kind))
+        fail(BIE_ERR_UNSUPPORTED, "fast operators take continuous physics only");
     triangle_gauss_rule(n_gauss);   // validates n_gauss
     auto op = std::make_unique<FastOp>();
     op->base = &c;
@@ -75,6 +77,7 @@ std::unique_ptr<FastOp> create_fastop(Ctx &c, double k_re, double k_im, int whic
     d.sources = c.sources.data();
     d.quad_n = c.quad_n;
     d.quad_m = c.quad_m;
+    d.physics_beta = c.physics_beta;
     op->g = std::make_unique<Ctx>();
     try {
         build_context(*op->g, d, c.device, n_gauss);

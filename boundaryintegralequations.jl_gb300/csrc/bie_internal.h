@@ -49,6 +49,10 @@ Rule triangle_gauss_rule(int n);
 
 // Shape functions of the 3- and 6-node triangles (src/3d/surface_functions.jl:191-236).
 int  n_nodes_of_kind(int kind);
+bool is_discontinuous(int kind);
+// physics basis: shape_values for continuous kinds, the discontinuous
+// triangle bases (node offset beta) otherwise
+void physics_values(int kind, double beta, double u, double v, double *N);
 void shape_values(int kind, double u, double v, double *N);
 void shape_derivs(int kind, double u, double v, double *dNu, double *dNv);
 
@@ -143,6 +147,7 @@ struct Ctx {
 
     // mesh (host copies, 0-based)
     int shape_kind = 0, physics_kind = 0;
+    double physics_beta = 0.0;
     int64_t n_coords = 0, n_elements = 0, n_sources = 0;
     int NS = 0;                          // geometry nodes per element
     std::vector<double> coords;          // 3 x Nc

@@ -143,6 +143,8 @@ void tangential_derivatives(int shape_kind, int physics_kind, const double *coor
                             const int32_t *topo, const int32_t *ptopo, int64_t N, std::vector<int64_t> &row_ptr,
                             std::vector<int32_t> &cols, std::vector<double> &Dx, std::vector<double> &Dy,
                             std::vector<double> &Dz) {
+    if (is_discontinuous(physics_kind))
+        fail(BIE_ERR_UNSUPPORTED, "tangential derivatives take continuous physics only");
     const int NS = n_nodes_of_kind(shape_kind), NP = n_nodes_of_kind(physics_kind);
     node_pattern(N, E, NP, ptopo, row_ptr, cols);
     Dx.assign(cols.size(), 0.0);

@@ -360,6 +360,8 @@ void LossyOp::outer(const double2 *x, double2 *y) {
 }
 
 LossyOp *create_lossy(Ctx &c, double freq, const bie_lossy_opts &o) {
+    if (is_discontinuous(c.physics_kind))
+        fail(BIE_ERR_UNSUPPORTED, "the lossy system takes continuous physics only");
     auto L = std::make_unique<LossyOp>();
     L->c = &c;
     const int64_t N = c.n_sources, E = c.n_elements;

@@ -621,7 +621,10 @@ void run_mixed_noalloc(Ctx &c, const MatvecArgs &a) {
 void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a) {
     if (!a.x && !a.v) return;
     const bool cplx = a.k_im != 0.0;
-    if (c.lay.NP == 3) {
+    if (c.lay.NP == 1) {
+        if (cplx) run_mixed_noalloc<1, true>(c, a);
+        else run_mixed_noalloc<1, false>(c, a);
+    } else if (c.lay.NP == 3) {
         if (cplx) run_mixed_noalloc<3, true>(c, a);
         else run_mixed_noalloc<3, false>(c, a);
     } else {
@@ -634,7 +637,10 @@ void launch_matvec(Ctx &c, const MatvecArgs &a) {
     if (!a.x && !a.v) return;
     const bool cplx = a.k_im != 0.0;
     if (a.precision == BIE_PREC_MIXED) {
-        if (c.lay.NP == 3) {
+        if (c.lay.NP == 1) {
+            if (cplx) run_mixed<1, true>(c, a);
+            else run_mixed<1, false>(c, a);
+        } else if (c.lay.NP == 3) {
             if (cplx) run_mixed<3, true>(c, a);
             else run_mixed<3, false>(c, a);
         } else {
@@ -642,7 +648,10 @@ void launch_matvec(Ctx &c, const MatvecArgs &a) {
             else run_mixed<6, false>(c, a);
         }
     } else {
-        if (c.lay.NP == 3) {
+        if (c.lay.NP == 1) {
+            if (cplx) run_fp64<1, true>(c, a);
+            else run_fp64<1, false>(c, a);
+        } else if (c.lay.NP == 3) {
             if (cplx) run_fp64<3, true>(c, a);
             else run_fp64<3, false>(c, a);
         } else {

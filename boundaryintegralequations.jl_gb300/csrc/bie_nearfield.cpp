@@ -219,6 +219,10 @@ void free_nearfield(NearField &nf) {
 }
 
 NearField &get_nearfield(Ctx &c, int depth, double offset, int n_gauss) {
+    // the reference integrates discontinuous physics near the source with
+    // polar rules (assembly_collocation_losses.jl:409-447), not restated here
+    if (is_discontinuous(c.physics_kind))
+        fail(BIE_ERR_UNSUPPORTED, "the near field takes continuous physics only");
     for (auto &p : c.nearfields)
         if (p->depth == depth && p->offset == offset && p->n_gauss == n_gauss) return *p;
     c.nearfields.emplace_back(new NearField());

@@ -230,9 +230,42 @@ Rule triangle_gauss_rule(int n) {
 }
 
 int n_nodes_of_kind(int kind) {
-    if (kind == BIE_TRI_LINEAR) return 3;
-    if (kind == BIE_TRI_QUADRATIC) return 6;
+    if (kind == BIE_TRI_LINEAR || kind == BIE_TRI_DISC_LINEAR) return 3;
+    if (kind == BIE_TRI_QUADRATIC || kind == BIE_TRI_DISC_QUADRATIC) return 6;
+    if (kind == BIE_TRI_DISC_CONSTANT) return 1;
     fail(BIE_ERR_UNSUPPORTED, "unknown element kind " + std::to_string(kind));
+}
+
+bool is_discontinuous(int kind) {
+    return kind == BIE_TRI_DISC_CONSTANT || kind == BIE_TRI_DISC_LINEAR || kind == BIE_TRI_DISC_QUADRATIC;
+}
+
+void physics_values(int kind, double beta, double u, double v, double *N) {
+    // discontinuous triangles (src/3d/surface_functions.jl:236-318): the
+    // continuous bases in psi(s) = (s - beta) / (1 - 3 beta) of the
+    // barycentric coordinates
+    if (kind == BIE_TRI_DISC_CONSTANT) {
+        N[0] = 1.0;
+        return;
+    }
+    if (kind != BIE_TRI_DISC_LINEAR && kind != BIE_TRI_DISC_QUADRATIC) {
+        shape_values(kind, u, v, N);
+        return;
+    }
+    const double den = 1.0 - 3.0 * beta;
+    const double p3 = (((1.0 - u) - v) - beta) / den, pu = (u - beta) / den, pv = (v - beta) / den;
+    if (kind == BIE_TRI_DISC_LINEAR) {
+        N[0] = p3;
+        N[1] = pu;
+        N[2] = pv;
+    } else {
+        N[0] = p3 * (2.0 * p3 - 1.0);
+        N[1] = pu * (2.0 * pu - 1.0);
+        N[2] = pv * (2.0 * pv - 1.0);
+        N[3] = 4.0 * pu * p3;
+        N[4] = 4.0 * pu * pv;
+        N[5] = 4.0 * pv * p3;
+    }
 }
 
 void shape_values(int kind, double u, double v, double *N) {
@@ -355,19 +388,30 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
         fail(BIE_ERR_INVALID, "mesh arrays must not be NULL");
     if (d.n_coordinates > INT32_MAX || d.n_sources > INT32_MAX || d.n_elements > INT32_MAX)
         fail(BIE_ERR_INVALID, "mesh too large for 32-bit node indices");
+    if (d.shape_kind != BIE_TRI_LINEAR && d.shape_kind != BIE_TRI_QUADRATIC)
+        fail(BIE_ERR_UNSUPPORTED, "geometry must be 3- or 6-node triangles (kind " +
+                                      std::to_string(d.shape_kind) + ")");
     const int NS = n_nodes_of_kind(d.shape_kind);
     const int NP = n_nodes_of_kind(d.physics_kind);
     if (d.shape_kind == BIE_TRI_LINEAR && d.physics_kind == BIE_TRI_QUADRATIC)
         fail(BIE_ERR_UNSUPPORTED, "quadratic physics on linear geometry is not supported");
+    const bool disc = is_discontinuous(d.physics_kind);
+    if (disc && d.physics_kind != BIE_TRI_DISC_CONSTANT &&
+        !(d.physics_beta > 0.0 && d.physics_beta < 1.0 / 3.0))
+        fail(BIE_ERR_INVALID, "physics_beta of discontinuous physics must lie in (0, 1/3)");
     const bool own_rules = gauss_rule <= 0 && !explicit_rules;
     if (own_rules && (d.quad_n < 1 || d.quad_m < 1 || d.quad_n > 32 || d.quad_m > 32))
         fail(BIE_ERR_INVALID, "quad_n and quad_m must be in 1..32");
-    const int R = (d.shape_kind == BIE_TRI_LINEAR) ? 3 : NP;
+    // one rule per physics node; linear geometry has the three corner rules
+    // only, so its nodes 4-6 (6-node discontinuous physics) take corner 3's
+    const int R = NP;
+    const int n_tables = (d.shape_kind == BIE_TRI_LINEAR) ? std::min(NP, 3) : NP;
     if (explicit_rules) {
-        if ((int)explicit_rules->size() != R)
-            fail(BIE_ERR_INVALID, "expected " + std::to_string(R) + " rule tables for this element kind, got " +
+        if ((int)explicit_rules->size() != n_tables)
+            fail(BIE_ERR_INVALID, "expected " + std::to_string(n_tables) +
+                                      " rule tables for this element kind, got " +
                                       std::to_string(explicit_rules->size()));
-        for (int r = 0; r < R; ++r) {
+        for (int r = 0; r < n_tables; ++r) {
             const Rule &t = (*explicit_rules)[r];
             if (t.size() < 1 || t.size() > kMaxQ || (int)t.u.size() != t.size() || (int)t.v.size() != t.size())
                 fail(BIE_ERR_INVALID, "rule table " + std::to_string(r) + " must hold 1.." +
@@ -384,6 +428,7 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     }
     c.shape_kind = d.shape_kind;
     c.physics_kind = d.physics_kind;
+    c.physics_beta = disc ? d.physics_beta : 0.0;
     c.n_coords = d.n_coordinates;
     c.n_elements = d.n_elements;
     c.n_sources = d.n_sources;
@@ -421,11 +466,12 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     // src/3d/fast_multipole_method.jl:163-170), whatever the nearest node.
     c.rules.clear();
     for (int r = 0; r < R; ++r) {
-        if (explicit_rules) c.rules.push_back((*explicit_rules)[r]);
+        const int t = std::min(r, n_tables - 1);
+        if (explicit_rules) c.rules.push_back((*explicit_rules)[t]);
         else if (gauss_rule > 0) c.rules.push_back(triangle_gauss_rule(gauss_rule));
         else
-            c.rules.push_back(r < 3 ? duffy_corner_rule(d.quad_n, d.quad_m, r + 1)
-                                    : duffy_midpoint_rule(d.quad_n, d.quad_m, r + 1));
+            c.rules.push_back(t < 3 ? duffy_corner_rule(d.quad_n, d.quad_m, t + 1)
+                                    : duffy_midpoint_rule(d.quad_n, d.quad_m, t + 1));
     }
     RecordLayout &L = c.lay;
     L = RecordLayout{};
@@ -448,7 +494,7 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     c.phi.assign((size_t)R * L.qmax * NP, 0.0);
     for (int r = 0; r < R; ++r)
         for (int q = 0; q < L.Q[r]; ++q)
-            shape_values(d.physics_kind, c.rules[r].u[q], c.rules[r].v[q],
+            physics_values(d.physics_kind, c.physics_beta, c.rules[r].u[q], c.rules[r].v[q],
                          &c.phi[((size_t)r * L.qmax + q) * NP]);
 
     // ---- element order: Morton order of element centroids -------------------

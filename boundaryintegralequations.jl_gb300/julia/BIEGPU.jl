@@ -46,6 +46,7 @@ struct MeshDesc
     sources::Ptr{Float64}
     quad_n::Int32
     quad_m::Int32
+    physics_beta::Float64
 end
 
 struct BIEError <: Exception
@@ -63,6 +64,16 @@ end
 element_kind(n_nodes::Integer) = n_nodes == 3 ? BIE_TRI_LINEAR :
                                  n_nodes == 6 ? BIE_TRI_QUADRATIC :
                                  throw(ArgumentError("only 3- and 6-node triangles are supported"))
+
+# physics kind and node offset of `mesh.physics_function`: the discontinuous
+# triangles (src/3d/SurfaceFunction.jl:81-105) by type name, else by node count
+function physics_kind(pf, n_nodes::Integer)
+    name = nameof(typeof(pf))
+    name === :DiscontinuousTriangularConstant && return (Int32(3), 0.0)
+    name === :DiscontinuousTriangularLinear && return (Int32(4), Float64(pf.beta))
+    name === :DiscontinuousTriangularQuadratic && return (Int32(5), Float64(pf.beta))
+    return (element_kind(n_nodes), 0.0)
+end
 
 # bie_rule_table (include/biegpu.h)
 struct RuleTable
@@ -92,11 +103,12 @@ mutable struct Context
         ptopo = Matrix{Int64}(mesh.physics_topology)
         src = Matrix{Float64}(mesh.sources)
         h = Ref{Ptr{Cvoid}}(C_NULL)
+        pk, pb = physics_kind(mesh.physics_function, size(ptopo, 1))
         GC.@preserve coords topo ptopo src begin
             desc = Ref(MeshDesc(size(coords, 2), pointer(coords), size(topo, 2),
-                                element_kind(size(topo, 1)), element_kind(size(ptopo, 1)),
+                                element_kind(size(topo, 1)), pk,
                                 pointer(topo), pointer(ptopo), size(src, 2), pointer(src),
-                                Int32(n), Int32(m)))
+                                Int32(n), Int32(m), pb))
             if rules === nothing
                 check(ccall((:bie_ctx_create, libbiegpu), Cint,
                             (Ref{Ptr{Cvoid}}, Ref{MeshDesc}, Cint), h, desc, device))

@@ -49,6 +49,18 @@ extern "C" {
 /* ---- element kinds (Julia: TriangularLinear, TriangularQuadratic) ----- */
 #define BIE_TRI_LINEAR    1   /* 3-node triangle, N = [1-u-v, u, v]            */
 #define BIE_TRI_QUADRATIC 2   /* 6-node triangle, nodes 1 2 3 corners, 4 5 6 mid */
+/* Discontinuous physics (physics_kind only; Julia: DiscontinuousTriangular-
+ * Constant / -Linear / -Quadratic, src/3d/SurfaceFunction.jl:81-105,430-439,
+ * src/3d/surface_functions.jl:236-318).  With b = physics_beta and
+ * psi(s) = (s - b) / (1 - 3 b): constant N = [1] (node at (1/3, 1/3));
+ * linear N = [psi(1-u-v), psi(u), psi(v)] (nodes (b,b), (1-2b,b), (b,1-2b));
+ * quadratic N = the 6-node quadratic basis in those psi (edge nodes
+ * ((1-b)/2, b), ((1-b)/2, (1-b)/2), (b, (1-b)/2)).  The collocation nodes
+ * (`sources`) are the physics nodes of every element, as compute_sources
+ * places them (src/3d/mesh.jl:115-145).                                    */
+#define BIE_TRI_DISC_CONSTANT  3
+#define BIE_TRI_DISC_LINEAR    4
+#define BIE_TRI_DISC_QUADRATIC 5
 
 /* ---- assembly selection flags (Julia keywords fOn, gOn, cOn) ---------- */
 #define BIE_F 1   /* double-layer matrix F  */
@@ -76,6 +88,13 @@ typedef struct bie_ctx bie_ctx;
  * `sources`, `physics_topology` and the element kinds of `shape_function` and
  * `physics_function`.  `quad_n`, `quad_m` are the `n`, `m` keywords of
  * `assemble_parallel!` (src/3d/assembly_collocation.jl:259-260).
+ * The rule used for a (target, element) pair is the one clustered at the
+ * element's physics node nearest to the target (find_closest_corner); for
+ * linear geometry nodes 4-6 of 6-node physics use the rule of corner 3, as
+ * the reference's linear-geometry method does (:330-346).
+ * Dense assembly, operator products, GMRES and sweeps take every kind; the
+ * near-field, fast-operator near-field, lossy, tangential-derivative and
+ * adjoint paths take continuous physics only (BIE_ERR_UNSUPPORTED).
  * The library copies everything it needs; the caller keeps ownership.
  */
 typedef struct bie_mesh_desc {
@@ -90,6 +109,8 @@ typedef struct bie_mesh_desc {
     const double  *sources;           /* 3 x N                                  */
     int32_t        quad_n;            /* Gauss-Legendre points along u (>= 1)   */
     int32_t        quad_m;            /* Gauss-Legendre points along v (>= 1)   */
+    double         physics_beta;      /* node offset b of discontinuous physics
+                                         (0 < b < 1/3); ignored otherwise      */
 } bie_mesh_desc;
 
 /* Library version string, e.g. "biegpu 0.1.0 sm_103a". */
@@ -135,8 +156,9 @@ typedef struct bie_rule_table {
  * bie_ctx_create with the caller's own rule tables instead of the rules built
  * from (quad_n, quad_m), which are then ignored: `rules[r]` is the rule used
  * when element node r+1 is the nearest physics node to the collocation point
- * (n_rules = 3 for linear geometry, = the physics nodes per element, 3 or 6,
- * for quadratic geometry), points summed in table order.  Passing the
+ * (n_rules = min(NP, 3) for linear geometry and NP for quadratic geometry,
+ * NP = physics nodes per element; with linear geometry and NP = 6, nodes 4-6
+ * use table 3), points summed in table order.  Passing the
  * `gauss_u`, `gauss_v`, `weights` of the shape functions that
  * create_rotated_element returns (src/3d/assembly_collocation.jl:122-136,
  * 284-305, 369-413) reproduces the reference's quadrature bit for bit.

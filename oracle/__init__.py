@@ -68,13 +68,21 @@ def lib():
                                                  P, P, P, I]
             L.oracle_singular_rule.restype = I
             L.oracle_singular_rule.argtypes = [I, D, P, P, P, I]
+            L.oracle_set_beta.restype = None
+            L.oracle_set_beta.argtypes = [D]
             L.oracle_nearfield.restype = I
             L.oracle_nearfield.argtypes = [P, P, I, P, I, P, P, I64, I64, D, I, I, D, D, I, P, P, I]
             _lib = L
         return _lib
 
 
-_KIND = {"linear": 1, "quadratic": 2}
+_KIND = {"linear": 1, "quadratic": 2, "disctriconstant": 3, "disctrilinear": 4, "disctriquadratic": 5}
+
+
+def _physics(mesh) -> int:
+    """Physics kind code; sets the node offset of discontinuous kinds."""
+    lib().oracle_set_beta(float(getattr(mesh, "physics_beta", 0.0)))
+    return _KIND[mesh.physics_function]
 
 
 def rule(n: int, m: int, corner: int):
@@ -126,6 +134,8 @@ def connected_sources(mesh, depth: int = 1):
 def nearfield(mesh, k, depth=1, offset=0.0, coarse=False, n_gauss=3, fOn=True, gOn=True, threads=0):
     """Near-field F, G (CSR: row_ptr, cols, values) of sparse_assemble_parallel!
     (coarse=False) or partial_assemble_parallel! (coarse=True)."""
+    if mesh.physics_function.startswith("disc"):
+        raise NotImplementedError("the near field of discontinuous physics (polar rules) is not restated")
     k = complex(k)
     econ, scon = connected_sources(mesh, depth)
     N = mesh.n_sources
@@ -150,7 +160,7 @@ def nearfield(mesh, k, depth=1, offset=0.0, coarse=False, n_gauss=3, fOn=True, g
     s = np.asfortranarray(mesh.sources, dtype=np.float64)
     flags = (1 if fOn else 0) | (2 if gOn else 0)
     st = lib().oracle_nearfield(c.ctypes.data, t.ctypes.data, _KIND[mesh.shape_function], pt.ctypes.data,
-                                _KIND[mesh.physics_function], s.ctypes.data, pairs.ctypes.data,
+                                _physics(mesh), s.ctypes.data, pairs.ctypes.data,
                                 len(pairs), nnz, float(offset), 1 if coarse else 0, int(n_gauss),
                                 k.real, k.imag, flags, F.ctypes.data, G.ctypes.data, int(threads))
     if st != 0:
@@ -192,7 +202,7 @@ def taylor_assemble(mesh, k0, order, targets=None, n=3, m=3, fOn=True, gOn=True,
     flags = (1 if fOn else 0) | (2 if gOn else 0) | (4 if cOn else 0)
     addr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
     st = lib().oracle_taylor_assemble(c.ctypes.data, c.shape[1], t.ctypes.data, _KIND[mesh.shape_function],
-                                      pt.ctypes.data, _KIND[mesh.physics_function], t.shape[1], s.ctypes.data,
+                                      pt.ctypes.data, _physics(mesh), t.shape[1], s.ctypes.data,
                                       N, tg.ctypes.data, M, n, m, k0.real, k0.imag, flags, int(order),
                                       addr(F), addr(G), addr(Cv), int(threads))
     if st != 0:
@@ -236,7 +246,7 @@ def assemble(mesh, k, targets=None, n=4, m=4, fOn=True, gOn=True, cOn=True, thre
     addr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
     gw = None if g_weight is None else np.ascontiguousarray(g_weight, dtype=np.complex128)
     lib().oracle_assemble_w(c.ctypes.data, c.shape[1], t.ctypes.data, _KIND[mesh.shape_function],
-                            pt.ctypes.data, _KIND[mesh.physics_function], t.shape[1], s.ctypes.data,
+                            pt.ctypes.data, _physics(mesh), t.shape[1], s.ctypes.data,
                             N, tg.ctypes.data, M, n, m, k.real, k.imag, flags, addr(F), addr(G),
                             addr(Cv), int(threads), addr(gw))
     return F, G, Cv

@@ -9,6 +9,8 @@
  *   triangularQuadpoints / rotated     src/3d/quadrature.jl:70-113
  *   rotated_midpoint_triangular_...    src/3d/quadrature.jl:116-144
  *   shape functions                    src/3d/surface_functions.jl:191-236
+ *   discontinuous triangle physics     src/3d/surface_functions.jl:236-318,
+ *                                      src/3d/SurfaceFunction.jl:430-439
  *   create_rotated_element             src/3d/assembly_collocation.jl:122-136
  *   interpolate_elements, jacobian!    src/3d/assembly_collocation.jl:27-66, src/3d/jacobian.jl:78-87
  *   find_closest_corner                src/3d/assembly_collocation.jl:102-115
@@ -25,7 +27,7 @@
  * Julia's 3-argument hypot (maximum-abs scaling, used for distances and the
  * nearest-node choice) is restated in julia_hypot3 below.
  *
- * Build: oracle/build.py (gcc -O2 -fopenmp -ffp-contract=off -shared).
+ * Build: oracle.build() in oracle/__init__.py (gcc -O2 -fopenmp -ffp-contract=off -shared).
  */
 #include <complex.h>
 #include <math.h>
@@ -38,6 +40,9 @@
 
 #define OR_LINEAR 1
 #define OR_QUADRATIC 2
+#define OR_DISC_CONSTANT 3    /* physics only: one node at the centroid            */
+#define OR_DISC_LINEAR 4      /* physics only: psi_k = (s_k - beta) / (1 - 3 beta) */
+#define OR_DISC_QUADRATIC 5   /* physics only: quadratic in the psi_k              */
 #define OR_F 1
 #define OR_G 2
 #define OR_C 4
@@ -169,10 +174,33 @@ int oracle_duffy_rule(int n, int m, double *U, double *V, double *W) {
     return oracle_rule(n, m, 2, U, V, W);
 }
 
-static int nnodes(int kind) { return kind == OR_LINEAR ? 3 : 6; }
+static int nnodes(int kind) {
+    if (kind == OR_DISC_CONSTANT) return 1;
+    return (kind == OR_LINEAR || kind == OR_DISC_LINEAR) ? 3 : 6;
+}
+
+/* node offset beta of the discontinuous kinds (set by the caller per mesh) */
+static double g_beta = 0.0;
+void oracle_set_beta(double beta) { g_beta = beta; }
+
+static double psik(double s) { return (s - g_beta) / (1.0 - 3.0 * g_beta); }
 
 static void basis(int kind, double u, double v, double *N) {
-    if (kind == OR_LINEAR) {
+    if (kind == OR_DISC_CONSTANT) {
+        N[0] = 1.0;
+    } else if (kind == OR_DISC_LINEAR || kind == OR_DISC_QUADRATIC) {
+        const double p3 = psik(1.0 - u - v), pu = psik(u), pv = psik(v);
+        if (kind == OR_DISC_LINEAR) {
+            N[0] = p3; N[1] = pu; N[2] = pv;
+        } else {
+            N[0] = p3 * (2.0 * p3 - 1.0);
+            N[1] = pu * (2.0 * pu - 1.0);
+            N[2] = pv * (2.0 * pv - 1.0);
+            N[3] = 4.0 * pu * p3;
+            N[4] = 4.0 * pu * pv;
+            N[5] = 4.0 * pv * p3;
+        }
+    } else if (kind == OR_LINEAR) {
         N[0] = (1.0 - u) - v; N[1] = u; N[2] = v;
     } else {
         N[0] = ((1.0 - v) - u) * ((1.0 - 2.0 * v) - 2.0 * u);
@@ -309,7 +337,9 @@ static int assemble_impl(const double *coords, int64_t Nc, const int64_t *topo, 
         if (-n > 16 || gauss_triangle(-n, tu, tv, tw) <= 0) return -1;
     }
     const int NP = nnodes(pkind);
-    const int R = (skind == OR_LINEAR) ? 3 : NP;
+    /* linear geometry: the three corner rules; quadratic geometry: one rule
+     * per physics node up to 6 (assembly_collocation.jl:287-289, 372-387) */
+    const int R = (skind == OR_LINEAR || NP < 6) ? 3 : 6;
     int Q[6];
     double *U[6], *V[6], *W[6], *PHI[6];
     double *X[6], *NR[6], *JW[6];
@@ -356,9 +386,10 @@ static int assemble_impl(const double *coords, int64_t Nc, const int64_t *topo, 
                 double d = julia_hypot3(P[0] - s[0], P[1] - s[1], P[2] - s[2]);
                 if (d < best) { best = d; c = a; }
             }
-            /* k-derivative assembly: corner rules only, nodes 4-6 -> rule 3
-             * (taylor_assemble!, src/3d/rosebem.jl:114-127) */
-            if (tm >= 0 && c > 2) c = 2;
+            /* the linear-geometry method's if/elseif/else: nodes 4-6 -> rule 3
+             * (assembly_collocation.jl:330-346); the k-derivative assembly uses
+             * the corner rules the same way (taylor_assemble!, src/3d/rosebem.jl:114-127) */
+            if ((tm >= 0 || skind == OR_LINEAR) && c > 2) c = 2;
             const int Qr = Q[c];
             const double *x = X[c] + (size_t)e * 3 * Qr;
             const double *nr = NR[c] + (size_t)e * 3 * Qr;

@@ -138,3 +138,31 @@ def test_ctx_create_rules_rejects_invalid_tables(case):
     assert st == _capi.BIE_ERR_INVALID
     assert h.value is None
     assert len(_capi.lib().bie_last_error()) > 0
+
+
+@pytest.mark.parametrize("beta", [0.0, 1.0 / 3.0, -0.1, float("nan")])
+def test_ctx_create_rejects_bad_discontinuous_beta(beta):
+    """Discontinuous linear/quadratic physics need 0 < beta < 1/3 (checked on
+    the host before any device call)."""
+    mesh = biegpu.icosphere(2, physics="disctrilinear")
+    d, keep = _desc(mesh)
+    d.physics_beta = beta
+    h = C.c_void_p()
+    assert _capi.lib().bie_ctx_create(C.byref(h), C.byref(d), 0) == _capi.BIE_ERR_INVALID
+    assert h.value is None
+
+
+def test_discontinuous_kinds_and_unsupported_host_paths():
+    mesh = biegpu.icosphere(2, geometry="quadratic", physics="disctriquadratic")
+    assert mesh.physics_topology.shape == (6, mesh.n_elements)
+    assert mesh.n_sources == 6 * mesh.n_elements
+    # quadratic geometry: the nodes lie on the sphere (interpolated by the
+    # 6-node map, so only approximately on it)
+    assert np.allclose(np.linalg.norm(mesh.sources, axis=0), 1.0, atol=2e-2)
+    with pytest.raises(biegpu.BIEError) as e:
+        biegpu.tangential_derivatives(mesh)
+    assert e.value.code == _capi.BIE_ERR_UNSUPPORTED
+    # geometry must be a continuous kind
+    d, keep = _desc(mesh, kind=_capi.BIE_TRI_DISC_LINEAR)
+    h = C.c_void_p()
+    assert _capi.lib().bie_ctx_create(C.byref(h), C.byref(d), 0) == _capi.BIE_ERR_UNSUPPORTED

@@ -1,7 +1,8 @@
 """Pins the CPU oracle to the reference's own known-answer tests.
 
 * rigid-sphere scattering error table, test/3d/assembly_test.jl:12-44
-  (continuous physics rows: linear/linear, quadratic/linear, quadratic/geometry)
+  (every geometry x physics entry the reference tests, continuous and
+  discontinuous physics)
 * total quadrature weight = sphere area 4 pi, test/3d/fmm_test.jl:11-28
 * rule weights sum to 1/2, test/3d/surface_functions_test.jl:16,37
 * mesh sizes, test/3d/meshing_test.jl:23
@@ -16,8 +17,11 @@ import oracle.analytic as an
 from biegpu import mesh as bm
 
 # test/3d/assembly_test.jl:22-23 (geometry x physics)
-ERROR_TABLE = {("linear", "linear"): 0.037, ("quadratic", "linear"): 0.048,
-               ("quadratic", "geometry"): 2.8e-5}
+ERROR_TABLE = {("linear", "linear"): 0.037, ("linear", "disctriconstant"): 0.0073,
+               ("linear", "disctrilinear"): 0.0044, ("linear", "disctriquadratic"): 0.004,
+               ("quadratic", "linear"): 0.048, ("quadratic", "geometry"): 2.8e-5,
+               ("quadratic", "disctriconstant"): 0.0008, ("quadratic", "disctrilinear"): 4.2e-4,
+               ("quadratic", "disctriquadratic"): 4.9e-5}
 
 
 @pytest.mark.parametrize("go,po", list(ERROR_TABLE))
