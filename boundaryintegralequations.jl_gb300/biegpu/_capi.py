@@ -211,6 +211,7 @@ SIGNATURES = {
     "bie_version": (C.c_char_p, []),
     "bie_last_error": (C.c_char_p, []),
     "bie_quadrature_rule": (_I, [_I, _I, _I, _P, _P, _P, _I, C.POINTER(_I)]),
+    "bie_basis": (_I, [_I, _D, _I64, _P, _P, _P, _P, _P]),
     "bie_ctx_create": (_I, [C.POINTER(_P), C.POINTER(MeshDesc), _I]),
     "bie_ctx_create_rules": (_I, [C.POINTER(_P), C.POINTER(MeshDesc), C.POINTER(RuleTable), _I, _I]),
     "bie_ctx_destroy": (_I, [_P]),

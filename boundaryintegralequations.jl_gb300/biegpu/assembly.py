@@ -30,6 +30,24 @@ def quadrature_rule(n: int, m: int, node: int):
     return u[:q].copy(), v[:q].copy(), w[:q].copy()
 
 
+def basis(kind: str, u, v, beta: float = 0.0):
+    """(N, dN/du, dN/dv) of element kind ``kind`` ("linear", "quadratic",
+    "disctriconstant", "disctrilinear", "disctriquadratic"; node offset
+    ``beta`` for the discontinuous ones) at the points (u, v), each an
+    n_nodes x len(u) array like basisFunction / basisFunctionDerivative
+    (src/3d/surface_functions.jl:191-318) - bie_basis, host only."""
+    from .mesh import KIND_NODES
+    u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+    v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+    if u.shape != v.shape:
+        raise ValueError("u and v must have the same length")
+    NP = KIND_NODES[kind]
+    out = [np.zeros((NP, u.size), order="F") for _ in range(3)]
+    _capi.check(_capi.lib().bie_basis(_capi.KIND[kind], float(beta), u.size, u.ctypes.data, v.ctypes.data,
+                                      out[0].ctypes.data, out[1].ctypes.data, out[2].ctypes.data))
+    return tuple(out)
+
+
 class Context:
     """A libbiegpu context: one mesh, one quadrature order (n, m), one device.
 

@@ -120,6 +120,26 @@ int bie_quadrature_rule(int n, int m, int node, double *u, double *v, double *w,
     });
 }
 
+int bie_basis(int kind, double beta, int64_t n, const double *u, const double *v, double *N, double *dNu,
+              double *dNv) {
+    return guarded([&] {
+        const int NP = bie::n_nodes_of_kind(kind);
+        if (n < 0 || (n > 0 && (!u || !v))) bie::fail(BIE_ERR_INVALID, "u and v must hold n >= 0 points");
+        if (bie::is_discontinuous(kind) && kind != BIE_TRI_DISC_CONSTANT && !(beta > 0.0 && beta < 1.0 / 3.0))
+            bie::fail(BIE_ERR_INVALID, "beta of discontinuous physics must lie in (0, 1/3)");
+        double nv[6], du[6], dv[6];
+        for (int64_t q = 0; q < n; ++q) {
+            bie::physics_values(kind, beta, u[q], v[q], nv);
+            bie::physics_derivs(kind, beta, u[q], v[q], du, dv);
+            for (int a = 0; a < NP; ++a) {
+                if (N) N[q * NP + a] = nv[a];
+                if (dNu) dNu[q * NP + a] = du[a];
+                if (dNv) dNv[q * NP + a] = dv[a];
+            }
+        }
+    });
+}
+
 int bie_ctx_create(bie_ctx **out, const bie_mesh_desc *desc, int device) {
     return guarded([&] {
         if (!out || !desc) bie::fail(BIE_ERR_INVALID, "out and desc must not be NULL");

@@ -53,6 +53,7 @@ bool is_discontinuous(int kind);
 // physics basis: shape_values for continuous kinds, the discontinuous
 // triangle bases (node offset beta) otherwise
 void physics_values(int kind, double beta, double u, double v, double *N);
+void physics_derivs(int kind, double beta, double u, double v, double *dNu, double *dNv);
 void shape_values(int kind, double u, double v, double *N);
 void shape_derivs(int kind, double u, double v, double *dNu, double *dNv);
 

@@ -284,6 +284,30 @@ void shape_values(int kind, double u, double v, double *N) {
     }
 }
 
+void physics_derivs(int kind, double beta, double u, double v, double *dNu, double *dNv) {
+    // d psi / ds = 1 / (1 - 3 beta) (src/3d/surface_functions.jl:262-318)
+    if (kind == BIE_TRI_DISC_CONSTANT) {
+        dNu[0] = dNv[0] = 0.0;
+        return;
+    }
+    if (kind != BIE_TRI_DISC_LINEAR && kind != BIE_TRI_DISC_QUADRATIC) {
+        shape_derivs(kind, u, v, dNu, dNv);
+        return;
+    }
+    const double den = 1.0 - 3.0 * beta, d = 1.0 / den;
+    if (kind == BIE_TRI_DISC_LINEAR) {
+        dNu[0] = -d; dNu[1] = d; dNu[2] = 0.0;
+        dNv[0] = -d; dNv[1] = 0.0; dNv[2] = d;
+        return;
+    }
+    const double p3 = (((1.0 - u) - v) - beta) / den, pu = (u - beta) / den, pv = (v - beta) / den;
+    const double a3 = -(4.0 * p3 - 1.0) * d;
+    dNu[0] = a3; dNu[1] = (4.0 * pu - 1.0) * d; dNu[2] = 0.0;
+    dNu[3] = 4.0 * d * p3 - 4.0 * pu * d; dNu[4] = 4.0 * d * pv; dNu[5] = -4.0 * pv * d;
+    dNv[0] = a3; dNv[1] = 0.0; dNv[2] = (4.0 * pv - 1.0) * d;
+    dNv[3] = -4.0 * pu * d; dNv[4] = 4.0 * pu * d; dNv[5] = 4.0 * d * p3 - 4.0 * pv * d;
+}
+
 void shape_derivs(int kind, double u, double v, double *dNu, double *dNv) {
     if (kind == BIE_TRI_LINEAR) {
         dNu[0] = -1; dNu[1] = 1; dNu[2] = 0;

@@ -133,6 +133,17 @@ BIE_API int bie_quadrature_rule(int n, int m, int node, double *u, double *v, do
                                 int capacity, int *count);
 
 /*
+ * Basis functions of element kind `kind` (BIE_TRI_* including the
+ * discontinuous kinds, node offset `beta`) and their u- and v-derivatives at
+ * n points: N, dNu, dNv are n_nodes x n column-major (NULL to skip), the
+ * layout of basisFunction / basisFunctionDerivative
+ * (src/3d/surface_functions.jl:191-318).  Host-only (needs no GPU); these are
+ * the values the assembly tabulates at its quadrature points.
+ */
+BIE_API int bie_basis(int kind, double beta, int64_t n, const double *u, const double *v, double *N,
+                      double *dNu, double *dNv);
+
+/*
  * Create a context on CUDA device `device`: validates and uploads the mesh,
  * builds the Duffy rules clustered at each element node and the per-element
  * quadrature geometry (points, unit normals, jacobian x weight).

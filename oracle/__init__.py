@@ -68,6 +68,8 @@ def lib():
                                                  P, P, P, I]
             L.oracle_singular_rule.restype = I
             L.oracle_singular_rule.argtypes = [I, D, P, P, P, I]
+            L.oracle_basis.restype = None
+            L.oracle_basis.argtypes = [I, D, I64, P, P, P]
             L.oracle_set_beta.restype = None
             L.oracle_set_beta.argtypes = [D]
             L.oracle_nearfield.restype = I
@@ -83,6 +85,16 @@ def _physics(mesh) -> int:
     """Physics kind code; sets the node offset of discontinuous kinds."""
     lib().oracle_set_beta(float(getattr(mesh, "physics_beta", 0.0)))
     return _KIND[mesh.physics_function]
+
+
+def basis(kind: str, u, v, beta: float = 0.0):
+    """Basis values (n_nodes x len(u)) of the restated shape functions."""
+    u = np.ascontiguousarray(u, dtype=np.float64).ravel()
+    v = np.ascontiguousarray(v, dtype=np.float64).ravel()
+    nn = {1: 3, 2: 6, 3: 1, 4: 3, 5: 6}[_KIND[kind]]
+    N = np.zeros((nn, u.size), order="F")
+    lib().oracle_basis(_KIND[kind], float(beta), u.size, u.ctypes.data, v.ctypes.data, N.ctypes.data)
+    return N
 
 
 def rule(n: int, m: int, corner: int):

@@ -212,6 +212,14 @@ static void basis(int kind, double u, double v, double *N) {
     }
 }
 
+/* basis values of `kind` at n points (N: nnodes x n, column-major) */
+void oracle_basis(int kind, double beta, int64_t n, const double *u, const double *v, double *N) {
+    const double saved = g_beta;
+    g_beta = beta;
+    for (int64_t q = 0; q < n; ++q) basis(kind, u[q], v[q], N + (size_t)q * nnodes(kind));
+    g_beta = saved;
+}
+
 static void basis_deriv(int kind, double u, double v, double *du, double *dv) {
     if (kind == OR_LINEAR) {
         du[0] = -1; du[1] = 1; du[2] = 0;
