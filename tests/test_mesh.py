@@ -70,6 +70,33 @@ def test_comsol_reader(reference_meshes):
     assert C.shape == (3, 1682) and T.shape == (6, 840)
 
 
+@pytest.mark.parametrize("go", ["linear", "quadratic"])
+@pytest.mark.parametrize("po", ["linear", "quadratic", "disctriconstant", "disctrilinear", "disctriquadratic"])
+def test_comsol_mesh_invariants_every_physics(reference_meshes, go, po):
+    """test/3d/meshing_test.jl:13-44 for every triangle physics: 840 elements,
+    sources = the distinct physics nodes, normals orthogonal to the tangents;
+    discontinuous nodes lie inside their element and its geometry."""
+    if go == "linear" and po == "quadratic":
+        pytest.skip("the reference skips quadratic physics on linear geometry")
+    m = bm.load_comsol(reference_meshes / "sphere_1m", go, "geometry" if po == go else po)
+    assert m.topology.shape[1] == 840 and m.physics_topology.shape[1] == 840
+    assert m.sources.shape == (3, len(np.unique(m.physics_topology)))
+    assert m.normals.shape == m.tangents.shape == m.sangents.shape
+    assert abs(np.sum(m.normals * m.tangents)) <= 1e-12
+    assert abs(np.sum(m.tangents * m.sangents)) <= 1e-12
+    if po.startswith("disc"):
+        NP = {"disctriconstant": 1, "disctrilinear": 3, "disctriquadratic": 6}[po]
+        assert m.n_sources == NP * 840
+        # every node of element e is closer to e's centroid than to any vertex
+        X = m.coordinates[:, m.topology[:3] - 1]          # 3 x 3 x E
+        cen = X.mean(axis=1)
+        S = m.sources[:, m.physics_topology - 1]          # 3 x NP x E
+        dc = np.linalg.norm(S - cen[:, None, :], axis=0)
+        dv = np.min(np.linalg.norm(S[:, :, None, :] - X[:, None, :, :], axis=0), axis=1)
+        assert np.all(dc < np.max(np.linalg.norm(X - cen[:, None, :], axis=0), axis=0))
+        assert np.all(dv > 0.0)
+
+
 def test_comsol_native_reader_matches_python(reference_meshes):
     # the C reader (bie_read_comsol) and the Python reader agree on every
     # triangle fixture the reference ships
