@@ -75,27 +75,43 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, device: int):
+    def __init__(self, device: int, interval_ms: int = 20):
         self.device = device
+        self.interval_ms = interval_ms
         self.proc = None
         self.lines: list[str] = []
+        self._stamped: list[tuple[float, str]] = []
+        self._t0 = self._t1 = None
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.interval_ms)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
+            # the timed region starts once the sampler reports (nvidia-smi
+            # takes a moment to start), so that its samples fall inside it
+            deadline = time.monotonic() + 5.0
+            while not self._stamped and time.monotonic() < deadline and self.proc.poll() is None:
+                time.sleep(0.005)
         except (OSError, FileNotFoundError):
             self.proc = None
+        self._t0 = time.monotonic()
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self._stamped.append((time.monotonic(), line.strip()))
 
     def __exit__(self, *exc):
+        self._t1 = time.monotonic()
+        # keep the samples taken inside the region (the last one before it
+        # when the region was shorter than the sampling interval)
+        inside = [ln for t, ln in self._stamped if self._t0 <= t <= self._t1 + 0.001 * self.interval_ms]
+        if not inside and self._stamped:
+            inside = [self._stamped[-1][1]]
+        self.lines = inside
         if self.proc:
             self.proc.terminate()
             try:
