@@ -33,6 +33,7 @@ BIE_PREC_FP16 = 2
 BIE_PREC_BF16 = 3
 BIE_PREC_FP16_SPLIT = 4
 BIE_PREC_BF16_SPLIT = 5
+BIE_PREC_DF64 = 6
 
 BIE_TRI_DISC_CONSTANT = 3
 BIE_TRI_DISC_LINEAR = 4
@@ -41,7 +42,7 @@ BIE_TRI_DISC_QUADRATIC = 5
 KIND = {"linear": BIE_TRI_LINEAR, "quadratic": BIE_TRI_QUADRATIC, "disctriconstant": BIE_TRI_DISC_CONSTANT,
         "disctrilinear": BIE_TRI_DISC_LINEAR, "disctriquadratic": BIE_TRI_DISC_QUADRATIC}
 PRECISION = {"fp64": BIE_PREC_FP64, "mixed": BIE_PREC_MIXED, "fp16": BIE_PREC_FP16, "bf16": BIE_PREC_BF16,
-             "fp16_split": BIE_PREC_FP16_SPLIT, "bf16_split": BIE_PREC_BF16_SPLIT}
+             "fp16_split": BIE_PREC_FP16_SPLIT, "bf16_split": BIE_PREC_BF16_SPLIT, "df64": BIE_PREC_DF64}
 
 _ERRNAMES = {
     BIE_ERR_INVALID: "invalid argument",

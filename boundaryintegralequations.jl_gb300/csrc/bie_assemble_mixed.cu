@@ -341,6 +341,8 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
 
 }  // namespace
 
+void build_df64_records(Ctx &c, const std::vector<double> &rec64, const std::vector<float> &mrec);
+
 void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
     const RecordLayout &L = c.lay;
     MixedLayout &X = c.mlay;
@@ -410,6 +412,7 @@ void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
     BIE_CUDA(cudaMalloc(&c.d_mphi, phi32.size() * sizeof(float)));
     BIE_CUDA(cudaMemcpy(c.d_mrecords, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice));
     BIE_CUDA(cudaMemcpy(c.d_mphi, phi32.data(), phi32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    build_df64_records(c, rec64, rec);
 }
 
 void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
@@ -498,6 +501,480 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
         }
     }
     run(level);
+}
+
+// ===========================================================================
+// K9: FP64-grade assembly in double-float arithmetic (BIE_PREC_DF64).
+//
+// GB300 runs FP32 FMAs at ~73x its FP64 rate.  K9 keeps K2's structure
+// (thread per target, element records staged in shared memory, near pairs and
+// nearest-node near-ties deferred to the FP64 correction kernel) but evaluates
+// every regular quadrature point in double-float arithmetic (pairs of floats,
+// ~48-bit significand) instead of FP32, so F, G and C agree with the FP64
+// assembly to ~1e-14 relative rather than ~1e-7:
+//   * per pair: D = c_e - t and r0 = |D| in double-float; e^{i k r0} from a
+//     double-float sine/cosine with a quadrant reduction by a four-part pi/2;
+//   * per point: r = |D + o| (o = x_q - c_e stored in double-float), the
+//     phase rotation e^{i k (r - r0)} from Taylor polynomials whose degree the
+//     host picks from k and the largest |o| of the mesh, the kernels of
+//     greens3d! / freens3d! / freens3dk0! (src/3d/kernels.jl:13-55) and the
+//     per-node sums (mygemm_vec!, src/2d/assembly_collocation.jl:142-150)
+//     all in double-float;
+//   * F, G are written as complex128 (the owning thread's read-modify-write,
+//     or FP64 atomics on nodes shared between element slices), C per slice.
+// The Taylor coefficients (-1)^j/(2j)!, (-1)^j/(2j+1)!, 1/j! are stored as
+// hi + lo float pairs (to ~2^-49 relative).
+// ===========================================================================
+namespace {
+
+__constant__ float2 kDfCos[13] = {
+    {0x1.0000000000000p+0f, 0x0.0p+0f}, {-0x1.0000000000000p-1f, 0x0.0p+0f},
+    {0x1.5555560000000p-5f, -0x1.5555560000000p-30f}, {-0x1.6c16c20000000p-10f, 0x1.27d27e0000000p-35f},
+    {0x1.a01a020000000p-16f, -0x1.7f97fa0000000p-42f}, {-0x1.27e4fc0000000p-22f, 0x1.10ec140000000p-47f},
+    {0x1.1eed8e0000000p-29f, 0x1.ff1b120000000p-54f}, {-0x1.93974a0000000p-37f, -0x1.180f940000000p-62f},
+    {0x1.ae7f3e0000000p-45f, 0x1.ccee080000000p-71f}, {-0x1.6827860000000p-53f, -0x1.dcbecc0000000p-80f},
+    {0x1.e542ba0000000p-62f, 0x1.00808a0000000p-88f}, {-0x1.0ce3960000000p-70f, -0x1.b6ff0a0000000p-95f},
+    {0x1.f2cf020000000p-80f, -0x1.a342a20000000p-106f},
+};
+__constant__ float2 kDfSin[13] = {
+    {0x1.0000000000000p+0f, 0x0.0p+0f}, {-0x1.5555560000000p-3f, 0x1.5555560000000p-28f},
+    {0x1.1111120000000p-7f, -0x1.ddddde0000000p-32f}, {-0x1.a01a020000000p-13f, 0x1.7f97fa0000000p-39f},
+    {0x1.71de3a0000000p-19f, 0x1.55b1cc0000000p-45f}, {-0x1.ae64560000000p-26f, -0x1.fd51380000000p-52f},
+    {0x1.6124620000000p-33f, -0x1.8af25e0000000p-58f}, {-0x1.ae7f3e0000000p-41f, -0x1.ccee080000000p-67f},
+    {0x1.952c780000000p-49f, -0x1.f9ea560000000p-74f}, {-0x1.2f49b40000000p-57f, -0x1.a050560000000p-83f},
+    {0x1.71b8f00000000p-66f, -0x1.2461520000000p-91f}, {-0x1.761b420000000p-75f, 0x1.9d38fc0000000p-100f},
+    {0x1.3f3cce0000000p-84f, -0x1.74d02c0000000p-111f},
+};
+__constant__ float2 kDfExp[25] = {
+    {0x1.0000000000000p+0f, 0x0.0p+0f}, {0x1.0000000000000p+0f, 0x0.0p+0f},
+    {0x1.0000000000000p-1f, 0x0.0p+0f}, {0x1.5555560000000p-3f, -0x1.5555560000000p-28f},
+    {0x1.5555560000000p-5f, -0x1.5555560000000p-30f}, {0x1.1111120000000p-7f, -0x1.ddddde0000000p-32f},
+    {0x1.6c16c20000000p-10f, -0x1.27d27e0000000p-35f}, {0x1.a01a020000000p-13f, -0x1.7f97fa0000000p-39f},
+    {0x1.a01a020000000p-16f, -0x1.7f97fa0000000p-42f}, {0x1.71de3a0000000p-19f, 0x1.55b1cc0000000p-45f},
+    {0x1.27e4fc0000000p-22f, -0x1.10ec140000000p-47f}, {0x1.ae64560000000p-26f, 0x1.fd51380000000p-52f},
+    {0x1.1eed8e0000000p-29f, 0x1.ff1b120000000p-54f}, {0x1.6124620000000p-33f, -0x1.8af25e0000000p-58f},
+    {0x1.93974a0000000p-37f, 0x1.180f940000000p-62f}, {0x1.ae7f3e0000000p-41f, 0x1.ccee080000000p-67f},
+    {0x1.ae7f3e0000000p-45f, 0x1.ccee080000000p-71f}, {0x1.952c780000000p-49f, -0x1.f9ea560000000p-74f},
+    {0x1.6827860000000p-53f, 0x1.dcbecc0000000p-80f}, {0x1.2f49b40000000p-57f, 0x1.a050560000000p-83f},
+    {0x1.e542ba0000000p-62f, 0x1.00808a0000000p-88f}, {0x1.71b8f00000000p-66f, -0x1.2461520000000p-91f},
+    {0x1.0ce3960000000p-70f, 0x1.b6ff0a0000000p-95f}, {0x1.761b420000000p-75f, -0x1.9d38fc0000000p-100f},
+    {0x1.f2cf020000000p-80f, -0x1.a342a20000000p-106f},
+};
+constexpr int kDfMaxTrig = 12;   // highest coefficient index of kDfCos / kDfSin
+constexpr int kDfMaxExp = 24;    // of kDfExp
+
+// pi/2 = P1 + P2 + P3 + P4 (P1, P2 with 12 significant bits: n * P1 and
+// n * P2 are exact for |n| < 2^12; the sum is pi/2 to ~2e-25)
+constexpr float kPio2P1 = 0x1.922p+0f;
+constexpr float kPio2P2 = -0x1.2aep-18f;
+constexpr float kPio2P3 = -0x1.de973ep-31f;
+constexpr float kPio2P4 = 0x1.a62634p-58f;
+constexpr float kTwoOverPi = 0x1.45f306p-1f;
+constexpr float kDfMaxPhase = 4000.0f;    // beyond: pair deferred to FP64
+
+namespace dd {
+using dev::df;
+
+__device__ __forceinline__ df add_f(df a, float b) {
+    df s = dev::two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return dev::fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ df neg(df a) { return {-a.hi, -a.lo}; }
+// 1 / a: correctly rounded float reciprocal plus one correction, which
+// squares its error (relative error ~2^-47)
+__device__ __forceinline__ df rcp(df a) {
+    const float q1 = __frcp_rn(a.hi);
+    float r = __fmaf_rn(-a.hi, q1, 1.0f);
+    r = __fmaf_rn(-a.lo, q1, r);
+    return dev::fast_two_sum(q1, __fmul_rn(q1, r));
+}
+// sqrt(a), a > 0: correctly rounded float square root plus one Newton
+// correction whose 1/(2 y) only needs float accuracy (relative error ~2^-46)
+__device__ __forceinline__ df sqrt_df(df a) {
+    const float y = __fsqrt_rn(a.hi);
+    const float e = __fadd_rn(__fmaf_rn(-y, y, a.hi), a.lo);
+    return dev::fast_two_sum(y, __fmul_rn(e, 0.5f * rsqrtf(a.hi)));
+}
+// a * b with the product left unnormalised (hi, lo): for sums that
+// renormalise later
+__device__ __forceinline__ df mul_raw(df a, df b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return {p, e};
+}
+__device__ __forceinline__ df coef(const float2 *c, int j) {
+    const float2 v = c[j];
+    return {v.x, v.y};
+}
+// sum_{j <= J} c_j z^j by Horner's rule
+__device__ __forceinline__ df poly(const float2 *c, int J, df z) {
+    df acc = coef(c, J);
+    for (int j = J - 1; j >= 0; --j) acc = dev::df_add(dev::df_mul(acc, z), coef(c, j));
+    return acc;
+}
+// sin and cos of x (|x| < kDfMaxPhase): x - n pi/2 in double-float, then the
+// Taylor series to x^17 / x^16 on |y| <= pi/4 (truncation below 1e-17)
+__device__ __forceinline__ void sincos_df(df x, df &s, df &c) {
+    const float n = rintf(__fmul_rn(x.hi, kTwoOverPi));
+    df y = add_f(x, -__fmul_rn(n, kPio2P1));
+    y = add_f(y, -__fmul_rn(n, kPio2P2));
+    const float p = __fmul_rn(n, kPio2P3);
+    y = dev::df_sub(y, df{p, __fmaf_rn(n, kPio2P3, -p)});
+    y = add_f(y, -__fmul_rn(n, kPio2P4));
+    const df z = dev::df_sqr(y);
+    const df sn = dev::df_mul(y, poly(kDfSin, 8, z));
+    const df cs = poly(kDfCos, 8, z);
+    const int q = ((int)n) & 3;
+    if (q == 0) { s = sn; c = cs; }
+    else if (q == 1) { s = cs; c = neg(sn); }
+    else if (q == 2) { s = neg(sn); c = neg(cs); }
+    else { s = neg(cs); c = sn; }
+}
+// running sum of double-float terms with the error term carried in float
+// (renormalised once at the end of a pair)
+struct Acc {
+    float hi, lo;
+};
+__device__ __forceinline__ void acc_add(Acc &s, df p) {
+    const df t = dev::two_sum(s.hi, p.hi);
+    s.hi = t.hi;
+    s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, p.lo));
+}
+__device__ __forceinline__ double acc_value(const Acc &s) {
+    return dev::f2d(s.hi) + dev::f2d(s.lo);
+}
+__device__ __forceinline__ df to_df(double x) { return dev::df_from_double(x); }
+}  // namespace dd
+
+struct DfDegrees {
+    int Jc, Js, Je;   // Taylor degrees (coefficient counts - 1) of cos, sin, exp
+};
+
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(kThreads, 2)
+assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
+                     const uint32_t *__restrict__ smask, const float2 *__restrict__ phi, int nphi, int qmax,
+                     RuleInfo ri, const double *__restrict__ tgt, int64_t M, double kre, double kim,
+                     int flags, double2 *__restrict__ F, double2 *__restrict__ G,
+                     double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
+                     unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
+                     DfDegrees deg, unsigned long long *__restrict__ qpe_count) {
+    using dev::df;
+    extern __shared__ __align__(16) float smemf[];
+    float2 *s_phi = reinterpret_cast<float2 *>(smemf);             // nphi (hi, lo) pairs
+    float *s_rec = smemf + ((2 * nphi + 3) & ~3);                     // chunk * stride floats
+    uint32_t *s_mask = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);
+
+    const int s = blockIdx.y;
+    const int64_t e0 = (int64_t)s * E / S;
+    const int64_t e1 = (int64_t)(s + 1) * E / S;
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = i < M;
+    const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
+
+    double tx = 0, ty = 0, tz = 0;
+    if (active) {
+        tx = tgt[3 * i + 0];
+        ty = tgt[3 * i + 1];
+        tz = tgt[3 * i + 2];
+    }
+    const mixed::Target T{dev::df_from_double(tx), dev::df_from_double(ty), dev::df_from_double(tz)};
+    const df K = dd::to_df(kre);
+    const df Ki = dd::to_df(kim);
+    for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+
+    dd::Acc cacc{0.f, 0.f};
+    unsigned long long nqpe = 0;
+    for (int64_t cb = e0; cb < e1; cb += chunk) {
+        const int n = (int)min((int64_t)chunk, e1 - cb);
+        __syncthreads();
+        {
+            const float4 *src = reinterpret_cast<const float4 *>(rec + cb * stride);
+            float4 *dst = reinterpret_cast<float4 *>(s_rec);
+            const int n4 = n * stride / 4;
+            for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
+            for (int t = threadIdx.x; t < n; t += kThreads) s_mask[t] = smask[cb + t];
+        }
+        __syncthreads();
+        if (!active) continue;
+
+        for (int el = 0; el < n; ++el) {
+            const float *r = s_rec + (size_t)el * stride;
+            const mixed::PairSetup P = mixed::pair_setup<NP>(r, T);
+            // r0 = |c_e - t| and the phase k r0 in double-float
+            const df r0 = dd::sqrt_df(dev::df_add(dev::df_add(dev::df_sqr(P.Dxd), dev::df_sqr(P.Dyd)),
+                                                  dev::df_sqr(P.Dzd)));
+            const df kr0 = dev::df_mul(K, r0);
+            if (P.deferred || !(fabsf(kr0.hi) < kDfMaxPhase)) {
+                const unsigned int slot = atomicAdd(defer_count, 1u);
+                if (slot < defer_cap) {
+                    defer[slot] = make_int2((int)i, (int)(cb + el));
+                    continue;
+                }
+                // list full: the pair in FP64 here (slower, same result)
+                const double *r64 = v64.rec + (size_t)(cb + el) * v64.stride;
+                const int cn = dev::nearest_node<NP>(r64, tx, ty, tz);
+                double fr[NP], fi[NP], gr[NP], gi[NP];
+                const double ce = dev::element_fp64<NP, CPLX_K>(r64 + v64.ri.off[cn], v64.ri.Q[cn],
+                                                                 v64.phi + (size_t)cn * v64.qmax * NP, tx, ty,
+                                                                 tz, kre, kim, fr, fi, gr, gi);
+                dd::acc_add(cacc, dd::to_df(ce));
+                const int32_t *nid = reinterpret_cast<const int32_t *>(r64 + v64.nidx_off);
+#pragma unroll
+                for (int a = 0; a < NP; ++a) {
+                    const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
+                    if (doF) add_entry(F + off, fr[a], fi[a]);
+                    if (doG) add_entry(G + off, gr[a], gi[a]);
+                }
+                continue;
+            }
+            // E0 = e^{i k r0} (times e^{-Im k r0})
+            df E0r, E0i;
+            dd::sincos_df(kr0, E0i, E0r);
+            if (CPLX_K) {
+                const df damp = dd::to_df(exp(-kim * (dev::f2d(r0.hi) + dev::f2d(r0.lo))));
+                E0r = dev::df_mul(E0r, damp);
+                E0i = dev::df_mul(E0i, damp);
+            }
+            const int c = P.c;
+            const int Q = ri.Q[c];
+            nqpe += Q;
+            const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
+            const float2 *phc = s_phi + (size_t)c * qmax * NP;
+            dd::Acc fr[NP], fi[NP], gr[NP], gi[NP];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = dd::Acc{0.f, 0.f};
+            dd::Acc ce{0.f, 0.f};
+            for (int q = 0; q < Q; ++q) {
+                const float4 A = g4[4 * q], B = g4[4 * q + 1], Cn = g4[4 * q + 2], Dn = g4[4 * q + 3];
+                const df dx = dev::df_add(P.Dxd, df{A.x, B.x});
+                const df dy = dev::df_add(P.Dyd, df{A.y, B.y});
+                const df dz = dev::df_add(P.Dzd, df{A.z, B.z});
+                const df rr = dd::sqrt_df(dev::df_add(dev::df_add(dev::df_sqr(dx), dev::df_sqr(dy)),
+                                                      dev::df_sqr(dz)));
+                const df ri_ = dd::rcp(rr);
+                // e^{i k (r - r0)}
+                const df th = dev::df_mul(K, dev::df_sub(rr, r0));
+                const df z = dev::df_sqr(th);
+                df ct = dd::poly(kDfCos, deg.Jc, z);
+                df st = dev::df_mul(th, dd::poly(kDfSin, deg.Js, z));
+                if (CPLX_K) {
+                    const df damp = dd::poly(kDfExp, deg.Je, dd::neg(dev::df_mul(Ki, dev::df_sub(rr, r0))));
+                    ct = dev::df_mul(ct, damp);
+                    st = dev::df_mul(st, damp);
+                }
+                const df er = dev::df_sub(dev::df_mul(E0r, ct), dev::df_mul(E0i, st));
+                const df ei = dev::df_add(dev::df_mul(E0r, st), dev::df_mul(E0i, ct));
+                // G = e jw / (4 pi r); t = (x - y).n jw / (4 pi r^3)
+                const df sw = dev::df_mul(df{A.w, B.w}, ri_);
+                const df Gr = dev::df_mul(er, sw), Gi = dev::df_mul(ei, sw);
+                const df dn = dev::df_add(dev::df_add(dev::df_mul(dx, df{Cn.x, Dn.x}), dev::df_mul(dy, df{Cn.y, Dn.y})),
+                                          dev::df_mul(dz, df{Cn.z, Dn.z}));
+                const df tq = dev::df_mul(dev::df_mul(dn, sw), dev::df_sqr(ri_));
+                dd::acc_add(ce, tq);
+                // F = e (i k r - 1) t
+                const df kr = dev::df_mul(K, rr);
+                df ar = {-1.0f, 0.0f};
+                if (CPLX_K) ar = dev::df_sub(ar, dev::df_mul(Ki, rr));
+                const df Fr = dev::df_mul(dev::df_sub(dev::df_mul(er, ar), dev::df_mul(ei, kr)), tq);
+                const df Fi = dev::df_mul(dev::df_add(dev::df_mul(er, kr), dev::df_mul(ei, ar)), tq);
+                const float2 *pq = phc + q * NP;
+#pragma unroll
+                for (int a = 0; a < NP; ++a) {
+                    const float2 pv = pq[a];
+                    const df ph{pv.x, pv.y};
+                    dd::acc_add(fr[a], dd::mul_raw(Fr, ph));
+                    dd::acc_add(fi[a], dd::mul_raw(Fi, ph));
+                    dd::acc_add(gr[a], dd::mul_raw(Gr, ph));
+                    dd::acc_add(gi[a], dd::mul_raw(Gi, ph));
+                }
+            }
+            // C = -sum t
+            dd::acc_add(cacc, dd::neg(dev::fast_two_sum(ce.hi, ce.lo)));
+            const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
+            const uint32_t m = s_mask[el];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
+                if ((m >> a) & 1u) {
+                    if (doF) add_entry(F + off, dd::acc_value(fr[a]), dd::acc_value(fi[a]));
+                    if (doG) add_entry(G + off, dd::acc_value(gr[a]), dd::acc_value(gi[a]));
+                } else {
+                    if (doF) {
+                        double2 w = F[off];
+                        w.x += dd::acc_value(fr[a]);
+                        w.y += dd::acc_value(fi[a]);
+                        F[off] = w;
+                    }
+                    if (doG) {
+                        double2 w = G[off];
+                        w.x += dd::acc_value(gr[a]);
+                        w.y += dd::acc_value(gi[a]);
+                        G[off] = w;
+                    }
+                }
+            }
+        }
+    }
+    if (active && doC) Cpart[(int64_t)s * M + i] = dd::acc_value(cacc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+// Taylor degrees for |k (r - r0)| <= theta (and |Im k (r - r0)| <= kappa):
+// the first omitted term below 2^-53; false if a table is too short
+bool df_degrees(double theta, double kappa, DfDegrees &d) {
+    auto need = [](double x, int first, int step, int jmax, int &J) {
+        // term index n = first + step * j; stop once x^n / n! < 2^-53
+        for (int j = 0; j <= jmax; ++j) {
+            const int n = first + step * (j + 1);
+            double t = 1.0;
+            for (int m = 1; m <= n; ++m) t *= x / m;
+            if (t < 0x1p-53) {
+                J = j;
+                return true;
+            }
+        }
+        return false;
+    };
+    return need(theta, 0, 2, kDfMaxTrig, d.Jc) && need(theta, 1, 2, kDfMaxTrig, d.Js) &&
+           need(kappa, 0, 1, kDfMaxExp, d.Je);
+}
+
+template <int NP, bool CPLX>
+void launch_df64_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem, int chunk, double *Cpart,
+                    int2 *defer, unsigned int *dcount, unsigned int dcap, double *Cnear, DfDegrees deg) {
+    const RecordLayout &L = c.lay;
+    const Df64Layout &X = c.dlay;
+    RuleInfo ri{}, ri64{};
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = L.Q[r];
+        ri.off[r] = X.rule_off[r];
+        ri64.Q[r] = L.Q[r];
+        ri64.off[r] = L.rule_off[r];
+    }
+    Fp64View v{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
+    auto kern = assemble_df64_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((a.M + kThreads - 1) / kThreads), (unsigned)S);
+    cudaEvent_t t0 = c.timer_begin();
+    kern<<<grid, kThreads, smem, c.stream>>>(
+        c.d_drecords, X.stride, X.nidx_off, c.n_elements, S, c.d_shared_mask + (size_t)level * c.n_elements,
+        reinterpret_cast<const float2 *>(c.d_dphi), L.R * L.qmax * NP, L.qmax, ri, a.targets, a.M, a.k_re,
+        a.k_im, a.flags, reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cpart, chunk, defer,
+        dcount, dcap, v, deg, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    c.timer_end(t0);
+    ++c.kernel_launches;
+    correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+        defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
+        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, nullptr);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+}
+
+}  // namespace
+
+void build_df64_records(Ctx &c, const std::vector<double> &rec64, const std::vector<float> &mrec) {
+    const RecordLayout &L = c.lay;
+    Df64Layout &X = c.dlay;
+    X = Df64Layout{};
+    const int NP = L.NP;
+    // header as the mixed records (centroid hi/lo, near radius^2, node offsets)
+    int off = (8 + 3 * NP + 3) & ~3;
+    for (int r = 0; r < L.R; ++r) {
+        X.rule_off[r] = off;
+        off += 16 * L.Q[r];
+    }
+    X.nidx_off = off;
+    off += NP;
+    X.stride = (off + 3) & ~3;
+    const int64_t E = c.n_elements;
+    std::vector<float> rec((size_t)E * X.stride, 0.f);
+    auto split = [](double x, float &hi, float &lo) {
+        hi = (float)x;
+        lo = (float)(x - (double)hi);
+    };
+    double rho = 0.0;
+    for (int64_t p = 0; p < E; ++p) {
+        const float *M0 = &mrec[(size_t)p * c.mlay.stride];
+        const double *R0 = &rec64[(size_t)p * L.stride];
+        float *W = &rec[(size_t)p * X.stride];
+        std::copy(M0, M0 + 8 + 3 * NP, W);
+        const double cen[3] = {(double)M0[0] + (double)M0[3], (double)M0[1] + (double)M0[4],
+                               (double)M0[2] + (double)M0[5]};
+        for (int r = 0; r < L.R; ++r) {
+            const int Q = L.Q[r];
+            const double *g = R0 + L.rule_off[r];
+            float *w = W + X.rule_off[r];
+            for (int q = 0; q < Q; ++q) {
+                float *P = w + 16 * q;
+                const double o[3] = {g[q] - cen[0], g[Q + q] - cen[1], g[2 * Q + q] - cen[2]};
+                rho = std::max(rho, std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]));
+                // (ox oy oz jw/4pi)_hi, (...)_lo, (nx ny nz 0)_hi, (...)_lo
+                split(o[0], P[0], P[4]);
+                split(o[1], P[1], P[5]);
+                split(o[2], P[2], P[6]);
+                split(g[6 * Q + q] * 0.079577471545947667884, P[3], P[7]);
+                split(g[3 * Q + q], P[8], P[12]);
+                split(g[4 * Q + q], P[9], P[13]);
+                split(g[5 * Q + q], P[10], P[14]);
+            }
+        }
+        std::copy(M0 + c.mlay.nidx_off, M0 + c.mlay.nidx_off + NP, W + X.nidx_off);
+    }
+    c.df_rho_max = rho;
+    std::vector<float> phi((size_t)L.R * L.qmax * NP * 2, 0.f);
+    for (size_t j = 0; j < (size_t)L.R * L.qmax * NP; ++j) split(c.phi[j], phi[2 * j], phi[2 * j + 1]);
+    BIE_CUDA(cudaMalloc(&c.d_drecords, rec.size() * sizeof(float)));
+    BIE_CUDA(cudaMalloc(&c.d_dphi, phi.size() * sizeof(float)));
+    BIE_CUDA(cudaMemcpy(c.d_drecords, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMemcpy(c.d_dphi, phi.data(), phi.size() * sizeof(float), cudaMemcpyHostToDevice));
+}
+
+bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
+    const RecordLayout &L = c.lay;
+    if (a.g_weight || a.taylor_m >= 0 || a.k_dev) return false;
+    DfDegrees deg{};
+    const double kabs = std::hypot(a.k_re, a.k_im);
+    if (!df_degrees(kabs * c.df_rho_max, std::fabs(a.k_im) * c.df_rho_max, deg)) return false;
+    const int64_t N = c.n_sources;
+    if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
+    if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));
+    if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return true;
+
+    const unsigned int dcap = (unsigned int)std::min<int64_t>(a.M * 64 + 4096, (int64_t)1 << 30);
+    const size_t dbytes = (size_t)dcap * sizeof(int2);
+    char *dbuf = static_cast<char *>(c.scratch(kScratchDefer, dbytes + 256 + (size_t)a.M * 8));
+    int2 *defer = reinterpret_cast<int2 *>(dbuf);
+    unsigned int *dcount = reinterpret_cast<unsigned int *>(dbuf + dbytes);
+    double *Cnear = reinterpret_cast<double *>(dbuf + dbytes + 256);
+    BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
+
+    const int level = choose_slice_level(c, a.M, kThreads);
+    const int S = 1 << level;
+    const size_t rec_bytes = (size_t)c.dlay.stride * sizeof(float);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(32, (32u << 10) / rec_bytes));
+    const size_t phi_f = (size_t)((2 * L.R * L.qmax * L.NP + 3) & ~3);
+    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes + (size_t)chunk * 4;
+    double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
+    const bool cplx = a.k_im != 0.0;
+    if (L.NP == 1) {
+        if (cplx) launch_df64_np<1, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+        else launch_df64_np<1, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+    } else if (L.NP == 3) {
+        if (cplx) launch_df64_np<3, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+        else launch_df64_np<3, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+    } else {
+        if (cplx) launch_df64_np<6, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+        else launch_df64_np<6, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+    }
+    if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
+    return true;
 }
 
 }  // namespace bie

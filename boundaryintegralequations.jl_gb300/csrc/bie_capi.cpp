@@ -54,7 +54,7 @@ void check_assemble_args(bie::Ctx &c, double kr, double ki, int64_t M, int flags
     if (!std::isfinite(kr) || !std::isfinite(ki)) bie::fail(BIE_ERR_INVALID, "k must be finite");
     if (M <= 0) bie::fail(BIE_ERR_INVALID, "number of targets must be positive");
     if (flags & ~(BIE_F | BIE_G | BIE_C)) bie::fail(BIE_ERR_INVALID, "unknown flag bits");
-    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED)
+    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED && precision != BIE_PREC_DF64)
         bie::fail(BIE_ERR_INVALID, "unknown precision");
     if ((flags & BIE_F) && !F) bie::fail(BIE_ERR_INVALID, "F requested but NULL");
     if ((flags & BIE_G) && !G) bie::fail(BIE_ERR_INVALID, "G requested but NULL");
@@ -78,6 +78,7 @@ void check_matvec_args(bie::Ctx &c, double kr, double ki, int64_t M, int precisi
 
 void run_assemble(bie::Ctx &c, const bie::AssembleArgs &a, int precision) {
     if (precision == BIE_PREC_MIXED) bie::launch_assemble_mixed(c, a);
+    else if (precision == BIE_PREC_DF64 && bie::launch_assemble_df64(c, a)) return;
     else bie::launch_assemble_fp64(c, a);
 }
 

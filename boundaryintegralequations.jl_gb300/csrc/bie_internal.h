@@ -112,6 +112,16 @@ struct MixedLayout {
     int stride = 0;
 };
 
+// Double-float element records (K9, BIE_PREC_DF64): the mixed header (centroid
+// hi/lo, near radius^2, FP32 node offsets), then per rule and point 16 floats
+// (o = x_q - c_e and jw / 4 pi as hi, lo; the unit normal as hi, lo), then the
+// physics node indices.
+struct Df64Layout {
+    int rule_off[kMaxRules] = {};
+    int nidx_off = 0;
+    int stride = 0;
+};
+
 // Near-field (sparse) structure for one (depth, offset, n_gauss): CSR pattern of
 // connected nodes per collocation node, the (row, element, CSR slots) pairs and
 // the rule tables (adaptive singular rules per element node + the coarse
@@ -174,6 +184,10 @@ struct Ctx {
     MixedLayout mlay;
     float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)
+    Df64Layout dlay;
+    float *d_drecords = nullptr;         // E x dlay.stride words, Morton order
+    float *d_dphi = nullptr;             // R x qmax x NP (hi, lo) pairs
+    double df_rho_max = 0.0;             // largest |x_q - c_e| over the mesh
     double *d_coords = nullptr;          // 3 x Nc geometry nodes (near-field kernels)
     int32_t *d_topo = nullptr;           // NS x E, 0-based
     std::vector<std::unique_ptr<NearField>> nearfields;
@@ -414,6 +428,10 @@ void launch_nearfield(Ctx &c, const NearField &nf, double k_re, double k_im, int
 // host: builds d_mrecords / d_mphi from the FP64 records (E x lay.stride) and uploads them
 void build_mixed_records(Ctx &c, const std::vector<double> &rec64);
 void launch_assemble_mixed(Ctx &c, const AssembleArgs &a);
+// Double-float assembly (K9); false when the arguments need the FP64 kernel
+// (element factors, k-derivatives, device-resident k, or phase rotations
+// beyond the Taylor tables)
+bool launch_assemble_df64(Ctx &c, const AssembleArgs &a);
 
 // FMA throughput probe (bie_peaks.cu)
 void measure_peaks(int device, bie_peaks &out);

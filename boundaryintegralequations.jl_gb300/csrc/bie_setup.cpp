@@ -657,6 +657,10 @@ void destroy_context(Ctx &c) {
     cudaFree(c.d_mphi);
     c.d_mrecords = nullptr;
     c.d_mphi = nullptr;
+    cudaFree(c.d_drecords);
+    cudaFree(c.d_dphi);
+    c.d_drecords = nullptr;
+    c.d_dphi = nullptr;
     for (auto &nf : c.nearfields) free_nearfield(*nf);
     c.nearfields.clear();
     cudaFree(c.d_coords);

@@ -1,0 +1,90 @@
+"""Double-float assembly (BIE_PREC_DF64, kernel K9) against the CPU oracle
+and the FP64 GPU assembly.  Tolerance: the FP64 parity bar, <= 1e-12 relative
+Frobenius error against the oracle for F, G and C (the double-float
+arithmetic itself is good to ~1e-14), on linear and quadratic geometry,
+continuous and discontinuous physics, real and complex k, collocation and
+field points."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import biegpu
+import oracle
+from biegpu import mesh as bm
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def check(mesh, k, n=2, m=2, targets=None, tol=TOL):
+    F, G, C = biegpu.assemble_parallel(mesh, k, targets, n=n, m=m, precision="df64")
+    Fo, Go, Co = oracle.assemble(mesh, k, targets=targets, n=n, m=m)
+    errs = {name: rel(a, b) for a, b, name in [(F, Fo, "F"), (G, Go, "G"), (C, Co, "C")]}
+    for name, e in errs.items():
+        assert e <= tol, f"{name}: {e:.3e}"
+    return errs
+
+
+@pytest.mark.parametrize("geo,phys,f,k", [("linear", "geometry", 6, 3.0), ("linear", "geometry", 4, 0.5),
+                                          ("quadratic", "geometry", 4, 5.0), ("quadratic", "linear", 4, 2.0),
+                                          ("linear", "disctrilinear", 3, 2.5),
+                                          ("quadratic", "disctriquadratic", 2, 2.0),
+                                          ("linear", "disctriconstant", 4, 1.0)])
+def test_df64_matches_oracle(geo, phys, f, k):
+    errs = check(bm.icosphere(f, geometry=geo, physics=phys), k)
+    # well inside the FP64 bar: the double-float arithmetic is good to ~1e-14
+    assert max(errs.values()) <= 1e-13
+
+
+@pytest.mark.parametrize("k", [1.0 + 0.5j, 3.0 + 0.2j])
+def test_df64_complex_wavenumber(k):
+    check(bm.icosphere(5), k)
+    check(bm.icosphere(3, geometry="quadratic"), k)
+
+
+def test_df64_field_points_and_quadrature_orders():
+    z = np.linspace(0.1, 0.9, 20)
+    X = np.vstack([0.02 + 0 * z, 0.05 + 0 * z, z])
+    check(bm.icosphere(5), 2.0, targets=X)
+    check(bm.icosphere(3, geometry="quadratic"), 2.0, n=4, m=4)
+    check(bm.ellipsoid(5), 4.0, n=3, m=2)
+    # far field points (radius 10): phases k r up to ~60.  C (the solid-angle
+    # term) vanishes there up to the quadrature error (~1e-12), so it is
+    # compared absolutely against the size of its terms (~1e-5)
+    rng = np.random.default_rng(2)
+    Y = rng.normal(size=(3, 16))
+    Y *= 10.0 / np.linalg.norm(Y, axis=0)
+    mesh = bm.ellipsoid(5)
+    F, G, C = biegpu.assemble_parallel(mesh, 6.0, Y, n=2, m=2, precision="df64")
+    Fo, Go, Co = oracle.assemble(mesh, 6.0, targets=Y, n=2, m=2)
+    assert rel(F, Fo) <= TOL and rel(G, Go) <= TOL
+    assert np.max(np.abs(C - Co)) <= 1e-16
+
+
+def test_df64_matches_fp64_gpu_at_size():
+    """A 4842-node P2-geometry ellipsoid at ka = 10: df64 against the FP64
+    kernel (<= 1e-13; the two differ only in arithmetic)."""
+    mesh = bm.icosphere(11, geometry="quadratic", axes=(1.0, 2 / 3, 1 / 3))
+    F, G, C = biegpu.assemble_parallel(mesh, 10.0, n=2, m=2, precision="df64")
+    F64, G64, C64 = biegpu.assemble_parallel(mesh, 10.0, n=2, m=2, precision="fp64")
+    assert max(rel(F, F64), rel(G, G64), rel(C, C64)) <= 1e-13
+
+
+def test_df64_falls_back_to_fp64_for_large_element_phase():
+    """|k| x element radius beyond the Taylor tables: the FP64 kernel runs
+    instead (same result)."""
+    mesh = bm.icosphere(2)
+    check(mesh, 60.0)
+
+
+def test_df64_rejects_nothing_the_fp64_path_takes():
+    mesh = bm.icosphere(3)
+    ctx = biegpu.Context(mesh, n=2, m=2)
+    F, G, C = ctx.assemble(1.5, precision="df64", gOn=False)
+    Fo, _, Co = oracle.assemble(mesh, 1.5, n=2, m=2, gOn=False)
+    assert G is None and rel(F, Fo) <= TOL and rel(C, Co) <= TOL
