@@ -224,7 +224,9 @@ def assemble_parallel(mesh: Mesh3d, k, sources=None, fOn=True, gOn=True, cOn=Tru
 
     ``sources`` are the collocation/field points (3 x M); passing
     ``mesh.sources`` (or None) assembles the square BEM matrices.  ``progress``
-    is accepted and ignored.  ``sparse=True`` (the near-field-only assembly)
+    is accepted and ignored.  ``precision``: "fp64" (the reference's
+    arithmetic), "mixed" (FP32 regular pairs, ~1e-7) or "df64" (double-float
+    regular pairs, FP64-grade ~1e-14, faster than "fp64" on GB300).  ``sparse=True`` (the near-field-only assembly)
     is not part of this library yet and raises.
     """
     if sparse:

@@ -151,8 +151,11 @@ function reference_rules(create_rotated_element, rotated_midpoint_triangular_qua
     end
 end
 
+# :df64 (assembly only): FP64-grade results from double-float arithmetic on
+# the FP32 pipes (BIE_PREC_DF64)
 precision_code(p::Symbol) = p === :fp64 ? BIE_PREC_FP64 : p === :mixed ? BIE_PREC_MIXED :
-                            throw(ArgumentError("precision must be :fp64 or :mixed"))
+                            p === :df64 ? Cint(6) :
+                            throw(ArgumentError("precision must be :fp64, :mixed or :df64"))
 
 """
     assemble_parallel_gpu!(mesh, k, sources; fOn=true, gOn=true, cOn=true, m=4, n=4,
