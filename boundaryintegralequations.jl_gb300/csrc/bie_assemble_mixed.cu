@@ -653,6 +653,33 @@ struct DfDegrees {
     int Jc, Js, Je;   // Taylor degrees (coefficient counts - 1) of cos, sin, exp
 };
 
+// entry (re, im) kept as double-float pairs: += (a, b)
+__device__ __forceinline__ void dd_rmw(float4 *p, const dd::Acc &a, const dd::Acc &b) {
+    float4 w = *p;
+    const dev::df re = dev::df_add(dev::df{w.x, w.y}, dev::fast_two_sum(a.hi, a.lo));
+    const dev::df im = dev::df_add(dev::df{w.z, w.w}, dev::fast_two_sum(b.hi, b.lo));
+    w.x = re.hi;
+    w.y = re.lo;
+    w.z = im.hi;
+    w.w = im.lo;
+    *p = w;
+}
+
+// complex128 entries of the nodes not shared between element slices held
+// (re_hi, re_lo, im_hi, im_lo) floats during the assembly: widen them in
+// place (entry (i, j) at j M + i; shared nodes already hold doubles)
+__global__ void df_widen_kernel(double2 *__restrict__ F, int64_t M, int64_t N,
+                                const uint8_t *__restrict__ node_shared) {
+    const int64_t total = M * N;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
+        const int64_t j = t / M;
+        if (node_shared[j]) continue;
+        const float4 w = reinterpret_cast<const float4 *>(F)[t];
+        F[t] = make_double2(dev::f2d(w.x) + dev::f2d(w.y), dev::f2d(w.z) + dev::f2d(w.w));
+    }
+}
+
 template <int NP, bool CPLX_K>
 __global__ void __launch_bounds__(kThreads, 2)
 assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
@@ -723,11 +750,21 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                                                                  tz, kre, kim, fr, fi, gr, gi);
                 dd::acc_add(cacc, dd::to_df(ce));
                 const int32_t *nid = reinterpret_cast<const int32_t *>(r64 + v64.nidx_off);
+                const uint32_t m = s_mask[el];
+                auto acc_of = [](double x) {
+                    const df t = dd::to_df(x);
+                    return dd::Acc{t.hi, t.lo};
+                };
 #pragma unroll
                 for (int a = 0; a < NP; ++a) {
                     const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
-                    if (doF) add_entry(F + off, fr[a], fi[a]);
-                    if (doG) add_entry(G + off, gr[a], gi[a]);
+                    if ((m >> a) & 1u) {
+                        if (doF) add_entry(F + off, fr[a], fi[a]);
+                        if (doG) add_entry(G + off, gr[a], gi[a]);
+                    } else {   // float-pair entry (see below)
+                        if (doF) dd_rmw(reinterpret_cast<float4 *>(F + off), acc_of(fr[a]), acc_of(fi[a]));
+                        if (doG) dd_rmw(reinterpret_cast<float4 *>(G + off), acc_of(gr[a]), acc_of(gi[a]));
+                    }
                 }
                 continue;
             }
@@ -800,21 +837,15 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
             for (int a = 0; a < NP; ++a) {
                 const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
                 if ((m >> a) & 1u) {
+                    // node shared with another element slice: FP64 atomics into
+                    // the complex128 entry
                     if (doF) add_entry(F + off, dd::acc_value(fr[a]), dd::acc_value(fi[a]));
                     if (doG) add_entry(G + off, dd::acc_value(gr[a]), dd::acc_value(gi[a]));
                 } else {
-                    if (doF) {
-                        double2 w = F[off];
-                        w.x += dd::acc_value(fr[a]);
-                        w.y += dd::acc_value(fi[a]);
-                        F[off] = w;
-                    }
-                    if (doG) {
-                        double2 w = G[off];
-                        w.x += dd::acc_value(gr[a]);
-                        w.y += dd::acc_value(gi[a]);
-                        G[off] = w;
-                    }
+                    // owned by this thread: the entry holds (re_hi, re_lo, im_hi,
+                    // im_lo) floats until df_widen_kernel, no FP64 instruction here
+                    if (doF) dd_rmw(reinterpret_cast<float4 *>(F + off), fr[a], fi[a]);
+                    if (doG) dd_rmw(reinterpret_cast<float4 *>(G + off), gr[a], gi[a]);
                 }
             }
         }
@@ -870,6 +901,15 @@ void launch_df64_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;
+    const uint8_t *nsh = c.d_node_shared + (size_t)level * c.n_sources;
+    const unsigned wgrid = (unsigned)std::min<int64_t>((a.M * c.n_sources + 255) / 256, 16LL * c.num_sms);
+    for (double *X : {a.F, a.G}) {
+        if (!X) continue;
+        df_widen_kernel<<<std::max(1u, wgrid), 256, 0, c.stream>>>(reinterpret_cast<double2 *>(X), a.M,
+                                                                    c.n_sources, nsh);
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
     correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
         defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
         reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, nullptr);

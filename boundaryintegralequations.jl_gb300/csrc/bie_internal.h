@@ -181,6 +181,7 @@ struct Ctx {
     double *d_sources = nullptr;         // 3 x N (AoS)
     uint32_t *d_shared_mask = nullptr;   // kMaxLevels x E: bit a set -> node a is
                                          // touched by elements of another slice
+    uint8_t *d_node_shared = nullptr;    // kMaxLevels x N: the same per node
     MixedLayout mlay;
     float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)

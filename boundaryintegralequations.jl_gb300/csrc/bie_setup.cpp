@@ -597,6 +597,7 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     std::vector<uint32_t> masks((size_t)kMaxLevels * E, 0u);
     std::vector<int32_t> first(d.n_sources);
     std::vector<uint8_t> shared(d.n_sources);
+    std::vector<uint8_t> node_shared((size_t)kMaxLevels * d.n_sources);
     for (int l = 0; l < kMaxLevels; ++l) {
         const int64_t S = int64_t(1) << l;
         std::fill(first.begin(), first.end(), -1);
@@ -619,6 +620,7 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
                 if (shared[c.ptopo[NP * e + a]]) m |= 1u << a;
             masks[(size_t)l * E + p] = m;
         }
+        std::copy(shared.begin(), shared.end(), node_shared.begin() + (size_t)l * d.n_sources);
     }
 
     // ---- device upload --------------------------------------------------------
@@ -635,6 +637,8 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     BIE_CUDA(cudaMalloc(&c.d_phi, c.phi.size() * sizeof(double)));
     BIE_CUDA(cudaMalloc(&c.d_sources, c.sources.size() * sizeof(double)));
     BIE_CUDA(cudaMalloc(&c.d_shared_mask, masks.size() * sizeof(uint32_t)));
+    BIE_CUDA(cudaMalloc(&c.d_node_shared, node_shared.size()));
+    BIE_CUDA(cudaMemcpy(c.d_node_shared, node_shared.data(), node_shared.size(), cudaMemcpyHostToDevice));
     BIE_CUDA(cudaMalloc(&c.d_qpe, sizeof(unsigned long long)));
     BIE_CUDA(cudaMemset(c.d_qpe, 0, sizeof(unsigned long long)));
     BIE_CUDA(cudaMemcpy(c.d_records, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -653,6 +657,8 @@ void destroy_context(Ctx &c) {
     cudaFree(c.d_phi);
     cudaFree(c.d_sources);
     cudaFree(c.d_shared_mask);
+    cudaFree(c.d_node_shared);
+    c.d_node_shared = nullptr;
     cudaFree(c.d_mrecords);
     cudaFree(c.d_mphi);
     c.d_mrecords = nullptr;
