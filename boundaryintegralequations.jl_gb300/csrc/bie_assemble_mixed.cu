@@ -680,8 +680,16 @@ __global__ void df_widen_kernel(double2 *__restrict__ F, int64_t M, int64_t N,
     }
 }
 
+#ifndef BIE_K9_MIN_BLOCKS
+#define BIE_K9_MIN_BLOCKS 2   // resident 128-thread blocks per SM (register budget)
+#endif
+#ifndef BIE_K9_UNROLL
+#define BIE_K9_UNROLL 1       // quadrature points interleaved per iteration
+#endif
+constexpr int kK9Unroll = BIE_K9_UNROLL;
+
 template <int NP, bool CPLX_K>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, BIE_K9_MIN_BLOCKS)
 assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
                      const uint32_t *__restrict__ smask, const float2 *__restrict__ phi, int nphi, int qmax,
                      RuleInfo ri, const double *__restrict__ tgt, int64_t M, double kre, double kim,
@@ -785,6 +793,7 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
 #pragma unroll
             for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = dd::Acc{0.f, 0.f};
             dd::Acc ce{0.f, 0.f};
+#pragma unroll(kK9Unroll)
             for (int q = 0; q < Q; ++q) {
                 const float4 A = g4[4 * q], B = g4[4 * q + 1], Cn = g4[4 * q + 2], Dn = g4[4 * q + 3];
                 const df dx = dev::df_add(P.Dxd, df{A.x, B.x});
