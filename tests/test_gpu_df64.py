@@ -88,3 +88,13 @@ def test_df64_rejects_nothing_the_fp64_path_takes():
     F, G, C = ctx.assemble(1.5, precision="df64", gOn=False)
     Fo, _, Co = oracle.assemble(mesh, 1.5, n=2, m=2, gOn=False)
     assert G is None and rel(F, Fo) <= TOL and rel(C, Co) <= TOL
+
+
+def test_df64_host_call_with_row_blocks():
+    """The host-buffer call pipelines row blocks (outputs >= 256 MB): each
+    block is its own double-float assembly with its own widening pass."""
+    mesh = bm.icosphere(24)          # 5762 nodes: 2 x 531 MB of complex128
+    ctx = biegpu.Context(mesh, n=2, m=2)
+    F, G, C = ctx.assemble(2.0, precision="df64")
+    F64, G64, C64 = ctx.assemble(2.0, precision="fp64")
+    assert max(rel(F, F64), rel(G, G64), rel(C, C64)) <= 1e-13
