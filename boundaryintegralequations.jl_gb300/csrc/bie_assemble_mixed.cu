@@ -27,6 +27,7 @@
 #include "bie_internal.h"
 #include "bie_device.cuh"
 #include "bie_mixed.cuh"
+#include "bie_df64.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -527,131 +528,7 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
 // ===========================================================================
 namespace {
 
-__constant__ float2 kDfCos[13] = {
-    {0x1.0000000000000p+0f, 0x0.0p+0f}, {-0x1.0000000000000p-1f, 0x0.0p+0f},
-    {0x1.5555560000000p-5f, -0x1.5555560000000p-30f}, {-0x1.6c16c20000000p-10f, 0x1.27d27e0000000p-35f},
-    {0x1.a01a020000000p-16f, -0x1.7f97fa0000000p-42f}, {-0x1.27e4fc0000000p-22f, 0x1.10ec140000000p-47f},
-    {0x1.1eed8e0000000p-29f, 0x1.ff1b120000000p-54f}, {-0x1.93974a0000000p-37f, -0x1.180f940000000p-62f},
-    {0x1.ae7f3e0000000p-45f, 0x1.ccee080000000p-71f}, {-0x1.6827860000000p-53f, -0x1.dcbecc0000000p-80f},
-    {0x1.e542ba0000000p-62f, 0x1.00808a0000000p-88f}, {-0x1.0ce3960000000p-70f, -0x1.b6ff0a0000000p-95f},
-    {0x1.f2cf020000000p-80f, -0x1.a342a20000000p-106f},
-};
-__constant__ float2 kDfSin[13] = {
-    {0x1.0000000000000p+0f, 0x0.0p+0f}, {-0x1.5555560000000p-3f, 0x1.5555560000000p-28f},
-    {0x1.1111120000000p-7f, -0x1.ddddde0000000p-32f}, {-0x1.a01a020000000p-13f, 0x1.7f97fa0000000p-39f},
-    {0x1.71de3a0000000p-19f, 0x1.55b1cc0000000p-45f}, {-0x1.ae64560000000p-26f, -0x1.fd51380000000p-52f},
-    {0x1.6124620000000p-33f, -0x1.8af25e0000000p-58f}, {-0x1.ae7f3e0000000p-41f, -0x1.ccee080000000p-67f},
-    {0x1.952c780000000p-49f, -0x1.f9ea560000000p-74f}, {-0x1.2f49b40000000p-57f, -0x1.a050560000000p-83f},
-    {0x1.71b8f00000000p-66f, -0x1.2461520000000p-91f}, {-0x1.761b420000000p-75f, 0x1.9d38fc0000000p-100f},
-    {0x1.3f3cce0000000p-84f, -0x1.74d02c0000000p-111f},
-};
-__constant__ float2 kDfExp[25] = {
-    {0x1.0000000000000p+0f, 0x0.0p+0f}, {0x1.0000000000000p+0f, 0x0.0p+0f},
-    {0x1.0000000000000p-1f, 0x0.0p+0f}, {0x1.5555560000000p-3f, -0x1.5555560000000p-28f},
-    {0x1.5555560000000p-5f, -0x1.5555560000000p-30f}, {0x1.1111120000000p-7f, -0x1.ddddde0000000p-32f},
-    {0x1.6c16c20000000p-10f, -0x1.27d27e0000000p-35f}, {0x1.a01a020000000p-13f, -0x1.7f97fa0000000p-39f},
-    {0x1.a01a020000000p-16f, -0x1.7f97fa0000000p-42f}, {0x1.71de3a0000000p-19f, 0x1.55b1cc0000000p-45f},
-    {0x1.27e4fc0000000p-22f, -0x1.10ec140000000p-47f}, {0x1.ae64560000000p-26f, 0x1.fd51380000000p-52f},
-    {0x1.1eed8e0000000p-29f, 0x1.ff1b120000000p-54f}, {0x1.6124620000000p-33f, -0x1.8af25e0000000p-58f},
-    {0x1.93974a0000000p-37f, 0x1.180f940000000p-62f}, {0x1.ae7f3e0000000p-41f, 0x1.ccee080000000p-67f},
-    {0x1.ae7f3e0000000p-45f, 0x1.ccee080000000p-71f}, {0x1.952c780000000p-49f, -0x1.f9ea560000000p-74f},
-    {0x1.6827860000000p-53f, 0x1.dcbecc0000000p-80f}, {0x1.2f49b40000000p-57f, 0x1.a050560000000p-83f},
-    {0x1.e542ba0000000p-62f, 0x1.00808a0000000p-88f}, {0x1.71b8f00000000p-66f, -0x1.2461520000000p-91f},
-    {0x1.0ce3960000000p-70f, 0x1.b6ff0a0000000p-95f}, {0x1.761b420000000p-75f, -0x1.9d38fc0000000p-100f},
-    {0x1.f2cf020000000p-80f, -0x1.a342a20000000p-106f},
-};
-constexpr int kDfMaxTrig = 12;   // highest coefficient index of kDfCos / kDfSin
-constexpr int kDfMaxExp = 24;    // of kDfExp
-
-// pi/2 = P1 + P2 + P3 + P4 (P1, P2 with 12 significant bits: n * P1 and
-// n * P2 are exact for |n| < 2^12; the sum is pi/2 to ~2e-25)
-constexpr float kPio2P1 = 0x1.922p+0f;
-constexpr float kPio2P2 = -0x1.2aep-18f;
-constexpr float kPio2P3 = -0x1.de973ep-31f;
-constexpr float kPio2P4 = 0x1.a62634p-58f;
-constexpr float kTwoOverPi = 0x1.45f306p-1f;
-constexpr float kDfMaxPhase = 4000.0f;    // beyond: pair deferred to FP64
-
-namespace dd {
-using dev::df;
-
-__device__ __forceinline__ df add_f(df a, float b) {
-    df s = dev::two_sum(a.hi, b);
-    s.lo = __fadd_rn(s.lo, a.lo);
-    return dev::fast_two_sum(s.hi, s.lo);
-}
-__device__ __forceinline__ df neg(df a) { return {-a.hi, -a.lo}; }
-// 1 / a: correctly rounded float reciprocal plus one correction, which
-// squares its error (relative error ~2^-47)
-__device__ __forceinline__ df rcp(df a) {
-    const float q1 = __frcp_rn(a.hi);
-    float r = __fmaf_rn(-a.hi, q1, 1.0f);
-    r = __fmaf_rn(-a.lo, q1, r);
-    return dev::fast_two_sum(q1, __fmul_rn(q1, r));
-}
-// sqrt(a), a > 0: correctly rounded float square root plus one Newton
-// correction whose 1/(2 y) only needs float accuracy (relative error ~2^-46)
-__device__ __forceinline__ df sqrt_df(df a) {
-    const float y = __fsqrt_rn(a.hi);
-    const float e = __fadd_rn(__fmaf_rn(-y, y, a.hi), a.lo);
-    return dev::fast_two_sum(y, __fmul_rn(e, 0.5f * rsqrtf(a.hi)));
-}
-// a * b with the product left unnormalised (hi, lo): for sums that
-// renormalise later
-__device__ __forceinline__ df mul_raw(df a, df b) {
-    const float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e = __fmaf_rn(a.hi, b.lo, e);
-    e = __fmaf_rn(a.lo, b.hi, e);
-    return {p, e};
-}
-__device__ __forceinline__ df coef(const float2 *c, int j) {
-    const float2 v = c[j];
-    return {v.x, v.y};
-}
-// sum_{j <= J} c_j z^j by Horner's rule
-__device__ __forceinline__ df poly(const float2 *c, int J, df z) {
-    df acc = coef(c, J);
-    for (int j = J - 1; j >= 0; --j) acc = dev::df_add(dev::df_mul(acc, z), coef(c, j));
-    return acc;
-}
-// sin and cos of x (|x| < kDfMaxPhase): x - n pi/2 in double-float, then the
-// Taylor series to x^17 / x^16 on |y| <= pi/4 (truncation below 1e-17)
-__device__ __forceinline__ void sincos_df(df x, df &s, df &c) {
-    const float n = rintf(__fmul_rn(x.hi, kTwoOverPi));
-    df y = add_f(x, -__fmul_rn(n, kPio2P1));
-    y = add_f(y, -__fmul_rn(n, kPio2P2));
-    const float p = __fmul_rn(n, kPio2P3);
-    y = dev::df_sub(y, df{p, __fmaf_rn(n, kPio2P3, -p)});
-    y = add_f(y, -__fmul_rn(n, kPio2P4));
-    const df z = dev::df_sqr(y);
-    const df sn = dev::df_mul(y, poly(kDfSin, 8, z));
-    const df cs = poly(kDfCos, 8, z);
-    const int q = ((int)n) & 3;
-    if (q == 0) { s = sn; c = cs; }
-    else if (q == 1) { s = cs; c = neg(sn); }
-    else if (q == 2) { s = neg(sn); c = neg(cs); }
-    else { s = neg(cs); c = sn; }
-}
-// running sum of double-float terms with the error term carried in float
-// (renormalised once at the end of a pair)
-struct Acc {
-    float hi, lo;
-};
-__device__ __forceinline__ void acc_add(Acc &s, df p) {
-    const df t = dev::two_sum(s.hi, p.hi);
-    s.hi = t.hi;
-    s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, p.lo));
-}
-__device__ __forceinline__ double acc_value(const Acc &s) {
-    return dev::f2d(s.hi) + dev::f2d(s.lo);
-}
-__device__ __forceinline__ df to_df(double x) { return dev::df_from_double(x); }
-}  // namespace dd
-
-struct DfDegrees {
-    int Jc, Js, Je;   // Taylor degrees (coefficient counts - 1) of cos, sin, exp
-};
+using namespace df64;
 
 // entry (re, im) kept as double-float pairs: += (a, b)
 __device__ __forceinline__ void dd_rmw(float4 *p, const dd::Acc &a, const dd::Acc &b) {
@@ -776,14 +653,8 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                 }
                 continue;
             }
-            // E0 = e^{i k r0} (times e^{-Im k r0})
             df E0r, E0i;
-            dd::sincos_df(kr0, E0i, E0r);
-            if (CPLX_K) {
-                const df damp = dd::to_df(exp(-kim * (dev::f2d(r0.hi) + dev::f2d(r0.lo))));
-                E0r = dev::df_mul(E0r, damp);
-                E0i = dev::df_mul(E0i, damp);
-            }
+            pair_phase_df64<CPLX_K>(kr0, r0, kim, E0r, E0i);
             const int c = P.c;
             const int Q = ri.Q[c];
             nqpe += Q;
@@ -795,38 +666,10 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
             dd::Acc ce{0.f, 0.f};
 #pragma unroll(kK9Unroll)
             for (int q = 0; q < Q; ++q) {
-                const float4 A = g4[4 * q], B = g4[4 * q + 1], Cn = g4[4 * q + 2], Dn = g4[4 * q + 3];
-                const df dx = dev::df_add(P.Dxd, df{A.x, B.x});
-                const df dy = dev::df_add(P.Dyd, df{A.y, B.y});
-                const df dz = dev::df_add(P.Dzd, df{A.z, B.z});
-                const df rr = dd::sqrt_df(dev::df_add(dev::df_add(dev::df_sqr(dx), dev::df_sqr(dy)),
-                                                      dev::df_sqr(dz)));
-                const df ri_ = dd::rcp(rr);
-                // e^{i k (r - r0)}
-                const df th = dev::df_mul(K, dev::df_sub(rr, r0));
-                const df z = dev::df_sqr(th);
-                df ct = dd::poly(kDfCos, deg.Jc, z);
-                df st = dev::df_mul(th, dd::poly(kDfSin, deg.Js, z));
-                if (CPLX_K) {
-                    const df damp = dd::poly(kDfExp, deg.Je, dd::neg(dev::df_mul(Ki, dev::df_sub(rr, r0))));
-                    ct = dev::df_mul(ct, damp);
-                    st = dev::df_mul(st, damp);
-                }
-                const df er = dev::df_sub(dev::df_mul(E0r, ct), dev::df_mul(E0i, st));
-                const df ei = dev::df_add(dev::df_mul(E0r, st), dev::df_mul(E0i, ct));
-                // G = e jw / (4 pi r); t = (x - y).n jw / (4 pi r^3)
-                const df sw = dev::df_mul(df{A.w, B.w}, ri_);
-                const df Gr = dev::df_mul(er, sw), Gi = dev::df_mul(ei, sw);
-                const df dn = dev::df_add(dev::df_add(dev::df_mul(dx, df{Cn.x, Dn.x}), dev::df_mul(dy, df{Cn.y, Dn.y})),
-                                          dev::df_mul(dz, df{Cn.z, Dn.z}));
-                const df tq = dev::df_mul(dev::df_mul(dn, sw), dev::df_sqr(ri_));
+                df Fr, Fi, Gr, Gi, tq;
+                qpe_df64<CPLX_K>(g4[4 * q], g4[4 * q + 1], g4[4 * q + 2], g4[4 * q + 3], P, r0, E0r, E0i, K, Ki,
+                                 deg, Fr, Fi, Gr, Gi, tq);
                 dd::acc_add(ce, tq);
-                // F = e (i k r - 1) t
-                const df kr = dev::df_mul(K, rr);
-                df ar = {-1.0f, 0.0f};
-                if (CPLX_K) ar = dev::df_sub(ar, dev::df_mul(Ki, rr));
-                const df Fr = dev::df_mul(dev::df_sub(dev::df_mul(er, ar), dev::df_mul(ei, kr)), tq);
-                const df Fi = dev::df_mul(dev::df_add(dev::df_mul(er, kr), dev::df_mul(ei, ar)), tq);
                 const float2 *pq = phc + q * NP;
 #pragma unroll
                 for (int a = 0; a < NP; ++a) {
@@ -863,26 +706,6 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
     if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
-}
-
-// Taylor degrees for |k (r - r0)| <= theta (and |Im k (r - r0)| <= kappa):
-// the first omitted term below 2^-53; false if a table is too short
-bool df_degrees(double theta, double kappa, DfDegrees &d) {
-    auto need = [](double x, int first, int step, int jmax, int &J) {
-        // term index n = first + step * j; stop once x^n / n! < 2^-53
-        for (int j = 0; j <= jmax; ++j) {
-            const int n = first + step * (j + 1);
-            double t = 1.0;
-            for (int m = 1; m <= n; ++m) t *= x / m;
-            if (t < 0x1p-53) {
-                J = j;
-                return true;
-            }
-        }
-        return false;
-    };
-    return need(theta, 0, 2, kDfMaxTrig, d.Jc) && need(theta, 1, 2, kDfMaxTrig, d.Js) &&
-           need(kappa, 0, 1, kDfMaxExp, d.Je);
 }
 
 template <int NP, bool CPLX>
@@ -988,9 +811,9 @@ void build_df64_records(Ctx &c, const std::vector<double> &rec64, const std::vec
 bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
     if (a.g_weight || a.taylor_m >= 0 || a.k_dev) return false;
-    DfDegrees deg{};
+    df64::DfDegrees deg{};
     const double kabs = std::hypot(a.k_re, a.k_im);
-    if (!df_degrees(kabs * c.df_rho_max, std::fabs(a.k_im) * c.df_rho_max, deg)) return false;
+    if (!df64::df_degrees(kabs * c.df_rho_max, std::fabs(a.k_im) * c.df_rho_max, deg)) return false;
     const int64_t N = c.n_sources;
     if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
     if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));

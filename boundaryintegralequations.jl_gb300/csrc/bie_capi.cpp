@@ -69,7 +69,7 @@ void check_matvec_args(bie::Ctx &c, double kr, double ki, int64_t M, int precisi
     (void)c;
     if (!std::isfinite(kr) || !std::isfinite(ki)) bie::fail(BIE_ERR_INVALID, "k must be finite");
     if (M <= 0) bie::fail(BIE_ERR_INVALID, "number of targets must be positive");
-    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED)
+    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED && precision != BIE_PREC_DF64)
         bie::fail(BIE_ERR_INVALID, "unknown precision");
     if (!x && !v) bie::fail(BIE_ERR_INVALID, "neither x nor v given");
     if (x && !yF) bie::fail(BIE_ERR_INVALID, "x given without yF");
@@ -674,7 +674,7 @@ int bie_gmres_device(bie_ctx *ctx, const bie_operator *op, const double *d_b, do
             bie::fail(BIE_ERR_INVALID, "k and scale must be finite");
         bie_gmres_opts o{};
         if (opts) o = *opts;
-        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
+        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED && o.precision != BIE_PREC_DF64)
             bie::fail(BIE_ERR_INVALID, "unknown precision");
         if (!(o.reltol >= 0) || !(o.abstol >= 0)) bie::fail(BIE_ERR_INVALID, "tolerances must be >= 0");
         std::lock_guard<std::mutex> lock(c.mu);
@@ -708,7 +708,7 @@ int bie_gmres(bie_ctx *ctx, const bie_operator *op, const double *b, double *x, 
             bie::fail(BIE_ERR_INVALID, "k and scale must be finite");
         bie_gmres_opts o{};
         if (opts) o = *opts;
-        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
+        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED && o.precision != BIE_PREC_DF64)
             bie::fail(BIE_ERR_INVALID, "unknown precision");
         if (!(o.reltol >= 0) || !(o.abstol >= 0)) bie::fail(BIE_ERR_INVALID, "tolerances must be >= 0");
         // one device block: [A (16 N^2)] [A32 (8 N^2)] [diag (16 N)] b (16 N) x (16 N),

@@ -21,6 +21,7 @@
 #include "bie_internal.h"
 #include "bie_device.cuh"
 #include "bie_mixed.cuh"
+#include "bie_df64.cuh"
 
 #include <algorithm>
 
@@ -618,6 +619,245 @@ void run_mixed_noalloc(Ctx &c, const MatvecArgs &a) {
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// FP64-grade product in double-float arithmetic (BIE_PREC_DF64): x and v are
+// interpolated to the quadrature points in FP64 and stored as (re_hi, re_lo,
+// im_hi, im_lo); each regular pair then costs the double-float kernel values
+// of its points and one complex product-sum per point; near pairs, near-ties
+// and very large phases go to the FP64 correction.
+// ---------------------------------------------------------------------------
+namespace {
+using namespace df64;
+
+__global__ void interp_df_kernel(const double *__restrict__ rec64, int stride64, int nidx_off,
+                                 const double *__restrict__ phi, int qmax, int NP, int R, RuleInfo ri, int QT,
+                                 int QTp, int64_t E, const double2 *__restrict__ x, const double2 *__restrict__ v,
+                                 float4 *__restrict__ xiF, float4 *__restrict__ xiG) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= E * QT) return;
+    const int64_t p = j / QT;
+    int slot = (int)(j - p * QT);
+    int r = 0;
+    while (r + 1 < R && slot >= ri.Q[r]) {
+        slot -= ri.Q[r];
+        ++r;
+    }
+    const int q = slot;
+    const int32_t *nid = reinterpret_cast<const int32_t *>(rec64 + (size_t)p * stride64 + nidx_off);
+    const double *ph = phi + ((size_t)r * qmax + q) * NP;
+    double fr = 0, fi = 0, gr = 0, gi = 0;
+    for (int a = 0; a < NP; ++a) {
+        const double w = ph[a];
+        if (x) {
+            const double2 xa = x[nid[a]];
+            fr += w * xa.x;
+            fi += w * xa.y;
+        }
+        if (v) {
+            const double2 va = v[nid[a]];
+            gr += w * va.x;
+            gi += w * va.y;
+        }
+    }
+    const int64_t o = p * QTp + (j - p * QT);
+    auto pack = [](double re, double im) {
+        const df a = dd::to_df(re), b = dd::to_df(im);
+        return make_float4(a.hi, a.lo, b.hi, b.lo);
+    };
+    if (xiF) xiF[o] = pack(fr, fi);
+    if (xiG) xiG[o] = pack(gr, gi);
+}
+
+// y += (ar + i ai) (b.x + b.y i ...) with b = (re_hi, re_lo, im_hi, im_lo)
+__device__ __forceinline__ void cmul_acc(dd::Acc &yr, dd::Acc &yi, df ar, df ai, const float4 b) {
+    const df br{b.x, b.y}, bi{b.z, b.w};
+    dd::acc_add(yr, dd::mul_raw(ar, br));
+    dd::acc_add(yr, dd::mul_raw(dd::neg(ai), bi));
+    dd::acc_add(yi, dd::mul_raw(ar, bi));
+    dd::acc_add(yi, dd::mul_raw(ai, br));
+}
+
+template <int NP, bool CPLX_K>
+__global__ void __launch_bounds__(kThreads, 3)
+matvec_df64_kernel(const float *__restrict__ rec, int stride, int64_t E, int S, RuleInfo ri, RuleInfo rxi,
+                   int QTp, const float4 *__restrict__ xiF, const float4 *__restrict__ xiG,
+                   const double *__restrict__ tgt, int64_t M, double kre, double kim,
+                   double2 *__restrict__ yFpart, double2 *__restrict__ yGpart, int chunk,
+                   int2 *__restrict__ defer, unsigned int *__restrict__ defer_count, unsigned int defer_cap,
+                   Fp64Rec v64, const double2 *__restrict__ x64, const double2 *__restrict__ v64in,
+                   DfDegrees deg, unsigned long long *__restrict__ qpe_count) {
+    extern __shared__ __align__(16) float smemf[];
+    float *s_rec = smemf;                                                   // chunk * stride
+    float4 *s_xiF = reinterpret_cast<float4 *>(s_rec + (size_t)chunk * stride);
+    float4 *s_xiG = s_xiF + (xiF ? (size_t)chunk * QTp : 0);
+
+    const int s = blockIdx.y;
+    const int64_t e0 = (int64_t)s * E / S;
+    const int64_t e1 = (int64_t)(s + 1) * E / S;
+    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const bool active = i < M;
+    const bool doF = xiF != nullptr, doG = xiG != nullptr;
+
+    double tx = 0, ty = 0, tz = 0;
+    if (active) {
+        tx = tgt[3 * i + 0];
+        ty = tgt[3 * i + 1];
+        tz = tgt[3 * i + 2];
+    }
+    const mixed::Target T{dev::df_from_double(tx), dev::df_from_double(ty), dev::df_from_double(tz)};
+    const df K = dd::to_df(kre), Ki = dd::to_df(kim);
+
+    dd::Acc yFr{0.f, 0.f}, yFi{0.f, 0.f}, yGr{0.f, 0.f}, yGi{0.f, 0.f};
+    unsigned long long nqpe = 0;
+    for (int64_t cb = e0; cb < e1; cb += chunk) {
+        const int n = (int)min((int64_t)chunk, e1 - cb);
+        __syncthreads();
+        {
+            const float4 *src = reinterpret_cast<const float4 *>(rec + cb * stride);
+            float4 *dst = reinterpret_cast<float4 *>(s_rec);
+            const int n4 = n * stride / 4;
+            for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
+            const int nx = n * QTp;
+            if (doF)
+                for (int t = threadIdx.x; t < nx; t += kThreads) s_xiF[t] = xiF[cb * QTp + t];
+            if (doG)
+                for (int t = threadIdx.x; t < nx; t += kThreads) s_xiG[t] = xiG[cb * QTp + t];
+        }
+        __syncthreads();
+        if (!active) continue;
+
+        for (int el = 0; el < n; ++el) {
+            const float *r = s_rec + (size_t)el * stride;
+            const mixed::PairSetup P = mixed::pair_setup<NP>(r, T);
+            const df r0 = dd::sqrt_df(dev::df_add(dev::df_add(dev::df_sqr(P.Dxd), dev::df_sqr(P.Dyd)),
+                                                  dev::df_sqr(P.Dzd)));
+            const df kr0 = dev::df_mul(K, r0);
+            if (P.deferred || !(fabsf(kr0.hi) < kDfMaxPhase)) {
+                const unsigned int slot = atomicAdd(defer_count, 1u);
+                if (slot < defer_cap) {
+                    defer[slot] = make_int2((int)i, (int)(cb + el));
+                } else {   // list full: this pair in FP64 in place
+                    double2 pf, pg;
+                    pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in, &pf, &pg);
+                    if (doF) {
+                        dd::acc_add(yFr, dd::to_df(pf.x));
+                        dd::acc_add(yFi, dd::to_df(pf.y));
+                    }
+                    if (doG) {
+                        dd::acc_add(yGr, dd::to_df(pg.x));
+                        dd::acc_add(yGi, dd::to_df(pg.y));
+                    }
+                }
+                continue;
+            }
+            df E0r, E0i;
+            pair_phase_df64<CPLX_K>(kr0, r0, kim, E0r, E0i);
+            const int c = P.c;
+            const int Q = ri.Q[c];
+            nqpe += Q;
+            const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
+            const float4 *xf = s_xiF + (size_t)el * QTp + rxi.off[c];
+            const float4 *xg = s_xiG + (size_t)el * QTp + rxi.off[c];
+            for (int q = 0; q < Q; ++q) {
+                df Fr, Fi, Gr, Gi, tq;
+                qpe_df64<CPLX_K>(g4[4 * q], g4[4 * q + 1], g4[4 * q + 2], g4[4 * q + 3], P, r0, E0r, E0i, K, Ki,
+                                 deg, Fr, Fi, Gr, Gi, tq);
+                if (doF) cmul_acc(yFr, yFi, Fr, Fi, xf[q]);
+                if (doG) cmul_acc(yGr, yGi, Gr, Gi, xg[q]);
+            }
+        }
+    }
+    if (active) {
+        if (doF) yFpart[(int64_t)s * M + i] = make_double2(dd::acc_value(yFr), dd::acc_value(yFi));
+        if (doG) yGpart[(int64_t)s * M + i] = make_double2(dd::acc_value(yGr), dd::acc_value(yGi));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
+    if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+template <int NP, bool CPLX>
+void run_df64(Ctx &c, const MatvecArgs &a, DfDegrees deg) {
+    const RecordLayout &L = c.lay;
+    const Df64Layout &X = c.dlay;
+    RuleInfo ri{}, ri64{}, rxi{};
+    int QT = 0;
+    for (int r = 0; r < L.R; ++r) {
+        ri.Q[r] = ri64.Q[r] = rxi.Q[r] = L.Q[r];
+        ri.off[r] = X.rule_off[r];
+        ri64.off[r] = L.rule_off[r];
+        rxi.off[r] = QT;
+        QT += L.Q[r];
+    }
+    const int QTp = (QT + 1) & ~1;
+    const int64_t E = c.n_elements, M = a.M;
+    const bool doF = a.x != nullptr, doG = a.v != nullptr;
+
+    const int level = choose_slice_level(c, M, kThreads);
+    const int S = 1 << level;
+    const size_t xi_bytes = (size_t)E * QTp * sizeof(float4);
+    char *xb = static_cast<char *>(c.scratch(kScratchMatvecXi, 2 * xi_bytes));
+    float4 *xiF = doF ? reinterpret_cast<float4 *>(xb) : nullptr;
+    float4 *xiG = doG ? reinterpret_cast<float4 *>(xb + xi_bytes) : nullptr;
+    const size_t part_bytes = (size_t)S * M * sizeof(double2);
+    char *pb = static_cast<char *>(c.scratch(kScratchMatvecPart, 2 * part_bytes));
+    double2 *yFpart = reinterpret_cast<double2 *>(pb);
+    double2 *yGpart = reinterpret_cast<double2 *>(pb + part_bytes);
+    const unsigned int dcap = (unsigned int)std::min<int64_t>(M * 64 + 4096, (int64_t)1 << 30);
+    const size_t dbytes = (size_t)dcap * sizeof(int2);
+    char *db = static_cast<char *>(c.scratch(kScratchDefer, dbytes + 256 + 2 * (size_t)M * 16));
+    int2 *defer = reinterpret_cast<int2 *>(db);
+    unsigned int *dcount = reinterpret_cast<unsigned int *>(db + dbytes);
+    double2 *yFn = reinterpret_cast<double2 *>(db + dbytes + 256);
+    double2 *yGn = yFn + M;
+    BIE_CUDA(cudaMemsetAsync(db + dbytes, 0, 256 + 2 * (size_t)M * 16, c.stream));
+
+    const int64_t nslots = E * QT;
+    interp_df_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, c.stream>>>(
+        c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, L.NP, L.R, ri64, QT, QTp, E,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), xiF, xiG);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+
+    const size_t rec_bytes = (size_t)X.stride * sizeof(float);
+    const size_t per_el = rec_bytes + (size_t)(doF + doG) * QTp * sizeof(float4);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(32, (32u << 10) / per_el));
+    const size_t smem = (size_t)chunk * per_el;
+    auto kern = matvec_df64_kernel<NP, CPLX>;
+    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((M + kThreads - 1) / kThreads), (unsigned)S);
+    cudaEvent_t t0 = c.timer_begin();
+    const Fp64Rec v64{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
+    kern<<<grid, kThreads, smem, c.stream>>>(c.d_drecords, X.stride, E, S, ri, rxi, QTp, xiF, xiG, a.targets, M,
+                                             a.k_re, a.k_im, yFpart, yGpart, chunk, defer, dcount, dcap, v64,
+                                             reinterpret_cast<const double2 *>(a.x),
+                                             reinterpret_cast<const double2 *>(a.v), deg, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    c.timer_end(t0);
+    ++c.kernel_launches;
+
+    matvec_correct_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+        defer, dcount, dcap, c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64,
+        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), a.targets,
+        a.k_re, a.k_im, yFn, yGn, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+    if (doF) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yFpart, S, yFn, M, reinterpret_cast<double2 *>(a.yF));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+    if (doG) {
+        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+            yGpart, S, yGn, M, reinterpret_cast<double2 *>(a.yG));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
+}
+
+}  // namespace
+
 void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a) {
     if (!a.x && !a.v) return;
     const bool cplx = a.k_im != 0.0;
@@ -636,6 +876,23 @@ void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a) {
 void launch_matvec(Ctx &c, const MatvecArgs &a) {
     if (!a.x && !a.v) return;
     const bool cplx = a.k_im != 0.0;
+    if (a.precision == BIE_PREC_DF64) {
+        df64::DfDegrees deg{};
+        if (df64::df_degrees(std::hypot(a.k_re, a.k_im) * c.df_rho_max, std::fabs(a.k_im) * c.df_rho_max, deg)) {
+            if (c.lay.NP == 1) {
+                if (cplx) run_df64<1, true>(c, a, deg);
+                else run_df64<1, false>(c, a, deg);
+            } else if (c.lay.NP == 3) {
+                if (cplx) run_df64<3, true>(c, a, deg);
+                else run_df64<3, false>(c, a, deg);
+            } else {
+                if (cplx) run_df64<6, true>(c, a, deg);
+                else run_df64<6, false>(c, a, deg);
+            }
+            return;
+        }
+        // phase rotations beyond the Taylor tables: the FP64 product
+    }
     if (a.precision == BIE_PREC_MIXED) {
         if (c.lay.NP == 1) {
             if (cplx) run_mixed<1, true>(c, a);

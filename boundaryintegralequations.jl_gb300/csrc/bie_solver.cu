@@ -1038,7 +1038,7 @@ void capture_gmres(Ctx &c, const bie_operator &op, const double *b_, double *x_,
         S.stream = body[0];
         if (refine) {
             S.stop = &rf->outer_zero;
-            S.apply(op, BIE_PREC_FP64, x, w);
+            S.apply(op, o.precision == BIE_PREC_DF64 ? BIE_PREC_DF64 : BIE_PREC_FP64, x, w);
             S.stop = nullptr;
             resid_flag_kernel<<<blocks(n), 256, 0, S.stream>>>(b, w, rr, n, &rf->outer_zero);
             BIE_CUDA(cudaGetLastError());
@@ -1169,7 +1169,7 @@ void gmres_solve(Ctx &c, const bie_operator &op, DevOp *devop, int64_t n, int le
         const int max_outer = o.max_refine > 0 ? o.max_refine : 10;
         bie_operator low = op;
         for (outer = 0; outer < max_outer; ++outer) {
-            S.apply(op, BIE_PREC_FP64, x, w);
+            S.apply(op, o.precision == BIE_PREC_DF64 ? BIE_PREC_DF64 : BIE_PREC_FP64, x, w);
             ++matvecs;
             S.sub(b, w, rr);
             res = S.norm(rr);

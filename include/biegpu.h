@@ -79,12 +79,13 @@ extern "C" {
 #define BIE_PREC_BF16       3   /* ~4e-3                        */
 #define BIE_PREC_FP16_SPLIT 4   /* ~1e-6                        */
 #define BIE_PREC_BF16_SPLIT 5   /* ~2e-5                        */
-/* Assembly only (bie_assemble, bie_assemble_device): FP64-grade F, G, C with
- * the regular pairs in double-float arithmetic (pairs of floats, ~48-bit
- * significand) on the FP32 pipes and the near pairs in FP64; ~1e-14 relative
- * to BIE_PREC_FP64.  Falls back to the FP64 kernel where the phase rotation
- * k (r - r0) over one element exceeds the Taylor tables (|k| x element
- * radius > ~2.5).                                                           */
+/* Assembly, matrix-free products and GMRES operator arithmetic (bie_assemble*,
+ * bie_matvec*, bie_gmres*; with `refine`, the residuals of refinement):
+ * FP64-grade results with the regular pairs in double-float arithmetic (pairs
+ * of floats, ~48-bit significand) on the FP32 pipes, the near pairs in FP64 and
+ * every sum compensated; assembled entries ~1e-14 from BIE_PREC_FP64.  Falls
+ * back to the FP64 kernels where the phase rotation k (r - r0) over one
+ * element exceeds the Taylor tables (|k| x element radius > ~2.5).          */
 #define BIE_PREC_DF64       6
 
 typedef struct bie_ctx bie_ctx;

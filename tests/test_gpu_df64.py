@@ -98,3 +98,41 @@ def test_df64_host_call_with_row_blocks():
     F, G, C = ctx.assemble(2.0, precision="df64")
     F64, G64, C64 = ctx.assemble(2.0, precision="fp64")
     assert max(rel(F, F64), rel(G, G64), rel(C, C64)) <= 1e-13
+
+
+@pytest.mark.parametrize("geo,f,k", [("linear", 6, 3.0), ("quadratic", 4, 5.0), ("linear", 5, 2.0 + 0.5j),
+                                     ("quadratic", 3, 1.0 + 0.3j)])
+def test_df64_matrix_free_products(geo, f, k):
+    """F x and G v in double-float against the dense oracle product (<= 1e-12)."""
+    mesh = bm.icosphere(f, geometry=geo)
+    F, G, _ = oracle.assemble(mesh, k, n=2, m=2, cOn=False)
+    r = np.random.default_rng(4)
+    x = r.normal(size=mesh.n_sources) + 1j * r.normal(size=mesh.n_sources)
+    v = r.normal(size=mesh.n_sources) + 1j * r.normal(size=mesh.n_sources)
+    Ff = biegpu.GPUFOperator(mesh, k, precision="df64")
+    Gf = biegpu.GPUGOperator(mesh, k, precision="df64")
+    assert rel(Ff @ x, F @ x) <= TOL
+    assert rel(Gf @ v, G @ v) <= TOL
+    z = np.linspace(0.1, 0.9, 10)
+    X = np.vstack([0 * z, 0.02 + 0 * z, z])
+    Fp, Gp, _ = oracle.assemble(mesh, k, targets=X, n=2, m=2, cOn=False)
+    assert rel(Ff.evaluate_targets(x, X), Fp @ x) <= TOL
+    assert rel(Gf.evaluate_targets(v, X), Gp @ v) <= TOL
+
+
+def test_df64_matrix_free_gmres():
+    """examples/3d_pulsating_sphere.jl's interior system with double-float
+    matrix-free products: plain GMRES, and mixed inner iterations refined
+    with double-float residuals, against a dense direct solve."""
+    mesh = bm.icosphere(5, geometry="quadratic")
+    k, Z0 = 1.0, 1.21 * 343.0
+    F, G, C = oracle.assemble(mesh, k, n=2, m=2)
+    vs = 1j * Z0 * k * np.ones(mesh.n_sources)
+    p_dense = np.linalg.solve(np.diag(1.0 - C) - F, G @ vs)
+    Ff = biegpu.GPUFOperator(mesh, k, precision="df64")
+    b = biegpu.GPUGOperator(mesh, k, precision="df64") @ vs
+    x, res = biegpu.gmres(biegpu.Diagonal(1.0 - C) - Ff, b, precision="df64", log=True)
+    assert res.converged and rel(x, p_dense) <= 1e-7
+    x2, res2 = biegpu.gmres(biegpu.Diagonal(1.0 - C) - biegpu.GPUFOperator(mesh, k, precision="mixed"), b,
+                            precision="df64", refine=True, log=True, reltol=1e-12)
+    assert res2.converged and rel(x2, p_dense) <= 1e-10
