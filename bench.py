@@ -645,6 +645,10 @@ def main():
                          "ms_per_step": d_ms / psteps, "speedup_vs_fp64": p_ms / d_ms,
                          "kernel": "assemble_df64_kernel (regular pairs in float-pair arithmetic on the "
                                    "FP32 pipes) + correct_fp64_kernel (near pairs in FP64)",
+                         # FP64-equivalent algorithmic flops of the double-float kernel against
+                         # the FP64 FMA peak: how far FP64-grade results beat the FP64 pipe
+                         "roofline_vs_fp64_pipe": roofline_entry(dst, "assemble_df64_kernel", "fp64",
+                                                                 peaks["fp64_flops"], args.workload, nphys),
                          "accuracy_vs_fp64": df_acc}
 
     # ---- end to end through the host-buffer C-ABI call -----------------------
