@@ -379,7 +379,7 @@ def nearfield_bench(args, max_over_ranks):
     offset 0.2 (sparse_assemble_parallel!), (2) one product of the fast
     operator (FMMFOperator algorithm: Gauss-rule far field summed exactly +
     near-field correction) against (3) the matrix-free product of the exact
-    dense rows (GPUFOperator), FP64 and mixed."""
+    dense rows (GPUFOperator), FP64, double-float (FP64-grade) and mixed."""
     import biegpu
     from biegpu import FMMFOperator, GPUFOperator
     from biegpu import mesh as bm
@@ -405,7 +405,7 @@ def nearfield_bench(args, max_over_ranks):
     t0 = time.perf_counter()
     op = FMMFOperator(mesh, k, precision="fp64")
     out["fast_operator_setup_ms"] = 1e3 * (time.perf_counter() - t0)
-    for prec in ("fp64", "mixed"):
+    for prec in ("fp64", "df64", "mixed"):
         op.precision = prec
         dense = GPUFOperator(mesh, k, precision=prec)
         op @ x

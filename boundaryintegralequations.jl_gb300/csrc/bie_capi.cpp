@@ -45,8 +45,8 @@ bie::FastOp &as_fastop(bie_fastop *op) {
 }
 
 void check_prec2(int precision) {
-    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED)
-        bie::fail(BIE_ERR_INVALID, "precision must be BIE_PREC_FP64 or BIE_PREC_MIXED");
+    if (precision != BIE_PREC_FP64 && precision != BIE_PREC_MIXED && precision != BIE_PREC_DF64)
+        bie::fail(BIE_ERR_INVALID, "precision must be BIE_PREC_FP64, BIE_PREC_MIXED or BIE_PREC_DF64");
 }
 
 void check_assemble_args(bie::Ctx &c, double kr, double ki, int64_t M, int flags, int precision,

@@ -428,8 +428,9 @@ BIE_API int bie_fastop_create(bie_ctx *ctx, double k_re, double k_im, int which,
                               double offset, int depth, bie_fastop **out);
 BIE_API int bie_fastop_destroy(bie_fastop *op);
 /* y = A x at the collocation nodes (LinearMaps._unsafe_mul!, :238-247, :392-404).
- * precision: BIE_PREC_FP64 (exact sum) or BIE_PREC_MIXED.  Device pointers,
- * asynchronous on the context stream. */
+ * precision: BIE_PREC_FP64 (exact sum), BIE_PREC_DF64 (the same in
+ * double-float arithmetic) or BIE_PREC_MIXED.  Device pointers, asynchronous
+ * on the context stream. */
 BIE_API int bie_fastop_apply_device(bie_fastop *op, const double *d_x, double *d_y, int precision);
 /* Same with host buffers (blocking). */
 BIE_API int bie_fastop_apply(bie_fastop *op, const double *x, double *y, int precision);

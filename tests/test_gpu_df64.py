@@ -136,3 +136,24 @@ def test_df64_matrix_free_gmres():
     x2, res2 = biegpu.gmres(biegpu.Diagonal(1.0 - C) - biegpu.GPUFOperator(mesh, k, precision="mixed"), b,
                             precision="df64", refine=True, log=True, reltol=1e-12)
     assert res2.converged and rel(x2, p_dense) <= 1e-10
+
+
+def test_df64_fast_operator_product_and_solve():
+    """The fast operator (FMMFOperator algorithm) with its Gauss-rule far field
+    in double-float: the same product as its FP64 form (<= 1e-12), and the
+    interior pulsating-sphere solve through it."""
+    mesh = bm.icosphere(6)
+    k = 2.0
+    r = np.random.default_rng(6)
+    x = r.normal(size=mesh.n_sources) + 1j * r.normal(size=mesh.n_sources)
+    op = biegpu.FMMFOperator(mesh, k, precision="fp64")
+    y64 = op @ x
+    op.precision = "df64"
+    ydf = op @ x
+    assert rel(ydf, y64) <= TOL
+    _, _, C = oracle.assemble(mesh, k, n=2, m=2, fOn=False, gOn=False)
+    b = biegpu.GPUGOperator(mesh, k, precision="df64") @ np.ones(mesh.n_sources)
+    xs, res = biegpu.gmres(biegpu.Diagonal(1.0 - C) - op, b, precision="df64", log=True, reltol=1e-10)
+    op.precision = "fp64"
+    x64, res64 = biegpu.gmres(biegpu.Diagonal(1.0 - C) - op, b, precision="fp64", log=True, reltol=1e-10)
+    assert res.converged and res64.converged and rel(xs, x64) <= 1e-8
