@@ -270,6 +270,11 @@ def sweep_bench(args, rank, world, max_over_ranks):
     for a, b in zip(pm, p64):
         for jj, j in enumerate(sel):
             errs.append(float(np.linalg.norm(a[:, j] - b[:, jj]) / np.linalg.norm(b[:, jj])))
+    # the same wavenumbers with FP64-grade double-float assembly + FP64 GMRES
+    t0 = time.perf_counter()
+    pdf, idf = biegpu.sweep(meshes, ks[sel], ws, precision="df64", refine=False)
+    t_df = max_over_ranks(time.perf_counter() - t0)
+    errs_df = [float(np.linalg.norm(a - b) / np.linalg.norm(b)) for a, b in zip(pdf, p64)]
     solves = im["solves"] * world
     v_mixed = solves / t_mixed
     v_fp64 = i64["solves"] * world / t_fp64
@@ -280,6 +285,11 @@ def sweep_bench(args, rank, world, max_over_ranks):
             "converged": im["converged"], "gmres_iterations_mean": im["iterations"] / max(im["solves"], 1),
             "plain_fp64": {"value": v_fp64, "unit": "solves/s", "solves": i64["solves"] * world,
                            "seconds": t_fp64, "assemble_ms": i64["assemble_ms"], "solve_ms": i64["solve_ms"]},
+            "df64": {"value": idf["solves"] * world / t_df, "unit": "solves/s", "seconds": t_df,
+                     "assemble_ms": idf["assemble_ms"], "solve_ms": idf["solve_ms"],
+                     "speedup_vs_plain_fp64": (idf["solves"] / t_df) / (i64["solves"] / t_fp64),
+                     "max_rel_err_vs_fp64": max(errs_df),
+                     "path": "double-float (FP64-grade) assembly + FP64 GMRES on complex128 matrices"},
             "speedup_vs_plain_fp64": v_mixed / v_fp64,
             "max_rel_err_vs_fp64": max(errs), "median_rel_err_vs_fp64": float(np.median(errs)),
             "path": "mixed assembly into complex64 matrices + GMRES with complex64 products and double-float sums (restart 20, reltol sqrt(eps))"}

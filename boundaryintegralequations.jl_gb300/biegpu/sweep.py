@@ -24,7 +24,9 @@ def sweep(meshes, ks, ws, precision: str = "mixed", refine: bool = True, n: int 
     ``ks``: wavenumbers (real or complex), ``ws``: per-mesh boundary data
     (length N_m complex).  ``precision="mixed"`` with ``refine=True`` is the
     fast path (mixed assembly, complex64 inner GMRES, complex128 residual);
-    ``precision="fp64", refine=False`` is the plain FP64 path.  By default
+    ``precision="fp64", refine=False`` is the plain FP64 path;
+    ``precision="df64", refine=False`` the same with FP64-grade double-float
+    assembly.  By default
     everything after each mesh's first wavenumber is one launch of a recorded
     CUDA graph (device-side loops over wavenumbers and GMRES iterations);
     ``eager=True`` launches kernel by kernel from the host.

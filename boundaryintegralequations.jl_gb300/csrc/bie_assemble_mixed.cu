@@ -573,8 +573,12 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                      int flags, double2 *__restrict__ F, double2 *__restrict__ G,
                      double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
                      unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
-                     DfDegrees deg, unsigned long long *__restrict__ qpe_count) {
+                     DfDegrees deg, unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
     using dev::df;
+    if (kdev) {   // wavenumber read from device memory (recorded sweeps)
+        kre = kdev[0];
+        kim = kdev[1];
+    }
     extern __shared__ __align__(16) float smemf[];
     float2 *s_phi = reinterpret_cast<float2 *>(smemf);             // nphi (hi, lo) pairs
     float *s_rec = smemf + ((2 * nphi + 3) & ~3);                     // chunk * stride floats
@@ -729,7 +733,7 @@ void launch_df64_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem
         c.d_drecords, X.stride, X.nidx_off, c.n_elements, S, c.d_shared_mask + (size_t)level * c.n_elements,
         reinterpret_cast<const float2 *>(c.d_dphi), L.R * L.qmax * NP, L.qmax, ri, a.targets, a.M, a.k_re,
         a.k_im, a.flags, reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cpart, chunk, defer,
-        dcount, dcap, v, deg, c.d_qpe);
+        dcount, dcap, v, deg, c.d_qpe, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;
@@ -744,7 +748,7 @@ void launch_df64_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem
     }
     correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
         defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
-        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, nullptr);
+        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     ++c.kernel_launches;
 }
@@ -810,10 +814,11 @@ void build_df64_records(Ctx &c, const std::vector<double> &rec64, const std::vec
 
 bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
-    if (a.g_weight || a.taylor_m >= 0 || a.k_dev) return false;
+    if (a.g_weight || a.taylor_m >= 0 || (a.k_dev && !(a.k_abs_max > 0))) return false;
     df64::DfDegrees deg{};
-    const double kabs = std::hypot(a.k_re, a.k_im);
-    if (!df64::df_degrees(kabs * c.df_rho_max, std::fabs(a.k_im) * c.df_rho_max, deg)) return false;
+    const double kabs = std::max(std::hypot(a.k_re, a.k_im), a.k_dev ? a.k_abs_max : 0.0);
+    const double kimb = a.k_dev ? kabs : std::fabs(a.k_im);
+    if (!df64::df_degrees(kabs * c.df_rho_max, kimb * c.df_rho_max, deg)) return false;
     const int64_t N = c.n_sources;
     if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
     if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));

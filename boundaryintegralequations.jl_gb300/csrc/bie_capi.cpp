@@ -782,7 +782,7 @@ int bie_sweep(bie_ctx *const *ctxs, int nmesh, const double *ks, int nk, const d
         o.precision = BIE_PREC_MIXED;
         o.refine = 1;
         if (opts) o = *opts;
-        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED)
+        if (o.precision != BIE_PREC_FP64 && o.precision != BIE_PREC_MIXED && o.precision != BIE_PREC_DF64)
             bie::fail(BIE_ERR_INVALID, "unknown precision");
         bie_sweep_info inf{};
         bie::run_sweep(cs.data(), nmesh, ks, nk, w, p, o, inf, iters);

@@ -252,6 +252,8 @@ struct AssembleArgs {
     const double *k_dev = nullptr;      // device (re, im): the kernels read k here instead
                                         // of k_re, k_im (which then only select the real-
                                         // or complex-k code path: k_im != 0)
+    double k_abs_max = 0.0;             // double-float kernel with k_dev: a bound on |k|
+                                        // (its phase polynomials' degrees)
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);

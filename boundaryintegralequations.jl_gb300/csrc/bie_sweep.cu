@@ -106,6 +106,8 @@ struct MeshRun {
     int64_t N;
     int nk;
     bool mixed;
+    bool df64;        // FP64-grade assembly in double-float arithmetic
+    double kmax = 0;  // largest |k| of the sweep (the double-float phase tables' bound)
     DevBuf F, G, vec, P, dinfo, kb, ctl, tsb;
     double2 *Cv, *dg, *b, *wd, *X;
     bie_gmres_info *dgi;
@@ -119,6 +121,7 @@ struct MeshRun {
 
     MeshRun(Ctx &ctx, int nk_, const double *ks, const double *w, const bie_sweep_opts &o)
         : c(ctx), N(ctx.n_sources), nk(nk_), mixed(o.precision == BIE_PREC_MIXED),
+          df64(o.precision == BIE_PREC_DF64),
           F((size_t)N * N * (mixed ? 8 : 16)), G((size_t)N * N * (mixed ? 8 : 16)), vec(4 * (size_t)N * 16),
           P((size_t)(nk + 1) * N * 16), dinfo((size_t)nk * sizeof(bie_gmres_info)),
           kb(((size_t)2 * nk + 2) * sizeof(double)), ctl(256), tsb((size_t)3 * nk * 8), hinfo(nk) {
@@ -164,8 +167,9 @@ struct MeshRun {
                        reinterpret_cast<double *>(Cv)};
         a.c64_out = mixed;
         a.k_dev = kd;
+        a.k_abs_max = kmax;
         if (mixed) launch_assemble_mixed(c, a);
-        else launch_assemble_fp64(c, a);
+        else if (!(df64 && launch_assemble_df64(c, a))) launch_assemble_fp64(c, a);
     }
     // diag = 1 - C, b = G w (the exact complex64 product in the mixed path)
     void rhs() {
@@ -342,6 +346,7 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
         Ctx &c = *ctxs[m];
         c.autotune = true;
         runs.push_back(std::make_unique<MeshRun>(c, nk, ks, w[m], o));
+        for (int j = 0; j < nk; ++j) runs.back()->kmax = std::max(runs.back()->kmax, std::hypot(ks[2 * j], ks[2 * j + 1]));
         runs.back()->eager(0, ks, ev.e);   // sizes the scratch, tunes the slicing
     }
     GraphScope gs(uniq);

@@ -157,3 +157,17 @@ def test_df64_fast_operator_product_and_solve():
     op.precision = "fp64"
     x64, res64 = biegpu.gmres(biegpu.Diagonal(1.0 - C) - op, b, precision="fp64", log=True, reltol=1e-10)
     assert res.converged and res64.converged and rel(xs, x64) <= 1e-8
+
+
+@pytest.mark.parametrize("eager", [False, True])
+def test_df64_sweep_matches_fp64_sweep(eager):
+    """Sweeps with double-float assembly (recorded graph reading k from device
+    memory, or launch by launch) against the plain FP64 sweep."""
+    meshes = [bm.icosphere(5), bm.ellipsoid(4, geometry="quadratic")]
+    ks = [0.5, 2.0, 4.0 + 0.2j]
+    r = np.random.default_rng(8)
+    ws = [r.normal(size=m.n_sources) + 1j * r.normal(size=m.n_sources) for m in meshes]
+    p64, _ = biegpu.sweep(meshes, ks, ws, precision="fp64", refine=False, eager=eager)
+    pdf, info = biegpu.sweep(meshes, ks, ws, precision="df64", refine=False, eager=eager)
+    for a, b in zip(pdf, p64):
+        assert rel(a, b) <= 1e-10
