@@ -498,6 +498,12 @@ def adjoint_bench(args, max_over_ranks):
     for _ in range(steps):
         biegpu.farfield_objective(mesh, k, Z, Xf, rho_c=rho_c, gradient=False)
     t_fwd = max_over_ranks(time.perf_counter() - t0) / steps
+    # forward model assembled in double-float (FP64-grade), reverse pass FP64
+    biegpu.farfield_objective(mesh, k, Z, Xf, rho_c=rho_c, precision="df64")
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        Jd, _, dXd, _, _ = biegpu.farfield_objective(mesh, k, Z, Xf, rho_c=rho_c, precision="df64")
+    t_grad_df = max_over_ranks(time.perf_counter() - t0) / steps
     h = 1e-6
     v, c = 1234, 2
     Pp = mesh.coordinates.copy()
@@ -513,6 +519,9 @@ def adjoint_bench(args, max_over_ranks):
             "workload": f"ellipsoid 3:2:1 f=22 ({mesh.n_sources} nodes, {mesh.n_elements} elements), ka=3, "
                         "32 field points at radius 10",
             "ms_per_gradient": 1e3 * t_grad, "ms_per_forward": 1e3 * t_fwd, "parameters": n_params,
+            "df64_forward": {"ms_per_gradient": 1e3 * t_grad_df,
+                             "J_rel_diff": abs(Jd - J) / abs(J),
+                             "dX_rel_diff": float(np.linalg.norm(dXd - dX) / np.linalg.norm(dX))},
             "central_fd_equivalent_s": 2 * n_params * t_fwd,
             "fd_check": {"component": f"dX[{c},{v}]", "adjoint": float(dX[c, v]), "central_fd_h1e-6": fd,
                          "rel_to_max": abs(fd - dX[c, v]) / float(np.abs(dX).max())},

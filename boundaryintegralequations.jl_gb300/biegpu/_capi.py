@@ -170,7 +170,8 @@ class SweepInfo(C.Structure):
 
 
 class AdjointOpts(C.Structure):
-    _fields_ = [("rho_c", C.c_double), ("dir", C.c_double * 3), ("reltol", C.c_double)]
+    _fields_ = [("rho_c", C.c_double), ("dir", C.c_double * 3), ("reltol", C.c_double),
+                ("precision", C.c_int32)]
 
 
 class AdjointInfo(C.Structure):

@@ -20,8 +20,10 @@ from .mesh import Mesh3d
 
 def farfield_objective(mesh: Mesh3d, k: float, Z, field_points, rho_c: float = 1.21 * 343.0,
                        direction=(0.0, 0.0, 1.0), gradient: bool = True, reltol: float = 1e-13,
-                       n: int = 2, m: int = 2, device: int = 0):
-    """(J, p_field, dJ/dX (3 x N_c) or None, dJ/dZ (E complex) or None, info)."""
+                       n: int = 2, m: int = 2, device: int = 0, precision: str = "fp64"):
+    """(J, p_field, dJ/dX (3 x N_c) or None, dJ/dZ (E complex) or None, info).
+    ``precision="df64"`` assembles the forward model in double-float
+    arithmetic (FP64-grade, faster on GB300); the reverse pass is FP64."""
     ctx = get_context(mesh, n=n, m=m, device=device)
     Zc = np.ascontiguousarray(Z, dtype=np.complex128)
     if Zc.shape != (mesh.n_elements,):
@@ -30,7 +32,10 @@ def farfield_objective(mesh: Mesh3d, k: float, Z, field_points, rho_c: float = 1
     M = X.shape[1]
     d = np.asarray(direction, dtype=np.float64)
     d = d / np.linalg.norm(d)
-    opts = _capi.AdjointOpts(rho_c=float(rho_c), dir=(C.c_double * 3)(*d), reltol=float(reltol))
+    if precision not in ("fp64", "df64"):
+        raise ValueError("precision must be 'fp64' or 'df64'")
+    opts = _capi.AdjointOpts(rho_c=float(rho_c), dir=(C.c_double * 3)(*d), reltol=float(reltol),
+                             precision=_capi.PRECISION[precision])
     J = C.c_double()
     pf = np.empty(M, dtype=np.complex128)
     dX = np.empty((3, mesh.coordinates.shape[1]), dtype=np.float64, order="F") if gradient else None

@@ -333,13 +333,13 @@ void run_adjoint(Ctx &c, const AdjointArgs &a, AdjointOut &out) {
     {
         AssembleArgs s{a.k_re, a.k_im, c.d_sources, N, BIE_F | BIE_G | BIE_C, A.d(), G.d(), Cv.d()};
         s.g_weight = Y.d();
-        launch_assemble_fp64(c, s);
+        if (!(a.precision == BIE_PREC_DF64 && launch_assemble_df64(c, s))) launch_assemble_fp64(c, s);
         combine_system_kernel<<<std::min<unsigned>(nblocks(N * N), 65535u), 256, 0, st>>>(
             A.d2(), G.d2(), aAc, Cv.d2(), N, N);
         BIE_CUDA(cudaGetLastError());
         AssembleArgs f{a.k_re, a.k_im, fp.d(), M, BIE_F | BIE_G, B.d(), Gx.d(), nullptr};
         f.g_weight = Y.d();
-        launch_assemble_fp64(c, f);
+        if (!(a.precision == BIE_PREC_DF64 && launch_assemble_df64(c, f))) launch_assemble_fp64(c, f);
         // stored: F_x - i rho c k G_x  (= -B)
         combine_system_kernel<<<std::min<unsigned>(nblocks(M * N), 65535u), 256, 0, st>>>(
             B.d2(), Gx.d2(), make_double2(-aBc.x, -aBc.y), nullptr, M, N);

@@ -248,7 +248,8 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
                     unsigned int defer_cap, Fp64View v, const double *__restrict__ tgt, int64_t M,
                     double kre, double kim, int flags, T2 *__restrict__ F,
                     T2 *__restrict__ G, double *__restrict__ Cnear,
-                    unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
+                    unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev,
+                    const double2 *__restrict__ gweight = nullptr) {
     if (kdev) {
         kre = kdev[0];
         kim = kdev[1];
@@ -267,6 +268,15 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
         const double ce = dev::element_fp64<NP, CPLX_K>(r + v.ri.off[c], v.ri.Q[c],
                                                         v.phi + (size_t)c * v.qmax * NP, tx, ty, tz,
                                                         kre, kim, fr, fi, gr, gi);
+        if (gweight && doG) {   // element factor on the single layer
+            const double2 w = gweight[pr.y];
+#pragma unroll
+            for (int a = 0; a < NP; ++a) {
+                const double t = gr[a] * w.x - gi[a] * w.y;
+                gi[a] = gr[a] * w.y + gi[a] * w.x;
+                gr[a] = t;
+            }
+        }
         const int32_t *nid = reinterpret_cast<const int32_t *>(r + v.nidx_off);
 #pragma unroll
         for (int a = 0; a < NP; ++a) {
@@ -573,7 +583,8 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                      int flags, double2 *__restrict__ F, double2 *__restrict__ G,
                      double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
                      unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
-                     DfDegrees deg, unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
+                     DfDegrees deg, unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev,
+                     const double2 *__restrict__ gweight) {
     using dev::df;
     if (kdev) {   // wavenumber read from device memory (recorded sweeps)
         kre = kdev[0];
@@ -637,6 +648,15 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                 const double ce = dev::element_fp64<NP, CPLX_K>(r64 + v64.ri.off[cn], v64.ri.Q[cn],
                                                                  v64.phi + (size_t)cn * v64.qmax * NP, tx, ty,
                                                                  tz, kre, kim, fr, fi, gr, gi);
+                if (gweight && doG) {
+                    const double2 w = gweight[cb + el];
+#pragma unroll
+                    for (int a = 0; a < NP; ++a) {
+                        const double t = gr[a] * w.x - gi[a] * w.y;
+                        gi[a] = gr[a] * w.y + gi[a] * w.x;
+                        gr[a] = t;
+                    }
+                }
                 dd::acc_add(cacc, dd::to_df(ce));
                 const int32_t *nid = reinterpret_cast<const int32_t *>(r64 + v64.nidx_off);
                 const uint32_t m = s_mask[el];
@@ -687,6 +707,18 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
             }
             // C = -sum t
             dd::acc_add(cacc, dd::neg(dev::fast_two_sum(ce.hi, ce.lo)));
+            if (gweight && doG) {   // element factor on the single layer, in double-float
+                const double2 w = gweight[cb + el];
+                const df wr = dd::to_df(w.x), wi = dd::to_df(w.y);
+#pragma unroll
+                for (int a = 0; a < NP; ++a) {
+                    const df xr = dev::fast_two_sum(gr[a].hi, gr[a].lo), xi = dev::fast_two_sum(gi[a].hi, gi[a].lo);
+                    const df yr = dev::df_sub(dev::df_mul(xr, wr), dev::df_mul(xi, wi));
+                    const df yi = dev::df_add(dev::df_mul(xr, wi), dev::df_mul(xi, wr));
+                    gr[a] = dd::Acc{yr.hi, yr.lo};
+                    gi[a] = dd::Acc{yi.hi, yi.lo};
+                }
+            }
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
             const uint32_t m = s_mask[el];
 #pragma unroll
@@ -733,7 +765,7 @@ void launch_df64_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem
         c.d_drecords, X.stride, X.nidx_off, c.n_elements, S, c.d_shared_mask + (size_t)level * c.n_elements,
         reinterpret_cast<const float2 *>(c.d_dphi), L.R * L.qmax * NP, L.qmax, ri, a.targets, a.M, a.k_re,
         a.k_im, a.flags, reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cpart, chunk, defer,
-        dcount, dcap, v, deg, c.d_qpe, a.k_dev);
+        dcount, dcap, v, deg, c.d_qpe, a.k_dev, reinterpret_cast<const double2 *>(a.g_weight));
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;
@@ -748,7 +780,8 @@ void launch_df64_np(Ctx &c, const AssembleArgs &a, int S, int level, size_t smem
     }
     correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
         defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
-        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, a.k_dev);
+        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, a.k_dev,
+        reinterpret_cast<const double2 *>(a.g_weight));
     BIE_CUDA(cudaGetLastError());
     ++c.kernel_launches;
 }
@@ -814,7 +847,7 @@ void build_df64_records(Ctx &c, const std::vector<double> &rec64, const std::vec
 
 bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
-    if (a.g_weight || a.taylor_m >= 0 || (a.k_dev && !(a.k_abs_max > 0))) return false;
+    if (a.taylor_m >= 0 || (a.k_dev && !(a.k_abs_max > 0))) return false;
     df64::DfDegrees deg{};
     const double kabs = std::max(std::hypot(a.k_re, a.k_im), a.k_dev ? a.k_abs_max : 0.0);
     const double kimb = a.k_dev ? kabs : std::fabs(a.k_im);

@@ -811,6 +811,9 @@ int bie_adjoint(bie_ctx *ctx, double k_re, double k_im, const double *Z, const d
         BIE_CUDA(cudaSetDevice(c.device));
         bie::AdjointArgs a{k_re, k_im, opts->rho_c, Z, {opts->dir[0], opts->dir[1], opts->dir[2]},
                            field, n_field, opts->reltol, pf, dX, dZ};
+        if (opts->precision != BIE_PREC_FP64 && opts->precision != BIE_PREC_DF64)
+            bie::fail(BIE_ERR_INVALID, "adjoint precision must be BIE_PREC_FP64 or BIE_PREC_DF64");
+        a.precision = opts->precision;
         bie::AdjointOut o;
         bie::run_adjoint(c, a, o);
         *J = o.J;

@@ -376,6 +376,7 @@ struct AdjointArgs {
     double *pf;              // out: n_field complex field pressures (may be null)
     double *dX;              // out: 3 x N vertex gradient (may be null)
     double *dZ;              // out: E complex (dJ/dRe Z, dJ/dIm Z) (may be null)
+    int precision = BIE_PREC_FP64;   // forward-model assembly (BIE_PREC_FP64 | BIE_PREC_DF64)
 };
 struct AdjointOut {
     double J = 0;

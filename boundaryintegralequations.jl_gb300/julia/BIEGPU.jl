@@ -361,6 +361,7 @@ struct AdjointOpts
     rho_c::Float64
     dir::NTuple{3,Float64}
     reltol::Float64
+    precision::Int32   # 0: FP64 forward assembly, 6: double-float (BIE_PREC_DF64)
 end
 struct AdjointInfo
     forward_iterations::Int32; forward_converged::Int32
@@ -386,7 +387,7 @@ function farfield_objective(coordinates, Z, mesh, k, field; rho_c=1.21 * 343.0, 
     dX = gradient ? zeros(Float64, size(coordinates)) : Matrix{Float64}(undef, 0, 0)
     dZ = gradient ? zeros(ComplexF64, length(Zv)) : Vector{ComplexF64}(undef, 0)
     d = collect(Float64, dir); d ./= norm(d)
-    opts = Ref(AdjointOpts(rho_c, (d[1], d[2], d[3]), reltol))
+    opts = Ref(AdjointOpts(rho_c, (d[1], d[2], d[3]), reltol, Int32(0)))
     info = Ref{AdjointInfo}()
     GC.@preserve Zv X pf dX dZ begin
         check(ccall((:bie_adjoint, libbiegpu), Cint,

@@ -550,6 +550,7 @@ typedef struct bie_adjoint_opts {
     double rho_c;        /* characteristic impedance rho0 c of the fluid (e.g. 1.21 * 343) */
     double dir[3];       /* incident plane-wave direction (unit vector)                  */
     double reltol;       /* GMRES tolerance of the forward and adjoint solves (<= 0: 1e-13) */
+    int32_t precision;   /* forward-model assembly: BIE_PREC_FP64 (0) or BIE_PREC_DF64       */
 } bie_adjoint_opts;
 
 typedef struct bie_adjoint_info {

@@ -171,3 +171,19 @@ def test_df64_sweep_matches_fp64_sweep(eager):
     pdf, info = biegpu.sweep(meshes, ks, ws, precision="df64", refine=False, eager=eager)
     for a, b in zip(pdf, p64):
         assert rel(a, b) <= 1e-10
+
+
+def test_df64_adjoint_matches_fp64():
+    """The adjoint gradient with the forward model assembled in double-float
+    (element admittances on G in the double-float kernel and its FP64 near-pair
+    correction) against the FP64 forward model."""
+    mesh = bm.icosphere(5, axes=(1.0, 2 / 3, 1 / 3))
+    r = np.random.default_rng(9)
+    Z = 1.21 * 343.0 * np.exp(1j * r.uniform(-1, 1, mesh.n_elements))
+    X = r.normal(size=(3, 8))
+    X *= 10.0 / np.linalg.norm(X, axis=0)
+    J, pf, dX, dZ, _ = biegpu.farfield_objective(mesh, 3.0, Z, X)
+    J2, pf2, dX2, dZ2, _ = biegpu.farfield_objective(mesh, 3.0, Z, X, precision="df64")
+    assert abs(J2 - J) <= 1e-11 * abs(J)
+    assert rel(pf2, pf) <= 1e-11
+    assert rel(dX2, dX) <= 1e-10 and rel(dZ2, dZ) <= 1e-10
