@@ -376,7 +376,7 @@ vertices moved to `coordinates` (3 x N_c) and element impedances `Z`; with
 `gradient=true` also dJ/dcoordinates (3 x N_c) and dJ/dZ (dJ/dRe Z + i dJ/dIm Z).
 """
 function farfield_objective(coordinates, Z, mesh, k, field; rho_c=1.21 * 343.0, dir=(0.0, 0.0, 1.0),
-                            gradient=false, reltol=1e-13)
+                            gradient=false, reltol=1e-13, precision=:fp64)
     moved = (coordinates=Matrix{Float64}(coordinates), topology=mesh.topology,
              physics_topology=mesh.physics_topology, sources=Matrix{Float64}(coordinates))
     c = Context(moved; n=2, m=2)
@@ -387,7 +387,8 @@ function farfield_objective(coordinates, Z, mesh, k, field; rho_c=1.21 * 343.0, 
     dX = gradient ? zeros(Float64, size(coordinates)) : Matrix{Float64}(undef, 0, 0)
     dZ = gradient ? zeros(ComplexF64, length(Zv)) : Vector{ComplexF64}(undef, 0)
     d = collect(Float64, dir); d ./= norm(d)
-    opts = Ref(AdjointOpts(rho_c, (d[1], d[2], d[3]), reltol, Int32(0)))
+    # precision: forward-model assembly, :fp64 or :df64 (double-float)
+    opts = Ref(AdjointOpts(rho_c, (d[1], d[2], d[3]), reltol, precision_code(precision)))
     info = Ref{AdjointInfo}()
     GC.@preserve Zv X pf dX dZ begin
         check(ccall((:bie_adjoint, libbiegpu), Cint,
