@@ -82,6 +82,14 @@ def test_df64_falls_back_to_fp64_for_large_element_phase():
     check(mesh, 60.0)
 
 
+def test_df64_with_caller_rule_tables():
+    mesh = bm.icosphere(3, geometry="quadratic")
+    ctx = biegpu.Context(mesh, rules=[oracle.rule(3, 2, r) for r in range(1, 7)])
+    F, G, C = ctx.assemble(2.5, precision="df64")
+    Fo, Go, Co = oracle.assemble(mesh, 2.5, n=3, m=2)
+    assert max(rel(F, Fo), rel(G, Go), rel(C, Co)) <= TOL
+
+
 def test_df64_rejects_nothing_the_fp64_path_takes():
     mesh = bm.icosphere(3)
     ctx = biegpu.Context(mesh, n=2, m=2)
@@ -100,11 +108,14 @@ def test_df64_host_call_with_row_blocks():
     assert max(rel(F, F64), rel(G, G64), rel(C, C64)) <= 1e-13
 
 
-@pytest.mark.parametrize("geo,f,k", [("linear", 6, 3.0), ("quadratic", 4, 5.0), ("linear", 5, 2.0 + 0.5j),
-                                     ("quadratic", 3, 1.0 + 0.3j)])
-def test_df64_matrix_free_products(geo, f, k):
+@pytest.mark.parametrize("geo,f,k,phys", [("linear", 6, 3.0, "geometry"), ("quadratic", 4, 5.0, "geometry"),
+                                          ("linear", 5, 2.0 + 0.5j, "geometry"),
+                                          ("quadratic", 3, 1.0 + 0.3j, "geometry"),
+                                          ("linear", 4, 2.0, "disctriconstant"),
+                                          ("quadratic", 2, 2.0, "disctriquadratic")])
+def test_df64_matrix_free_products(geo, f, k, phys):
     """F x and G v in double-float against the dense oracle product (<= 1e-12)."""
-    mesh = bm.icosphere(f, geometry=geo)
+    mesh = bm.icosphere(f, geometry=geo, physics=phys)
     F, G, _ = oracle.assemble(mesh, k, n=2, m=2, cOn=False)
     r = np.random.default_rng(4)
     x = r.normal(size=mesh.n_sources) + 1j * r.normal(size=mesh.n_sources)
