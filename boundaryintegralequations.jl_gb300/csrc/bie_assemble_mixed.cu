@@ -839,6 +839,16 @@ void build_df64_records(Ctx &c, const std::vector<double> &rec64, const std::vec
     c.df_rho_max = rho;
     std::vector<float> phi((size_t)L.R * L.qmax * NP * 2, 0.f);
     for (size_t j = 0; j < (size_t)L.R * L.qmax * NP; ++j) split(c.phi[j], phi[2 * j], phi[2 * j + 1]);
+    // phase table e^{i j h}: cos and sin in FP64 (correctly rounded to ~1 ulp), split
+    std::vector<float> tab((size_t)4 * (2 * df64::kPhaseTabHalf + 1));
+    for (int j = -df64::kPhaseTabHalf; j <= df64::kPhaseTabHalf; ++j) {
+        const double th = (double)j * (double)df64::kPhaseTabStep;
+        float *t = &tab[(size_t)4 * (j + df64::kPhaseTabHalf)];
+        split(std::cos(th), t[0], t[1]);
+        split(std::sin(th), t[2], t[3]);
+    }
+    BIE_CUDA(cudaMalloc(&c.d_phase_tab, tab.size() * sizeof(float)));
+    BIE_CUDA(cudaMemcpy(c.d_phase_tab, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
     BIE_CUDA(cudaMalloc(&c.d_drecords, rec.size() * sizeof(float)));
     BIE_CUDA(cudaMalloc(&c.d_dphi, phi.size() * sizeof(float)));
     BIE_CUDA(cudaMemcpy(c.d_drecords, rec.data(), rec.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -852,6 +862,7 @@ bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
     const double kabs = std::max(std::hypot(a.k_re, a.k_im), a.k_dev ? a.k_abs_max : 0.0);
     const double kimb = a.k_dev ? kabs : std::fabs(a.k_im);
     if (!df64::df_degrees(kabs * c.df_rho_max, kimb * c.df_rho_max, deg)) return false;
+    deg.tab = reinterpret_cast<const float4 *>(c.d_phase_tab);
     const int64_t N = c.n_sources;
     if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
     if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));

@@ -137,13 +137,21 @@ __device__ __forceinline__ double acc_value(const Acc &s) {
 __device__ __forceinline__ df to_df(double x) { return dev::df_from_double(x); }
 }  // namespace dd
 
+// e^{i j h}, h = 2^-7, j = -kPhaseTabHalf..kPhaseTabHalf as (cos hi, cos lo,
+// sin hi, sin lo): the per-point rotation e^{i theta} is the table entry at
+// the nearest j h times a short Taylor series of the remainder (|.| <= 2^-8)
+constexpr int kPhaseTabHalf = 512;
+constexpr float kPhaseTabStep = 0x1p-7f;
+
 struct DfDegrees {
-    int Jc, Js, Je;   // Taylor degrees (coefficient counts - 1) of cos, sin, exp
+    int Jc, Js, Je;        // Taylor degrees (coefficient counts - 1) of cos, sin, exp
+    const float4 *tab;     // device phase table (2 kPhaseTabHalf + 1 entries)
 };
 
 // Taylor degrees for |k (r - r0)| <= theta (and |Im k (r - r0)| <= kappa):
 // the first omitted term below 2^-53; false if a table is too short
 inline bool df_degrees(double theta, double kappa, DfDegrees &d) {
+    if (!(theta < 0.9 * kPhaseTabHalf * (double)kPhaseTabStep)) return false;   // table range
     auto need = [](double x, int first, int step, int jmax, int &J) {
         // term index n = first + step * j; stop once x^n / n! < 2^-53
         for (int j = 0; j <= jmax; ++j) {
@@ -178,11 +186,20 @@ __device__ __forceinline__ void qpe_df64(const float4 A, const float4 B, const f
     const df dz = dev::df_add(P.Dzd, df{A.z, B.z});
     const df rr = dd::sqrt_df(dev::df_add(dev::df_add(dev::df_sqr(dx), dev::df_sqr(dy)), dev::df_sqr(dz)));
     const df ri_ = dd::rcp(rr);
-    // e^{i k (r - r0)}
+    // e^{i k (r - r0)} = e^{i j h} e^{i (theta - j h)}, |theta| < kPhaseTabHalf h
     const df th = dev::df_mul(K, dev::df_sub(rr, r0));
-    const df z = dev::df_sqr(th);
-    df ct = dd::poly(kDfCos, deg.Jc, z);
-    df st = dev::df_mul(th, dd::poly(kDfSin, deg.Js, z));
+    const float jf = rintf(__fmul_rn(th.hi, 1.0f / kPhaseTabStep));
+    const df dl = dd::add_f(th, -__fmul_rn(jf, kPhaseTabStep));    // exact product
+    const df z = dev::df_sqr(dl);
+    const df cd = dd::poly(kDfCos, 2, z);                            // to dl^4: dl^6/6! < 5e-18
+    const df sd = dev::df_mul(dl, dd::poly(kDfSin, 2, z));
+    // (|jf| <= 0.9 kPhaseTabHalf by the host's bound on |k| x element radius;
+    // clamped so that no value can index outside the table)
+    const int jt = min(kPhaseTabHalf, max(-kPhaseTabHalf, __float2int_rn(jf)));
+    const float4 T = __ldg(deg.tab + kPhaseTabHalf + jt);
+    const df Tc{T.x, T.y}, Ts{T.z, T.w};
+    df ct = dev::df_sub(dev::df_mul(Tc, cd), dev::df_mul(Ts, sd));
+    df st = dev::df_add(dev::df_mul(Ts, cd), dev::df_mul(Tc, sd));
     if (CPLX_K) {
         const df damp = dd::poly(kDfExp, deg.Je, dd::neg(dev::df_mul(Ki, dev::df_sub(rr, r0))));
         ct = dev::df_mul(ct, damp);

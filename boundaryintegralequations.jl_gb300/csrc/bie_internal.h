@@ -189,6 +189,7 @@ struct Ctx {
     float *d_drecords = nullptr;         // E x dlay.stride words, Morton order
     float *d_dphi = nullptr;             // R x qmax x NP (hi, lo) pairs
     double df_rho_max = 0.0;             // largest |x_q - c_e| over the mesh
+    float *d_phase_tab = nullptr;        // e^{i j h} as (cos hi, lo, sin hi, lo), double-float kernels
     double *d_coords = nullptr;          // 3 x Nc geometry nodes (near-field kernels)
     int32_t *d_topo = nullptr;           // NS x E, 0-based
     std::vector<std::unique_ptr<NearField>> nearfields;

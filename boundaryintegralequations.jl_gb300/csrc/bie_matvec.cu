@@ -879,6 +879,7 @@ void launch_matvec(Ctx &c, const MatvecArgs &a) {
     if (a.precision == BIE_PREC_DF64) {
         df64::DfDegrees deg{};
         if (df64::df_degrees(std::hypot(a.k_re, a.k_im) * c.df_rho_max, std::fabs(a.k_im) * c.df_rho_max, deg)) {
+            deg.tab = reinterpret_cast<const float4 *>(c.d_phase_tab);
             if (c.lay.NP == 1) {
                 if (cplx) run_df64<1, true>(c, a, deg);
                 else run_df64<1, false>(c, a, deg);

@@ -665,6 +665,8 @@ void destroy_context(Ctx &c) {
     c.d_mphi = nullptr;
     cudaFree(c.d_drecords);
     cudaFree(c.d_dphi);
+    cudaFree(c.d_phase_tab);
+    c.d_phase_tab = nullptr;
     c.d_drecords = nullptr;
     c.d_dphi = nullptr;
     for (auto &nf : c.nearfields) free_nearfield(*nf);
