@@ -154,7 +154,7 @@ class GmresInfo(C.Structure):
 
 class SweepOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("refine", C.c_int32), ("gmres", GmresOpts),
-                ("eager", C.c_int32)]
+                ("eager", C.c_int32), ("target_error", C.c_double), ("sensitivity", C.c_void_p)]
 
 
 class SweepInfo(C.Structure):
@@ -166,6 +166,7 @@ class SweepInfo(C.Structure):
         ("solve_ms", C.c_double),
         ("record_ms", C.c_double),
         ("graph_launches", C.c_int64),
+        ("accurate_solves", C.c_int64),
     ]
 
 
@@ -230,6 +231,7 @@ SIGNATURES = {
     "bie_matvec_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_matvec_multi": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_lowp_gemm_device": (_I, [_P, _I, _I64, _I64, _I64, _P, _P, _P]),
+    "bie_ctx_set_gemm_wait": (_I, [_P, _I64, _I]),
     "bie_taylor_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
     "bie_fastop_create": (_I, [_P, _D, _D, _I, _I, _I, _D, _I, C.POINTER(_P)]),
     "bie_fastop_destroy": (_I, [_P]),

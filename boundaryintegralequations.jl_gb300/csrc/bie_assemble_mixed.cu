@@ -11,9 +11,16 @@
 //     r - r0 = (2 D.o + |o|^2) / (r + r0)  (o = x_q - c_e) stays accurate to
 //     ~1e-7 even for k r ~ 20.  sin/cos are evaluated with a quadrant reduction
 //     and Taylor polynomials on the FMA pipe.  Per-node sums are FP32 over the
-//     <= 8 points of one element; F and G accumulate across elements in
-//     complex64 with vector FP32 reductions (no read-modify-write round trip)
-//     and are widened to complex128 by a streaming pass.
+//     <= 8 points of one element.  Each (row, node) entry is written by the
+//     thread that owns the row, in the element slice the node belongs to: the
+//     node's first element in the slice stores its FP32 sums, later elements
+//     add to them in place, the last one converts the sum to complex128 and
+//     stores it (or keeps complex64 when the caller asks for complex64
+//     matrices).  The F and G partial sums travel together as one float4 in
+//     the F entry's 16 bytes, so no memset, no atomics and no widening pass
+//     touch the matrices.  Nodes touched by several slices sum their slice's
+//     contributions in a side slot; a fix-up pass adds the slots and writes
+//     those columns.
 //   * near pairs (target within one element size of the centroid, or within half
 //     an element size of a physics node: the singular and near-singular
 //     elements, which include every element containing the target node) and
@@ -31,6 +38,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 namespace bie {
 
@@ -119,12 +127,82 @@ __device__ __forceinline__ void quad_loop(const float4 *g4, const float *phc, in
 #define BIE_K2_MIN_BLOCKS 4   // resident 128-thread blocks per SM (register budget)
 #endif
 
-template <int NP, bool CPLX_K>
+__device__ __forceinline__ double2 widen2(float re, float im) { return make_double2(dev::f2d(re), dev::f2d(im)); }
+
+// fire-and-forget vector FP32 reductions (red.global.add.v4 / .v2)
+__device__ __forceinline__ void red4(float4 *p, float4 v) { atomicAdd(p, v); }
+__device__ __forceinline__ void red2(float2 *p, float2 v) { atomicAdd(p, v); }
+
+// Output of one pair's per-node sums to node a of its element under the write
+// protocol (flag word fw: first / last / shared bits of the element's nodes).
+// The widening of entries whose last contribution is not also their first
+// happens after the chunk (k2_finish_chunk).
+template <bool C64>
+__device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t side_slot, size_t off, int64_t i, int64_t M,
+                                         bool doF, bool doG, float fr, float fi, float gr, float gi,
+                                         void *__restrict__ Fo, void *__restrict__ Go, float4 *__restrict__ side) {
+    const bool first = (fw >> a) & 1u;
+    if ((fw >> (16 + a)) & 1u) {   // shared node: this slice's sum in its side slot
+        float4 *q = side + (size_t)side_slot * (size_t)M + (size_t)i;
+        const float4 v = make_float4(fr, fi, gr, gi);
+        if (first) *q = v;
+        else red4(q, v);
+        return;
+    }
+    if (C64) {   // complex64 matrices: the entry accumulates its own sum
+        float2 *pf = static_cast<float2 *>(Fo) + off, *pg = static_cast<float2 *>(Go) + off;
+        if (doF) {
+            if (first) *pf = make_float2(fr, fi);
+            else red2(pf, make_float2(fr, fi));
+        }
+        if (doG) {
+            if (first) *pg = make_float2(gr, gi);
+            else red2(pg, make_float2(gr, gi));
+        }
+        return;
+    }
+    double2 *pf = static_cast<double2 *>(Fo) + off, *pg = static_cast<double2 *>(Go) + off;
+    if (first && ((fw >> (8 + a)) & 1u)) {   // the only contribution: final value at once
+        if (doF) __stcs(pf, widen2(fr, fi));
+        if (doG) __stcs(pg, widen2(gr, gi));
+        return;
+    }
+    // partial sums (F re, F im, G re, G im) in the 16 bytes of one entry
+    float4 *q = reinterpret_cast<float4 *>(doF ? pf : pg);
+    const float4 v = make_float4(fr, fi, gr, gi);
+    if (first) *q = v;
+    else red4(q, v);
+}
+
+// After a chunk: entries whose last contribution came from the chunk (and not
+// also their first) are read back, widened to complex128 and stored; `fin`
+// lists their nodes.  Four independent loads at a time.
+__device__ __forceinline__ void k2_finish_chunk(const int32_t *fin, int nfin, int64_t i, int64_t M, bool doF,
+                                                bool doG, double2 *__restrict__ F, double2 *__restrict__ G) {
+    for (int k0 = 0; k0 < nfin; k0 += 4) {
+        float4 v[4];
+        size_t off[4];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            off[b] = (size_t)fin[min(k0 + b, nfin - 1)] * (size_t)M + (size_t)i;
+            v[b] = __ldcg(reinterpret_cast<const float4 *>((doF ? F : G) + off[b]));
+        }
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            if (k0 + b >= nfin) break;
+            if (doF) __stcs(F + off[b], widen2(v[b].x, v[b].y));
+            if (doG) __stcs(G + off[b], widen2(v[b].z, v[b].w));
+        }
+    }
+}
+
+template <int NP, bool CPLX_K, bool C64>
 __global__ void __launch_bounds__(kThreads, BIE_K2_MIN_BLOCKS)
 assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
                       const float *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
                       const double *__restrict__ tgt, int64_t M, double kre, double kim, int flags,
-                      float2 *__restrict__ F32, float2 *__restrict__ G32,
+                      void *__restrict__ Fo, void *__restrict__ Go, float4 *__restrict__ side,
+                      const uint32_t *__restrict__ kflags, const int32_t *__restrict__ kside,
                       double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
                       unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
                       unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
@@ -136,6 +214,9 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     extern __shared__ __align__(16) float smemf[];
     float *s_phi = smemf;                                   // nphi floats (padded to 4)
     float *s_rec = smemf + ((nphi + 3) & ~3);               // chunk * stride floats
+    uint32_t *s_flags = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);   // chunk
+    int32_t *s_fin = reinterpret_cast<int32_t *>(s_flags + chunk);                     // chunk * NP
+    __shared__ int s_nfin;
 
     const int s = blockIdx.y;
     const int64_t e0 = (int64_t)s * E / S;
@@ -143,6 +224,7 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
     const bool active = i < M;
     const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
+    const bool doFG = doF || doG;
 
     double tx = 0, ty = 0, tz = 0;
     if (active) {
@@ -166,25 +248,50 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             float4 *dst = reinterpret_cast<float4 *>(s_rec);
             const int n4 = n * stride / 4;
             for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
+            for (int t = threadIdx.x; t < n; t += kThreads) s_flags[t] = kflags[cb + t];
+        }
+        __syncthreads();
+        if (!C64 && doFG && threadIdx.x < 32) {
+            // nodes whose entries the chunk finishes: last, not first, not shared
+            int cnt = 0;
+            for (int b = 0; b < n * NP; b += 32) {
+                const int idx = b + (int)threadIdx.x;
+                bool need = false;
+                int32_t nd = 0;
+                if (idx < n * NP) {
+                    const int el = idx / NP, a = idx - el * NP;
+                    const uint32_t fw = s_flags[el];
+                    need = ((fw >> (8 + a)) & 1u) && !((fw >> a) & 1u) && !((fw >> (16 + a)) & 1u);
+                    nd = reinterpret_cast<const int32_t *>(s_rec + (size_t)el * stride + nidx_off)[a];
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, need);
+                if (need) s_fin[cnt + __popc(m & ((1u << threadIdx.x) - 1u))] = nd;
+                cnt += __popc(m);
+            }
+            if (threadIdx.x == 0) s_nfin = cnt;
         }
         __syncthreads();
         if (!active) continue;
 
         for (int el = 0; el < n; ++el) {
             const float *r = s_rec + (size_t)el * stride;
+            const int64_t p = cb + el;
             const mixed::PairSetup P = mixed::pair_setup<NP>(r, T);
             float fr[NP], fi[NP], gr[NP], gi[NP];
             float ce = 0.f;
+            bool listed = false;   // integrated later by the FP64 correction kernel
+#pragma unroll
+            for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.f;
             if (P.deferred) {
                 const unsigned int slot = atomicAdd(defer_count, 1u);
                 if (slot < defer_cap) {
-                    defer[slot] = make_int2((int)i, (int)(cb + el));
-                    continue;
+                    defer[slot] = make_int2((int)i, (int)p);
+                    listed = true;
+                } else {
+                    double ced;
+                    pair_fp64_inplace<NP, CPLX_K>(v64, p, tx, ty, tz, kre, kim, fr, fi, gr, gi, &ced);
+                    ce = (float)(-ced);   // stored with the sign of the FP32 path below
                 }
-                double ced;
-                pair_fp64_inplace<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, fr, fi, gr, gi,
-                                              &ced);
-                ce = (float)(-ced);   // stored with the sign of the FP32 path below
             } else {
                 const mixed::Phase ph = mixed::pair_phase(P, K);
                 const int c = P.c;
@@ -192,22 +299,25 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                 nqpe += Q;
                 const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
                 const float *phc = s_phi + (size_t)c * qmax * NPP;
-#pragma unroll
-                for (int a = 0; a < NP; ++a) fr[a] = fi[a] = gr[a] = gi[a] = 0.f;
                 if (Q == 4) quad_loop<NP, CPLX_K, 4>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
                 else if (Q == 8) quad_loop<NP, CPLX_K, 8>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
                 else quad_loop<NP, CPLX_K, 0>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
             }
-            mixed::df_accum(cacc, -ce);   // C = -sum tq
-            // F, G: vector FP32 reductions (fire-and-forget, no return value)
+            if (!listed) mixed::df_accum(cacc, -ce);   // C = -sum tq
+            if (!doFG) continue;
+            const uint32_t fw = s_flags[el];
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
 #pragma unroll
             for (int a = 0; a < NP; ++a) {
-                const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
-                if (doF) atomicAdd(F32 + off, make_float2(fr[a], fi[a]));
-                if (doG) atomicAdd(G32 + off, make_float2(gr[a], gi[a]));
+                // a listed pair adds nothing: only its first stores remain
+                if (listed && !((fw >> a) & 1u)) continue;
+                const int32_t sslot = ((fw >> (16 + a)) & 1u) ? __ldg(kside + p * NP + a) : 0;
+                k2_write<C64>(a, fw, sslot, (size_t)nid[a] * (size_t)M + (size_t)i, i, M, doF, doG, fr[a],
+                              fi[a], gr[a], gi[a], Fo, Go, side);
             }
         }
+        if (!C64 && doFG)
+            k2_finish_chunk(s_fin, s_nfin, i, M, doF, doG, static_cast<double2 *>(Fo), static_cast<double2 *>(Go));
     }
     if (active && doC) Cpart[(int64_t)s * M + i] = dev::f2d(cacc.hi) + dev::f2d(cacc.lo);
 #pragma unroll
@@ -215,19 +325,34 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
 }
 
-// complex64 -> complex128, two entries per thread per iteration (16-byte stores)
-__global__ void widen_kernel(const float4 *__restrict__ in, double2 *__restrict__ out, int64_t n2,
-                             const float2 *__restrict__ in_tail, double2 *__restrict__ out_tail,
-                             int tail) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n2; j += stride) {
-        const float4 v = in[j];
-        out[2 * j] = make_double2(dev::f2d(v.x), dev::f2d(v.y));
-        out[2 * j + 1] = make_double2(dev::f2d(v.z), dev::f2d(v.w));
-    }
-    if (tail && blockIdx.x == 0 && threadIdx.x == 0) {
-        const float2 v = in_tail[0];
-        out_tail[0] = make_double2(dev::f2d(v.x), dev::f2d(v.y));
+// Columns of the nodes shared between slices: sum of the slices' side slots
+// (nodes touched by no element: zero), written as complex128 or complex64.
+template <bool C64>
+__global__ void k2_fixup_kernel(const float4 *__restrict__ side, int64_t M, const int32_t *__restrict__ fnode,
+                                const int32_t *__restrict__ fptr, const int32_t *__restrict__ fslot, int64_t nfix,
+                                int flags, void *__restrict__ Fo, void *__restrict__ Go) {
+    const bool doF = flags & BIE_F, doG = flags & BIE_G;
+    const int64_t total = nfix * M;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t n = t / M;
+        const int64_t i = t - n * M;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int32_t q = fptr[n]; q < fptr[n + 1]; ++q) {
+            const float4 v = __ldcs(side + (size_t)fslot[q] * (size_t)M + (size_t)i);
+            acc.x += v.x;
+            acc.y += v.y;
+            acc.z += v.z;
+            acc.w += v.w;
+        }
+        const size_t off = (size_t)fnode[n] * (size_t)M + (size_t)i;
+        if (C64) {
+            if (doF) static_cast<float2 *>(Fo)[off] = make_float2(acc.x, acc.y);
+            if (doG) static_cast<float2 *>(Go)[off] = make_float2(acc.z, acc.w);
+        } else {
+            if (doF) static_cast<double2 *>(Fo)[off] = widen2(acc.x, acc.y);
+            if (doG) static_cast<double2 *>(Go)[off] = widen2(acc.z, acc.w);
+        }
     }
 }
 
@@ -291,12 +416,12 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
     if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
 }
 
-template <int NP, bool CPLX>
-void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, float2 *F32,
-               float2 *G32, double *Cpart, int2 *defer, unsigned int *dcount, unsigned int dcap,
-               double *Cnear) {
+template <int NP, bool CPLX, bool C64>
+void launch_np(Ctx &c, const AssembleArgs &a, int level, size_t smem, int chunk, float4 *side, double *Cpart,
+               int2 *defer, unsigned int *dcount, unsigned int dcap, double *Cnear) {
     const RecordLayout &L = c.lay;
     const MixedLayout &X = c.mlay;
+    const int S = 1 << level;
     RuleInfo ri{}, ri64{};
     for (int r = 0; r < L.R; ++r) {
         ri.Q[r] = L.Q[r];
@@ -305,47 +430,35 @@ void launch_np(Ctx &c, const AssembleArgs &a, int S, size_t smem, int chunk, flo
         ri64.off[r] = L.rule_off[r];
     }
     Fp64View v{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
-    auto kern = assemble_mixed_kernel<NP, CPLX>;
+    auto kern = assemble_mixed_kernel<NP, CPLX, C64>;
     BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)((a.M + kThreads - 1) / kThreads), (unsigned)S);
+    const int64_t E = c.n_elements;
     cudaEvent_t t0 = c.timer_begin();
     kern<<<grid, kThreads, smem, c.stream>>>(
-        c.d_mrecords, X.stride, X.nidx_off, c.n_elements, S, c.d_mphi,
-        L.R * L.qmax * PhiPad<NP>::value, L.qmax, ri, a.targets, a.M, a.k_re, a.k_im, a.flags,
-        F32, G32, Cpart, chunk, defer, dcount, dcap, v, c.d_qpe, a.k_dev);
+        c.d_mrecords, X.stride, X.nidx_off, E, S, c.d_mphi, L.R * L.qmax * PhiPad<NP>::value, L.qmax, ri,
+        a.targets, a.M, a.k_re, a.k_im, a.flags, a.F, a.G, side, c.d_k2_flags + (size_t)level * E,
+        c.d_k2_side + (size_t)level * E * NP, Cpart, chunk, defer, dcount, dcap, v, c.d_qpe, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     c.timer_end(t0);
     ++c.kernel_launches;
 
-    const int64_t N = c.n_sources;
-    const int64_t total = a.M * N;                 // complex entries per matrix
-    const int64_t n2 = total / 2;
-    const int tail = (int)(total & 1);
-    const unsigned wgrid = (unsigned)std::min<int64_t>((n2 + 255) / 256, 8LL * c.num_sms * 8);
-    if (a.c64_out) {   // complex64 matrices requested: add the FP64 corrections in place
-        correct_fp64_kernel<NP, CPLX, float2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
-            defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags, F32, G32, Cnear, c.d_qpe, a.k_dev);
-        BIE_CUDA(cudaGetLastError());
-        ++c.kernel_launches;
-        return;
-    }
-    if (a.flags & BIE_F) {
-        widen_kernel<<<std::max(1u, wgrid), 256, 0, c.stream>>>(
-            reinterpret_cast<const float4 *>(F32), reinterpret_cast<double2 *>(a.F), n2,
-            F32 + 2 * n2, reinterpret_cast<double2 *>(a.F) + 2 * n2, tail);
+    const int64_t nfix = c.k2_nfix[level];
+    if (nfix > 0 && (a.flags & (BIE_F | BIE_G))) {
+        const int32_t *fnode = c.d_k2_fix + c.k2_fix_off[level];
+        const int32_t *fptr = fnode + nfix;
+        const int32_t *fslot = fptr + nfix + 1;
+        const int64_t total = nfix * a.M;
+        const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 16LL * c.num_sms));
+        k2_fixup_kernel<C64><<<g, 256, 0, c.stream>>>(side, a.M, fnode, fptr, fslot, nfix, a.flags, a.F, a.G);
         BIE_CUDA(cudaGetLastError());
         ++c.kernel_launches;
     }
-    if (a.flags & BIE_G) {
-        widen_kernel<<<std::max(1u, wgrid), 256, 0, c.stream>>>(
-            reinterpret_cast<const float4 *>(G32), reinterpret_cast<double2 *>(a.G), n2,
-            G32 + 2 * n2, reinterpret_cast<double2 *>(a.G) + 2 * n2, tail);
-        BIE_CUDA(cudaGetLastError());
-        ++c.kernel_launches;
-    }
-    correct_fp64_kernel<NP, CPLX, double2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
-        defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags,
-        reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G), Cnear, c.d_qpe, a.k_dev);
+    // FP64 corrections of the deferred pairs, added to the finished entries
+    using T2 = typename std::conditional<C64, float2, double2>::type;
+    correct_fp64_kernel<NP, CPLX, T2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+        defer, dcount, dcap, v, a.targets, a.M, a.k_re, a.k_im, a.flags, reinterpret_cast<T2 *>(a.F),
+        reinterpret_cast<T2 *>(a.G), Cnear, c.d_qpe, a.k_dev);
     BIE_CUDA(cudaGetLastError());
     ++c.kernel_launches;
 }
@@ -428,18 +541,6 @@ void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
 
 void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
-    const int64_t N = c.n_sources;
-    const size_t mat32 = (size_t)a.M * N * 8;
-    float2 *F32 = nullptr, *G32 = nullptr;
-    if (a.c64_out) {   // the caller's buffers are the complex64 accumulators
-        F32 = (a.flags & BIE_F) ? reinterpret_cast<float2 *>(a.F) : nullptr;
-        G32 = (a.flags & BIE_G) ? reinterpret_cast<float2 *>(a.G) : nullptr;
-    } else {
-        F32 = (a.flags & BIE_F) ? static_cast<float2 *>(c.scratch(kScratchF32, mat32)) : nullptr;
-        G32 = (a.flags & BIE_G) ? static_cast<float2 *>(c.scratch(kScratchG32, mat32)) : nullptr;
-    }
-    if (F32) BIE_CUDA(cudaMemsetAsync(F32, 0, mat32, c.stream));
-    if (G32) BIE_CUDA(cudaMemsetAsync(G32, 0, mat32, c.stream));
     if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;
 
     // deferred-pair list: M x 64 entries + counter + near C (M doubles)
@@ -455,26 +556,31 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
     const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
     const size_t phi_f = (size_t)((L.R * L.qmax * NPP + 3) & ~3);
-    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes;
+    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * (rec_bytes + 4 + 4 * (size_t)L.NP);
     const bool cplx = a.k_im != 0.0;
+    const bool fg = (a.flags & (BIE_F | BIE_G)) != 0;
     auto run = [&](int level) {
         const int S = 1 << level;
         double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
-        if (L.NP == 1) {
-            if (cplx) launch_np<1, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-            else launch_np<1, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        } else if (L.NP == 3) {
-            if (cplx) launch_np<3, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-            else launch_np<3, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        } else {
-            if (cplx) launch_np<6, true>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-            else launch_np<6, false>(c, a, S, smem, chunk, F32, G32, Cpart, defer, dcount, dcap, Cnear);
-        }
+        float4 *side = fg ? static_cast<float4 *>(c.scratch(kScratchK2Side, (size_t)c.k2_nside[level] * a.M * 16))
+                          : nullptr;
+#define BIE_K2_LAUNCH(NP_)                                                                                       \
+    do {                                                                                                         \
+        if (a.c64_out) {                                                                                         \
+            if (cplx) launch_np<NP_, true, true>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear);  \
+            else launch_np<NP_, false, true>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear);     \
+        } else {                                                                                                 \
+            if (cplx) launch_np<NP_, true, false>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear); \
+            else launch_np<NP_, false, false>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear);    \
+        }                                                                                                        \
+    } while (0)
+        if (L.NP == 1) BIE_K2_LAUNCH(1);
+        else if (L.NP == 3) BIE_K2_LAUNCH(3);
+        else BIE_K2_LAUNCH(6);
+#undef BIE_K2_LAUNCH
         if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
     };
-    auto reset = [&] {   // fresh accumulators and deferred list
-        if (F32) BIE_CUDA(cudaMemsetAsync(F32, 0, mat32, c.stream));
-        if (G32) BIE_CUDA(cudaMemsetAsync(G32, 0, mat32, c.stream));
+    auto reset = [&] {   // fresh deferred list (every entry of F, G is overwritten)
         BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
     };
     int level = choose_slice_level(c, a.M, kThreads);
@@ -483,8 +589,8 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
         if (it != c.tuned_mixed_level.end()) {
             level = it->second;
         } else if (!c.capturing) {   // (timing needs host synchronisation)
-            // time the neighbouring slicings once (each a complete assembly on
-            // fresh accumulators) and keep the fastest for this M
+            // time the neighbouring slicings once (each a complete assembly) and
+            // keep the fastest for this M
             int best = level;
             float best_ms = 3.4e38f;
             cudaEvent_t e0, e1;

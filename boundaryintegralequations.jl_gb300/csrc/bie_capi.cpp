@@ -521,6 +521,15 @@ int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int6
     });
 }
 
+int bie_ctx_set_gemm_wait(bie_ctx *ctx, int64_t cycles, int stall) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        c.gemm_wait_cycles = cycles < 0 ? -1 : cycles;
+        c.gemm_stall = stall != 0;
+    });
+}
+
 int bie_singular_rule(int node, double offset, double *u, double *v, double *w, int capacity,
                       int *count) {
     return guarded([&] {

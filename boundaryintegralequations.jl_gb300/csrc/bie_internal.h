@@ -95,7 +95,8 @@ enum ScratchSlot {
     kScratchLowp = 12,     // multi-RHS products: strips, 16-bit tiles, partial sums
     kScratchSolverNested = 13,  // GMRES workspace + partials of nested solves, two slots
                                 // per level 1, 2 (solves inside another solve's product)
-    kScratchCount = 17
+    kScratchK2Side = 17,   // mixed assembly: per-slice partial sums of nodes shared between slices
+    kScratchCount = 18
 };
 
 // Mixed-precision element record (32-bit words, same element order as the FP64
@@ -182,6 +183,22 @@ struct Ctx {
     uint32_t *d_shared_mask = nullptr;   // kMaxLevels x E: bit a set -> node a is
                                          // touched by elements of another slice
     uint8_t *d_node_shared = nullptr;    // kMaxLevels x N: the same per node
+    // Write protocol of the mixed assembly (K2), per slicing level l, slice s
+    // covering sorted positions [s*E/S, (s+1)*E/S): for the element at
+    // position p and its local node a (node j),
+    //   bit a      : p is the first position of slice s whose element has j,
+    //   bit 8 + a  : p is the last such position,
+    //   bit 16 + a : j is touched by elements of other slices too (shared);
+    // the slice then sums its contributions to j in its side slot
+    // d_k2_side[l][p][a] (one slot per (slice, shared node)), and a fix-up pass
+    // adds the slots of every shared node (d_k2_fix[l]: nodes | CSR pointers |
+    // slots; nodes touched by no element get no slot and are written as zero).
+    uint32_t *d_k2_flags = nullptr;      // kMaxLevels x E
+    int32_t *d_k2_side = nullptr;        // kMaxLevels x E x NP (-1: not shared)
+    int32_t *d_k2_fix = nullptr;         // per level: nfix nodes, nfix + 1 pointers, slots
+    int64_t k2_fix_off[kMaxLevels] = {};
+    int64_t k2_nfix[kMaxLevels] = {};
+    int64_t k2_nside[kMaxLevels] = {};
     MixedLayout mlay;
     float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)
@@ -206,6 +223,15 @@ struct Ctx {
     // a target count M the neighbouring slicing levels are timed and the
     // fastest is kept (bie_ctx_set_autotune; bie_sweep turns it on)
     bool autotune = false;
+
+    // tensor-core GEMM pipeline waits: clock-cycle budget (negative: ~2 s) and
+    // the failure-detection test switch (bie_ctx_set_gemm_wait)
+    int64_t gemm_wait_cycles = -1;
+    bool gemm_stall = false;
+
+    // device address of the allocation-free product's static scratch array
+    // (bie_matvec_device_noalloc), looked up when the context is created
+    char *noalloc_base = nullptr;
 
     // launch statistics (bie_ctx_stats)
     std::map<int64_t, int> tuned_mixed_level;
@@ -275,6 +301,11 @@ void launch_matvec(Ctx &c, const MatvecArgs &a);
 // Mixed-precision product whose temporaries live in a fixed static device array
 // (no device allocation by the library); rejects meshes that do not fit.
 void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a);
+// At context creation: load the module holding the allocation-free product's
+// static scratch array and kernels, store the array's device address in
+// c.noalloc_base and launch those kernels once on empty work, so that a later
+// bie_matvec_device_noalloc call needs no module load and no stack growth.
+void prepare_noalloc(Ctx &c);
 
 // GMRES (bie_solver.cu); b, x device, N = n_sources
 void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,

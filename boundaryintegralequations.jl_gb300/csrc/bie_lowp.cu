@@ -44,8 +44,11 @@
 //                  tensor-memory lanes 32w .. 32w+31 = tile rows) and
 //                  coalesced stores of the partial sums, column-major.
 // Every mbarrier wait is bounded by a clock64 budget; a wait that gives up sets
-// a bit in a device error word (reported as BIE_ERR_TIMEOUT), the CTA drains
-// its own copies in flight (bounded again), frees its tensor memory and exits.
+// a bit in a device error word (reported as BIE_ERR_TIMEOUT), the CTA waits for
+// its own MMAs and copies in flight (bounded again, with the long budget),
+// frees its tensor memory and exits.  After the tensor-memory allocation no
+// path returns before the deallocation.  The pipeline waits' budget is the
+// context's (bie_ctx_set_gemm_wait), so a test can make one run out.
 #include "bie_internal.h"
 
 #include <cuda_bf16.h>
@@ -93,11 +96,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false (and bit `code` set in *err) when the budget runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code) {
+// Bounded wait: false (and bit `code` set in *err) when `budget` clock cycles
+// pass without the phase completing.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, int code,
+                                          long long budget = kWaitCycles) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > budget) {
             atomicOr(err, 1 << code);
             return false;
         }
@@ -175,6 +180,9 @@ struct GemmArgs {
     int64_t mrows_pad, ncols_pad;
     int nkb, kb_per;
     int *err;
+    long long wait_cycles;   // budget of the pipeline waits (producer, MMA issuer)
+    int stall;               // failure-detection test: the MMA issuer first waits on a
+                             // barrier that nothing completes, so its wait runs out
 };
 
 template <int NT> struct StageShape {
@@ -190,7 +198,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1) lowp_gemm_kernel(GemmArgs g) 
     uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * kStage);
     uint64_t *empty = full + STAGES;
     uint64_t *done = empty + STAGES;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    uint64_t *never = done + 1;   // completed by nothing (the stall test's wait)
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 2);
     __shared__ int s_issued, s_consumed;
 
     const int mb = blockIdx.x, nb = blockIdx.y, ks = blockIdx.z;
@@ -210,6 +219,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) lowp_gemm_kernel(GemmArgs g) 
             mbar_init(&empty[s], 1);
         }
         mbar_init(done, 1);
+        mbar_init(never, 1);
         s_issued = 0;
         s_consumed = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -226,7 +236,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) lowp_gemm_kernel(GemmArgs g) 
         int it = 0;
         for (; it < nit; ++it) {
             const int s = it % STAGES, n = it / STAGES;
-            if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, g.err, 0)) break;
+            if (n > 0 && !mbar_wait(&empty[s], (n - 1) & 1, g.err, 0, g.wait_cycles)) break;
             mbar_expect_tx(&full[s], kStage);
             uint8_t *st = smem + (size_t)s * kStage;
             const int64_t kb = kb0 + it;
@@ -243,9 +253,12 @@ __global__ void __launch_bounds__(kGemmThreads, 1) lowp_gemm_kernel(GemmArgs g) 
         // ---- MMA issuer ----
         constexpr uint32_t idesc = idesc_f16(BF ? 1u : 0u);
         int it = 0;
-        for (; it < nit; ++it) {
+        // stall test: a wait on a barrier that nothing completes runs out and
+        // the issuer gives up before its first MMA, as after a lost copy
+        if (g.stall) mbar_wait(never, 0, g.err, 4, g.wait_cycles);
+        for (; !g.stall && it < nit; ++it) {
             const int s = it % STAGES, n = it / STAGES;
-            if (!mbar_wait(&full[s], n & 1, g.err, 1)) break;
+            if (!mbar_wait(&full[s], n & 1, g.err, 1, g.wait_cycles)) break;
             tc_fence_after();
             const uint32_t a0 = smem_u32(smem + (size_t)s * kStage);
             const uint32_t b0 = a0 + NT * kATile;
@@ -299,7 +312,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) lowp_gemm_kernel(GemmArgs g) 
 template <bool SPLIT> constexpr int stages() { return SPLIT ? 2 : 4; }
 template <bool SPLIT> constexpr size_t gemm_smem() {
     return (size_t)stages<SPLIT>() * StageShape<SPLIT ? 2 : 1>::kBytes + 1024 +
-           (2 * stages<SPLIT>() + 1) * sizeof(uint64_t) + 16;
+           (2 * stages<SPLIT>() + 2) * sizeof(uint64_t) + 16;
 }
 
 // ---------------------------------------------------------------------------
@@ -593,6 +606,8 @@ void launch_gemm(Ctx &c, Format f, const uint8_t *Ahi, const uint8_t *Alo, const
     g.nkb = nkb;
     g.kb_per = kb_per;
     g.err = err;
+    g.wait_cycles = c.gemm_wait_cycles < 0 ? kWaitCycles : (long long)c.gemm_wait_cycles;
+    g.stall = c.gemm_stall ? 1 : 0;
     if (mt > 0x7fffffff || nt > 65535 || ksplit > 65535) fail(BIE_ERR_INVALID, "GEMM grid too large");
     dim3 grid((unsigned)mt, (unsigned)nt, (unsigned)ksplit);
     const double executed = 2.0 * (double)(mt * kBM) * (double)(nt * kBN) * (double)nkb * kBK * (f.split ? 3 : 1);

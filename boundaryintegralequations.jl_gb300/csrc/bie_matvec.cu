@@ -170,13 +170,19 @@ matvec_mixed_kernel(const float *__restrict__ rec, int stride, int64_t E, int S,
                 } else {   // list full: integrate this pair in FP64 in place
                     double2 pf, pg;
                     pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in, &pf, &pg);
+                    // both float parts of each FP64 value, so that the pair
+                    // keeps double-float accuracy in the row sums
                     if (doF) {
                         mixed::df_accum(yFr, (float)pf.x);
+                        mixed::df_accum(yFr, (float)(pf.x - (double)(float)pf.x));
                         mixed::df_accum(yFi, (float)pf.y);
+                        mixed::df_accum(yFi, (float)(pf.y - (double)(float)pf.y));
                     }
                     if (doG) {
                         mixed::df_accum(yGr, (float)pg.x);
+                        mixed::df_accum(yGr, (float)(pg.x - (double)(float)pg.x));
                         mixed::df_accum(yGi, (float)pg.y);
+                        mixed::df_accum(yGi, (float)(pg.y - (double)(float)pg.y));
                     }
                 }
                 continue;
@@ -499,35 +505,71 @@ void run_fp64(Ctx &c, const MatvecArgs &a) {
 // capture of a CUDA graph.  For them bie_matvec_device_noalloc keeps every
 // temporary of the product (interpolated densities, per-slice partial sums,
 // the list of pairs integrated in FP64) in one file-scope device array of
-// kNoAllocScratchBytes, which every GPU that loads the library holds until
-// the process exits.
+// kNoAllocScratchBytes.
 //
-// The array's host-side name is only a stand-in for the device symbol; its
-// device address is looked up with cudaGetSymbolAddress once per device, with
-// that device current, on the first call of the entry point on that device
-// (so that first call belongs before any stream capture).  All calls share
-// the array: the parts that must start at zero are cleared on every call, and
-// calls whose executions overlap on the GPU (different streams or contexts of
-// the same device) race on it.
+// The array belongs to this file's module, which the CUDA runtime may load
+// lazily; loading it commits the array's device memory.  prepare_noalloc runs
+// when a context is created: it looks the array's device address up with
+// cudaGetSymbolAddress (with the context's device current; the host-side name
+// of the array is only a stand-in for the device symbol), keeps it in the
+// context, and launches the product's kernels once on empty work, so that the
+// module, the kernels and their stack reservation are in place before the
+// first product.  From the first context on a device until the process exits
+// that device holds the array.  All calls share it: the parts that must start
+// at zero are cleared on every call, and calls whose executions overlap on the
+// GPU (different streams or contexts of the same device) race on it.
 // ---------------------------------------------------------------------------
 constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;   // 32 MiB
+// the last 256 bytes hold a zero word for the priming launches, outside the
+// part a product carves up, so that creating a context never disturbs a
+// product in flight on the same device
+constexpr size_t kNoAllocUsable = kNoAllocScratchBytes - 256;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void *g_noalloc_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device (looked up once).
-char *noalloc_scratch(int device) {
-    if (device < 0 || device >= kMaxDevices) fail(BIE_ERR_INVALID, "device index out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[device]) {
-        void *p = nullptr;
-        BIE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_addr[device] = p;
-    }
-    return static_cast<char *>(g_noalloc_addr[device]);
+template <int NP, bool CPLX>
+void prime_noalloc_kernels(Ctx &c, unsigned int *zero_word) {
+    // empty work: E = 0 elements and M = 0 targets, so no thread reads or
+    // writes anything but the zeroed counter
+    RuleInfo ri{};
+    const Fp64Rec v64{c.d_records, c.lay.stride, c.lay.nidx_off, c.d_phi, c.lay.qmax, ri};
+    matvec_mixed_kernel<NP, CPLX><<<dim3(1, 1), kThreads, 0, c.stream>>>(
+        c.d_mrecords, c.mlay.stride, 0, 1, ri, ri, 2, nullptr, nullptr, c.d_sources, 0, 0.0, 0.0,
+        nullptr, nullptr, 1, nullptr, zero_word, 0, v64, nullptr, nullptr, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
+    matvec_correct_kernel<NP, CPLX><<<1, 128, 0, c.stream>>>(
+        nullptr, zero_word, 0, c.d_records, c.lay.stride, c.lay.nidx_off, c.d_phi, c.lay.qmax, ri,
+        nullptr, nullptr, c.d_sources, 0.0, 0.0, nullptr, nullptr, c.d_qpe);
+    BIE_CUDA(cudaGetLastError());
 }
+
+}  // namespace
+
+void prepare_noalloc(Ctx &c) {
+    void *p = nullptr;
+    BIE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    c.noalloc_base = static_cast<char *>(p);
+    unsigned int *zero_word = reinterpret_cast<unsigned int *>(c.noalloc_base + kNoAllocUsable);
+    BIE_CUDA(cudaMemsetAsync(zero_word, 0, 256, c.stream));
+    RuleInfo ri{};
+    interp_kernel<<<1, 256, 0, c.stream>>>(c.d_records, c.lay.stride, c.lay.nidx_off, c.d_phi, c.lay.qmax,
+                                           c.lay.NP, 1, ri, 1, 2, 0, nullptr, nullptr, nullptr, nullptr);
+    BIE_CUDA(cudaGetLastError());
+    reduce_y_kernel<<<1, 256, 0, c.stream>>>(nullptr, 0, nullptr, 0, nullptr);
+    BIE_CUDA(cudaGetLastError());
+    if (c.lay.NP == 1) {
+        prime_noalloc_kernels<1, false>(c, zero_word);
+        prime_noalloc_kernels<1, true>(c, zero_word);
+    } else if (c.lay.NP == 3) {
+        prime_noalloc_kernels<3, false>(c, zero_word);
+        prime_noalloc_kernels<3, true>(c, zero_word);
+    } else {
+        prime_noalloc_kernels<6, false>(c, zero_word);
+        prime_noalloc_kernels<6, true>(c, zero_word);
+    }
+    BIE_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+namespace {
 
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -553,17 +595,27 @@ void run_mixed_noalloc(Ctx &c, const MatvecArgs &a) {
     // carve the static array: xiF | xiG | yFpart | yGpart | defer list | counter | yFn, yGn
     const size_t xi_bytes = align256((size_t)E * QTp * sizeof(float2));
     const size_t part_bytes = align256((size_t)S * M * sizeof(double2));
-    const unsigned int dcap = (unsigned int)std::min<int64_t>(M * 16 + 1024, (int64_t)1 << 30);
-    const size_t dbytes = align256((size_t)dcap * sizeof(int2));
+    // deferred-pair list: the capacity of bie_matvec_device (M*64 + 4096
+    // pairs) where it fits, shrunk for large meshes down to M*16 + 1024; a pair
+    // beyond the capacity is integrated in FP64 inside the product kernel
+    // (slower, equally accurate)
     const size_t near_bytes = align256(256 + 2 * (size_t)M * sizeof(double2));
-    const size_t need = (doF ? xi_bytes : 0) + (doG ? xi_bytes : 0) + (doF ? part_bytes : 0) +
-                        (doG ? part_bytes : 0) + dbytes + near_bytes;
-    if (need > kNoAllocScratchBytes)
+    const size_t fixed = (doF ? xi_bytes : 0) + (doG ? xi_bytes : 0) + (doF ? part_bytes : 0) +
+                         (doG ? part_bytes : 0) + near_bytes;
+    const int64_t cap_full = std::min<int64_t>(M * 64 + 4096, (int64_t)1 << 30);
+    const int64_t cap_min = M * 16 + 1024;
+    const int64_t cap_fit =
+        fixed + 256 < kNoAllocUsable ? (int64_t)((kNoAllocUsable - fixed - 256) / sizeof(int2)) : 0;
+    const unsigned int dcap = (unsigned int)std::min(cap_full, cap_fit);
+    const size_t dbytes = align256((size_t)dcap * sizeof(int2));
+    const size_t need = fixed + align256((size_t)std::max<int64_t>(dcap, cap_min) * sizeof(int2));
+    if ((int64_t)dcap < cap_min || need > kNoAllocUsable)
         fail(BIE_ERR_INVALID, "bie_matvec_device_noalloc: this mesh needs " + std::to_string(need) +
                                   " bytes of scratch, more than the fixed " +
-                                  std::to_string(kNoAllocScratchBytes) +
+                                  std::to_string(kNoAllocUsable) +
                                   "; use bie_matvec_device");
-    char *base = noalloc_scratch(c.device);
+    if (!c.noalloc_base) fail(BIE_ERR_CUDA, "allocation-free scratch was not set up for this context");
+    char *base = c.noalloc_base;
     size_t off = 0;
     float2 *xiF = nullptr, *xiG = nullptr;
     double2 *yFpart = nullptr, *yGpart = nullptr;

@@ -623,6 +623,78 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
         std::copy(shared.begin(), shared.end(), node_shared.begin() + (size_t)l * d.n_sources);
     }
 
+    // ---- write protocol of the mixed assembly per slicing level --------------
+    // Each (row, node) entry is written by the one thread that owns its row in
+    // the node's slice: its first contribution stores, later ones add, the last
+    // one converts; nodes shared between slices go through side slots.
+    std::vector<uint32_t> k2_flags((size_t)kMaxLevels * E, 0u);
+    std::vector<int32_t> k2_side((size_t)kMaxLevels * E * NP, -1);
+    std::vector<int32_t> k2_fix;
+    {
+        const int64_t Nn = d.n_sources;
+        std::vector<int64_t> stamp(Nn), fpos(Nn), lpos(Nn);
+        std::vector<int32_t> slot_of(Nn);
+        std::vector<std::vector<int32_t>> node_slots(Nn);
+        std::vector<uint8_t> touched(Nn);
+        for (int l = 0; l < kMaxLevels; ++l) {
+            const int64_t S = int64_t(1) << l;
+            const uint8_t *sh = node_shared.data() + (size_t)l * Nn;
+            std::fill(stamp.begin(), stamp.end(), -1);
+            std::fill(touched.begin(), touched.end(), 0);
+            for (auto &v : node_slots) v.clear();
+            int64_t nside = 0;
+            for (int64_t s = 0; s < S; ++s) {
+                const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
+                for (int64_t p = p0; p < p1; ++p) {
+                    const int64_t e = c.order[p];
+                    for (int a = 0; a < NP; ++a) {
+                        const int32_t nd = c.ptopo[NP * e + a];
+                        touched[nd] = 1;
+                        if (stamp[nd] != s) {
+                            stamp[nd] = s;
+                            fpos[nd] = p;
+                            if (sh[nd]) {
+                                if (nside >= INT32_MAX) fail(BIE_ERR_INVALID, "mesh too large for the slot index");
+                                slot_of[nd] = (int32_t)nside;
+                                node_slots[nd].push_back((int32_t)nside);
+                                ++nside;
+                            }
+                        }
+                        lpos[nd] = p;
+                    }
+                }
+                for (int64_t p = p0; p < p1; ++p) {
+                    const int64_t e = c.order[p];
+                    uint32_t w = 0;
+                    for (int a = 0; a < NP; ++a) {
+                        const int32_t nd = c.ptopo[NP * e + a];
+                        if (fpos[nd] == p) w |= 1u << a;
+                        if (lpos[nd] == p) w |= 1u << (8 + a);
+                        if (sh[nd]) {
+                            w |= 1u << (16 + a);
+                            k2_side[((size_t)l * E + p) * NP + a] = slot_of[nd];
+                        }
+                    }
+                    k2_flags[(size_t)l * E + p] = w;
+                }
+            }
+            // fix-up list: shared nodes with their slots, untouched nodes with none
+            std::vector<int32_t> nodes, ptr{0}, slots;
+            for (int64_t nd = 0; nd < Nn; ++nd) {
+                if (!(sh[nd] || !touched[nd])) continue;
+                nodes.push_back((int32_t)nd);
+                for (int32_t k : node_slots[nd]) slots.push_back(k);
+                ptr.push_back((int32_t)slots.size());
+            }
+            c.k2_fix_off[l] = (int64_t)k2_fix.size();
+            c.k2_nfix[l] = (int64_t)nodes.size();
+            c.k2_nside[l] = nside;
+            k2_fix.insert(k2_fix.end(), nodes.begin(), nodes.end());
+            k2_fix.insert(k2_fix.end(), ptr.begin(), ptr.end());
+            k2_fix.insert(k2_fix.end(), slots.begin(), slots.end());
+        }
+    }
+
     // ---- device upload --------------------------------------------------------
     int ndev = 0;
     BIE_CUDA(cudaGetDeviceCount(&ndev));
@@ -647,7 +719,15 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
                         cudaMemcpyHostToDevice));
     BIE_CUDA(cudaMemcpy(c.d_shared_mask, masks.data(), masks.size() * sizeof(uint32_t),
                         cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMalloc(&c.d_k2_flags, k2_flags.size() * sizeof(uint32_t)));
+    BIE_CUDA(cudaMalloc(&c.d_k2_side, k2_side.size() * sizeof(int32_t)));
+    BIE_CUDA(cudaMalloc(&c.d_k2_fix, std::max<size_t>(1, k2_fix.size()) * sizeof(int32_t)));
+    BIE_CUDA(cudaMemcpy(c.d_k2_flags, k2_flags.data(), k2_flags.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    BIE_CUDA(cudaMemcpy(c.d_k2_side, k2_side.data(), k2_side.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (!k2_fix.empty())
+        BIE_CUDA(cudaMemcpy(c.d_k2_fix, k2_fix.data(), k2_fix.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     build_mixed_records(c, rec);
+    prepare_noalloc(c);
 }
 
 void destroy_context(Ctx &c) {
@@ -659,6 +739,12 @@ void destroy_context(Ctx &c) {
     cudaFree(c.d_shared_mask);
     cudaFree(c.d_node_shared);
     c.d_node_shared = nullptr;
+    cudaFree(c.d_k2_flags);
+    cudaFree(c.d_k2_side);
+    cudaFree(c.d_k2_fix);
+    c.d_k2_flags = nullptr;
+    c.d_k2_side = nullptr;
+    c.d_k2_fix = nullptr;
     cudaFree(c.d_mrecords);
     cudaFree(c.d_mphi);
     c.d_mrecords = nullptr;

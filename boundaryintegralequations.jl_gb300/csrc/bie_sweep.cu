@@ -41,6 +41,11 @@ namespace bie {
 
 namespace {
 
+// Typical relative surface-pressure error of a mixed solve at unit
+// sensitivity (the FP32 rounding of the assembly and of the complex64
+// matrices), the scale of the sensitivity estimate in the re-solve test.
+constexpr double kMixedSweepError = 1.5e-7;
+
 __global__ void one_minus_kernel(const double2 *__restrict__ C, double2 *__restrict__ d, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) d[i] = make_double2(1.0 - C[i].x, -C[i].y);
@@ -90,6 +95,57 @@ __global__ void sweep_next_kernel(int *j, int nk, unsigned long long *__restrict
     cudaGraphSetConditional(h, jj + 1 < nk ? 1u : 0u);
 }
 
+// Sensitivity estimate of a mixed solve (no reference counterpart): with z a
+// fixed pseudo-random vector, y ~ A^{-1} z (a short GMRES solve with the
+// complex64 matrix) and wz = A z,  amp = |A z| |y| / |z|^2  estimates how much
+// the solve magnifies a relative perturbation of A or b that is spread over
+// all singular directions, as the FP32 rounding of the mixed assembly is
+// (about 1 away from the mesh's interior resonances, large near them).
+__global__ void sweep_probe_init_kernel(double2 *__restrict__ z, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        // (+-1 +- i) / sqrt 2 from a 64-bit hash of the index
+        uint64_t h = (uint64_t)i * 0x9E3779B97F4A7C15ull;
+        h ^= h >> 31;
+        h *= 0xBF58476D1CE4E5B9ull;
+        h ^= h >> 29;
+        const double a = 0.7071067811865476;
+        z[i] = make_double2((h & 1u) ? a : -a, (h & 2u) ? a : -a);
+    }
+}
+
+__global__ void sweep_amp_kernel(const double2 *__restrict__ wz, const double2 *__restrict__ y,
+                                 const double2 *__restrict__ z, int64_t n, const int *__restrict__ jd, int jhost,
+                                 double *__restrict__ amp) {
+    __shared__ double s[3][32];
+    double a = 0, b = 0, c = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        a += wz[i].x * wz[i].x + wz[i].y * wz[i].y;
+        b += y[i].x * y[i].x + y[i].y * y[i].y;
+        c += z[i].x * z[i].x + z[i].y * z[i].y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        s[0][w] = a;
+        s[1][w] = b;
+        s[2][w] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = b = c = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            a += s[0][k];
+            b += s[1][k];
+            c += s[2][k];
+        }
+        amp[jd ? *jd : jhost] = c > 0 ? sqrt(a * b) / c : 0.0;
+    }
+}
+
 struct DevBuf {
     void *p = nullptr;
     explicit DevBuf(size_t bytes) { BIE_CUDA(cudaMalloc(&p, bytes)); }
@@ -110,6 +166,11 @@ struct MeshRun {
     double kmax = 0;  // largest |k| of the sweep (the double-float phase tables' bound)
     DevBuf F, G, vec, P, dinfo, kb, ctl, tsb;
     double2 *Cv, *dg, *b, *wd, *X;
+    double2 *pz = nullptr, *py = nullptr, *pw = nullptr;   // sensitivity probe: z, y ~ A^-1 z, A z
+    double *amp = nullptr;                                 // nk sensitivity estimates (device)
+    bool probe = false;
+    bie_gmres_opts gp{};                                   // the probe's short solve
+    bie_gmres_info *dgi_probe = nullptr;
     bie_gmres_info *dgi;
     double *ks_d, *kcur;
     int *jd;
@@ -122,15 +183,35 @@ struct MeshRun {
     MeshRun(Ctx &ctx, int nk_, const double *ks, const double *w, const bie_sweep_opts &o)
         : c(ctx), N(ctx.n_sources), nk(nk_), mixed(o.precision == BIE_PREC_MIXED),
           df64(o.precision == BIE_PREC_DF64),
-          F((size_t)N * N * (mixed ? 8 : 16)), G((size_t)N * N * (mixed ? 8 : 16)), vec(4 * (size_t)N * 16),
-          P((size_t)(nk + 1) * N * 16), dinfo((size_t)nk * sizeof(bie_gmres_info)),
+          F((size_t)N * N * (mixed ? 8 : 16)), G((size_t)N * N * (mixed ? 8 : 16)),
+          vec(7 * (size_t)N * 16 + (size_t)nk * 8),
+          P((size_t)(nk + 1) * N * 16), dinfo((size_t)(nk + 1) * sizeof(bie_gmres_info)),
           kb(((size_t)2 * nk + 2) * sizeof(double)), ctl(256), tsb((size_t)3 * nk * 8), hinfo(nk) {
         Cv = vec.as<double2>();
         dg = Cv + N;
         b = dg + N;
         wd = b + N;
+        pz = wd + N;
+        py = pz + N;
+        pw = py + N;
+        amp = reinterpret_cast<double *>(pw + N);
         X = P.as<double2>();
         dgi = dinfo.as<bie_gmres_info>();
+        dgi_probe = dgi + nk;
+        probe = mixed && o.target_error > 0;
+        if (probe) {
+            BIE_CUDA(cudaMemsetAsync(amp, 0, (size_t)nk * 8, c.stream));
+            sweep_probe_init_kernel<<<(unsigned)std::min<int64_t>((N + 255) / 256, 4LL * c.num_sms), 256, 0,
+                                      c.stream>>>(pz, N);
+            BIE_CUDA(cudaGetLastError());
+            ++c.kernel_launches;
+            // a few Arnoldi cycles to 1e-4: enough to resolve the near-null
+            // direction, whose share of a random z is about 1 / sqrt(N)
+            gp.restart = 20;
+            gp.maxiter = 40;
+            gp.reltol = 1e-4;
+            gp.precision = BIE_PREC_MIXED;
+        }
         ks_d = kb.as<double>();
         kcur = ks_d + 2 * nk;
         jd = ctl.as<int>();
@@ -186,6 +267,11 @@ struct MeshRun {
         rhs();
         run_gmres(c, op, reinterpret_cast<const double *>(b), reinterpret_cast<double *>(X + (size_t)j * N), go,
                   hinfo[j]);
+        if (probe) {
+            bie_gmres_info pi{};
+            run_gmres(c, op, reinterpret_cast<const double *>(pz), reinterpret_cast<double *>(py), gp, pi);
+            finish_probe(nullptr, j);
+        }
         BIE_CUDA(cudaEventRecord(e[2], c.stream));
         BIE_CUDA(cudaStreamSynchronize(c.stream));
         float ta = 0, tsv = 0;
@@ -193,6 +279,13 @@ struct MeshRun {
         BIE_CUDA(cudaEventElapsedTime(&tsv, e[1], e[2]));
         asm_ms += ta;
         sol_ms += tsv;
+    }
+    // amp[j] from y and A z
+    void finish_probe(const int *jdev, int jhost) {
+        apply_operator(c, op, BIE_PREC_MIXED, reinterpret_cast<const double *>(pz), reinterpret_cast<double *>(pw));
+        sweep_amp_kernel<<<1, 1024, 0, c.stream>>>(pw, py, pz, N, jdev, jhost, amp);
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
     }
     // record wavenumbers 1 .. nk-1 as a WHILE node appended on `top`; the loop
     // body is captured on the context stream, the GMRES bodies on body[0..3]
@@ -212,6 +305,11 @@ struct MeshRun {
         // the solve writes the extra column X[nk] and dgi[0]; the store moves them
         double2 *xs = X + (size_t)nk * N;
         capture_gmres(c, op, reinterpret_cast<const double *>(b), reinterpret_cast<double *>(xs), go, dgi, body);
+        if (probe) {
+            capture_gmres(c, op, reinterpret_cast<const double *>(pz), reinterpret_cast<double *>(py), gp, dgi_probe,
+                          body);
+            finish_probe(jd, 0);
+        }
         sweep_store_kernel<<<(unsigned)std::min<int64_t>((N + 255) / 256, 4LL * c.num_sms), 256, 0, c.stream>>>(
             xs, X, N, jd, dgi, dgi);
         BIE_CUDA(cudaGetLastError());
@@ -231,6 +329,43 @@ struct MeshRun {
             asm_ms += 1e-6 * (double)(hts[3 * j + 1] - hts[3 * j]);
             sol_ms += 1e-6 * (double)(hts[3 * j + 2] - hts[3 * j + 1]);
         }
+    }
+    // Solves whose sensitivity estimate times the mixed path's typical error
+    // exceeds opts.target_error are solved again at FP64 grade: double-float
+    // assembly of complex128 F, G, C and FP64 GMRES, launch by launch.
+    void accurate_pass(int m, const double *ks, const double *w, const bie_sweep_opts &o, bie_sweep_info &info,
+                       const cudaEvent_t *e) {
+        if (!probe) return;
+        std::vector<double> amph((size_t)nk);
+        BIE_CUDA(cudaMemcpyAsync(amph.data(), amp, (size_t)nk * 8, cudaMemcpyDeviceToHost, c.stream));
+        BIE_CUDA(cudaStreamSynchronize(c.stream));
+        if (o.sensitivity)
+            for (int j = 0; j < nk; ++j) o.sensitivity[(size_t)m * nk + j] = amph[j];
+        std::vector<int> flag;
+        for (int j = 0; j < nk; ++j)
+            if (!(amph[j] * kMixedSweepError <= o.target_error)) flag.push_back(j);   // NaN: re-solve too
+        if (flag.empty()) return;
+        const int nf = (int)flag.size();
+        std::vector<double> kf((size_t)2 * nf);
+        for (int t = 0; t < nf; ++t) {
+            kf[2 * t] = ks[2 * flag[t]];
+            kf[2 * t + 1] = ks[2 * flag[t] + 1];
+        }
+        bie_sweep_opts od = o;
+        od.precision = BIE_PREC_DF64;
+        od.refine = 0;
+        od.target_error = 0;
+        od.eager = 1;
+        MeshRun rd(c, nf, kf.data(), w, od);
+        for (int t = 0; t < nf; ++t) {
+            rd.eager(t, kf.data(), e);
+            BIE_CUDA(cudaMemcpyAsync(X + (size_t)flag[t] * N, rd.X + (size_t)t * N, (size_t)N * 16,
+                                     cudaMemcpyDeviceToDevice, c.stream));
+            hinfo[flag[t]] = rd.hinfo[t];
+        }
+        asm_ms += rd.asm_ms;
+        sol_ms += rd.sol_ms;
+        info.accurate_solves += nf;
     }
     void finish(double *p_host, int m, bie_sweep_info &info, int32_t *iters) {
         BIE_CUDA(cudaMemcpyAsync(p_host, X, (size_t)nk * N * 16, cudaMemcpyDeviceToHost, c.stream));
@@ -335,6 +470,7 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
             c.autotune = true;   // the first wavenumber of a mesh picks its slicing
             MeshRun r(c, nk, ks, w[m], o);
             for (int j = 0; j < nk; ++j) r.eager(j, ks, ev.e);
+            r.accurate_pass(m, ks, w[m], o, info, ev.e);
             r.finish(p[m], m, info, iters);
         }
         return;
@@ -361,6 +497,7 @@ void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const doub
     BIE_CUDA(cudaStreamSynchronize(gs.top));
     for (int m = 0; m < nmesh; ++m) {
         runs[m]->collect();
+        runs[m]->accurate_pass(m, ks, w[m], o, info, ev.e);
         runs[m]->finish(p[m], m, info, iters);
     }
 }

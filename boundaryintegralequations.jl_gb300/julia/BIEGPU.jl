@@ -322,10 +322,12 @@ struct SweepOpts
     gprecision::Int32; grefine::Int32; inner_reltol::Float64; max_refine::Int32
     initially_nonzero::Int32
     eager::Int32                 # 0: the sweep of each mesh replays one CUDA graph
+    target_error::Float64        # mixed: re-solve at FP64 grade where 1.5e-7 x sensitivity exceeds it
+    sensitivity::Ptr{Float64}    # optional nmesh x nk output of the sensitivity estimates
 end
 struct SweepInfo
     solves::Int64; converged::Int64; iterations::Int64; assemble_ms::Float64; solve_ms::Float64
-    record_ms::Float64; graph_launches::Int64
+    record_ms::Float64; graph_launches::Int64; accurate_solves::Int64
 end
 
 """
@@ -333,14 +335,17 @@ end
 
 For every mesh m and wavenumber k_j: assemble F, G, C on the device and solve
 (F + Diagonal(1 .- C)) p = G w_m with GMRES; returns one N_m x length(ks)
-matrix per mesh.
+matrix per mesh.  With `precision=:mixed`, solves whose estimated error
+exceeds `target_error` (near the mesh's interior resonances) are solved again
+at FP64 grade.
 """
-function sweep_gpu(meshes, ks, ws; precision=:mixed, refine=true, ctxs=nothing)
+function sweep_gpu(meshes, ks, ws; precision=:mixed, refine=true, ctxs=nothing, target_error=1e-6)
     cs = ctxs === nothing ? [Context(m; n=2, m=2) for m in meshes] : ctxs
     kv = ComplexF64.(ks)
     wv = [Vector{ComplexF64}(w) for w in ws]
     ps = [Matrix{ComplexF64}(undef, c.n_sources, length(kv)) for c in cs]
-    opts = Ref(SweepOpts(precision_code(precision), refine, 0, 0, 0.0, 0.0, 0, 0, 0.0, 0, 0, 0))
+    tgt = precision == :mixed ? Float64(target_error) : 0.0
+    opts = Ref(SweepOpts(precision_code(precision), refine, 0, 0, 0.0, 0.0, 0, 0, 0.0, 0, 0, 0, tgt, C_NULL))
     info = Ref{SweepInfo}()
     GC.@preserve cs kv wv ps begin
         hs = [c.handle for c in cs]

@@ -302,13 +302,19 @@ BIE_API int bie_matvec_device(bie_ctx *ctx, double k_re, double k_im,
  * synchronise the device.  Such a caller creates the context once at set-up,
  * then calls this function as often as it likes; it performs no cudaMalloc or
  * cudaFree.  All temporaries live in one fixed 32 MiB device array inside the
- * library (held by every GPU that loads the library until the process exits);
- * a mesh whose product needs more returns BIE_ERR_INVALID with the size in the
- * message.  The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress), so make it before any stream capture.  Every call
- * reuses the same array: calls whose executions overlap on the GPU race and
- * must be serialised by the caller.  Inputs and outputs are device pointers as
- * in bie_matvec_device; the call is asynchronous on the context stream.
+ * library (32 MiB - 256 bytes usable); a mesh whose product needs more returns
+ * BIE_ERR_INVALID with the size in the message.  The array is committed when
+ * the first context on a device is created (bie_ctx_create and
+ * bie_ctx_create_rules load the module holding it, look its device address up
+ * into the context and launch its kernels once on empty work) and stays held
+ * by that device until the process exits.  The address is kept per context, so
+ * a context must not be used across a reset of its device (cudaDeviceReset,
+ * CUDA.jl's device_reset!).  Every call reuses the same array: calls whose
+ * executions overlap on the GPU race and must be serialised by the caller.
+ * Inputs and outputs are device pointers as in bie_matvec_device; the call is
+ * asynchronous on the context stream.  Results agree with bie_matvec_device
+ * to the mixed-precision tolerance (same deferred-pair capacity, M*64+4096
+ * pairs integrated by the FP64 correction kernel).
  */
 BIE_API int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im,
                                       const double *d_targets, int64_t n_targets,
@@ -351,6 +357,19 @@ BIE_API int bie_matvec_multi(bie_ctx *ctx, double k_re, double k_im, int64_t nrh
  */
 BIE_API int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int64_t K,
                                  const float *d_A, const float *d_B, double *d_C);
+
+/*
+ * Failure detection of the tensor-core GEMM (no reference counterpart; the
+ * reference has no device code).  Every mbarrier wait of the GEMM kernel gives
+ * up after a clock-cycle budget, sets a bit in a device error word and lets
+ * the CTA wait for its own MMAs and copies, free its tensor memory and exit;
+ * the call then returns BIE_ERR_TIMEOUT and the context stays usable.
+ * `cycles` sets the budget of the pipeline waits of this context's later GEMMs
+ * (negative: the default, about 2 s at 2 GHz); `stall` != 0 makes their MMA
+ * issuer first wait on a barrier that nothing completes, so that the wait runs
+ * out (for tests of this path).  The clean-up waits keep the default budget.
+ */
+BIE_API int bie_ctx_set_gemm_wait(bie_ctx *ctx, int64_t cycles, int stall);
 
 /* ---- near field (sparse) --------------------------------------------- */
 /*
@@ -509,6 +528,14 @@ typedef struct bie_sweep_opts {
                                   the rest of the sweep is one launch of a recorded CUDA
                                   graph (every mesh's matrices resident at once);
                                   1: launch by launch, one mesh's matrices at a time     */
+    double  target_error;      /* mixed only; > 0: after each solve a short GMRES solve
+                                  with a fixed pseudo-random right-hand side estimates the
+                                  system's sensitivity s (about 1 away from interior
+                                  resonances, large near them); solves whose predicted
+                                  error 1.5e-7 s exceeds target_error are solved again at
+                                  FP64 grade (double-float assembly + FP64 GMRES).
+                                  0: off                                                 */
+    double *sensitivity;       /* optional host output, nmesh x nk: the estimates s     */
 } bie_sweep_opts;
 
 typedef struct bie_sweep_info {
@@ -519,6 +546,7 @@ typedef struct bie_sweep_info {
     double  solve_ms;          /* device time of right-hand sides + GMRES                */
     double  record_ms;         /* host time spent recording + instantiating graphs       */
     int64_t graph_launches;    /* CUDA graph launches (1 per sweep unless eager)         */
+    int64_t accurate_solves;   /* solves redone at FP64 grade (opts.target_error)        */
 } bie_sweep_info;
 
 /*

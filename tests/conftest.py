@@ -1,6 +1,7 @@
 """Shared test set-up: import paths, the ``gpu`` marker and common meshes."""
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
@@ -12,9 +13,13 @@ for p in (str(PKG), str(ROOT)):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-# The reference's COMSOL mesh fixtures are read in place when the reference
-# tree is mounted (CPU tests only); tests that need them skip otherwise.
-REFERENCE_MESHES = Path("/root/reference/examples/meshes")
+# The reference's COMSOL mesh fixtures (its examples/meshes folder) are read in
+# place where a checkout of the reference is available (CPU tests only): the
+# folder named by BIE_REFERENCE_MESHES, else examples/meshes of a checkout
+# named "reference" beside this repository.  Tests that need them skip
+# otherwise.
+REFERENCE_MESHES = Path(os.environ.get("BIE_REFERENCE_MESHES")
+                        or ROOT.parent / "reference" / "examples" / "meshes")
 
 
 def pytest_configure(config):

@@ -68,6 +68,36 @@ def test_gemm_integer_exact(small_ctx, prec, M, N, K):
     assert torch.equal(Cm, ref), float((Cm - ref).abs().max())
 
 
+@pytest.mark.parametrize("prec", ["fp16", "fp16_split"])
+def test_gemm_wait_gives_up_and_context_recovers(prec):
+    """The GEMM's bounded waits: with the stall switch its MMA issuer waits on a
+    barrier that nothing completes, with a budget of 2e6 clock cycles (~1 ms).
+    The wait runs out, the CTAs wait for their own copies, free their tensor
+    memory and exit, and the call returns BIE_ERR_TIMEOUT.  The same context
+    then gives bit-exact results again (integer-valued operands)."""
+    torch = _torch()
+    ctx = biegpu.Context(bm.icosphere(3, geometry="quadratic"), n=2, m=2, device=0)
+    L = _capi.lib()
+    M, N, K = 300, 520, 1000
+    g = torch.Generator(device="cpu").manual_seed(5)
+    A = torch.randint(-15, 16, (M, K), generator=g).double()
+    B = torch.randint(-15, 16, (N, K), generator=g).double()
+    ref = A @ B.T
+    dev = torch.device("cuda:0")
+    Ad, Bd = A.float().to(dev), B.float().to(dev)
+    assert torch.equal(_gemm(ctx, prec, Ad, Bd).cpu(), ref)
+    _capi.check(L.bie_ctx_set_gemm_wait(ctx.handle, 2_000_000, 1))
+    Cm = torch.empty((M, N), dtype=torch.float64, device=dev)
+    st = L.bie_lowp_gemm_device(ctx.handle, _capi.PRECISION[prec], M, N, K, Ad.data_ptr(), Bd.data_ptr(),
+                                Cm.data_ptr())
+    assert st == _capi.BIE_ERR_TIMEOUT
+    assert "gave up" in L.bie_last_error().decode()
+    _capi.check(L.bie_ctx_set_gemm_wait(ctx.handle, -1, 0))
+    for _ in range(2):
+        assert torch.equal(_gemm(ctx, prec, Ad, Bd).cpu(), ref)
+    ctx.close()
+
+
 @pytest.mark.parametrize("prec", ["fp16", "bf16", "fp16_split", "bf16_split"])
 def test_gemm_gaussian(small_ctx, prec):
     torch = _torch()
