@@ -263,7 +263,7 @@ def sweep_bench(args, rank, world, max_over_ranks):
     ws = [rng.normal(size=m.n_sources) + 1j * rng.normal(size=m.n_sources) for m in meshes]
     biegpu.sweep(meshes, ks[:1], ws, precision="mixed")      # warm-up (contexts, modules)
     t0 = time.perf_counter()
-    pm, im = biegpu.sweep(meshes, ks, ws, precision="mixed")
+    pm, im = biegpu.sweep(meshes, ks, ws, precision="mixed", target_error=args.sweep_target)
     t_mixed = max_over_ranks(time.perf_counter() - t0)
     # FP64-grade: double-float assembly + FP64 GMRES on complex128 matrices, all wavenumbers
     t0 = time.perf_counter()
@@ -290,6 +290,8 @@ def sweep_bench(args, rank, world, max_over_ranks):
             "seconds": t_mixed, "assemble_ms": im["assemble_ms"], "solve_ms": im["solve_ms"],
             "graph_launches": im["graph_launches"], "converged": im["converged"],
             "gmres_iterations_mean": im["iterations"] / max(im["solves"], 1),
+            "target_error": args.sweep_target, "accurate_solves": im.get("accurate_solves", 0),
+            "sensitivity_max": float(np.max(im["sensitivity"])) if "sensitivity" in im else None,
             "plain_fp64": {"value": v_fp64, "solves": i64["solves"] * world, "wavenumbers_per_mesh": len(sel),
                            "seconds": t_fp64, "converged": i64["converged"]},
             "df64": {"value": v_df, "solves": idf["solves"] * world, "seconds": t_df,
@@ -305,7 +307,8 @@ def sweep_bench(args, rank, world, max_over_ranks):
             "max_rel_err_over": f"{len(err_mx_df)} solves against the FP64-grade double-float solutions "
                                 f"and {len(err_mx_64)} against plain FP64",
             "path": "mixed assembly into complex64 matrices + GMRES (restart 20, reltol sqrt(eps)) with "
-                    "complex64 products and double-float sums, refined with exact residuals"}
+                    "complex64 products and double-float sums, refined with exact residuals; per solve a "
+                    "sensitivity estimate, and FP64-grade re-solves where 5e-7 x estimate > target_error"}
 
 
 def multi_rhs_bench(args, local, max_over_ranks):
@@ -574,6 +577,8 @@ def main():
                     help="wavenumbers per mesh timed on the plain FP64 path (the error check set)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--sweep-nk", type=int, default=64, help="wavenumbers of the sweep")
+    ap.add_argument("--sweep-target", type=float, default=1e-6,
+                    help="mixed sweep: re-solve at FP64 grade where the predicted error exceeds this (0: off)")
     ap.add_argument("--sweep-meshes", type=int, default=3, help="use the first n of the three sweep meshes")
     ap.add_argument("--no-multi", action="store_true", help="skip the multi-RHS tensor-core measurement")
     ap.add_argument("--multi-rhs", type=int, default=256)

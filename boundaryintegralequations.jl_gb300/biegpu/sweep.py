@@ -34,7 +34,7 @@ def sweep(meshes, ks, ws, precision: str = "mixed", refine: bool = True, n: int 
     ``target_error`` (mixed only): after each mixed solve a short GMRES solve
     with a pseudo-random right-hand side estimates the system's sensitivity s
     (large near the interior resonances of the mesh); solves whose predicted
-    error 1.5e-7 s exceeds ``target_error`` are solved again at FP64 grade.
+    error 5e-7 s exceeds ``target_error`` are solved again at FP64 grade.
     ``None`` or 0 turns the estimate off.  ``info["sensitivity"]`` holds the
     estimates (nmesh x nk) and ``info["accurate_solves"]`` the number redone.
     """

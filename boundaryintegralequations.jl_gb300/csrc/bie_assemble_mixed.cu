@@ -135,8 +135,8 @@ __device__ __forceinline__ void red2(float2 *p, float2 v) { atomicAdd(p, v); }
 
 // Output of one pair's per-node sums to node a of its element under the write
 // protocol (flag word fw: first / last / shared bits of the element's nodes).
-// The widening of entries whose last contribution is not also their first
-// happens after the chunk (k2_finish_chunk).
+// Entries with several contributions keep float partial sums until the
+// widening pass (k2_widen_kernel).
 template <bool C64>
 __device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t side_slot, size_t off, int64_t i, int64_t M,
                                          bool doF, bool doG, float fr, float fi, float gr, float gi,
@@ -174,28 +174,6 @@ __device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t side_slot, 
     else red4(q, v);
 }
 
-// After a chunk: entries whose last contribution came from the chunk (and not
-// also their first) are read back, widened to complex128 and stored; `fin`
-// lists their nodes.  Four independent loads at a time.
-__device__ __forceinline__ void k2_finish_chunk(const int32_t *fin, int nfin, int64_t i, int64_t M, bool doF,
-                                                bool doG, double2 *__restrict__ F, double2 *__restrict__ G) {
-    for (int k0 = 0; k0 < nfin; k0 += 4) {
-        float4 v[4];
-        size_t off[4];
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            off[b] = (size_t)fin[min(k0 + b, nfin - 1)] * (size_t)M + (size_t)i;
-            v[b] = __ldcg(reinterpret_cast<const float4 *>((doF ? F : G) + off[b]));
-        }
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-            if (k0 + b >= nfin) break;
-            if (doF) __stcs(F + off[b], widen2(v[b].x, v[b].y));
-            if (doG) __stcs(G + off[b], widen2(v[b].z, v[b].w));
-        }
-    }
-}
-
 template <int NP, bool CPLX_K, bool C64>
 __global__ void __launch_bounds__(kThreads, BIE_K2_MIN_BLOCKS)
 assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
@@ -215,8 +193,6 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     float *s_phi = smemf;                                   // nphi floats (padded to 4)
     float *s_rec = smemf + ((nphi + 3) & ~3);               // chunk * stride floats
     uint32_t *s_flags = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);   // chunk
-    int32_t *s_fin = reinterpret_cast<int32_t *>(s_flags + chunk);                     // chunk * NP
-    __shared__ int s_nfin;
 
     const int s = blockIdx.y;
     const int64_t e0 = (int64_t)s * E / S;
@@ -249,26 +225,6 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             const int n4 = n * stride / 4;
             for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
             for (int t = threadIdx.x; t < n; t += kThreads) s_flags[t] = kflags[cb + t];
-        }
-        __syncthreads();
-        if (!C64 && doFG && threadIdx.x < 32) {
-            // nodes whose entries the chunk finishes: last, not first, not shared
-            int cnt = 0;
-            for (int b = 0; b < n * NP; b += 32) {
-                const int idx = b + (int)threadIdx.x;
-                bool need = false;
-                int32_t nd = 0;
-                if (idx < n * NP) {
-                    const int el = idx / NP, a = idx - el * NP;
-                    const uint32_t fw = s_flags[el];
-                    need = ((fw >> (8 + a)) & 1u) && !((fw >> a) & 1u) && !((fw >> (16 + a)) & 1u);
-                    nd = reinterpret_cast<const int32_t *>(s_rec + (size_t)el * stride + nidx_off)[a];
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, need);
-                if (need) s_fin[cnt + __popc(m & ((1u << threadIdx.x) - 1u))] = nd;
-                cnt += __popc(m);
-            }
-            if (threadIdx.x == 0) s_nfin = cnt;
         }
         __syncthreads();
         if (!active) continue;
@@ -309,20 +265,35 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
 #pragma unroll
             for (int a = 0; a < NP; ++a) {
-                // a listed pair adds nothing: only its first stores remain
+                // a listed pair adds nothing: only its first stores (zero) remain
                 if (listed && !((fw >> a) & 1u)) continue;
                 const int32_t sslot = ((fw >> (16 + a)) & 1u) ? __ldg(kside + p * NP + a) : 0;
                 k2_write<C64>(a, fw, sslot, (size_t)nid[a] * (size_t)M + (size_t)i, i, M, doF, doG, fr[a],
                               fi[a], gr[a], gi[a], Fo, Go, side);
             }
         }
-        if (!C64 && doFG)
-            k2_finish_chunk(s_fin, s_nfin, i, M, doF, doG, static_cast<double2 *>(Fo), static_cast<double2 *>(Go));
     }
     if (active && doC) Cpart[(int64_t)s * M + i] = dev::f2d(cacc.hi) + dev::f2d(cacc.lo);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nqpe += __shfl_down_sync(0xffffffffu, nqpe, o);
     if ((threadIdx.x & 31) == 0 && nqpe) atomicAdd(qpe_count, nqpe);
+}
+
+// Entries of the nodes with several contributions in their one slice: the
+// float4 partial sums (F re, F im, G re, G im) in the first 16 bytes of each
+// entry become the complex128 F and G entries, in place.
+__global__ void k2_widen_kernel(int64_t M, const int32_t *__restrict__ wnode, int64_t nw, int flags,
+                                double2 *__restrict__ F, double2 *__restrict__ G) {
+    const bool doF = flags & BIE_F, doG = flags & BIE_G;
+    const int64_t total = nw * M;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t n = t / M;
+        const size_t off = (size_t)wnode[n] * (size_t)M + (size_t)(t - n * M);
+        const float4 v = __ldcs(reinterpret_cast<const float4 *>((doF ? F : G) + off));
+        if (doF) __stcs(F + off, widen2(v.x, v.y));
+        if (doG) __stcs(G + off, widen2(v.z, v.w));
+    }
 }
 
 // Columns of the nodes shared between slices: sum of the slices' side slots
@@ -454,6 +425,15 @@ void launch_np(Ctx &c, const AssembleArgs &a, int level, size_t smem, int chunk,
         BIE_CUDA(cudaGetLastError());
         ++c.kernel_launches;
     }
+    const int64_t nw = c.k2_nwiden[level];
+    if (!C64 && nw > 0 && (a.flags & (BIE_F | BIE_G))) {
+        const int64_t total = nw * a.M;
+        const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 16LL * c.num_sms));
+        k2_widen_kernel<<<g, 256, 0, c.stream>>>(a.M, c.d_k2_fix + c.k2_widen_off[level], nw, a.flags,
+                                                 reinterpret_cast<double2 *>(a.F), reinterpret_cast<double2 *>(a.G));
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+    }
     // FP64 corrections of the deferred pairs, added to the finished entries
     using T2 = typename std::conditional<C64, float2, double2>::type;
     correct_fp64_kernel<NP, CPLX, T2><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
@@ -556,7 +536,7 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
     const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
     const size_t phi_f = (size_t)((L.R * L.qmax * NPP + 3) & ~3);
-    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * (rec_bytes + 4 + 4 * (size_t)L.NP);
+    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * (rec_bytes + 4);
     const bool cplx = a.k_im != 0.0;
     const bool fg = (a.flags & (BIE_F | BIE_G)) != 0;
     auto run = [&](int level) {

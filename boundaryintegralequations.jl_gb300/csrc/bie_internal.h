@@ -192,13 +192,17 @@ struct Ctx {
     // the slice then sums its contributions to j in its side slot
     // d_k2_side[l][p][a] (one slot per (slice, shared node)), and a fix-up pass
     // adds the slots of every shared node (d_k2_fix[l]: nodes | CSR pointers |
-    // slots; nodes touched by no element get no slot and are written as zero).
+    // slots; nodes touched by no element get no slot and are written as zero);
+    // nodes of one slice with several contributions are widened by a
+    // streaming pass (their list follows at k2_widen_off[l]).
     uint32_t *d_k2_flags = nullptr;      // kMaxLevels x E
     int32_t *d_k2_side = nullptr;        // kMaxLevels x E x NP (-1: not shared)
     int32_t *d_k2_fix = nullptr;         // per level: nfix nodes, nfix + 1 pointers, slots
     int64_t k2_fix_off[kMaxLevels] = {};
     int64_t k2_nfix[kMaxLevels] = {};
     int64_t k2_nside[kMaxLevels] = {};
+    int64_t k2_widen_off[kMaxLevels] = {};   // d_k2_fix offset of the widening list
+    int64_t k2_nwiden[kMaxLevels] = {};      // nodes of one slice with several contributions
     MixedLayout mlay;
     float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)

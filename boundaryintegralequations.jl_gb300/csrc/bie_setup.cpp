@@ -678,10 +678,15 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
                     k2_flags[(size_t)l * E + p] = w;
                 }
             }
-            // fix-up list: shared nodes with their slots, untouched nodes with none
-            std::vector<int32_t> nodes, ptr{0}, slots;
+            // fix-up list: shared nodes with their slots, untouched nodes with
+            // none; widening list: nodes of one slice with several contributions
+            // (their entries hold float partial sums until the widening pass)
+            std::vector<int32_t> nodes, ptr{0}, slots, widen;
             for (int64_t nd = 0; nd < Nn; ++nd) {
-                if (!(sh[nd] || !touched[nd])) continue;
+                if (touched[nd] && !sh[nd]) {
+                    if (fpos[nd] != lpos[nd]) widen.push_back((int32_t)nd);
+                    continue;
+                }
                 nodes.push_back((int32_t)nd);
                 for (int32_t k : node_slots[nd]) slots.push_back(k);
                 ptr.push_back((int32_t)slots.size());
@@ -689,9 +694,12 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
             c.k2_fix_off[l] = (int64_t)k2_fix.size();
             c.k2_nfix[l] = (int64_t)nodes.size();
             c.k2_nside[l] = nside;
+            c.k2_nwiden[l] = (int64_t)widen.size();
             k2_fix.insert(k2_fix.end(), nodes.begin(), nodes.end());
             k2_fix.insert(k2_fix.end(), ptr.begin(), ptr.end());
             k2_fix.insert(k2_fix.end(), slots.begin(), slots.end());
+            c.k2_widen_off[l] = (int64_t)k2_fix.size();
+            k2_fix.insert(k2_fix.end(), widen.begin(), widen.end());
         }
     }
 

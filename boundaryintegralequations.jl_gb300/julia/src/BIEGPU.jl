@@ -49,6 +49,17 @@ struct MeshDesc
     physics_beta::Float64
 end
 
+"""
+    GPU()
+
+Backend tag of the drop-in methods: with BoundaryIntegralEquations loaded, the
+package extension BIEGPUBoundaryIntegralEquationsExt adds
+`assemble_parallel!(mesh, k, sources, GPU(); kwargs...)`,
+`FMMFOperator(mesh, k, GPU(); kwargs...)` and `FMMGOperator(mesh, k, GPU(); kwargs...)`
+to the reference's own functions, with the reference's keyword arguments.
+"""
+struct GPU end
+
 struct BIEError <: Exception
     code::Cint
     msg::String
@@ -322,7 +333,7 @@ struct SweepOpts
     gprecision::Int32; grefine::Int32; inner_reltol::Float64; max_refine::Int32
     initially_nonzero::Int32
     eager::Int32                 # 0: the sweep of each mesh replays one CUDA graph
-    target_error::Float64        # mixed: re-solve at FP64 grade where 1.5e-7 x sensitivity exceeds it
+    target_error::Float64        # mixed: re-solve at FP64 grade where 5e-7 x sensitivity exceeds it
     sensitivity::Ptr{Float64}    # optional nmesh x nk output of the sensitivity estimates
 end
 struct SweepInfo
@@ -692,7 +703,7 @@ gmres_gpu(L::GPULossyGlobalOuter, b; kwargs...) = gmres_gpu(GPULossyBlock(L, Cin
 
 version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
-export Context, reference_rules, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
+export GPU, Context, reference_rules, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
        sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective, FastFOperator, FastGOperator,
        taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu
 

@@ -532,7 +532,7 @@ typedef struct bie_sweep_opts {
                                   with a fixed pseudo-random right-hand side estimates the
                                   system's sensitivity s (about 1 away from interior
                                   resonances, large near them); solves whose predicted
-                                  error 1.5e-7 s exceeds target_error are solved again at
+                                  error 5e-7 s exceeds target_error are solved again at
                                   FP64 grade (double-float assembly + FP64 GMRES).
                                   0: off                                                 */
     double *sensitivity;       /* optional host output, nmesh x nk: the estimates s     */

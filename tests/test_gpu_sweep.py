@@ -40,7 +40,37 @@ def test_sweep_mixed_matches_fp64():
     assert imx["converged"] == imx["solves"] == 10
     for a, b in zip(pmx, p64):
         for j in range(len(ks)):
-            assert rel(a[:, j], b[:, j]) <= 1e-5
+            assert rel(a[:, j], b[:, j]) <= 1e-6
+
+
+def test_sweep_sphere_2562_all_64_wavenumbers():
+    """The sweep workload's smallest mesh (sphere f=16, 2562 nodes) at all 64
+    wavenumbers ka in [0.1, 10], which pass near the sphere's interior
+    resonances (ka = 4.49, 5.76, 9.36 ...): every mixed solution within 1e-6
+    of the plain FP64 one (the solves the sensitivity estimate flags are
+    solved again at FP64 grade: at least one here), and the FP64-grade
+    double-float sweep within 1e-10 of it.  Without the estimate the mixed
+    sweep exceeds 1e-6 next to ka = 4.49."""
+    mesh = bm.icosphere(16)
+    ks = np.linspace(0.1, 10.0, 64)
+    rng = np.random.default_rng(2026)
+    w = rng.normal(size=mesh.n_sources) + 1j * rng.normal(size=mesh.n_sources)
+    p64, i64 = biegpu.sweep([mesh], ks, [w], precision="fp64", refine=False)
+    pmx, imx = biegpu.sweep([mesh], ks, [w], precision="mixed", refine=True, target_error=1e-6)
+    pdf, idf = biegpu.sweep([mesh], ks, [w], precision="df64", refine=False)
+    assert i64["converged"] == imx["converged"] == idf["converged"] == 64
+    assert imx["accurate_solves"] >= 1 and imx["sensitivity"].shape == (1, 64)
+    err_mx = [rel(pmx[0][:, j], p64[0][:, j]) for j in range(len(ks))]
+    err_df = [rel(pdf[0][:, j], p64[0][:, j]) for j in range(len(ks))]
+    assert max(err_mx) <= 1e-6, f"worst mixed error {max(err_mx):.3e} at ka={ks[int(np.argmax(err_mx))]:.3f}"
+    assert max(err_df) <= 1e-10, f"worst double-float error {max(err_df):.3e}"
+    # the flagged solves are the ones next to the resonances, and the estimate
+    # is the same whether the sweep runs as one graph or launch by launch
+    pe, ie = biegpu.sweep([mesh], ks, [w], precision="mixed", refine=True, target_error=1e-6, eager=True)
+    np.testing.assert_allclose(ie["sensitivity"], imx["sensitivity"], rtol=1e-3)
+    assert ie["accurate_solves"] == imx["accurate_solves"]
+    pn, inf = biegpu.sweep([mesh], ks[:4], [w], precision="mixed", refine=True, target_error=0)
+    assert inf["accurate_solves"] == 0 and "sensitivity" not in inf
 
 
 @pytest.mark.parametrize("precision,refine", [("mixed", True), ("fp64", False), ("mixed", False)])
