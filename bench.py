@@ -281,6 +281,10 @@ def sweep_bench(args, rank, world, max_over_ranks):
     err_mx_64 = [rel(a[:, j], b[:, jj]) for a, b in zip(pm, p64) for jj, j in enumerate(sel)]
     err_df_64 = [rel(a[:, j], b[:, jj]) for a, b in zip(pdf, p64) for jj, j in enumerate(sel)]
     worst = int(np.argmax(err_mx_df))
+    shapes = {}
+    for n, m in named:   # launch shapes the autotuner kept for each mesh's mixed assembly
+        sh = biegpu.get_context(m, n=2, m=2).shape("mixed_assembly")
+        shapes[n] = {"level": sh[0], "records_per_chunk": sh[1], "threads_per_block": sh[2]} if sh else None
     solves = im["solves"] * world
     v_mixed = solves / t_mixed
     v_fp64 = i64["solves"] * world / t_fp64
@@ -290,6 +294,7 @@ def sweep_bench(args, rank, world, max_over_ranks):
             "seconds": t_mixed, "assemble_ms": im["assemble_ms"], "solve_ms": im["solve_ms"],
             "graph_launches": im["graph_launches"], "converged": im["converged"],
             "gmres_iterations_mean": im["iterations"] / max(im["solves"], 1),
+            "tuned_assembly_shapes": shapes,
             "target_error": args.sweep_target, "accurate_solves": im.get("accurate_solves", 0),
             "sensitivity_max": float(np.max(im["sensitivity"])) if "sensitivity" in im else None,
             "plain_fp64": {"value": v_fp64, "solves": i64["solves"] * world, "wavenumbers_per_mesh": len(sel),
@@ -396,6 +401,57 @@ def multi_rhs_bench(args, local, max_over_ranks):
             "generation_ms_per_step": st["timed_ms"] / steps,
             "max_rel_err_vs_fp64": max(errs), "median_rel_err_vs_fp64": float(np.median(errs)),
             "per_column_mixed": {"ms_per_rhs_all_k": 1e3 * t_col, "speedup": t_col * R / t}}
+
+
+def multi_solve_bench(args, local, max_over_ranks):
+    """Multi-RHS solve workload (the same quadratic sphere, 256 seeded complex
+    N(0,1) right-hand sides, wavenumbers k, k_v, k_h of air at 100 Hz):
+    (F + Diagonal(1 - C)) X = B for all columns at once
+    (bie_solve_multi_device: lockstep GMRES with tcgen05 FP16-split products,
+    refined with exact complex64 residuals to sqrt(eps)).  One column per
+    wavenumber is checked against an FP64-grade matrix-free GMRES solve
+    (double-float products of F, C from the double-float assembly)."""
+    import torch
+    import biegpu
+    from biegpu import Diagonal, GPUFOperator, gmres
+    from biegpu import mesh as bm
+    from biegpu.lossy import boundary_layer_wavenumbers
+    mesh = bm.icosphere(args.multi_f, geometry="quadratic")
+    N, R = mesh.n_sources, args.multi_rhs
+    ctx = biegpu.get_context(mesh, n=2, m=2, device=local)
+    dev = torch.device(f"cuda:{local}")
+    g = torch.Generator(device="cpu").manual_seed(2027)
+    B = torch.complex(torch.randn(R, N, generator=g, dtype=torch.float64),
+                      torch.randn(R, N, generator=g, dtype=torch.float64)).to(dev).T
+    ks = boundary_layer_wavenumbers(100.0)
+    biegpu.solve_multi(mesh, ks[0], B[:, :2], ctx=ctx)          # warm-up (modules, scratch)
+    per_k, infos, errs = [], [], []
+    for k in ks:
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        X, info = biegpu.solve_multi(mesh, k, B, ctx=ctx)
+        torch.cuda.synchronize(dev)
+        per_k.append(time.perf_counter() - t0)
+        infos.append(info)
+        Cv = torch.empty(N, dtype=torch.complex128, device=dev)
+        ctx.assemble_device(k, None, None, Cv, precision="df64")
+        c = R - 1
+        xr = gmres(GPUFOperator(mesh, k) + Diagonal(1.0 - Cv), B[:, c].contiguous(), reltol=1e-12,
+                   precision="df64")
+        errs.append(float(torch.linalg.norm(X[:, c] - xr) / torch.linalg.norm(xr)))
+        del X
+        torch.cuda.empty_cache()
+    total = max_over_ranks(sum(per_k))
+    return {"metric": "multi-RHS solves/s", "value": len(ks) * R / total, "unit": "solves/s",
+            "workload": f"quadratic sphere f={args.multi_f} ({N} nodes), {R} RHS, k, k_v, k_h (air, 100 Hz)",
+            "seconds_per_wavenumber": per_k, "passes": [i["passes"] for i in infos],
+            "inner_steps": [i["inner_steps"] for i in infos],
+            "setup_ms": [i["setup_ms"] for i in infos], "tensor_ms": [i["tensor_ms"] for i in infos],
+            "exact_ms": [i["exact_ms"] for i in infos], "converged": [i["converged"] for i in infos],
+            "max_relres": max(i["max_relres"] for i in infos),
+            "rel_err_vs_df64_matrix_free_gmres": errs,
+            "path": "mixed assembly (complex64 F) quantised once to FP16 split tiles; lockstep GMRES (restart 20, "
+                    "inner 1e-4) on tcgen05 products; refinement with exact complex64 residuals to sqrt(eps)"}
 
 
 def nearfield_bench(args, max_over_ranks):
@@ -544,6 +600,60 @@ def adjoint_bench(args, max_over_ranks):
             "gmres_iterations": [info["forward_iterations"], info["adjoint_iterations"]]}
 
 
+def profile_case(name: str) -> None:
+    """Small runs of single kernels for ncu captures (profiles/*.md give the
+    commands): `multi` (multi-RHS products: strip generation, quantisation,
+    tcgen05 GEMM, reduction; 5762-node P2 sphere, 64 RHS), `df64mv` (double-
+    float matrix-free products, same mesh), `gemv` (dense GMRES on a 6252-node
+    sphere: complex128 FP64 products), `taylor` (ROSEBEM k-derivative
+    assembly, 2562-node P2 sphere), `sweep` (mixed frequency sweep of the
+    2562-node sphere, 8 wavenumbers, launch by launch: complex64 products and
+    the exact products of the refinement residuals)."""
+    import torch
+    import biegpu
+    from biegpu import _capi
+    from biegpu import mesh as bm
+    dev = torch.device("cuda:0")
+    L = _capi.lib()
+    if name == "multi":
+        mesh = bm.icosphere(12, geometry="quadratic")
+        N, R = mesh.n_sources, 64
+        g = torch.Generator().manual_seed(1)
+        X = torch.complex(torch.randn(R, N, generator=g, dtype=torch.float64),
+                          torch.randn(R, N, generator=g, dtype=torch.float64)).to(dev).T
+        ctx = biegpu.Context(mesh, n=2, m=2)
+        Y = torch.empty((R, N), dtype=torch.complex128, device=dev).T
+        for _ in range(4):
+            _capi.check(L.bie_matvec_multi_device(ctx.handle, 4.0, 0.0, R, X.data_ptr(), None, Y.data_ptr(),
+                                                  None, _capi.PRECISION["fp16_split"], 0))
+    elif name == "df64mv":
+        mesh = bm.icosphere(12, geometry="quadratic")
+        ctx = biegpu.Context(mesh, n=2, m=2)
+        x = torch.randn(mesh.n_sources, dtype=torch.complex128, device=dev)
+        y = torch.empty_like(x)
+        for _ in range(4):
+            _capi.check(L.bie_matvec_device(ctx.handle, 4.0, 0.0, None, 0, x.data_ptr(), None, y.data_ptr(), None,
+                                            _capi.BIE_PREC_DF64))
+    elif name == "gemv":
+        from biegpu import Diagonal, gmres
+        mesh = bm.icosphere(25)
+        Fp, _, Cp = biegpu.assemble_parallel(mesh, 3.0, mesh.sources, n=2, m=2, gOn=False)
+        b = np.random.default_rng(1).normal(size=mesh.n_sources) + 0j
+        gmres(Fp + Diagonal(1.0 - Cp), b, ctx=biegpu.get_context(mesh, n=2, m=2))
+    elif name == "taylor":
+        mesh = bm.icosphere(8, geometry="quadratic")
+        for _ in range(2):
+            biegpu.taylor_assemble(mesh, 3.0, M=2, n=2, m=2)
+    elif name == "sweep":
+        mesh = bm.icosphere(16)
+        w = np.random.default_rng(2).normal(size=mesh.n_sources) + 0j
+        biegpu.sweep([mesh], np.linspace(0.5, 8.0, 8), [w], precision="mixed", eager=True, target_error=0)
+    else:
+        raise SystemExit(f"unknown profile case {name}")
+    torch.cuda.synchronize()
+    print("profile case", name, "done")
+
+
 def roofline_entry(st, kernel, bound, peak_flops, workload_name, nphys):
     kernel_ms = st["timed_ms"] / max(st["timed_launches"], 1)
     flops = st["algorithmic_flops"] / max(st["timed_launches"], 1)
@@ -584,6 +694,7 @@ def main():
     ap.add_argument("--multi-rhs", type=int, default=256)
     ap.add_argument("--multi-f", type=int, default=32, help="sphere frequency of the multi-RHS mesh (32: 40962 nodes)")
     ap.add_argument("--multi-steps", type=int, default=3)
+    ap.add_argument("--no-multi-solve", action="store_true", help="skip the multi-RHS solve")
     ap.add_argument("--multi-precision", default="fp16_split",
                     choices=["fp16", "bf16", "fp16_split", "bf16_split"])
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-gradient measurement")
@@ -592,8 +703,13 @@ def main():
     ap.add_argument("--nearfield-steps", type=int, default=3)
     ap.add_argument("--no-lossy", action="store_true", help="skip the visco-thermal system measurement")
     ap.add_argument("--lossy-steps", type=int, default=3)
+    ap.add_argument("--profile-case", default=None,
+                    help="run one small kernel case for an ncu capture and exit (see profile_case)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
 
     if args.impl == "reference":
         run_reference(args)
@@ -735,6 +851,8 @@ def main():
     multi = None
     if not args.no_multi:
         multi = multi_rhs_bench(args, local, max_over_ranks)
+        if not args.no_multi_solve:
+            multi["solve"] = multi_solve_bench(args, local, max_over_ranks)
     adjoint = None
     if not args.no_adjoint:
         adjoint = adjoint_bench(args, max_over_ranks)

@@ -13,6 +13,7 @@ from .mesh import Mesh3d, ellipsoid, icosphere, load_comsol, read_comsol  # noqa
 from .operators import (Diagonal, FMMFOperator, FMMGOperator, GPUFOperator, GPUGOperator, I,  # noqa: F401
                         UniformScaling, gmres)
 from .sweep import sweep  # noqa: F401
+from .multisolve import solve_multi  # noqa: F401
 from .adjoint import farfield_objective  # noqa: F401
 from .rosebem import apply_taylor_expansion, taylor_assemble  # noqa: F401
 from .lossy import (LossyGlobalOuter, ambient_to_properties, tangential_derivatives,  # noqa: F401

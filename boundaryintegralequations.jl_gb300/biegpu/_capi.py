@@ -170,6 +170,18 @@ class SweepInfo(C.Structure):
     ]
 
 
+class MultisolveOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("restart", C.c_int32), ("maxiter", C.c_int32),
+                ("max_refine", C.c_int32), ("reltol", C.c_double), ("inner_reltol", C.c_double)]
+
+
+class MultisolveInfo(C.Structure):
+    _fields_ = [("passes", C.c_int32), ("inner_steps", C.c_int32), ("converged", C.c_int32),
+                ("tensor_products", C.c_int32), ("exact_products", C.c_int32), ("reserved", C.c_int32),
+                ("max_relres", C.c_double), ("setup_ms", C.c_double), ("tensor_ms", C.c_double),
+                ("exact_ms", C.c_double)]
+
+
 class AdjointOpts(C.Structure):
     _fields_ = [("rho_c", C.c_double), ("dir", C.c_double * 3), ("reltol", C.c_double),
                 ("precision", C.c_int32)]
@@ -232,6 +244,10 @@ SIGNATURES = {
     "bie_matvec_multi": (_I, [_P, _D, _D, _I64, _P, _P, _P, _P, _I, _I64]),
     "bie_lowp_gemm_device": (_I, [_P, _I, _I64, _I64, _I64, _P, _P, _P]),
     "bie_ctx_set_gemm_wait": (_I, [_P, _I64, _I]),
+    "bie_solve_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, C.POINTER(MultisolveOpts),
+                                    C.POINTER(MultisolveInfo)]),
+    "bie_ctx_get_shape": (_I, [_P, _I, _I64, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
+    "bie_ctx_set_shape": (_I, [_P, _I, _I64, _I, _I, _I]),
     "bie_taylor_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),
     "bie_fastop_create": (_I, [_P, _D, _D, _I, _I, _I, _D, _I, C.POINTER(_P)]),
     "bie_fastop_destroy": (_I, [_P]),

@@ -118,9 +118,27 @@ class Context:
         _capi.check(_capi.lib().bie_ctx_set_timing(self._h, 1 if on else 0))
 
     def set_autotune(self, on: bool) -> None:
-        """Time neighbouring element slicings on the first mixed assembly per
-        target count and keep the fastest (bie_ctx_set_autotune)."""
+        """Search the launch shape (slicing, records per chunk, block size) on
+        the first call per target count of the mixed and double-float
+        assemblies and the mixed product, and keep the fastest
+        (bie_ctx_set_autotune)."""
         _capi.check(_capi.lib().bie_ctx_set_autotune(self._h, 1 if on else 0))
+
+    SHAPE_KERNELS = {"mixed_assembly": 0, "df64_assembly": 1, "mixed_product": 2}
+
+    def shape(self, kernel: str, M: int | None = None):
+        """(level, chunk, threads per block) tuned or forced for `kernel` and M
+        targets (default: the collocation nodes), or None."""
+        found, lv, ch, tp = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        _capi.check(_capi.lib().bie_ctx_get_shape(self._h, self.SHAPE_KERNELS[kernel],
+                                                  int(self.n_sources if M is None else M), C.byref(found),
+                                                  C.byref(lv), C.byref(ch), C.byref(tp)))
+        return (lv.value, ch.value, tp.value) if found.value else None
+
+    def force_shape(self, kernel: str, level: int, chunk: int = 0, tpb: int = 0, M: int = 0) -> None:
+        """Use this shape for `kernel` (M = 0: every target count); level < 0 clears it."""
+        _capi.check(_capi.lib().bie_ctx_set_shape(self._h, self.SHAPE_KERNELS[kernel], int(M), int(level),
+                                                  int(chunk), int(tpb)))
 
     def stats(self, reset: bool = False) -> dict:
         st = _capi.Stats()

@@ -178,6 +178,62 @@ int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile) {
 void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
                      double *C);
 
+LaunchShape resolve_shape(Ctx &c, int kernel, int64_t M, const LaunchShape &base, const ShapeAxes &ax,
+                          const std::function<void(const LaunchShape &)> &run, const std::function<void()> &reset) {
+    for (const int64_t key : {M, int64_t(0)}) {
+        const auto f = c.forced_shapes.find({kernel, key});
+        if (f != c.forced_shapes.end()) {
+            LaunchShape sh = f->second;
+            if (sh.level < 0 || sh.level >= kMaxLevels) sh.level = base.level;
+            if (sh.chunk <= 0) sh.chunk = base.chunk;
+            if (sh.tpb != 128 && sh.tpb != 256) sh.tpb = base.tpb;
+            return sh;
+        }
+    }
+    const auto it = c.tuned_shapes.find({kernel, M});
+    if (it != c.tuned_shapes.end()) return it->second;
+    if (!c.autotune || c.capturing) return base;   // (timing needs host synchronisation)
+    cudaEvent_t e0, e1;
+    BIE_CUDA(cudaEventCreate(&e0));
+    BIE_CUDA(cudaEventCreate(&e1));
+    LaunchShape best = base;
+    float best_ms = 3.4e38f;
+    auto time_one = [&](const LaunchShape &sh) {
+        reset();
+        BIE_CUDA(cudaEventRecord(e0, c.stream));
+        run(sh);
+        BIE_CUDA(cudaEventRecord(e1, c.stream));
+        BIE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        BIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = sh;
+        }
+    };
+    try {
+        time_one(base);
+        const LaunchShape b0 = best;
+        for (int l : ax.levels)
+            if (l != b0.level) time_one(LaunchShape{l, b0.chunk, b0.tpb});
+        const LaunchShape b1 = best;
+        for (int ch : ax.chunks)
+            if (ch != b1.chunk) time_one(LaunchShape{b1.level, ch, b1.tpb});
+        const LaunchShape b2 = best;
+        for (int t : ax.tpbs)
+            if (t != b2.tpb) time_one(LaunchShape{b2.level, b2.chunk, t});
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.tuned_shapes[{kernel, M}] = best;
+    reset();
+    return best;
+}
+
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
     const int64_t N = c.n_sources;

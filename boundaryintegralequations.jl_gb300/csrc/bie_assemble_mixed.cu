@@ -174,8 +174,8 @@ __device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t side_slot, 
     else red4(q, v);
 }
 
-template <int NP, bool CPLX_K, bool C64>
-__global__ void __launch_bounds__(kThreads, BIE_K2_MIN_BLOCKS)
+template <int NP, bool CPLX_K, bool C64, int TPB>
+__global__ void __launch_bounds__(TPB, BIE_K2_MIN_BLOCKS * 128 / TPB)
 assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
                       const float *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
                       const double *__restrict__ tgt, int64_t M, double kre, double kim, int flags,
@@ -197,7 +197,7 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     const int s = blockIdx.y;
     const int64_t e0 = (int64_t)s * E / S;
     const int64_t e1 = (int64_t)(s + 1) * E / S;
-    const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
+    const int64_t i = (int64_t)blockIdx.x * TPB + threadIdx.x;
     const bool active = i < M;
     const bool doF = flags & BIE_F, doG = flags & BIE_G, doC = flags & BIE_C;
     const bool doFG = doF || doG;
@@ -212,7 +212,7 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     const df K = dev::df_from_double(kre);
     const float kf = K.hi;
     const float kimf = (float)kim;
-    for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+    for (int t = threadIdx.x; t < nphi; t += TPB) s_phi[t] = phi[t];
 
     df cacc = {0.f, 0.f};
     unsigned long long nqpe = 0;
@@ -223,8 +223,8 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             const float4 *src = reinterpret_cast<const float4 *>(rec + cb * stride);
             float4 *dst = reinterpret_cast<float4 *>(s_rec);
             const int n4 = n * stride / 4;
-            for (int t = threadIdx.x; t < n4; t += kThreads) dst[t] = src[t];
-            for (int t = threadIdx.x; t < n; t += kThreads) s_flags[t] = kflags[cb + t];
+            for (int t = threadIdx.x; t < n4; t += TPB) dst[t] = src[t];
+            for (int t = threadIdx.x; t < n; t += TPB) s_flags[t] = kflags[cb + t];
         }
         __syncthreads();
         if (!active) continue;
@@ -388,8 +388,8 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
 }
 
 template <int NP, bool CPLX, bool C64>
-void launch_np(Ctx &c, const AssembleArgs &a, int level, size_t smem, int chunk, float4 *side, double *Cpart,
-               int2 *defer, unsigned int *dcount, unsigned int dcap, double *Cnear) {
+void launch_np(Ctx &c, const AssembleArgs &a, int level, size_t smem, int chunk, int tpb, float4 *side,
+               double *Cpart, int2 *defer, unsigned int *dcount, unsigned int dcap, double *Cnear) {
     const RecordLayout &L = c.lay;
     const MixedLayout &X = c.mlay;
     const int S = 1 << level;
@@ -401,12 +401,12 @@ void launch_np(Ctx &c, const AssembleArgs &a, int level, size_t smem, int chunk,
         ri64.off[r] = L.rule_off[r];
     }
     Fp64View v{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
-    auto kern = assemble_mixed_kernel<NP, CPLX, C64>;
+    auto kern = tpb == 256 ? assemble_mixed_kernel<NP, CPLX, C64, 256> : assemble_mixed_kernel<NP, CPLX, C64, 128>;
     BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((unsigned)((a.M + kThreads - 1) / kThreads), (unsigned)S);
+    dim3 grid((unsigned)((a.M + tpb - 1) / tpb), (unsigned)S);
     const int64_t E = c.n_elements;
     cudaEvent_t t0 = c.timer_begin();
-    kern<<<grid, kThreads, smem, c.stream>>>(
+    kern<<<grid, tpb, smem, c.stream>>>(
         c.d_mrecords, X.stride, X.nidx_off, E, S, c.d_mphi, L.R * L.qmax * PhiPad<NP>::value, L.qmax, ri,
         a.targets, a.M, a.k_re, a.k_im, a.flags, a.F, a.G, side, c.d_k2_flags + (size_t)level * E,
         c.d_k2_side + (size_t)level * E * NP, Cpart, chunk, defer, dcount, dcap, v, c.d_qpe, a.k_dev);
@@ -534,25 +534,26 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
 
     const int NPP = L.NP <= 4 ? 4 : 8;
     const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
-    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
+    const int chunk0 = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
     const size_t phi_f = (size_t)((L.R * L.qmax * NPP + 3) & ~3);
-    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * (rec_bytes + 4);
     const bool cplx = a.k_im != 0.0;
     const bool fg = (a.flags & (BIE_F | BIE_G)) != 0;
-    auto run = [&](int level) {
+    auto run = [&](const LaunchShape &sh) {
+        const int level = sh.level, chunk = sh.chunk, tpb = sh.tpb;
+        const size_t smem = phi_f * sizeof(float) + (size_t)chunk * (rec_bytes + 4);
         const int S = 1 << level;
         double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
         float4 *side = fg ? static_cast<float4 *>(c.scratch(kScratchK2Side, (size_t)c.k2_nside[level] * a.M * 16))
                           : nullptr;
-#define BIE_K2_LAUNCH(NP_)                                                                                       \
-    do {                                                                                                         \
-        if (a.c64_out) {                                                                                         \
-            if (cplx) launch_np<NP_, true, true>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear);  \
-            else launch_np<NP_, false, true>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear);     \
-        } else {                                                                                                 \
-            if (cplx) launch_np<NP_, true, false>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear); \
-            else launch_np<NP_, false, false>(c, a, level, smem, chunk, side, Cpart, defer, dcount, dcap, Cnear);    \
-        }                                                                                                        \
+#define BIE_K2_LAUNCH(NP_)                                                                                      \
+    do {                                                                                                        \
+        if (a.c64_out) {                                                                                        \
+            if (cplx) launch_np<NP_, true, true>(c, a, level, smem, chunk, tpb, side, Cpart, defer, dcount, dcap, Cnear); \
+            else launch_np<NP_, false, true>(c, a, level, smem, chunk, tpb, side, Cpart, defer, dcount, dcap, Cnear);    \
+        } else {                                                                                                \
+            if (cplx) launch_np<NP_, true, false>(c, a, level, smem, chunk, tpb, side, Cpart, defer, dcount, dcap, Cnear); \
+            else launch_np<NP_, false, false>(c, a, level, smem, chunk, tpb, side, Cpart, defer, dcount, dcap, Cnear);    \
+        }                                                                                                       \
     } while (0)
         if (L.NP == 1) BIE_K2_LAUNCH(1);
         else if (L.NP == 3) BIE_K2_LAUNCH(3);
@@ -563,41 +564,16 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     auto reset = [&] {   // fresh deferred list (every entry of F, G is overwritten)
         BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
     };
-    int level = choose_slice_level(c, a.M, kThreads);
-    if (c.autotune) {
-        const auto it = c.tuned_mixed_level.find(a.M);
-        if (it != c.tuned_mixed_level.end()) {
-            level = it->second;
-        } else if (!c.capturing) {   // (timing needs host synchronisation)
-            // time the neighbouring slicings once (each a complete assembly) and
-            // keep the fastest for this M
-            int best = level;
-            float best_ms = 3.4e38f;
-            cudaEvent_t e0, e1;
-            BIE_CUDA(cudaEventCreate(&e0));
-            BIE_CUDA(cudaEventCreate(&e1));
-            for (int l = level - 1; l <= level + 1; ++l) {
-                if (l < 0 || l >= kMaxLevels || (int64_t(1) << l) > c.n_elements) continue;
-                reset();
-                BIE_CUDA(cudaEventRecord(e0, c.stream));
-                run(l);
-                BIE_CUDA(cudaEventRecord(e1, c.stream));
-                BIE_CUDA(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                BIE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = l;
-                }
-            }
-            cudaEventDestroy(e0);
-            cudaEventDestroy(e1);
-            c.tuned_mixed_level[a.M] = best;
-            level = best;
-            reset();
-        }
-    }
-    run(level);
+    // launch shape: the heuristic one, the autotuner's choice for this M, or
+    // one a caller forced (bie_ctx_set_shape)
+    const LaunchShape base{choose_slice_level(c, a.M, kThreads), chunk0, kThreads};
+    ShapeAxes ax;
+    for (int l = base.level - 1; l <= base.level + 1; ++l)
+        if (l >= 0 && l < kMaxLevels && (int64_t(1) << l) <= c.n_elements) ax.levels.push_back(l);
+    ax.chunks = {std::max(1, chunk0 / 2), chunk0, std::min(64, 2 * chunk0)};
+    ax.tpbs = {128, 256};
+    const LaunchShape sh = resolve_shape(c, kShapeK2, a.M, base, ax, run, reset);
+    run(sh);
 }
 
 // ===========================================================================
@@ -950,8 +926,6 @@ bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
     if (!df64::df_degrees(kabs * c.df_rho_max, kimb * c.df_rho_max, deg)) return false;
     deg.tab = reinterpret_cast<const float4 *>(c.d_phase_tab);
     const int64_t N = c.n_sources;
-    if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
-    if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));
     if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return true;
 
     const unsigned int dcap = (unsigned int)std::min<int64_t>(a.M * 64 + 4096, (int64_t)1 << 30);
@@ -960,27 +934,42 @@ bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
     int2 *defer = reinterpret_cast<int2 *>(dbuf);
     unsigned int *dcount = reinterpret_cast<unsigned int *>(dbuf + dbytes);
     double *Cnear = reinterpret_cast<double *>(dbuf + dbytes + 256);
-    BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
+    auto reset = [&] {   // zeroed outputs (entries accumulate in place) and deferred list
+        if (a.flags & BIE_F) BIE_CUDA(cudaMemsetAsync(a.F, 0, (size_t)a.M * N * 16, c.stream));
+        if (a.flags & BIE_G) BIE_CUDA(cudaMemsetAsync(a.G, 0, (size_t)a.M * N * 16, c.stream));
+        BIE_CUDA(cudaMemsetAsync(dbuf + dbytes, 0, 256 + (size_t)a.M * 8, c.stream));
+    };
+    reset();
 
-    const int level = choose_slice_level(c, a.M, kThreads);
-    const int S = 1 << level;
     const size_t rec_bytes = (size_t)c.dlay.stride * sizeof(float);
-    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(32, (32u << 10) / rec_bytes));
+    const int chunk0 = (int)std::max<size_t>(1, std::min<size_t>(32, (32u << 10) / rec_bytes));
     const size_t phi_f = (size_t)((2 * L.R * L.qmax * L.NP + 3) & ~3);
-    const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes + (size_t)chunk * 4;
-    double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
     const bool cplx = a.k_im != 0.0;
-    if (L.NP == 1) {
-        if (cplx) launch_df64_np<1, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
-        else launch_df64_np<1, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
-    } else if (L.NP == 3) {
-        if (cplx) launch_df64_np<3, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
-        else launch_df64_np<3, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
-    } else {
-        if (cplx) launch_df64_np<6, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
-        else launch_df64_np<6, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
-    }
-    if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
+    auto run = [&](const LaunchShape &sh) {
+        const int level = sh.level, chunk = sh.chunk;
+        const int S = 1 << level;
+        const size_t smem = phi_f * sizeof(float) + (size_t)chunk * rec_bytes + (size_t)chunk * 4;
+        double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
+        if (L.NP == 1) {
+            if (cplx) launch_df64_np<1, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+            else launch_df64_np<1, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+        } else if (L.NP == 3) {
+            if (cplx) launch_df64_np<3, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+            else launch_df64_np<3, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+        } else {
+            if (cplx) launch_df64_np<6, true>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+            else launch_df64_np<6, false>(c, a, S, level, smem, chunk, Cpart, defer, dcount, dcap, Cnear, deg);
+        }
+        if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
+    };
+    const LaunchShape base{choose_slice_level(c, a.M, kThreads), chunk0, kThreads};
+    ShapeAxes ax;
+    for (int l = base.level - 1; l <= base.level + 1; ++l)
+        if (l >= 0 && l < kMaxLevels && (int64_t(1) << l) <= c.n_elements) ax.levels.push_back(l);
+    ax.chunks = {std::max(1, chunk0 / 2), chunk0, std::min(64, 2 * chunk0)};
+    LaunchShape sh = resolve_shape(c, kShapeK9, a.M, base, ax, run, reset);
+    sh.tpb = kThreads;   // the double-float kernel has one block size
+    run(sh);
     return true;
 }
 

@@ -227,6 +227,51 @@ int bie_ctx_set_autotune(bie_ctx *ctx, int on) {
     });
 }
 
+int bie_ctx_get_shape(bie_ctx *ctx, int kernel, int64_t M, int *found, int *level, int *chunk, int *tpb) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (!found) bie::fail(BIE_ERR_INVALID, "found must not be NULL");
+        if (kernel < 0 || kernel >= bie::kShapeCount) bie::fail(BIE_ERR_INVALID, "unknown kernel id");
+        *found = 0;
+        const bie::LaunchShape *sh = nullptr;
+        for (const int64_t key : {M, int64_t(0)}) {
+            const auto f = c.forced_shapes.find({kernel, key});
+            if (f != c.forced_shapes.end()) {
+                sh = &f->second;
+                break;
+            }
+        }
+        if (!sh) {
+            const auto t = c.tuned_shapes.find({kernel, M});
+            if (t != c.tuned_shapes.end()) sh = &t->second;
+        }
+        if (!sh) return;
+        *found = 1;
+        if (level) *level = sh->level;
+        if (chunk) *chunk = sh->chunk;
+        if (tpb) *tpb = sh->tpb;
+    });
+}
+
+int bie_ctx_set_shape(bie_ctx *ctx, int kernel, int64_t M, int level, int chunk, int tpb) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (kernel < 0 || kernel >= bie::kShapeCount) bie::fail(BIE_ERR_INVALID, "unknown kernel id");
+        if (M < 0) bie::fail(BIE_ERR_INVALID, "M must be >= 0");
+        if (level < 0) {
+            c.forced_shapes.erase({kernel, M});
+            return;
+        }
+        if (level >= bie::kMaxLevels || (int64_t(1) << level) > c.n_elements)
+            bie::fail(BIE_ERR_INVALID, "level must be in 0.." + std::to_string(bie::kMaxLevels - 1) +
+                                           " with at most one slice per element");
+        if (chunk > 64) bie::fail(BIE_ERR_INVALID, "chunk must be at most 64 records");
+        c.forced_shapes[{kernel, M}] = bie::LaunchShape{level, chunk, tpb};
+    });
+}
+
 int bie_ctx_stats(bie_ctx *ctx, bie_stats *out, int reset) {
     return guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);
@@ -518,6 +563,23 @@ int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int6
             bie::fail(BIE_ERR_INVALID, "precision must be one of the 16-bit tensor-core forms");
         BIE_CUDA(cudaSetDevice(c.device));
         bie::run_lowp_gemm(c, precision, M, N, K, d_A, d_B, d_C);
+    });
+}
+
+int bie_solve_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *d_B, double *d_X,
+                           const bie_multisolve_opts *opts, bie_multisolve_info *info) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        std::lock_guard<std::mutex> lock(c.mu);
+        if (!std::isfinite(k_re) || !std::isfinite(k_im)) bie::fail(BIE_ERR_INVALID, "k must be finite");
+        if (nrhs < 1 || nrhs > 65535) bie::fail(BIE_ERR_INVALID, "nrhs must be in 1..65535");
+        if (!d_B || !d_X) bie::fail(BIE_ERR_INVALID, "B and X must not be NULL");
+        BIE_CUDA(cudaSetDevice(c.device));
+        bie_multisolve_opts o{};
+        if (opts) o = *opts;
+        bie_multisolve_info inf{};
+        bie::run_solve_multi(c, k_re, k_im, nrhs, d_B, d_X, o, inf);
+        if (info) *info = inf;
     });
 }
 

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <memory>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <string>
@@ -78,6 +79,16 @@ struct RecordLayout {
     int stride = 0;             // doubles per record
     int qmax = 0;
 };
+
+// Launch shape of the assembly / product kernels the autotuner chooses:
+// element-slicing level (S = 2^level slices), element records per shared-
+// memory chunk, threads per block (one target row per thread).
+struct LaunchShape {
+    int level = 0;
+    int chunk = 1;
+    int tpb = 128;
+};
+enum ShapeKernel { kShapeK2 = 0, kShapeK9 = 1, kShapeK3 = 2, kShapeCount = 3 };
 
 enum ScratchSlot {
     kScratchTargets = 0,   // uploaded target points (host entry points)
@@ -238,7 +249,8 @@ struct Ctx {
     char *noalloc_base = nullptr;
 
     // launch statistics (bie_ctx_stats)
-    std::map<int64_t, int> tuned_mixed_level;
+    std::map<std::pair<int, int64_t>, LaunchShape> tuned_shapes;   // (kernel, M) -> tuned shape
+    std::map<std::pair<int, int64_t>, LaunchShape> forced_shapes;  // bie_ctx_set_shape (M = 0: any M)
     bool timing = false;
     int64_t kernel_launches = 0;
     int64_t timed_launches = 0;
@@ -288,6 +300,17 @@ struct AssembleArgs {
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
+// Candidate values per axis of the shape search.
+struct ShapeAxes {
+    std::vector<int> levels, chunks, tpbs;
+};
+// The shape for (kernel, M): a forced one (bie_ctx_set_shape), else the cached
+// tuned one, else -- with autotuning on and no graph being recorded -- a
+// coordinate search (slicing level, then records per chunk, then block size,
+// each candidate timed as a complete operation by CUDA events on the context
+// stream after `reset`), cached per (kernel, M); else `base`.
+LaunchShape resolve_shape(Ctx &c, int kernel, int64_t M, const LaunchShape &base, const ShapeAxes &ax,
+                          const std::function<void(const LaunchShape &)> &run, const std::function<void()> &reset);
 void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
                      double *C);
 
@@ -431,6 +454,17 @@ struct MultiArgs {
     int64_t scratch_bytes;   // cap of the strip scratch (<= 0: default)
 };
 void run_matvec_multi(Ctx &c, const MultiArgs &a);
+// A complex64 N x N matrix (device, column-major) quantised once to resident
+// 16-bit tensor-core tiles (precision BIE_PREC_FP16 ... BF16_SPLIT), applied to
+// blocks of right-hand sides: Y = A X, X and Y N x R complex128 (device).  The
+// apply synchronises the context stream (it reads the GEMM's error word).
+struct LowpMatrix;
+LowpMatrix *lowp_matrix_create(Ctx &c, const float *A, int64_t n, int precision);
+void lowp_matrix_apply(Ctx &c, LowpMatrix &m, const double *X, int64_t R, double *Y);
+void lowp_matrix_destroy(LowpMatrix *m);
+// Multi-right-hand-side solve (bie_multisolve.cu)
+void run_solve_multi(Ctx &c, double k_re, double k_im, int64_t R, const double *B, double *X,
+                     const bie_multisolve_opts &o, bie_multisolve_info &info);
 void run_lowp_gemm(Ctx &c, int precision, int64_t M, int64_t N, int64_t K, const float *A, const float *B,
                    double *C);
 

@@ -848,4 +848,100 @@ void run_matvec_multi(Ctx &c, const MultiArgs &a) {
     check_err_word(c, err);
 }
 
+// ---------------------------------------------------------------------------
+// A complex64 N x N matrix quantised once to resident 16-bit tiles, applied to
+// blocks of right-hand sides (the inner products of the multi-RHS solve)
+// ---------------------------------------------------------------------------
+struct LowpMatrix {
+    Format f{};
+    int64_t n = 0, mt = 0;
+    int nkb = 0;
+    uint8_t *Ahi = nullptr, *Alo = nullptr;
+    unsigned *rmax = nullptr;
+    char *work = nullptr;   // B tiles, partial sums, column maxima, error word (grow-only)
+    size_t work_bytes = 0;
+};
+
+LowpMatrix *lowp_matrix_create(Ctx &c, const float *A, int64_t n, int precision) {
+    auto *m = new LowpMatrix();
+    try {
+        m->f = format_of(precision);
+        m->n = n;
+        m->mt = (n + kBM - 1) / kBM;
+        const int64_t nkb64 = (2 * n + kBK - 1) / kBK;
+        if (nkb64 > (1 << 30) || m->mt > 65535) fail(BIE_ERR_INVALID, "matrix too large for the tensor-core tiles");
+        m->nkb = (int)nkb64;
+        const size_t abytes = (size_t)m->mt * m->nkb * kATile;
+        BIE_CUDA(cudaMalloc(&m->Ahi, abytes));
+        if (m->f.split) BIE_CUDA(cudaMalloc(&m->Alo, abytes));
+        BIE_CUDA(cudaMalloc(&m->rmax, (size_t)n * 4));
+        BIE_CUDA(cudaMemsetAsync(m->rmax, 0, (size_t)n * 4, c.stream));
+        const float2 *S = reinterpret_cast<const float2 *>(A);
+        const int64_t cols_per = 512;
+        dim3 g((unsigned)((n + 255) / 256), (unsigned)((n + cols_per - 1) / cols_per));
+        strip_rowmax_kernel<<<g, 256, 0, c.stream>>>(S, n, n, n, cols_per, m->rmax);
+        BIE_CUDA(cudaGetLastError());
+        ++c.kernel_launches;
+        pack_strip_any(c, m->f, S, n, n, n, m->rmax, m->nkb, m->mt, m->Ahi, m->Alo);
+    } catch (...) {
+        lowp_matrix_destroy(m);
+        throw;
+    }
+    return m;
+}
+
+void lowp_matrix_destroy(LowpMatrix *m) {
+    if (!m) return;
+    cudaFree(m->Ahi);
+    cudaFree(m->Alo);
+    cudaFree(m->rmax);
+    cudaFree(m->work);
+    delete m;
+}
+
+// Y = A X for X, Y: n x R complex128 (column-major, device)
+void lowp_matrix_apply(Ctx &c, LowpMatrix &m, const double *X, int64_t R, double *Y) {
+    if (R <= 0) return;
+    if (R > 65535) fail(BIE_ERR_INVALID, "at most 65535 right-hand sides per product");
+    const int64_t Rp = (R + 127) / 128 * 128;
+    const int64_t nt = 2 * Rp / kBN;
+    int ksplit, kb_per;
+    choose_split(c, m.mt, nt, m.nkb, ksplit, kb_per);
+    const int nparts = m.f.split ? 2 : 1;
+    const size_t bbytes = (size_t)nt * m.nkb * kBTile;
+    const size_t pbytes = (size_t)ksplit * nt * kBN * m.mt * kBM * sizeof(float);
+    auto up = [](size_t b) { return (b + 1023) & ~size_t(1023); };
+    const size_t need = nparts * up(bbytes) + up(pbytes) + up((size_t)R * 8) + up(sizeof(int));
+    if (m.work_bytes < need) {
+        if (c.capturing) fail(BIE_ERR_INVALID, "device scratch would grow while a CUDA graph is recorded");
+        cudaFree(m.work);
+        m.work = nullptr;
+        m.work_bytes = 0;
+        BIE_CUDA(cudaMalloc(&m.work, need));
+        m.work_bytes = need;
+    }
+    Carve cv{m.work};
+    uint8_t *Bh = cv.take<uint8_t>(bbytes), *Bl = m.f.split ? cv.take<uint8_t>(bbytes) : nullptr;
+    float *P = cv.take<float>(pbytes);
+    unsigned long long *cm = cv.take<unsigned long long>((size_t)R * 8);
+    int *err = cv.take<int>(sizeof(int));
+    BIE_CUDA(cudaMemsetAsync(cm, 0, (size_t)R * 8, c.stream));
+    BIE_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c.stream));
+    const int64_t cper = 4096;
+    const double2 *Xd = reinterpret_cast<const double2 *>(X);
+    dim3 g((unsigned)((m.n + cper - 1) / cper), (unsigned)R);
+    rhs_colmax_kernel<<<g, 256, 0, c.stream>>>(Xd, m.n, cper, cm);
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+    pack_rhs_any(c, m.f, Xd, m.n, R, Rp, cm, m.nkb, Bh, Bl);
+    launch_gemm(c, m.f, m.Ahi, m.Alo, Bh, Bl, m.mt, nt, m.nkb, ksplit, kb_per, P, err,
+                8.0 * (double)m.n * m.n * R);
+    lowp_reduce_complex_kernel<<<grid1(m.n * R), 256, 0, c.stream>>>(P, ksplit, m.mt * kBM, nt * kBN, m.n, R, Rp,
+                                                                     m.rmax, cm, m.n, 0,
+                                                                     reinterpret_cast<double2 *>(Y));
+    BIE_CUDA(cudaGetLastError());
+    ++c.kernel_launches;
+    check_err_word(c, err);
+}
+
 }  // namespace bie

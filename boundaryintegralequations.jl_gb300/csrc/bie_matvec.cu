@@ -387,16 +387,10 @@ void run_mixed(Ctx &c, const MatvecArgs &a) {
     const bool doF = a.x != nullptr, doG = a.v != nullptr;
 
     // scratch: xiF, xiG | yFpart, yGpart | defer list, counter, yFn, yGn
-    const int level = choose_slice_level(c, M, kThreads);
-    const int S = 1 << level;
     const size_t xi_bytes = (size_t)E * QTp * sizeof(float2);
     char *xb = static_cast<char *>(c.scratch(kScratchMatvecXi, 2 * xi_bytes));
     float2 *xiF = doF ? reinterpret_cast<float2 *>(xb) : nullptr;
     float2 *xiG = doG ? reinterpret_cast<float2 *>(xb + xi_bytes) : nullptr;
-    const size_t part_bytes = (size_t)S * M * sizeof(double2);
-    char *pb = static_cast<char *>(c.scratch(kScratchMatvecPart, 2 * part_bytes));
-    double2 *yFpart = reinterpret_cast<double2 *>(pb);
-    double2 *yGpart = reinterpret_cast<double2 *>(pb + part_bytes);
     const unsigned int dcap = (unsigned int)std::min<int64_t>(M * 64 + 4096, (int64_t)1 << 30);
     const size_t dbytes = (size_t)dcap * sizeof(int2);
     char *db = static_cast<char *>(c.scratch(kScratchDefer, dbytes + 256 + 2 * (size_t)M * 16));
@@ -404,7 +398,6 @@ void run_mixed(Ctx &c, const MatvecArgs &a) {
     unsigned int *dcount = reinterpret_cast<unsigned int *>(db + dbytes);
     double2 *yFn = reinterpret_cast<double2 *>(db + dbytes + 256);
     double2 *yGn = yFn + M;
-    BIE_CUDA(cudaMemsetAsync(db + dbytes, 0, 256 + 2 * (size_t)M * 16, c.stream));
 
     const int64_t nslots = E * QT;
     interp_kernel<<<(unsigned)((nslots + 255) / 256), 256, 0, c.stream>>>(
@@ -415,40 +408,56 @@ void run_mixed(Ctx &c, const MatvecArgs &a) {
 
     const size_t rec_bytes = (size_t)X.stride * sizeof(float);
     const size_t per_el = rec_bytes + (size_t)(doF + doG) * QTp * sizeof(float2);
-    const int chunk = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / per_el));
-    const size_t smem = (size_t)chunk * per_el;
-    auto kern = matvec_mixed_kernel<NP, CPLX>;
-    BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((unsigned)((M + kThreads - 1) / kThreads), (unsigned)S);
-    cudaEvent_t t0 = c.timer_begin();
+    const int chunk0 = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / per_el));
     const Fp64Rec v64{c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64};
-    kern<<<grid, kThreads, smem, c.stream>>>(c.d_mrecords, X.stride, E, S, ri, rxi, QTp, xiF, xiG,
-                                             a.targets, M, a.k_re, a.k_im, yFpart, yGpart, chunk,
-                                             defer, dcount, dcap, v64,
-                                             reinterpret_cast<const double2 *>(a.x),
-                                             reinterpret_cast<const double2 *>(a.v), c.d_qpe);
-    BIE_CUDA(cudaGetLastError());
-    c.timer_end(t0);
-    ++c.kernel_launches;
-
-    matvec_correct_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
-        defer, dcount, dcap, c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64,
-        reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), a.targets,
-        a.k_re, a.k_im, yFn, yGn, c.d_qpe);
-    BIE_CUDA(cudaGetLastError());
-    ++c.kernel_launches;
-    if (doF) {
-        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
-            yFpart, S, yFn, M, reinterpret_cast<double2 *>(a.yF));
+    // one complete product (slice partials, deferred pairs, reductions) for a launch shape
+    auto run = [&](const LaunchShape &sh) {
+        const int S = 1 << sh.level, chunk = sh.chunk;
+        const size_t part_bytes = (size_t)S * M * sizeof(double2);
+        char *pb = static_cast<char *>(c.scratch(kScratchMatvecPart, 2 * part_bytes));
+        double2 *yFpart = reinterpret_cast<double2 *>(pb);
+        double2 *yGpart = reinterpret_cast<double2 *>(pb + part_bytes);
+        BIE_CUDA(cudaMemsetAsync(db + dbytes, 0, 256 + 2 * (size_t)M * 16, c.stream));
+        const size_t smem = (size_t)chunk * per_el;
+        auto kern = matvec_mixed_kernel<NP, CPLX>;
+        BIE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        dim3 grid((unsigned)((M + kThreads - 1) / kThreads), (unsigned)S);
+        cudaEvent_t t0 = c.timer_begin();
+        kern<<<grid, kThreads, smem, c.stream>>>(c.d_mrecords, X.stride, E, S, ri, rxi, QTp, xiF, xiG,
+                                                 a.targets, M, a.k_re, a.k_im, yFpart, yGpart, chunk,
+                                                 defer, dcount, dcap, v64,
+                                                 reinterpret_cast<const double2 *>(a.x),
+                                                 reinterpret_cast<const double2 *>(a.v), c.d_qpe);
+        BIE_CUDA(cudaGetLastError());
+        c.timer_end(t0);
+        ++c.kernel_launches;
+        matvec_correct_kernel<NP, CPLX><<<(unsigned)(4 * c.num_sms), 128, 0, c.stream>>>(
+            defer, dcount, dcap, c.d_records, L.stride, L.nidx_off, c.d_phi, L.qmax, ri64,
+            reinterpret_cast<const double2 *>(a.x), reinterpret_cast<const double2 *>(a.v), a.targets,
+            a.k_re, a.k_im, yFn, yGn, c.d_qpe);
         BIE_CUDA(cudaGetLastError());
         ++c.kernel_launches;
-    }
-    if (doG) {
-        reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
-            yGpart, S, yGn, M, reinterpret_cast<double2 *>(a.yG));
-        BIE_CUDA(cudaGetLastError());
-        ++c.kernel_launches;
-    }
+        if (doF) {
+            reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+                yFpart, S, yFn, M, reinterpret_cast<double2 *>(a.yF));
+            BIE_CUDA(cudaGetLastError());
+            ++c.kernel_launches;
+        }
+        if (doG) {
+            reduce_y_kernel<<<(unsigned)((M + 255) / 256), 256, 0, c.stream>>>(
+                yGpart, S, yGn, M, reinterpret_cast<double2 *>(a.yG));
+            BIE_CUDA(cudaGetLastError());
+            ++c.kernel_launches;
+        }
+    };
+    const LaunchShape base{choose_slice_level(c, M, kThreads), chunk0, kThreads};
+    ShapeAxes ax;
+    for (int l = base.level - 1; l <= base.level + 1; ++l)
+        if (l >= 0 && l < kMaxLevels && (int64_t(1) << l) <= c.n_elements) ax.levels.push_back(l);
+    ax.chunks = {std::max(1, chunk0 / 2), chunk0, std::min(64, 2 * chunk0)};
+    LaunchShape sh = resolve_shape(c, kShapeK3, M, base, ax, run, [] {});
+    sh.tpb = kThreads;
+    run(sh);
 }
 
 template <int NP, bool CPLX>

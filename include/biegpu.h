@@ -231,15 +231,30 @@ BIE_API int bie_measure_peaks(int device, bie_peaks *out);
 BIE_API int bie_ctx_set_timing(bie_ctx *ctx, int on);
 
 /*
- * Autotuning of the mixed-precision assembly (no reference counterpart: the
- * reference has no GPU launch shapes).  While on, the first mixed assembly of
- * the context for a given number of targets M times the element slicings next
- * to the default one (each a complete assembly, so that first call costs about
- * four assemblies) and keeps the fastest for later calls with that M.  Results
- * of different slicings differ only by FP32 rounding order.  bie_sweep turns it
- * on for the contexts it is given.
+ * Autotuning of launch shapes (no reference counterpart: the reference has no
+ * GPU launch shapes).  While on, the first call of the context for a given
+ * number of targets M of the mixed assembly (BIE_SHAPE_MIXED_ASSEMBLY), the
+ * double-float assembly (BIE_SHAPE_DF64_ASSEMBLY) and the mixed matrix-free
+ * product (BIE_SHAPE_MIXED_PRODUCT) searches the launch shape coordinate by
+ * coordinate: element slicing (2^level slices, the default level and its two
+ * neighbours), element records per shared-memory chunk (half, default,
+ * double) and, for the mixed assembly, threads per block (128, 256); each
+ * candidate is timed as a complete call with CUDA events on the context stream
+ * (about seven calls for the first M), and the fastest is kept per (kernel, M)
+ * for later calls.  Results of different shapes differ only by rounding order.
+ * bie_sweep turns it on for the contexts it is given.
  */
+#define BIE_SHAPE_MIXED_ASSEMBLY 0
+#define BIE_SHAPE_DF64_ASSEMBLY  1
+#define BIE_SHAPE_MIXED_PRODUCT  2
 BIE_API int bie_ctx_set_autotune(bie_ctx *ctx, int on);
+/* The shape in use for (kernel, M): *found = 1 and the shape if one was tuned
+ * or forced, else *found = 0. */
+BIE_API int bie_ctx_get_shape(bie_ctx *ctx, int kernel, int64_t M, int *found, int *level, int *chunk, int *tpb);
+/* Force a shape for (kernel, M) (M = 0: every M) until cleared with level < 0;
+ * chunk <= 0 or tpb other than 128 / 256 keep the default of that axis.  For
+ * tests and measurements of individual shapes. */
+BIE_API int bie_ctx_set_shape(bie_ctx *ctx, int kernel, int64_t M, int level, int chunk, int tpb);
 /* Synchronises the context stream, then fills *out; `reset` != 0 zeroes the counters. */
 BIE_API int bie_ctx_stats(bie_ctx *ctx, bie_stats *out, int reset);
 
@@ -357,6 +372,46 @@ BIE_API int bie_matvec_multi(bie_ctx *ctx, double k_re, double k_im, int64_t nrh
  */
 BIE_API int bie_lowp_gemm_device(bie_ctx *ctx, int precision, int64_t M, int64_t N, int64_t K,
                                  const float *d_A, const float *d_B, double *d_C);
+
+/*
+ * Solve of many right-hand sides at once,
+ *     (F + Diagonal(1 - C)) X = B,   B, X: N x nrhs complex (device, column-major),
+ * the exterior collocation system of test/3d/assembly_test.jl:37-38, which the
+ * reference solves one column at a time (IterativeSolvers.gmres per
+ * right-hand side; its operators accept matrices in batches of 32 columns,
+ * src/3d/fast_multipole_method.jl:249-287).  F and C come from the mixed
+ * assembly (complex64 F); the nrhs GMRES solves run in lockstep so that every
+ * Arnoldi step is one tcgen05 tensor-core product of F (quantised once to
+ * 16-bit tiles) with all Krylov vectors; the outer iterative refinement forms
+ * each column's residual B - A X with the exact product of the complex64
+ * matrix (double-float sums).  A column has converged when that residual is
+ * at most reltol times ||b||.  X is overwritten.  Synchronous.
+ */
+typedef struct bie_multisolve_opts {
+    int32_t precision;      /* tensor-core form of the inner products: BIE_PREC_FP16 ..
+                               BIE_PREC_BF16_SPLIT (<= 0: BIE_PREC_FP16_SPLIT)            */
+    int32_t restart;        /* inner GMRES restart (<= 0: 20, at most 64)                  */
+    int32_t maxiter;        /* inner Arnoldi steps per refinement pass (<= 0: 200)         */
+    int32_t max_refine;     /* refinement passes (<= 0: 10)                                */
+    double  reltol;         /* <= 0: sqrt(eps(Float64)), IterativeSolvers' default         */
+    double  inner_reltol;   /* inner solves, relative to the pass's residual (<= 0: 1e-4)  */
+} bie_multisolve_opts;
+
+typedef struct bie_multisolve_info {
+    int32_t passes;          /* refinement passes that ran an inner solve                 */
+    int32_t inner_steps;     /* lockstep Arnoldi steps, summed over passes                */
+    int32_t converged;       /* columns with ||b - A x|| <= reltol ||b||                  */
+    int32_t tensor_products; /* tensor-core products of all columns                       */
+    int32_t exact_products;  /* exact residual products of all columns                    */
+    int32_t reserved;
+    double  max_relres;      /* largest ||b - A x|| / ||b|| (exact product)               */
+    double  setup_ms;        /* assembly + quantisation of F (host wall time)             */
+    double  tensor_ms;       /* tensor-core products (host wall time)                     */
+    double  exact_ms;        /* exact residual products (host wall time)                  */
+} bie_multisolve_info;
+
+BIE_API int bie_solve_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *d_B,
+                                   double *d_X, const bie_multisolve_opts *opts, bie_multisolve_info *info);
 
 /*
  * Failure detection of the tensor-core GEMM (no reference counterpart; the

@@ -89,5 +89,15 @@ int main(void) {
     LEAF(bie_lossy_opts, normals);
     gmres_leaves(offsetof(bie_lossy_opts, solve));
     END();
+    BEGIN(bie_multisolve_opts);
+    LEAF(bie_multisolve_opts, precision); LEAF(bie_multisolve_opts, restart); LEAF(bie_multisolve_opts, maxiter);
+    LEAF(bie_multisolve_opts, max_refine); LEAF(bie_multisolve_opts, reltol); LEAF(bie_multisolve_opts, inner_reltol);
+    END();
+    BEGIN(bie_multisolve_info);
+    LEAF(bie_multisolve_info, passes); LEAF(bie_multisolve_info, inner_steps); LEAF(bie_multisolve_info, converged);
+    LEAF(bie_multisolve_info, tensor_products); LEAF(bie_multisolve_info, exact_products);
+    LEAF(bie_multisolve_info, reserved); LEAF(bie_multisolve_info, max_relres); LEAF(bie_multisolve_info, setup_ms);
+    LEAF(bie_multisolve_info, tensor_ms); LEAF(bie_multisolve_info, exact_ms);
+    END();
     return 0;
 }

@@ -29,7 +29,8 @@ PY = {"bie_mesh_desc": _capi.MeshDesc, "bie_rule_table": _capi.RuleTable, "bie_s
       "bie_peaks": _capi.Peaks, "bie_operator": _capi.Operator, "bie_gmres_opts": _capi.GmresOpts,
       "bie_gmres_info": _capi.GmresInfo, "bie_sweep_opts": _capi.SweepOpts, "bie_sweep_info": _capi.SweepInfo,
       "bie_adjoint_opts": _capi.AdjointOpts, "bie_adjoint_info": _capi.AdjointInfo,
-      "bie_lossy_constants": _capi.LossyConstants, "bie_lossy_opts": _capi.LossyOpts}
+      "bie_lossy_constants": _capi.LossyConstants, "bie_lossy_opts": _capi.LossyOpts,
+      "bie_multisolve_opts": _capi.MultisolveOpts, "bie_multisolve_info": _capi.MultisolveInfo}
 JL = {"bie_mesh_desc": "MeshDesc", "bie_rule_table": "RuleTable", "bie_operator": "OperatorC",
       "bie_gmres_opts": "GmresOptsC", "bie_gmres_info": "GmresInfoC", "bie_sweep_opts": "SweepOpts",
       "bie_sweep_info": "SweepInfo", "bie_adjoint_opts": "AdjointOpts", "bie_adjoint_info": "AdjointInfo",
