@@ -56,7 +56,8 @@ def _sources_newer_than(target: Path) -> bool:
     if not target.exists():
         return True
     t = target.stat().st_mtime
-    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + [PKG_ROOT.parent / "include" / "biegpu.h"]
+    deps = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + \
+        [PKG_ROOT.parent / "include" / "biegpu.h"]
     return any(d.exists() and d.stat().st_mtime > t for d in deps)
 
 

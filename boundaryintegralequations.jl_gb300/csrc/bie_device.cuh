@@ -216,16 +216,31 @@ __device__ __forceinline__ void sincos_f32(float x, float *s, float *c) {
     *c = ((q + 1) & 2) ? -b : b;
 }
 
-// float -> double by moving bits with integer instructions (normal numbers and
-// zero); subnormal inputs take the conversion instruction.
+// float -> double by moving bits with integer instructions only (GB300's
+// conversion instruction runs on the narrow FP64 pipe).  Normal numbers take a
+// five-instruction path (exponent rebias by adding 896 << 20 to the shifted
+// bits); zero, subnormals, infinities and NaNs take the general path, which
+// normalises subnormals with a leading-zero count.  Exact for every input.
+static __device__ __noinline__ double f2d_special(uint32_t u) {
+    const uint32_t sign = u & 0x80000000u;
+    const uint32_t ex = (u >> 23) & 0xffu;
+    const uint32_t man = u & 0x7fffffu;
+    if (ex == 0xffu)   // infinity or NaN (payload kept nonzero)
+        return __hiloint2double((int)(sign | 0x7ff00000u | (man >> 3) | ((man != 0u && (man >> 3) == 0u) ? 1u : 0u)),
+                                (int)(man << 29));
+    if (man == 0u) return __hiloint2double((int)sign, 0);   // signed zero
+    // subnormal: value man 2^-149, leading one moved to bit 23
+    const uint32_t lz = (uint32_t)__clz((int)man);          // 9..31
+    const uint32_t mn = (man << (lz - 8u)) & 0x7fffffu;
+    return __hiloint2double((int)(sign | ((905u - lz) << 20) | (mn >> 3)), (int)(mn << 29));
+}
+
 __device__ __forceinline__ double f2d(float f) {
     const uint32_t u = __float_as_uint(f);
-    const uint32_t ex = (u >> 23) & 0xffu;
-    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    if (ex == 0u || ex == 0xffu) return (double)f;
-    const uint32_t hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
-    const uint32_t lo = (u & 0x7u) << 29;
-    return __hiloint2double((int)hi, (int)lo);
+    const uint32_t a = u & 0x7fffffffu;
+    if (a - 0x00800000u < 0x7f000000u)   // normal: exponent field 1..254
+        return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + 0x38000000u)), (int)(u << 29));
+    return f2d_special(u);
 }
 
 }  // namespace dev

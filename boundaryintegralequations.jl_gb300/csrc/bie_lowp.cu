@@ -830,7 +830,7 @@ void run_matvec_multi(Ctx &c, const MultiArgs &a) {
             if (!S) continue;
             const unsigned long long *cm = op == 0 ? cmF : cmG;
             BIE_CUDA(cudaMemsetAsync(rmax, 0, (size_t)ms * 4, c.stream));
-            const int64_t cols_per = 512;
+            const int64_t cols_per = 64;   // column blocks per strip: enough blocks in flight
             dim3 g((unsigned)((ms + 255) / 256), (unsigned)((N + cols_per - 1) / cols_per));
             strip_rowmax_kernel<<<g, 256, 0, c.stream>>>(S, ms, ms, N, cols_per, rmax);
             BIE_CUDA(cudaGetLastError());
@@ -877,7 +877,7 @@ LowpMatrix *lowp_matrix_create(Ctx &c, const float *A, int64_t n, int precision)
         BIE_CUDA(cudaMalloc(&m->rmax, (size_t)n * 4));
         BIE_CUDA(cudaMemsetAsync(m->rmax, 0, (size_t)n * 4, c.stream));
         const float2 *S = reinterpret_cast<const float2 *>(A);
-        const int64_t cols_per = 512;
+        const int64_t cols_per = 64;   // column blocks per strip: enough blocks in flight
         dim3 g((unsigned)((n + 255) / 256), (unsigned)((n + cols_per - 1) / cols_per));
         strip_rowmax_kernel<<<g, 256, 0, c.stream>>>(S, n, n, n, cols_per, m->rmax);
         BIE_CUDA(cudaGetLastError());
