@@ -519,14 +519,21 @@ def lossy_bench(args, max_over_ranks):
     L = biegpu.LossyGlobalOuter(mesh, 100.0, depth=1, n=3)
     t_setup = time.perf_counter() - t0
     x = np.random.default_rng(4).normal(size=N) + 1j * np.random.default_rng(5).normal(size=N)
-    L @ x
-    L.stats(reset=True)
     reps = max(1, args.lossy_steps)
-    t0 = time.perf_counter()
-    for _ in range(reps):
+    per_op = {}
+    for one_launch in (False, True):   # sparse solves per operation, then as one cluster launch each
+        L.set_one_launch(one_launch)
         L @ x
-    t_prod = max_over_ranks(time.perf_counter() - t0) / reps
-    st = L.stats(reset=True)
+        L.stats(reset=True)
+        L.ctx.stats(reset=True)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            L @ x
+        t_prod = max_over_ranks(time.perf_counter() - t0) / reps
+        launches = L.ctx.stats(reset=True)["kernel_launches"] / reps
+        st = L.stats(reset=True)
+        if not one_launch:
+            per_op = {"product_ms": 1e3 * t_prod, "launches_per_product": launches}
     v0 = np.concatenate([0.01 * np.ones(N), np.zeros(2 * N)])
     t0 = time.perf_counter()
     rhs = L.rhs(v0)
@@ -535,7 +542,8 @@ def lossy_bench(args, max_over_ranks):
     st2 = L.stats(reset=True)
     res = float(np.linalg.norm(L @ pa - rhs) / np.linalg.norm(rhs))
     return {"workload": f"icosphere f=16 ({N} nodes, linear), 100 Hz, depth 1, n = m = 3, dense acoustic blocks",
-            "setup_s": t_setup, "product_ms": 1e3 * t_prod,
+            "setup_s": t_setup, "product_ms": 1e3 * t_prod, "launches_per_product": launches,
+            "per_operation_sparse_solves": per_op,
             "nested_solves_per_product": st["nested_solves"] / reps,
             "nested_iterations_per_product": st["nested_iterations"] / reps,
             "solve_s": t_solve, "outer_iterations": info["iterations"], "converged": info["converged"],

@@ -36,6 +36,7 @@ SOURCES = [
     "bie_lossy.cu",
     "bie_mesh_io.cpp",
     "bie_multisolve.cu",
+    "bie_cluster_gmres.cu",
 ]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code is compiled without FMA contraction so that the set-up arithmetic

@@ -277,6 +277,7 @@ SIGNATURES = {
     "bie_lossy_apply": (_I, [_P, _I, _P, _P]),
     "bie_lossy_solve": (_I, [_P, _I, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo)]),
     "bie_lossy_stats": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64), _I]),
+    "bie_lossy_set_one_launch": (_I, [_P, _I]),
 }
 
 

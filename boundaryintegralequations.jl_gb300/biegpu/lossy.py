@@ -189,6 +189,11 @@ class LossyGlobalOuter(LossyBlock):
         _capi.check(_capi.lib().bie_lossy_stats(self._h, C.byref(s), C.byref(i), 1 if reset else 0))
         return {"nested_solves": s.value, "nested_iterations": i.value}
 
+    def set_one_launch(self, on: bool = True) -> None:
+        """Sparse thermal / viscous solves as one cluster launch each (default)
+        or through the launch-per-operation device GMRES."""
+        _capi.check(_capi.lib().bie_lossy_set_one_launch(self._h, 1 if on else 0))
+
     def rhs(self, v0):
         """Ga gmres(inner, Dr v0 - Nd' gmres(Gv, Hv v0)): the right-hand side of a
         prescribed boundary velocity v0 (3N), test/3d/losses_test.jl:33."""

@@ -1144,4 +1144,12 @@ int bie_lossy_stats(bie_lossy *L, int64_t *nested_solves, int64_t *nested_iterat
     });
 }
 
+int bie_lossy_set_one_launch(bie_lossy *L, int on) {
+    return guarded([&] {
+        bie::LossyOp &op = as_lossy(L);
+        std::lock_guard<std::mutex> lock(bie::lossy_context(op).mu);
+        bie::lossy_set_one_launch(op, on != 0);
+    });
+}
+
 }  // extern "C"

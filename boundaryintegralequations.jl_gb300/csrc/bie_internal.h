@@ -402,6 +402,7 @@ void lossy_apply(LossyOp &L, int block, const double *x, double *y);   // device
 void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gmres_opts &o,
                  bie_gmres_info &info);
 void lossy_stats(LossyOp &L, int64_t *solves, int64_t *iterations, bool reset);
+void lossy_set_one_launch(LossyOp &L, bool on);
 
 // An operator that the library's GMRES applies through a virtual call (the
 // visco-thermal composite and its sparse blocks).  apply: y = A x on the
@@ -420,6 +421,24 @@ void run_gmres_devop(Ctx &c, DevOp &op, const double *b, double *x, const bie_gm
                      bie_gmres_info &info, int level);
 void capture_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
                    bie_gmres_info *d_info, const cudaStream_t *body);
+// (V + Diagonal(diag)) on nb diagonal blocks of N rows that share one CSR
+// pattern and value array (the thermal and viscous near-field blocks); diag
+// may be null.
+struct CsrSystem {
+    const int64_t *rp;
+    const int32_t *cols;
+    const double2 *val;
+    const double2 *diag;
+    int64_t N;
+    int nb;
+};
+// The restarted GMRES of run_gmres_devop (zero start) on a CsrSystem as one
+// thread-block-cluster launch on the context stream (bie_cluster_gmres.cu).
+// Writes the info to d_info and adds (1, iterations) to d_acc[0..1] on the
+// device (either may be null).  Returns false, launching nothing, when the
+// system or restart length does not fit the one-launch form.
+bool csr_gmres_one_launch(Ctx &c, const CsrSystem &A, const double2 *b, double2 *x, const bie_gmres_opts &o,
+                          int level, bie_gmres_info *d_info, unsigned long long *d_acc);
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
 // Frequency sweep (bie_sweep.cu); locks each context while it runs.
 void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,

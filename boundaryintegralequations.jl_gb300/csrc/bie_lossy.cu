@@ -183,9 +183,13 @@ struct LossyOp {
     // work vectors
     double2 *work = nullptr;
     double2 *o_t, *o_sh, *o_q, *o_hq, *o_sv, *o_r, *o_si, *o_w, *i_p, *i_hp, *i_g, *s_t;
-    // solve nesting and statistics
+    // solve nesting and statistics (host-counted solves, plus the one-launch
+    // sparse solves counted on the device in d_acc = {solves, iterations})
     int active = -1;
     int64_t nested_solves = 0, nested_iterations = 0;
+    bool one_launch = true;             // sparse solves as one cluster launch where they fit
+    unsigned long long *d_acc = nullptr;
+    bie_gmres_info *d_info = nullptr;
 
     ~LossyOp() {
         cudaFree(Fa);
@@ -204,6 +208,8 @@ struct LossyOp {
         cudaFree(Dz);
         cudaFree(nrm);
         cudaFree(work);
+        cudaFree(d_acc);
+        cudaFree(d_info);
     }
 
     cudaStream_t stream() const { return c->stream; }
@@ -282,6 +288,12 @@ struct LossyOp {
         }
     }
 
+    // gmres(V + Diagonal(d), b) on nb blocks of the near-field pattern: one
+    // cluster launch with the statistics kept on the device when it fits, else
+    // the launch-per-operation GMRES
+    void solve_csr(const double2 *v, const double2 *d, int nb, const double2 *b, double2 *x,
+                   const bie_gmres_opts &o, bie_gmres_info &info, bool count);
+
     // inner z = Dr Nd z - Nd' gmres(Gv, Hv Nd z)
     void inner(const double2 *z, double2 *y);
     // the LossyGlobalOuter product
@@ -317,12 +329,29 @@ struct BlockOp : DevOp {   // Ha, Ga, inner or outer
 
 }  // namespace
 
+void LossyOp::solve_csr(const double2 *v, const double2 *d, int nb, const double2 *b, double2 *x,
+                        const bie_gmres_opts &o, bie_gmres_info &info, bool count) {
+    const int lvl = active + 1;
+    if (lvl > kMaxSolveLevel) fail(BIE_ERR_INVALID, "lossy system: GMRES nested deeper than two levels");
+    if (one_launch) {
+        const CsrSystem A{nf_rp, nf_cols, v, d, N, nb};
+        if (csr_gmres_one_launch(*c, A, b, x, o, lvl, count ? nullptr : d_info, count ? d_acc : nullptr)) {
+            if (!count) {
+                BIE_CUDA(cudaMemcpyAsync(&info, d_info, sizeof(info), cudaMemcpyDeviceToHost, stream()));
+                BIE_CUDA(cudaStreamSynchronize(stream()));
+            }
+            return;
+        }
+    }
+    CsrOp op(*this, v, d, nb);
+    solve(op, b, x, o, info, count);
+}
+
 void LossyOp::inner(const double2 *z, double2 *y) {
     Nd(z, i_p);
     csr(Fv, C0, i_p, i_hp, 3);
-    CsrOp gv(*this, Gv, nullptr, 3);
     bie_gmres_info gi{};
-    solve(gv, i_hp, i_g, nested, gi, true);
+    solve_csr(Gv, nullptr, 3, i_hp, i_g, nested, gi, true);
     // y = Dr p - Nd' g with p = Nd z
     Dr_minus_NdT(i_p, i_g, y);
 }
@@ -336,14 +365,12 @@ void LossyOp::outer(const double2 *x, double2 *y) {
     launched();
     // sh = gmres(Gh, Hh x)
     csr(Fh, C0, x, o_t, 1);
-    CsrOp gh(*this, Gh, nullptr, 1);
     bie_gmres_info gi{};
-    solve(gh, o_t, o_sh, nested, gi, true);
+    solve_csr(Gh, nullptr, 1, o_t, o_sh, nested, gi, true);
     // r = Dr Dc x - Nd' gmres(Gv, Hv Dc x)
     Dc(x, o_q);
     csr(Fv, C0, o_q, o_hq, 3);
-    CsrOp gv(*this, Gv, nullptr, 3);
-    solve(gv, o_hq, o_sv, nested, gi, true);
+    solve_csr(Gv, nullptr, 3, o_hq, o_sv, nested, gi, true);
     Dr_minus_NdT(o_q, o_sv, o_r);
     // si = gmres(inner, r)
     BlockOp in(*this, BIE_LOSSY_INNER);
@@ -454,6 +481,9 @@ LossyOp *create_lossy(Ctx &c, double freq, const bie_lossy_opts &o) {
     L->i_hp = take(3);
     L->i_g = take(3);
     L->s_t = take(1);
+    L->d_acc = dev_alloc<unsigned long long>(2);
+    L->d_info = dev_alloc<bie_gmres_info>(1);
+    BIE_CUDA(cudaMemsetAsync(L->d_acc, 0, 2 * sizeof(unsigned long long), s));
     BIE_CUDA(cudaStreamSynchronize(s));   // host vectors above are released on return
     return L.release();
 }
@@ -509,26 +539,10 @@ void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gm
     go.refine = 0;
     go.initially_nonzero = 0;
     switch (block) {
-    case BIE_LOSSY_HH: {
-        CsrOp op(L, L.Fh, L.C0, 1);
-        L.solve(op, bb, xx, go, info, false);
-        break;
-    }
-    case BIE_LOSSY_GH: {
-        CsrOp op(L, L.Gh, nullptr, 1);
-        L.solve(op, bb, xx, go, info, false);
-        break;
-    }
-    case BIE_LOSSY_HV: {
-        CsrOp op(L, L.Fv, L.C0, 3);
-        L.solve(op, bb, xx, go, info, false);
-        break;
-    }
-    case BIE_LOSSY_GV: {
-        CsrOp op(L, L.Gv, nullptr, 3);
-        L.solve(op, bb, xx, go, info, false);
-        break;
-    }
+    case BIE_LOSSY_HH: L.solve_csr(L.Fh, L.C0, 1, bb, xx, go, info, false); break;
+    case BIE_LOSSY_GH: L.solve_csr(L.Gh, nullptr, 1, bb, xx, go, info, false); break;
+    case BIE_LOSSY_HV: L.solve_csr(L.Fv, L.C0, 3, bb, xx, go, info, false); break;
+    case BIE_LOSSY_GV: L.solve_csr(L.Gv, nullptr, 3, bb, xx, go, info, false); break;
     case BIE_LOSSY_OUTER:
     case BIE_LOSSY_HA:
     case BIE_LOSSY_GA:
@@ -543,9 +557,18 @@ void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gm
 }
 
 void lossy_stats(LossyOp &L, int64_t *solves, int64_t *iterations, bool reset) {
-    if (solves) *solves = L.nested_solves;
-    if (iterations) *iterations = L.nested_iterations;
-    if (reset) L.nested_solves = L.nested_iterations = 0;
+    unsigned long long acc[2] = {0, 0};
+    BIE_CUDA(cudaMemcpyAsync(acc, L.d_acc, sizeof(acc), cudaMemcpyDeviceToHost, L.stream()));
+    BIE_CUDA(cudaStreamSynchronize(L.stream()));
+    if (solves) *solves = L.nested_solves + (int64_t)acc[0];
+    if (iterations) *iterations = L.nested_iterations + (int64_t)acc[1];
+    if (reset) {
+        L.nested_solves = L.nested_iterations = 0;
+        BIE_CUDA(cudaMemsetAsync(L.d_acc, 0, sizeof(acc), L.stream()));
+        BIE_CUDA(cudaStreamSynchronize(L.stream()));
+    }
 }
+
+void lossy_set_one_launch(LossyOp &L, bool on) { L.one_launch = on; }
 
 }  // namespace bie

@@ -107,6 +107,57 @@ def test_lossy_solve_and_reference_identities(name):
     assert rel(lhs, v0) <= 1e-12
 
 
+@pytest.mark.parametrize("name", ["linear", "quadratic"])
+def test_one_launch_sparse_solves(name):
+    """The sparse thermal / viscous solves as one thread-block-cluster launch
+    (bie_lossy_set_one_launch, the default) against the launch-per-operation
+    device GMRES and the oracle's sparse direct solves: the same iterations,
+    restarts and products, solutions within the GMRES tolerance of each other
+    (1e-7) and of the direct solve (1e-6), fewer launches per product."""
+    mesh, L, O = systems(name)
+    N = mesh.n_sources
+    rng = np.random.default_rng(11)
+    b1, b3 = crandn(rng, N), crandn(rng, 3 * N)
+    x = crandn(rng, N)
+    runs = {}
+    for on in (False, True):
+        L.set_one_launch(on)
+        r = {}
+        for blk, b in (("Gh", b1), ("Hh", b1), ("Gv", b3), ("Hv", b3)):
+            r[blk] = getattr(L, blk).solve(b, return_info=True)
+        # a restart after every step and a step limit below what the tolerance needs
+        r["short"] = L.Gv.solve(b3, reltol=1e-15, restart=1, maxiter=3, return_info=True)
+        L.stats(reset=True)
+        L.ctx.stats(reset=True)
+        r["product"] = L @ x
+        r["launches"] = L.ctx.stats(reset=True)["kernel_launches"]
+        r["stats"] = L.stats(reset=True)
+        runs[on] = r
+    L.set_one_launch(True)
+    per_op, one = runs[False], runs[True]
+    for blk in ("Gh", "Hh", "Gv", "Hv", "short"):
+        (x0, i0), (x1, i1) = per_op[blk], one[blk]
+        for key in ("iterations", "restarts", "matvecs", "converged"):
+            assert i0[key] == i1[key], (blk, key, i0[key], i1[key])
+        assert rel(x1, x0) <= 1e-7, blk
+        assert abs(i1["residual_norm"] - i0["residual_norm"]) <= 1e-6 * i0["rhs_norm"]
+    short = one["short"][1]
+    assert short["iterations"] <= 3 and short["restarts"] == short["iterations"]
+    assert short["converged"] == 1 or short["iterations"] == 3
+    # against the oracle's sparse direct solves
+    ref = {"Gh": O._gh.solve(b1), "Hh": np.linalg.solve(O.Hh.toarray(), b1),
+           "Gv": np.concatenate([O._bv.solve(b3[k * N:(k + 1) * N]) for k in range(3)]),
+           "Hv": np.concatenate([np.linalg.solve(O.Av.toarray(), b3[k * N:(k + 1) * N]) for k in range(3)])}
+    for blk, xr in ref.items():
+        assert one[blk][1]["converged"] == 1
+        assert rel(one[blk][0], xr) <= 1e-6, blk
+    assert rel(one["product"], per_op["product"]) <= 1e-7
+    assert rel(one["product"], O.matvec(x)) <= 1e-6
+    assert one["stats"] == per_op["stats"]
+    assert one["launches"] < per_op["launches"] <= 4000
+    assert one["launches"] <= 1000
+
+
 def test_lossy_fast_acoustic_operators():
     """fmm_on = true: the acoustic blocks by the fast-operator algorithm."""
     mesh = bm.icosphere(3)
