@@ -616,7 +616,9 @@ def profile_case(name: str) -> None:
     sphere: complex128 FP64 products), `taylor` (ROSEBEM k-derivative
     assembly, 2562-node P2 sphere), `sweep` (mixed frequency sweep of the
     2562-node sphere, 8 wavenumbers, launch by launch: complex64 products and
-    the exact products of the refinement residuals)."""
+    the exact products of the refinement residuals), `lossy` (LossyGlobalOuter
+    products on the 2562-node sphere at 100 Hz: the one-launch sparse GMRES
+    solves and the rest of the product)."""
     import torch
     import biegpu
     from biegpu import _capi
@@ -656,6 +658,13 @@ def profile_case(name: str) -> None:
         mesh = bm.icosphere(16)
         w = np.random.default_rng(2).normal(size=mesh.n_sources) + 0j
         biegpu.sweep([mesh], np.linspace(0.5, 8.0, 8), [w], precision="mixed", eager=True, target_error=0)
+    elif name == "lossy":
+        mesh = bm.icosphere(16)
+        Lo = biegpu.LossyGlobalOuter(mesh, 100.0, depth=1, n=3)
+        x = np.random.default_rng(4).normal(size=mesh.n_sources) + 1j * np.random.default_rng(5).normal(
+            size=mesh.n_sources)
+        for _ in range(3):
+            Lo @ x
     else:
         raise SystemExit(f"unknown profile case {name}")
     torch.cuda.synchronize()

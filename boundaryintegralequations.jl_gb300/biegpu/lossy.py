@@ -189,10 +189,14 @@ class LossyGlobalOuter(LossyBlock):
         _capi.check(_capi.lib().bie_lossy_stats(self._h, C.byref(s), C.byref(i), 1 if reset else 0))
         return {"nested_solves": s.value, "nested_iterations": i.value}
 
-    def set_one_launch(self, on: bool = True) -> None:
-        """Sparse thermal / viscous solves as one cluster launch each (default)
-        or through the launch-per-operation device GMRES."""
-        _capi.check(_capi.lib().bie_lossy_set_one_launch(self._h, 1 if on else 0))
+    ONE_LAUNCH_MODES = {False: 0, True: 1, "off": 0, "auto": 1, "cluster": 2, "grid": 3}
+
+    def set_one_launch(self, mode=True) -> None:
+        """Sparse thermal / viscous solves as one launch each: True / "auto"
+        (default: a cooperative grid for more than 2048 rows, else a cluster),
+        "cluster" or "grid" (that form only); False / "off": the
+        launch-per-operation device GMRES."""
+        _capi.check(_capi.lib().bie_lossy_set_one_launch(self._h, self.ONE_LAUNCH_MODES[mode]))
 
     def rhs(self, v0):
         """Ga gmres(inner, Dr v0 - Nd' gmres(Gv, Hv v0)): the right-hand side of a

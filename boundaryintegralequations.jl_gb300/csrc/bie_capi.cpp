@@ -1144,11 +1144,11 @@ int bie_lossy_stats(bie_lossy *L, int64_t *nested_solves, int64_t *nested_iterat
     });
 }
 
-int bie_lossy_set_one_launch(bie_lossy *L, int on) {
+int bie_lossy_set_one_launch(bie_lossy *L, int mode) {
     return guarded([&] {
         bie::LossyOp &op = as_lossy(L);
         std::lock_guard<std::mutex> lock(bie::lossy_context(op).mu);
-        bie::lossy_set_one_launch(op, on != 0);
+        bie::lossy_set_one_launch(op, mode);
     });
 }
 

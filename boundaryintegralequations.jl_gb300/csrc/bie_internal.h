@@ -402,7 +402,7 @@ void lossy_apply(LossyOp &L, int block, const double *x, double *y);   // device
 void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gmres_opts &o,
                  bie_gmres_info &info);
 void lossy_stats(LossyOp &L, int64_t *solves, int64_t *iterations, bool reset);
-void lossy_set_one_launch(LossyOp &L, bool on);
+void lossy_set_one_launch(LossyOp &L, int mode);
 
 // An operator that the library's GMRES applies through a virtual call (the
 // visco-thermal composite and its sparse blocks).  apply: y = A x on the
@@ -433,12 +433,16 @@ struct CsrSystem {
     int nb;
 };
 // The restarted GMRES of run_gmres_devop (zero start) on a CsrSystem as one
-// thread-block-cluster launch on the context stream (bie_cluster_gmres.cu).
+// launch on the context stream (bie_cluster_gmres.cu): a cooperative grid of
+// up to one CTA per SM with a bounded grid barrier, or a thread-block cluster.
 // Writes the info to d_info and adds (1, iterations) to d_acc[0..1] on the
-// device (either may be null).  Returns false, launching nothing, when the
-// system or restart length does not fit the one-launch form.
+// device (either may be null); a grid barrier that gives up sets *d_err (the
+// grid form needs d_err).  `forms`: kOneLaunchAuto, kOneLaunchCluster or
+// kOneLaunchGrid.  Returns false, launching nothing, when the system or
+// restart length fits none of the allowed forms.
+constexpr int kOneLaunchAuto = 0, kOneLaunchCluster = 1, kOneLaunchGrid = 2;
 bool csr_gmres_one_launch(Ctx &c, const CsrSystem &A, const double2 *b, double2 *x, const bie_gmres_opts &o,
-                          int level, bie_gmres_info *d_info, unsigned long long *d_acc);
+                          int level, bie_gmres_info *d_info, unsigned long long *d_acc, int *d_err, int forms);
 void round_to_c64(Ctx &c, const double *in, float *out, int64_t n);
 // Frequency sweep (bie_sweep.cu); locks each context while it runs.
 void run_sweep(Ctx *const *ctxs, int nmesh, const double *ks, int nk, const double *const *w,

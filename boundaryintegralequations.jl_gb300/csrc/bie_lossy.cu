@@ -187,9 +187,11 @@ struct LossyOp {
     // sparse solves counted on the device in d_acc = {solves, iterations})
     int active = -1;
     int64_t nested_solves = 0, nested_iterations = 0;
-    bool one_launch = true;             // sparse solves as one cluster launch where they fit
+    int one_launch = 1;                 // sparse solves as one launch where they fit (0: off; 1: auto;
+                                        // 2: cluster form only; 3: grid form only)
     unsigned long long *d_acc = nullptr;
     bie_gmres_info *d_info = nullptr;
+    int *d_err = nullptr;               // set by a one-launch solve whose grid barrier gave up
 
     ~LossyOp() {
         cudaFree(Fa);
@@ -210,6 +212,7 @@ struct LossyOp {
         cudaFree(work);
         cudaFree(d_acc);
         cudaFree(d_info);
+        cudaFree(d_err);
     }
 
     cudaStream_t stream() const { return c->stream; }
@@ -288,9 +291,22 @@ struct LossyOp {
         }
     }
 
+    // After a synchronisation: fail if a one-launch solve's barrier gave up
+    // (the word is cleared, so the operator stays usable)
+    void check_error() {
+        int e = 0;
+        BIE_CUDA(cudaMemcpyAsync(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+        BIE_CUDA(cudaStreamSynchronize(stream()));
+        if (e) {
+            BIE_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), stream()));
+            BIE_CUDA(cudaStreamSynchronize(stream()));
+            fail(BIE_ERR_TIMEOUT, "lossy system: a one-launch GMRES barrier wait ran out");
+        }
+    }
+
     // gmres(V + Diagonal(d), b) on nb blocks of the near-field pattern: one
-    // cluster launch with the statistics kept on the device when it fits, else
-    // the launch-per-operation GMRES
+    // launch with the statistics kept on the device when it fits, else the
+    // launch-per-operation GMRES
     void solve_csr(const double2 *v, const double2 *d, int nb, const double2 *b, double2 *x,
                    const bie_gmres_opts &o, bie_gmres_info &info, bool count);
 
@@ -335,10 +351,13 @@ void LossyOp::solve_csr(const double2 *v, const double2 *d, int nb, const double
     if (lvl > kMaxSolveLevel) fail(BIE_ERR_INVALID, "lossy system: GMRES nested deeper than two levels");
     if (one_launch) {
         const CsrSystem A{nf_rp, nf_cols, v, d, N, nb};
-        if (csr_gmres_one_launch(*c, A, b, x, o, lvl, count ? nullptr : d_info, count ? d_acc : nullptr)) {
+        const int forms = one_launch == 2 ? kOneLaunchCluster : one_launch == 3 ? kOneLaunchGrid : kOneLaunchAuto;
+        if (csr_gmres_one_launch(*c, A, b, x, o, lvl, count ? nullptr : d_info, count ? d_acc : nullptr, d_err,
+                                 forms)) {
             if (!count) {
                 BIE_CUDA(cudaMemcpyAsync(&info, d_info, sizeof(info), cudaMemcpyDeviceToHost, stream()));
                 BIE_CUDA(cudaStreamSynchronize(stream()));
+                check_error();
             }
             return;
         }
@@ -483,7 +502,9 @@ LossyOp *create_lossy(Ctx &c, double freq, const bie_lossy_opts &o) {
     L->s_t = take(1);
     L->d_acc = dev_alloc<unsigned long long>(2);
     L->d_info = dev_alloc<bie_gmres_info>(1);
+    L->d_err = dev_alloc<int>(1);
     BIE_CUDA(cudaMemsetAsync(L->d_acc, 0, 2 * sizeof(unsigned long long), s));
+    BIE_CUDA(cudaMemsetAsync(L->d_err, 0, sizeof(int), s));
     BIE_CUDA(cudaStreamSynchronize(s));   // host vectors above are released on return
     return L.release();
 }
@@ -530,6 +551,7 @@ void lossy_apply(LossyOp &L, int block, const double *x_, double *y_) {
     default: fail(BIE_ERR_INVALID, "unknown lossy block");
     }
     BIE_CUDA(cudaStreamSynchronize(L.stream()));
+    L.check_error();
 }
 
 void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gmres_opts &o, bie_gmres_info &info) {
@@ -554,6 +576,7 @@ void lossy_solve(LossyOp &L, int block, const double *b, double *x, const bie_gm
     default: fail(BIE_ERR_INVALID, "lossy block is not square");
     }
     BIE_CUDA(cudaStreamSynchronize(L.stream()));
+    L.check_error();
 }
 
 void lossy_stats(LossyOp &L, int64_t *solves, int64_t *iterations, bool reset) {
@@ -569,6 +592,9 @@ void lossy_stats(LossyOp &L, int64_t *solves, int64_t *iterations, bool reset) {
     }
 }
 
-void lossy_set_one_launch(LossyOp &L, bool on) { L.one_launch = on; }
+void lossy_set_one_launch(LossyOp &L, int mode) {
+    if (mode < 0 || mode > 3) fail(BIE_ERR_INVALID, "one-launch mode must be 0, 1, 2 or 3");
+    L.one_launch = mode;
+}
 
 }  // namespace bie

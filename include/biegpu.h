@@ -767,11 +767,13 @@ BIE_API int bie_lossy_solve(bie_lossy *L, int block, const double *b, double *x,
                             const bie_gmres_opts *opts, bie_gmres_info *info);
 /* Nested GMRES solves and their iterations since creation (or the last reset). */
 BIE_API int bie_lossy_stats(bie_lossy *L, int64_t *nested_solves, int64_t *nested_iterations, int reset);
-/* on = 1 (default): the sparse thermal / viscous solves (gmres(Gh, .),
- * gmres(Gv, .) and solves of the HH, GH, HV, GV blocks) run as one
- * thread-block-cluster launch each where the system fits; 0: the
- * launch-per-operation device GMRES.  Same algorithm and tolerances. */
-BIE_API int bie_lossy_set_one_launch(bie_lossy *L, int on);
+/* The sparse thermal / viscous solves (gmres(Gh, .), gmres(Gv, .) and solves
+ * of the HH, GH, HV, GV blocks).  mode 1 (default): one launch each where the
+ * system fits, a cooperative grid over the SMs for more than 2048 rows, else
+ * a thread-block cluster; 2: the cluster form only; 3: the grid form only;
+ * 0: the launch-per-operation device GMRES.  Same algorithm and tolerances.
+ * A grid barrier wait that runs out makes the call return BIE_ERR_TIMEOUT. */
+BIE_API int bie_lossy_set_one_launch(bie_lossy *L, int mode);
 
 #ifdef __cplusplus
 }

@@ -107,21 +107,13 @@ def test_lossy_solve_and_reference_identities(name):
     assert rel(lhs, v0) <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["linear", "quadratic"])
-def test_one_launch_sparse_solves(name):
-    """The sparse thermal / viscous solves as one thread-block-cluster launch
-    (bie_lossy_set_one_launch, the default) against the launch-per-operation
-    device GMRES and the oracle's sparse direct solves: the same iterations,
-    restarts and products, solutions within the GMRES tolerance of each other
-    (1e-7) and of the direct solve (1e-6), fewer launches per product."""
-    mesh, L, O = systems(name)
-    N = mesh.n_sources
-    rng = np.random.default_rng(11)
+def _sparse_runs(L, N, modes, seed=11):
+    rng = np.random.default_rng(seed)
     b1, b3 = crandn(rng, N), crandn(rng, 3 * N)
     x = crandn(rng, N)
     runs = {}
-    for on in (False, True):
-        L.set_one_launch(on)
+    for mode in modes:
+        L.set_one_launch(mode)
         r = {}
         for blk, b in (("Gh", b1), ("Hh", b1), ("Gv", b3), ("Hv", b3)):
             r[blk] = getattr(L, blk).solve(b, return_info=True)
@@ -132,30 +124,59 @@ def test_one_launch_sparse_solves(name):
         r["product"] = L @ x
         r["launches"] = L.ctx.stats(reset=True)["kernel_launches"]
         r["stats"] = L.stats(reset=True)
-        runs[on] = r
+        runs[mode] = r
     L.set_one_launch(True)
-    per_op, one = runs[False], runs[True]
+    return runs, (b1, b3, x)
+
+
+def _same_solves(ref, got):
     for blk in ("Gh", "Hh", "Gv", "Hv", "short"):
-        (x0, i0), (x1, i1) = per_op[blk], one[blk]
+        (x0, i0), (x1, i1) = ref[blk], got[blk]
         for key in ("iterations", "restarts", "matvecs", "converged"):
             assert i0[key] == i1[key], (blk, key, i0[key], i1[key])
         assert rel(x1, x0) <= 1e-7, blk
         assert abs(i1["residual_norm"] - i0["residual_norm"]) <= 1e-6 * i0["rhs_norm"]
-    short = one["short"][1]
+    short = got["short"][1]
     assert short["iterations"] <= 3 and short["restarts"] == short["iterations"]
     assert short["converged"] == 1 or short["iterations"] == 3
-    # against the oracle's sparse direct solves
+    assert rel(got["product"], ref["product"]) <= 1e-7
+    assert got["stats"] == ref["stats"]
+    assert got["launches"] < ref["launches"]
+
+
+@pytest.mark.parametrize("name", ["linear", "quadratic"])
+def test_one_launch_sparse_solves(name):
+    """The sparse thermal / viscous solves as one launch (bie_lossy_set_one_launch:
+    thread-block cluster, cooperative grid) against the launch-per-operation
+    device GMRES and the oracle's sparse direct solves: the same iterations,
+    restarts and products, solutions within the GMRES tolerance of each other
+    (1e-7) and of the direct solve (1e-6), fewer launches per product."""
+    mesh, L, O = systems(name)
+    N = mesh.n_sources
+    runs, (b1, b3, x) = _sparse_runs(L, N, ("off", "cluster", "grid"))
+    for mode in ("cluster", "grid"):
+        _same_solves(runs["off"], runs[mode])
+    one = runs["cluster"]
     ref = {"Gh": O._gh.solve(b1), "Hh": np.linalg.solve(O.Hh.toarray(), b1),
            "Gv": np.concatenate([O._bv.solve(b3[k * N:(k + 1) * N]) for k in range(3)]),
            "Hv": np.concatenate([np.linalg.solve(O.Av.toarray(), b3[k * N:(k + 1) * N]) for k in range(3)])}
     for blk, xr in ref.items():
         assert one[blk][1]["converged"] == 1
         assert rel(one[blk][0], xr) <= 1e-6, blk
-    assert rel(one["product"], per_op["product"]) <= 1e-7
     assert rel(one["product"], O.matvec(x)) <= 1e-6
-    assert one["stats"] == per_op["stats"]
-    assert one["launches"] < per_op["launches"] <= 4000
     assert one["launches"] <= 1000
+
+
+def test_one_launch_sparse_solves_2562():
+    """The bench's 2562-node sphere (3N = 7686 rows: the grid form spread over
+    the SMs; the automatic choice) against the launch-per-operation GMRES."""
+    mesh = bm.icosphere(16)
+    L = biegpu.LossyGlobalOuter(mesh, FREQ, depth=1, n=3)
+    runs, _ = _sparse_runs(L, mesh.n_sources, ("off", "auto", "cluster"), seed=12)
+    _same_solves(runs["off"], runs["auto"])
+    _same_solves(runs["off"], runs["cluster"])
+    assert runs["auto"]["launches"] <= 100
+    L.close()
 
 
 def test_lossy_fast_acoustic_operators():
