@@ -403,6 +403,11 @@ def multi_rhs_bench(args, local, max_over_ranks):
             "per_column_mixed": {"ms_per_rhs_all_k": 1e3 * t_col, "speedup": t_col * R / t}}
 
 
+def progress(msg: str) -> None:
+    """One progress line on stderr (the JSON line stays alone on stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def multi_solve_bench(args, local, max_over_ranks):
     """Multi-RHS solve workload (the same quadratic sphere, 256 seeded complex
     N(0,1) right-hand sides, wavenumbers k, k_v, k_h of air at 100 Hz):
@@ -433,12 +438,18 @@ def multi_solve_bench(args, local, max_over_ranks):
         torch.cuda.synchronize(dev)
         per_k.append(time.perf_counter() - t0)
         infos.append(info)
+        progress(f"multi-RHS solve k={k:.4g}: {per_k[-1]:.2f} s, passes {info['passes']}, "
+                 f"inner steps {info['inner_steps']}, converged {info['converged']}/{R}")
         Cv = torch.empty(N, dtype=torch.complex128, device=dev)
         ctx.assemble_device(k, None, None, Cv, precision="df64")
+        torch.cuda.synchronize(dev)
         c = R - 1
-        xr = gmres(GPUFOperator(mesh, k) + Diagonal(1.0 - Cv), B[:, c].contiguous(), reltol=1e-12,
-                   precision="df64")
+        t1 = time.perf_counter()
+        xr, gres = gmres(GPUFOperator(mesh, k) + Diagonal(1.0 - Cv), B[:, c].contiguous(), reltol=1e-12,
+                         maxiter=600, precision="df64", log=True)
         errs.append(float(torch.linalg.norm(X[:, c] - xr) / torch.linalg.norm(xr)))
+        progress(f"  check column: df64 matrix-free GMRES {time.perf_counter() - t1:.2f} s, "
+                 f"{gres.iterations} iterations, error {errs[-1]:.2e}")
         del X
         torch.cuda.empty_cache()
     total = max_over_ranks(sum(per_k))
@@ -769,6 +780,7 @@ def main():
     entries_per_step = 2.0 * N * N
     peaks = biegpu._capi.measure_peaks(local)
 
+    progress(f"headline assembly: {args.workload}, {N} nodes, {args.steps} steps")
     with ClockSampler(local) as clk:
         dev_ms, wall, st = timed_steps(ctx, stream, ks, F, G, Cv, flush, args.steps, args.warmup,
                                        args.precision, barrier)
@@ -784,6 +796,7 @@ def main():
     plain = None
     accuracy = None
     if args.precision == "mixed" and not args.no_fp64:
+        progress("plain FP64 and double-float assemblies")
         p_ms, _, pst = timed_steps(ctx, stream, ks, F, G, Cv, flush, max(2, args.steps // 2), 1, "fp64", barrier)
         p_ms = max_over_ranks(p_ms)
         psteps = max(2, args.steps // 2)
@@ -828,6 +841,7 @@ def main():
     # ---- end to end through the host-buffer C-ABI call -----------------------
     e2e = None
     if not args.no_e2e:
+        progress("end to end through the host-buffer call")
         del F, G
         torch.cuda.empty_cache()
         pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
@@ -862,22 +876,28 @@ def main():
     # ---- batched frequency sweep (configs[2]): sweep solves/s ---------------
     sweep = None
     if not args.no_sweep:
+        progress("frequency sweep")
         sweep = sweep_bench(args, rank, world, max_over_ranks)
 
     # ---- multi-RHS tensor-core products and adjoint gradients ---------------
     multi = None
     if not args.no_multi:
+        progress("multi-RHS products")
         multi = multi_rhs_bench(args, local, max_over_ranks)
         if not args.no_multi_solve:
+            progress("multi-RHS solve")
             multi["solve"] = multi_solve_bench(args, local, max_over_ranks)
     adjoint = None
     if not args.no_adjoint:
+        progress("adjoint gradients")
         adjoint = adjoint_bench(args, max_over_ranks)
     nearfield = None
     if not args.no_nearfield:
+        progress("near field and fast operators")
         nearfield = nearfield_bench(args, max_over_ranks)
     lossy = None
     if not args.no_lossy:
+        progress("visco-thermal system")
         lossy = lossy_bench(args, max_over_ranks)
 
     if rank != 0:

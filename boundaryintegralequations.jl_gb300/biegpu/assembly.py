@@ -171,16 +171,30 @@ class Context:
         return F, G, Cv
 
     # ---- device-buffer assembly (torch tensors, enqueued on the context stream)
+    def _torch_streams(self):
+        """(torch's current stream, the library stream as a torch stream)."""
+        import torch
+        dev = torch.device(f"cuda:{self.device}")
+        if getattr(self, "_lib_stream", None) is None:
+            self._lib_stream = torch.cuda.ExternalStream(self.stream(), device=dev)
+        return torch.cuda.current_stream(dev), self._lib_stream
+
     def assemble_device(self, k, F=None, G=None, Cv=None, targets=None, precision="fp64"):
         """Fill device tensors: F, G complex128 of shape (N, M) in row-major torch
-        terms (= column-major M x N), Cv complex128 (M,).  Asynchronous."""
+        terms (= column-major M x N), Cv complex128 (M,).  Asynchronous and
+        ordered with torch's current stream: the assembly waits for the work
+        queued there before it, and later work queued there waits for the
+        assembly (device-side waits, no host synchronisation)."""
         k = complex(k)
         M = self.n_sources if targets is None else int(targets.shape[-1] if targets.ndim == 2 and targets.shape[0] == 3 else targets.shape[0])
         flags = (_capi.BIE_F if F is not None else 0) | (_capi.BIE_G if G is not None else 0) | \
                 (_capi.BIE_C if Cv is not None else 0)
+        cur, lib_stream = self._torch_streams()
+        lib_stream.wait_stream(cur)
         _capi.check(_capi.lib().bie_assemble_device(
             self._h, k.real, k.imag, _capi.ptr(targets), M, flags, _capi.PRECISION[precision],
             _capi.ptr(F), _capi.ptr(G), _capi.ptr(Cv)))
+        cur.wait_stream(lib_stream)
 
 
 def nearfield_pattern(ctx: "Context", depth: int = 1):
