@@ -58,24 +58,35 @@ struct Fp64View {
     RuleInfo ri;
 };
 
+// Per-node sums of one pair, returned by value from the out-of-line FP64 path
+// so that the caller's register arrays never have their address taken (an
+// address passed to a non-inlined call would keep them in local memory for
+// the whole element loop).
+template <int NP>
+struct PairSums {
+    float fr[NP], fi[NP], gr[NP], gi[NP];
+    double ce;
+};
+
 // FP64 integration of one deferred pair (exact rule choice), used in place when
 // the deferred list is full.
 template <int NP, bool CPLX>
-__device__ __noinline__ void pair_fp64_inplace(const Fp64View v, int64_t p, double tx, double ty,
-                                               double tz, double kre, double kim, float *fr,
-                                               float *fi, float *gr, float *gi, double *ce) {
+__device__ __noinline__ PairSums<NP> pair_fp64_inplace(const Fp64View &v, int64_t p, double tx, double ty,
+                                                       double tz, double kre, double kim) {
     const double *r = v.rec + (size_t)p * v.stride;
     const int c = dev::nearest_node<NP>(r, tx, ty, tz);
     double dfr[NP], dfi[NP], dgr[NP], dgi[NP];
-    *ce = dev::element_fp64<NP, CPLX>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP,
-                                      tx, ty, tz, kre, kim, dfr, dfi, dgr, dgi);
+    PairSums<NP> out;
+    out.ce = dev::element_fp64<NP, CPLX>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP,
+                                         tx, ty, tz, kre, kim, dfr, dfi, dgr, dgi);
 #pragma unroll
     for (int a = 0; a < NP; ++a) {
-        fr[a] = (float)dfr[a];
-        fi[a] = (float)dfi[a];
-        gr[a] = (float)dgr[a];
-        gi[a] = (float)dgi[a];
+        out.fr[a] = (float)dfr[a];
+        out.fi[a] = (float)dfi[a];
+        out.gr[a] = (float)dgr[a];
+        out.gi[a] = (float)dgi[a];
     }
+    return out;
 }
 
 // Quadrature loop of one regular pair: per-node sums of F, G and the C term.
@@ -177,13 +188,14 @@ __device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t side_slot, 
 template <int NP, bool CPLX_K, bool C64, int TPB>
 __global__ void __launch_bounds__(TPB, BIE_K2_MIN_BLOCKS * 128 / TPB)
 assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
-                      const float *__restrict__ phi, int nphi, int qmax, RuleInfo ri,
+                      const float *__restrict__ phi, int nphi, int qmax, const __grid_constant__ RuleInfo ri,
                       const double *__restrict__ tgt, int64_t M, double kre, double kim, int flags,
                       void *__restrict__ Fo, void *__restrict__ Go, float4 *__restrict__ side,
                       const uint32_t *__restrict__ kflags, const int32_t *__restrict__ kside,
                       double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
-                      unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
-                      unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev) {
+                      unsigned int *__restrict__ defer_count, unsigned int defer_cap,
+                      const __grid_constant__ Fp64View v64, unsigned long long *__restrict__ qpe_count,
+                      const double *__restrict__ kdev) {
     if (kdev) {   // wavenumber read from device memory (recorded sweeps)
         kre = kdev[0];
         kim = kdev[1];
@@ -213,6 +225,10 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
     const float kf = K.hi;
     const float kimf = (float)kim;
     for (int t = threadIdx.x; t < nphi; t += TPB) s_phi[t] = phi[t];
+    // the rule table in shared memory: indexed by each thread's nearest node,
+    // it would otherwise be copied to local memory (divergent dynamic index)
+    __shared__ RuleInfo s_ri;
+    if (threadIdx.x == 0) s_ri = ri;
 
     df cacc = {0.f, 0.f};
     unsigned long long nqpe = 0;
@@ -244,16 +260,22 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                     defer[slot] = make_int2((int)i, (int)p);
                     listed = true;
                 } else {
-                    double ced;
-                    pair_fp64_inplace<NP, CPLX_K>(v64, p, tx, ty, tz, kre, kim, fr, fi, gr, gi, &ced);
-                    ce = (float)(-ced);   // stored with the sign of the FP32 path below
+                    const PairSums<NP> ps = pair_fp64_inplace<NP, CPLX_K>(v64, p, tx, ty, tz, kre, kim);
+#pragma unroll
+                    for (int a = 0; a < NP; ++a) {
+                        fr[a] = ps.fr[a];
+                        fi[a] = ps.fi[a];
+                        gr[a] = ps.gr[a];
+                        gi[a] = ps.gi[a];
+                    }
+                    ce = (float)(-ps.ce);   // stored with the sign of the FP32 path below
                 }
             } else {
                 const mixed::Phase ph = mixed::pair_phase(P, K);
                 const int c = P.c;
-                const int Q = ri.Q[c];
+                const int Q = s_ri.Q[c];
                 nqpe += Q;
-                const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
+                const float4 *g4 = reinterpret_cast<const float4 *>(r + s_ri.off[c]);
                 const float *phc = s_phi + (size_t)c * qmax * NPP;
                 if (Q == 4) quad_loop<NP, CPLX_K, 4>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
                 else if (Q == 8) quad_loop<NP, CPLX_K, 8>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
@@ -341,7 +363,8 @@ __device__ __forceinline__ void add_entry(float2 *p, double re, double im) {
 template <int NP, bool CPLX_K, typename T2>
 __global__ void __launch_bounds__(128)
 correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restrict__ defer_count,
-                    unsigned int defer_cap, Fp64View v, const double *__restrict__ tgt, int64_t M,
+                    unsigned int defer_cap, const __grid_constant__ Fp64View v, const double *__restrict__ tgt,
+                    int64_t M,
                     double kre, double kim, int flags, T2 *__restrict__ F,
                     T2 *__restrict__ G, double *__restrict__ Cnear,
                     unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev,
@@ -644,8 +667,8 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                      RuleInfo ri, const double *__restrict__ tgt, int64_t M, double kre, double kim,
                      int flags, double2 *__restrict__ F, double2 *__restrict__ G,
                      double *__restrict__ Cpart, int chunk, int2 *__restrict__ defer,
-                     unsigned int *__restrict__ defer_count, unsigned int defer_cap, Fp64View v64,
-                     DfDegrees deg, unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev,
+                     unsigned int *__restrict__ defer_count, unsigned int defer_cap,
+                     const __grid_constant__ Fp64View v64, DfDegrees deg, unsigned long long *__restrict__ qpe_count, const double *__restrict__ kdev,
                      const double2 *__restrict__ gweight) {
     using dev::df;
     if (kdev) {   // wavenumber read from device memory (recorded sweeps)
@@ -674,6 +697,8 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
     const df K = dd::to_df(kre);
     const df Ki = dd::to_df(kim);
     for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+    __shared__ RuleInfo s_ri;   // indexed by each thread's nearest node (see the mixed kernel)
+    if (threadIdx.x == 0) s_ri = ri;
 
     dd::Acc cacc{0.f, 0.f};
     unsigned long long nqpe = 0;
@@ -742,9 +767,9 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
             df E0r, E0i;
             pair_phase_df64<CPLX_K>(kr0, r0, kim, E0r, E0i);
             const int c = P.c;
-            const int Q = ri.Q[c];
+            const int Q = s_ri.Q[c];
             nqpe += Q;
-            const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
+            const float4 *g4 = reinterpret_cast<const float4 *>(r + s_ri.off[c]);
             const float2 *phc = s_phi + (size_t)c * qmax * NP;
             dd::Acc fr[NP], fi[NP], gr[NP], gi[NP];
 #pragma unroll

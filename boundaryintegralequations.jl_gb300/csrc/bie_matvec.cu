@@ -79,12 +79,17 @@ struct Fp64Rec {
     RuleInfo ri;
 };
 
+// FP64 element integral of one pair dotted with x (f) and v (g), returned by
+// value: a pointer into the caller's registers would keep them in local memory
+struct PairDot {
+    double2 f, g;
+};
+
 // FP64 element integral of one pair dotted with x and v (deferred-list overflow)
 template <int NP, bool CPLX>
-__device__ __noinline__ void pair_fp64_dot(const Fp64Rec v, int64_t p, double tx, double ty,
-                                           double tz, double kre, double kim,
-                                           const double2 *x, const double2 *vin, double2 *yf,
-                                           double2 *yg) {
+__device__ __noinline__ PairDot pair_fp64_dot(const Fp64Rec &v, int64_t p, double tx, double ty,
+                                              double tz, double kre, double kim,
+                                              const double2 *x, const double2 *vin) {
     const double *r = v.rec + (size_t)p * v.stride;
     const int c = dev::nearest_node<NP>(r, tx, ty, tz);
     double fr[NP], fi[NP], gr[NP], gi[NP];
@@ -104,8 +109,7 @@ __device__ __noinline__ void pair_fp64_dot(const Fp64Rec v, int64_t p, double tx
             b1 += gr[a] * va.y + gi[a] * va.x;
         }
     }
-    *yf = make_double2(a0, a1);
-    *yg = make_double2(b0, b1);
+    return PairDot{make_double2(a0, a1), make_double2(b0, b1)};
 }
 
 template <int NP, bool CPLX_K>
@@ -116,8 +120,8 @@ matvec_mixed_kernel(const float *__restrict__ rec, int stride, int64_t E, int S,
                     double kre, double kim, double2 *__restrict__ yFpart,
                     double2 *__restrict__ yGpart, int chunk, int2 *__restrict__ defer,
                     unsigned int *__restrict__ defer_count, unsigned int defer_cap,
-                    Fp64Rec v64, const double2 *__restrict__ x64, const double2 *__restrict__ v64in,
-                    unsigned long long *__restrict__ qpe_count) {
+                    const __grid_constant__ Fp64Rec v64, const double2 *__restrict__ x64,
+                    const double2 *__restrict__ v64in, unsigned long long *__restrict__ qpe_count) {
     extern __shared__ __align__(16) float smemf[];
     float *s_rec = smemf;                                               // chunk * stride
     float2 *s_xiF = reinterpret_cast<float2 *>(s_rec + (size_t)chunk * stride);
@@ -129,6 +133,13 @@ matvec_mixed_kernel(const float *__restrict__ rec, int stride, int64_t E, int S,
     const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
     const bool active = i < M;
     const bool doF = xiF != nullptr, doG = xiG != nullptr;
+    // rule tables in shared memory: indexed by each thread's nearest node, they
+    // would otherwise be copied to local memory (divergent dynamic index)
+    __shared__ RuleInfo s_ri, s_rxi;
+    if (threadIdx.x == 0) {
+        s_ri = ri;
+        s_rxi = rxi;
+    }
 
     double tx = 0, ty = 0, tz = 0;
     if (active) {
@@ -168,8 +179,8 @@ matvec_mixed_kernel(const float *__restrict__ rec, int stride, int64_t E, int S,
                 if (slot < defer_cap) {
                     defer[slot] = make_int2((int)i, (int)(cb + el));
                 } else {   // list full: integrate this pair in FP64 in place
-                    double2 pf, pg;
-                    pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in, &pf, &pg);
+                    const PairDot pd = pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in);
+                    const double2 pf = pd.f, pg = pd.g;
                     // both float parts of each FP64 value, so that the pair
                     // keeps double-float accuracy in the row sums
                     if (doF) {
@@ -189,11 +200,11 @@ matvec_mixed_kernel(const float *__restrict__ rec, int stride, int64_t E, int S,
             }
             const mixed::Phase ph = mixed::pair_phase(P, K);
             const int c = P.c;
-            const int Q = ri.Q[c];
+            const int Q = s_ri.Q[c];
             nqpe += Q;
-            const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
-            const float2 *xf = s_xiF + (size_t)el * QTp + rxi.off[c];
-            const float2 *xg = s_xiG + (size_t)el * QTp + rxi.off[c];
+            const float4 *g4 = reinterpret_cast<const float4 *>(r + s_ri.off[c]);
+            const float2 *xf = s_xiF + (size_t)el * QTp + s_rxi.off[c];
+            const float2 *xg = s_xiG + (size_t)el * QTp + s_rxi.off[c];
             float afr = 0.f, afi = 0.f, agr = 0.f, agi = 0.f;
             for (int q = 0; q < Q; ++q) {
                 const mixed::QpeValues w = mixed::qpe<CPLX_K>(g4[2 * q], g4[2 * q + 1], P, ph, kf, kimf);
@@ -254,6 +265,8 @@ matvec_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off, int
         tz = tgt[3 * i + 2];
     }
     for (int t = threadIdx.x; t < nphi; t += kThreads) s_phi[t] = phi[t];
+    __shared__ RuleInfo s_ri;   // indexed by each thread's nearest node
+    if (threadIdx.x == 0) s_ri = ri;
     double yfr = 0, yfi = 0, ygr = 0, ygi = 0;
     unsigned long long nqpe = 0;
     for (int64_t cb = e0; cb < e1; cb += chunk) {
@@ -270,9 +283,9 @@ matvec_fp64_kernel(const double *__restrict__ rec, int stride, int nidx_off, int
         for (int el = 0; el < n; ++el) {
             const double *r = s_rec + (size_t)el * stride;
             const int c = dev::nearest_node<NP>(r, tx, ty, tz);
-            nqpe += ri.Q[c];
+            nqpe += s_ri.Q[c];
             double fr[NP], fi[NP], gr[NP], gi[NP];
-            dev::element_fp64<NP, CPLX_K>(r + ri.off[c], ri.Q[c], s_phi + (size_t)c * qmax * NP, tx,
+            dev::element_fp64<NP, CPLX_K>(r + s_ri.off[c], s_ri.Q[c], s_phi + (size_t)c * qmax * NP, tx,
                                           ty, tz, kre, kim, fr, fi, gr, gi);
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
 #pragma unroll
@@ -304,7 +317,7 @@ template <int NP, bool CPLX_K>
 __global__ void __launch_bounds__(128)
 matvec_correct_kernel(const int2 *__restrict__ defer, const unsigned int *__restrict__ defer_count,
                       unsigned int defer_cap, const double *__restrict__ rec, int stride,
-                      int nidx_off, const double *__restrict__ phi, int qmax, RuleInfo ri,
+                      int nidx_off, const double *__restrict__ phi, int qmax, const __grid_constant__ RuleInfo ri,
                       const double2 *__restrict__ x, const double2 *__restrict__ v,
                       const double *__restrict__ tgt, double kre, double kim,
                       double2 *__restrict__ yFn, double2 *__restrict__ yGn,
@@ -745,8 +758,8 @@ matvec_df64_kernel(const float *__restrict__ rec, int stride, int64_t E, int S, 
                    const double *__restrict__ tgt, int64_t M, double kre, double kim,
                    double2 *__restrict__ yFpart, double2 *__restrict__ yGpart, int chunk,
                    int2 *__restrict__ defer, unsigned int *__restrict__ defer_count, unsigned int defer_cap,
-                   Fp64Rec v64, const double2 *__restrict__ x64, const double2 *__restrict__ v64in,
-                   DfDegrees deg, unsigned long long *__restrict__ qpe_count) {
+                   const __grid_constant__ Fp64Rec v64, const double2 *__restrict__ x64,
+                   const double2 *__restrict__ v64in, DfDegrees deg, unsigned long long *__restrict__ qpe_count) {
     extern __shared__ __align__(16) float smemf[];
     float *s_rec = smemf;                                                   // chunk * stride
     float4 *s_xiF = reinterpret_cast<float4 *>(s_rec + (size_t)chunk * stride);
@@ -758,6 +771,13 @@ matvec_df64_kernel(const float *__restrict__ rec, int stride, int64_t E, int S, 
     const int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x;
     const bool active = i < M;
     const bool doF = xiF != nullptr, doG = xiG != nullptr;
+    // rule tables in shared memory: indexed by each thread's nearest node, they
+    // would otherwise be copied to local memory (divergent dynamic index)
+    __shared__ RuleInfo s_ri, s_rxi;
+    if (threadIdx.x == 0) {
+        s_ri = ri;
+        s_rxi = rxi;
+    }
 
     double tx = 0, ty = 0, tz = 0;
     if (active) {
@@ -798,8 +818,8 @@ matvec_df64_kernel(const float *__restrict__ rec, int stride, int64_t E, int S, 
                 if (slot < defer_cap) {
                     defer[slot] = make_int2((int)i, (int)(cb + el));
                 } else {   // list full: this pair in FP64 in place
-                    double2 pf, pg;
-                    pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in, &pf, &pg);
+                    const PairDot pd = pair_fp64_dot<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, x64, v64in);
+                    const double2 pf = pd.f, pg = pd.g;
                     if (doF) {
                         dd::acc_add(yFr, dd::to_df(pf.x));
                         dd::acc_add(yFi, dd::to_df(pf.y));
@@ -814,11 +834,11 @@ matvec_df64_kernel(const float *__restrict__ rec, int stride, int64_t E, int S, 
             df E0r, E0i;
             pair_phase_df64<CPLX_K>(kr0, r0, kim, E0r, E0i);
             const int c = P.c;
-            const int Q = ri.Q[c];
+            const int Q = s_ri.Q[c];
             nqpe += Q;
-            const float4 *g4 = reinterpret_cast<const float4 *>(r + ri.off[c]);
-            const float4 *xf = s_xiF + (size_t)el * QTp + rxi.off[c];
-            const float4 *xg = s_xiG + (size_t)el * QTp + rxi.off[c];
+            const float4 *g4 = reinterpret_cast<const float4 *>(r + s_ri.off[c]);
+            const float4 *xf = s_xiF + (size_t)el * QTp + s_rxi.off[c];
+            const float4 *xg = s_xiG + (size_t)el * QTp + s_rxi.off[c];
             for (int q = 0; q < Q; ++q) {
                 df Fr, Fi, Gr, Gi, tq;
                 qpe_df64<CPLX_K>(g4[4 * q], g4[4 * q + 1], g4[4 * q + 2], g4[4 * q + 3], P, r0, E0r, E0i, K, Ki,
