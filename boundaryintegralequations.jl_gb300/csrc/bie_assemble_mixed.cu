@@ -277,9 +277,13 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
                 nqpe += Q;
                 const float4 *g4 = reinterpret_cast<const float4 *>(r + s_ri.off[c]);
                 const float *phc = s_phi + (size_t)c * qmax * NPP;
-                if (Q == 4) quad_loop<NP, CPLX_K, 4>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
-                else if (Q == 8) quad_loop<NP, CPLX_K, 8>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
-                else quad_loop<NP, CPLX_K, 0>(g4, phc, Q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
+                // blocks of four points (one unrolled body for the 4- and
+                // 8-point rules keeps the kernel's code small), then the rest
+                int q = 0;
+                for (; q + 4 <= Q; q += 4)
+                    quad_loop<NP, CPLX_K, 4>(g4 + 2 * q, phc + q * NPP, 4, P, ph, kf, kimf, fr, fi, gr, gi, ce);
+                if (q < Q)
+                    quad_loop<NP, CPLX_K, 0>(g4 + 2 * q, phc + q * NPP, Q - q, P, ph, kf, kimf, fr, fi, gr, gi, ce);
             }
             if (!listed) mixed::df_accum(cacc, -ce);   // C = -sum tq
             if (!doFG) continue;
