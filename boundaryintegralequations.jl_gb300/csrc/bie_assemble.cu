@@ -175,6 +175,24 @@ int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile) {
     return level;
 }
 
+// Element slicing for the FP32-issue-bound kernels (mixed and double-float
+// assembly, mixed and double-float products): at least 32 blocks per SM, so
+// that the last partial wave of resident blocks is a small part of the launch,
+// but at least 64 elements per slice where the mesh allows it (finer slices
+// add partial sums, and for the mixed assembly nodes shared between slices),
+// and never coarser than choose_slice_level.  Rigid-sphere P2 (11562 rows,
+// 5780 elements): level 6 instead of 4; mixed assembly 2.31 -> 2.08 ms,
+// double-float assembly 16.9 -> 15.6 ms, mixed product 2.05 -> 1.80 ms.
+int wave_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile) {
+    const int64_t row_tiles = (M + threads_per_row_tile - 1) / threads_per_row_tile;
+    const int64_t want = 32LL * c.num_sms;
+    int level = 0;
+    while (level + 1 < kMaxLevels && row_tiles * (int64_t(1) << level) < want &&
+           (c.n_elements >> (level + 1)) >= 64)
+        ++level;
+    return std::max(level, choose_slice_level(c, M, threads_per_row_tile));
+}
+
 void launch_reduce_c(Ctx &c, const double *Cpart, int S, const double *Cextra, int64_t M,
                      double *C);
 

@@ -546,23 +546,6 @@ void build_mixed_records(Ctx &c, const std::vector<double> &rec64) {
     build_df64_records(c, rec64, rec);
 }
 
-// Element slicing of the mixed assembly when no shape is tuned or forced: at
-// least eight resident waves of blocks (4 blocks of 128 threads per SM), so the
-// last partial wave is a small part of the launch, but at least 64 elements
-// per slice where the mesh allows it (finer slices share more nodes between
-// slices, whose side slots and fix-up cost more than the waves save), and
-// never coarser than the generic choice.  Rigid-sphere P2 (11562 rows, 5780
-// elements): level 6, 3.56 ms per step against 3.74 ms at level 4.
-int mixed_slice_level(const Ctx &c, int64_t M) {
-    const int64_t row_tiles = (M + kThreads - 1) / kThreads;
-    const int64_t want = 32LL * c.num_sms;
-    int level = 0;
-    while (level + 1 < kMaxLevels && row_tiles * (int64_t(1) << level) < want &&
-           (c.n_elements >> (level + 1)) >= 64)
-        ++level;
-    return std::max(level, choose_slice_level(c, M, kThreads));
-}
-
 void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     const RecordLayout &L = c.lay;
     if (!(a.flags & (BIE_F | BIE_G | BIE_C))) return;
@@ -610,7 +593,7 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
     };
     // launch shape: the heuristic one, the autotuner's choice for this M, or
     // one a caller forced (bie_ctx_set_shape)
-    const LaunchShape base{mixed_slice_level(c, a.M), chunk0, kThreads};
+    const LaunchShape base{wave_slice_level(c, a.M, kThreads), chunk0, kThreads};
     ShapeAxes ax;
     for (int l = base.level - 1; l <= base.level + 1; ++l)
         if (l >= 0 && l < kMaxLevels && (int64_t(1) << l) <= c.n_elements) ax.levels.push_back(l);
@@ -1008,7 +991,7 @@ bool launch_assemble_df64(Ctx &c, const AssembleArgs &a) {
         }
         if (a.flags & BIE_C) launch_reduce_c(c, Cpart, S, Cnear, a.M, a.C);
     };
-    const LaunchShape base{choose_slice_level(c, a.M, kThreads), chunk0, kThreads};
+    const LaunchShape base{wave_slice_level(c, a.M, kThreads), chunk0, kThreads};
     ShapeAxes ax;
     for (int l = base.level - 1; l <= base.level + 1; ++l)
         if (l >= 0 && l < kMaxLevels && (int64_t(1) << l) <= c.n_elements) ax.levels.push_back(l);

@@ -300,6 +300,7 @@ struct AssembleArgs {
 };
 void launch_assemble_fp64(Ctx &c, const AssembleArgs &a);
 int choose_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
+int wave_slice_level(const Ctx &c, int64_t M, int threads_per_row_tile);
 // Candidate values per axis of the shape search.
 struct ShapeAxes {
     std::vector<int> levels, chunks, tpbs;

@@ -463,7 +463,7 @@ void run_mixed(Ctx &c, const MatvecArgs &a) {
             ++c.kernel_launches;
         }
     };
-    const LaunchShape base{choose_slice_level(c, M, kThreads), chunk0, kThreads};
+    const LaunchShape base{wave_slice_level(c, M, kThreads), chunk0, kThreads};
     ShapeAxes ax;
     for (int l = base.level - 1; l <= base.level + 1; ++l)
         if (l >= 0 && l < kMaxLevels && (int64_t(1) << l) <= c.n_elements) ax.levels.push_back(l);
@@ -874,7 +874,7 @@ void run_df64(Ctx &c, const MatvecArgs &a, DfDegrees deg) {
     const int64_t E = c.n_elements, M = a.M;
     const bool doF = a.x != nullptr, doG = a.v != nullptr;
 
-    const int level = choose_slice_level(c, M, kThreads);
+    const int level = wave_slice_level(c, M, kThreads);
     const int S = 1 << level;
     const size_t xi_bytes = (size_t)E * QTp * sizeof(float4);
     char *xb = static_cast<char *>(c.scratch(kScratchMatvecXi, 2 * xi_bytes));
