@@ -246,6 +246,7 @@ SIGNATURES = {
     "bie_ctx_set_gemm_wait": (_I, [_P, _I64, _I]),
     "bie_solve_multi_device": (_I, [_P, _D, _D, _I64, _P, _P, C.POINTER(MultisolveOpts),
                                     C.POINTER(MultisolveInfo)]),
+    "bie_solve_multi": (_I, [_P, _D, _D, _I64, _P, _P, C.POINTER(MultisolveOpts), C.POINTER(MultisolveInfo)]),
     "bie_ctx_get_shape": (_I, [_P, _I, _I64, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I), C.POINTER(_I)]),
     "bie_ctx_set_shape": (_I, [_P, _I, _I64, _I, _I, _I]),
     "bie_taylor_assemble": (_I, [_P, _D, _D, _P, _I64, _I, _I, _P, _P, _P]),

@@ -583,6 +583,31 @@ int bie_solve_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs,
     });
 }
 
+int bie_solve_multi(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *B, double *X,
+                    const bie_multisolve_opts *opts, bie_multisolve_info *info) {
+    return guarded([&] {
+        bie::Ctx &c = *as_ctx(ctx);
+        if (nrhs < 1 || nrhs > 65535) bie::fail(BIE_ERR_INVALID, "nrhs must be in 1..65535");
+        if (!B || !X) bie::fail(BIE_ERR_INVALID, "B and X must not be NULL");
+        const size_t bytes = (size_t)c.n_sources * (size_t)nrhs * 16;
+        char *d = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(c.mu);
+            BIE_CUDA(cudaSetDevice(c.device));
+            BIE_CUDA(cudaMalloc(&d, 2 * bytes));
+        }
+        struct Free {
+            void *p;
+            ~Free() { cudaFree(p); }
+        } guard{d};
+        double *dB = reinterpret_cast<double *>(d), *dX = reinterpret_cast<double *>(d + bytes);
+        BIE_CUDA(cudaMemcpy(dB, B, bytes, cudaMemcpyHostToDevice));
+        const int st = bie_solve_multi_device(ctx, k_re, k_im, nrhs, dB, dX, opts, info);
+        if (st != BIE_OK) bie::fail(st, bie_last_error());
+        BIE_CUDA(cudaMemcpy(X, dX, bytes, cudaMemcpyDeviceToHost));
+    });
+}
+
 int bie_ctx_set_gemm_wait(bie_ctx *ctx, int64_t cycles, int stall) {
     return guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);

@@ -284,6 +284,54 @@ function LinearMaps._unsafe_mul!(Y::AbstractMatrix, A::GPUOperator{W}, X::Abstra
     return Y
 end
 
+# Solve of many right-hand sides at once: (F + Diagonal(1 - C)) X = B, which
+# the reference solves column by column with gmres (test/3d/assembly_test.jl:37-38)
+struct MultisolveOpts
+    precision::Cint
+    restart::Cint
+    maxiter::Cint
+    max_refine::Cint
+    reltol::Float64
+    inner_reltol::Float64
+end
+
+struct MultisolveInfo
+    passes::Cint
+    inner_steps::Cint
+    converged::Cint
+    tensor_products::Cint
+    exact_products::Cint
+    reserved::Cint
+    max_relres::Float64
+    setup_ms::Float64
+    tensor_ms::Float64
+    exact_ms::Float64
+end
+
+"""
+    X, info = solve_multi_gpu(ctx, k, B; precision=:fp16_split, reltol=0.0, restart=0, maxiter=0,
+                              max_refine=0, inner_reltol=0.0)
+
+`X[:, j] = gmres(Fp + Diagonal(1 .- Cp), B[:, j])` for every column of `B` in
+one call (`bie_solve_multi`): lockstep GMRES on tensor-core products of the
+mixed-precision F, refined with exact complex64 residuals until each column's
+relative residual is at most `reltol` (0: sqrt(eps)).  `info.converged` counts
+the columns that met it.
+"""
+function solve_multi_gpu(ctx::Context, k, B::AbstractMatrix; precision=:fp16_split, reltol=0.0, restart=0,
+                         maxiter=0, max_refine=0, inner_reltol=0.0)
+    Bm = Matrix{ComplexF64}(B)
+    size(Bm, 1) == ctx.n_sources || throw(DimensionMismatch("B needs one row per collocation node"))
+    X = Matrix{ComplexF64}(undef, size(Bm))
+    opts = Ref(MultisolveOpts(MULTI_PRECISION[precision], restart, maxiter, max_refine, reltol, inner_reltol))
+    info = Ref{MultisolveInfo}()
+    GC.@preserve Bm X check(ccall((:bie_solve_multi, libbiegpu), Cint,
+                                  (Ptr{Cvoid}, Float64, Float64, Int64, Ptr{ComplexF64}, Ptr{ComplexF64},
+                                   Ref{MultisolveOpts}, Ref{MultisolveInfo}),
+                                  ctx.handle, real(k), imag(k), size(Bm, 2), Bm, X, opts, info))
+    return X, info[]
+end
+
 # ---------------------------------------------------------------------------
 # Near field: sparse_assemble_parallel! (src/3d/assembly_collocation_losses.jl:200-405)
 # ---------------------------------------------------------------------------
@@ -698,6 +746,20 @@ function LinearMaps._unsafe_mul!(y::AbstractVector, L::GPULossyGlobalOuter, x::A
     return y
 end
 
+"""
+    set_one_launch!(L, mode=:auto)
+
+The sparse thermal / viscous solves inside `L`'s products (`bie_lossy_set_one_launch`):
+`:auto` one launch each (a cooperative grid over the SMs for more than 2048
+rows, else a thread-block cluster), `:cluster`, `:grid`, or `:off` for the
+launch-per-operation device GMRES.
+"""
+function set_one_launch!(L::GPULossyGlobalOuter, mode::Symbol=:auto)
+    code = Dict(:off => 0, :auto => 1, :cluster => 2, :grid => 3)[mode]
+    check(ccall((:bie_lossy_set_one_launch, libbiegpu), Cint, (Ptr{Cvoid}, Cint), L.handle, code))
+    return L
+end
+
 "`gmres(L, b)` for the whole lossy system with the library's device GMRES."
 gmres_gpu(L::GPULossyGlobalOuter, b; kwargs...) = gmres_gpu(GPULossyBlock(L, Cint(0), (L.n, L.n)), b; kwargs...)
 
@@ -705,6 +767,6 @@ version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
 export GPU, Context, reference_rules, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
        sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective, FastFOperator, FastGOperator,
-       taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu
+       taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu, solve_multi_gpu, set_one_launch!
 
 end # module

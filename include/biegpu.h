@@ -412,6 +412,10 @@ typedef struct bie_multisolve_info {
 
 BIE_API int bie_solve_multi_device(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *d_B,
                                    double *d_X, const bie_multisolve_opts *opts, bie_multisolve_info *info);
+/* The same with host matrices (N x nrhs complex, column-major): B and X are
+ * copied to and from device memory the call allocates and frees. */
+BIE_API int bie_solve_multi(bie_ctx *ctx, double k_re, double k_im, int64_t nrhs, const double *B, double *X,
+                            const bie_multisolve_opts *opts, bie_multisolve_info *info);
 
 /*
  * Failure detection of the tensor-core GEMM (no reference counterpart; the

@@ -34,7 +34,8 @@ PY = {"bie_mesh_desc": _capi.MeshDesc, "bie_rule_table": _capi.RuleTable, "bie_s
 JL = {"bie_mesh_desc": "MeshDesc", "bie_rule_table": "RuleTable", "bie_operator": "OperatorC",
       "bie_gmres_opts": "GmresOptsC", "bie_gmres_info": "GmresInfoC", "bie_sweep_opts": "SweepOpts",
       "bie_sweep_info": "SweepInfo", "bie_adjoint_opts": "AdjointOpts", "bie_adjoint_info": "AdjointInfo",
-      "bie_lossy_opts": "LossyOpts"}
+      "bie_lossy_opts": "LossyOpts", "bie_multisolve_opts": "MultisolveOpts",
+      "bie_multisolve_info": "MultisolveInfo"}
 
 
 @pytest.fixture(scope="module")

@@ -1,4 +1,5 @@
-"""Many right-hand sides in one solve (bie_solve_multi_device): lockstep GMRES
+"""Many right-hand sides in one solve (bie_solve_multi with host matrices,
+bie_solve_multi_device with device ones): lockstep GMRES
 with tcgen05 16-bit products of the mixed-precision F, refined with exact
 residuals of the complex64 matrix, against the oracle's dense FP64 solve of
 (F + Diagonal(1 - C)) X = B (test/3d/assembly_test.jl:37-38) column by column.
@@ -50,3 +51,23 @@ def test_multi_rhs_solve_device_tensors_and_one_column():
     F, _, C = oracle.assemble(mesh, 1.5, n=2, m=2)
     xr = np.linalg.solve(F + np.diag(1.0 - C), B[:, 0])
     assert np.linalg.norm(X.cpu().numpy()[:, 0] - xr) / np.linalg.norm(xr) <= 1e-6
+
+
+def test_multi_rhs_solve_host_and_device_entries_agree():
+    """The host-buffer entry copies B in and X out around the same solve: the
+    same X bit for bit as the device entry, and argument errors reported."""
+    torch = pytest.importorskip("torch")
+    from biegpu import _capi
+    mesh = bm.icosphere(7, geometry="quadratic")
+    B = _rhs(mesh.n_sources, 9, 17)
+    ctx = biegpu.Context(mesh, n=2, m=2)
+    Xh, ih = biegpu.solve_multi(mesh, 2.5 + 0.1j, B, ctx=ctx)
+    Xd, idv = biegpu.solve_multi(mesh, 2.5 + 0.1j, torch.as_tensor(B, device="cuda:0"), ctx=ctx)
+    assert isinstance(Xh, np.ndarray) and Xh.shape == B.shape
+    assert np.array_equal(Xh, Xd.cpu().numpy())
+    assert ih["converged"] == idv["converged"] == 9 and ih["passes"] == idv["passes"]
+    with pytest.raises(ValueError):
+        biegpu.solve_multi(mesh, 1.0, B[:-1], ctx=ctx)
+    st = _capi.lib().bie_solve_multi(ctx.handle, 1.0, 0.0, 0, B.ctypes.data, B.ctypes.data, None, None)
+    assert st == _capi.BIE_ERR_INVALID
+    ctx.close()
