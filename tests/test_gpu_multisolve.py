@@ -55,7 +55,10 @@ def test_multi_rhs_solve_device_tensors_and_one_column():
 
 def test_multi_rhs_solve_host_and_device_entries_agree():
     """The host-buffer entry copies B in and X out around the same solve: the
-    same X bit for bit as the device entry, and argument errors reported."""
+    same X as the device entry to the solve's tolerance (not bit for bit: the
+    FP64 near-pair corrections reach the complex64 matrix through atomic
+    additions, whose order varies between assemblies), and argument errors
+    reported."""
     torch = pytest.importorskip("torch")
     from biegpu import _capi
     mesh = bm.icosphere(7, geometry="quadratic")
@@ -64,7 +67,8 @@ def test_multi_rhs_solve_host_and_device_entries_agree():
     Xh, ih = biegpu.solve_multi(mesh, 2.5 + 0.1j, B, ctx=ctx)
     Xd, idv = biegpu.solve_multi(mesh, 2.5 + 0.1j, torch.as_tensor(B, device="cuda:0"), ctx=ctx)
     assert isinstance(Xh, np.ndarray) and Xh.shape == B.shape
-    assert np.array_equal(Xh, Xd.cpu().numpy())
+    Xd = Xd.cpu().numpy()
+    assert np.linalg.norm(Xh - Xd) / np.linalg.norm(Xd) <= 1e-6
     assert ih["converged"] == idv["converged"] == 9 and ih["passes"] == idv["passes"]
     with pytest.raises(ValueError):
         biegpu.solve_multi(mesh, 1.0, B[:-1], ctx=ctx)
