@@ -77,7 +77,7 @@ __device__ __noinline__ PairSums<NP> pair_fp64_inplace(const Fp64View &v, int64_
     const int c = dev::nearest_node<NP>(r, tx, ty, tz);
     double dfr[NP], dfi[NP], dgr[NP], dgi[NP];
     PairSums<NP> out;
-    out.ce = dev::element_fp64<NP, CPLX>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP,
+    out.ce = dev::element_fp64<NP, CPLX, df64::TrigDf>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP,
                                          tx, ty, tz, kre, kim, dfr, dfi, dgr, dgi);
 #pragma unroll
     for (int a = 0; a < NP; ++a) {
@@ -388,7 +388,7 @@ correct_fp64_kernel(const int2 *__restrict__ defer, const unsigned int *__restri
         const int c = dev::nearest_node<NP>(r, tx, ty, tz);
         nqpe += v.ri.Q[c];
         double fr[NP], fi[NP], gr[NP], gi[NP];
-        const double ce = dev::element_fp64<NP, CPLX_K>(r + v.ri.off[c], v.ri.Q[c],
+        const double ce = dev::element_fp64<NP, CPLX_K, df64::TrigDf>(r + v.ri.off[c], v.ri.Q[c],
                                                         v.phi + (size_t)c * v.qmax * NP, tx, ty, tz,
                                                         kre, kim, fr, fi, gr, gi);
         if (gweight && doG) {   // element factor on the single layer
@@ -736,7 +736,7 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                 const double *r64 = v64.rec + (size_t)(cb + el) * v64.stride;
                 const int cn = dev::nearest_node<NP>(r64, tx, ty, tz);
                 double fr[NP], fi[NP], gr[NP], gi[NP];
-                const double ce = dev::element_fp64<NP, CPLX_K>(r64 + v64.ri.off[cn], v64.ri.Q[cn],
+                const double ce = dev::element_fp64<NP, CPLX_K, df64::TrigDf>(r64 + v64.ri.off[cn], v64.ri.Q[cn],
                                                                  v64.phi + (size_t)cn * v64.qmax * NP, tx, ty,
                                                                  tz, kre, kim, fr, fi, gr, gi);
                 if (gweight && doG) {

@@ -66,11 +66,18 @@ __device__ __forceinline__ int nearest_node(const double *P, double tx, double t
     return c;
 }
 
+// sin and cos of the phase k r in FP64: the plain FP64 kernels keep the
+// reference's arithmetic (Julia's sincos of a Float64)
+struct TrigFp64 {
+    static __device__ __forceinline__ void sincos_of(double x, double *s, double *c) { sincos(x, s, c); }
+};
+
 // FP64 integration of one element for one target with the rule clustered at
 // node c: computing_integrals! (src/3d/assembly_collocation.jl:213-252).
 // g: rule data x[Q] y[Q] z[Q] nx[Q] ny[Q] nz[Q] jw[Q]; ph: Phi[q][a].
-// Accumulates F, G per node and returns the C contribution.
-template <int NP, bool CPLX_K>
+// Accumulates F, G per node and returns the C contribution.  Trig: how the
+// sine and cosine of k r are formed (TrigFp64, or df64::TrigDf).
+template <int NP, bool CPLX_K, class Trig = TrigFp64>
 __device__ __forceinline__ double element_fp64(const double *g, int Q, const double *ph, double tx,
                                                double ty, double tz, double kre, double kim,
                                                double *fr, double *fi, double *gr, double *gi,
@@ -91,7 +98,7 @@ __device__ __forceinline__ double element_fp64(const double *g, int Q, const dou
         const double jw = g[6 * Q + q];
         const double dn = g[3 * Q + q] * dx + g[4 * Q + q] * dy + g[5 * Q + q] * dz;
         double sn, cs;
-        sincos(kre * rr, &sn, &cs);
+        Trig::sincos_of(kre * rr, &sn, &cs);
         if (CPLX_K) {
             const double damp = exp(-kim * rr);
             sn *= damp;

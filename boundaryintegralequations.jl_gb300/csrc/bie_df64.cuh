@@ -121,6 +121,29 @@ __device__ __forceinline__ void sincos_df(df x, df &s, df &c) {
     else if (q == 2) { s = neg(sn); c = neg(cs); }
     else { s = neg(cs); c = sn; }
 }
+}  // namespace dd
+
+// sin and cos of an FP64 phase through sincos_df on the FP32 pipes (relative
+// error ~2^-46, well inside the FP64-grade and mixed-precision budgets), FP64
+// sincos beyond its range.  For the FP64 element integrals of the deferred
+// (near) pairs of the mixed and double-float paths: the FP64 sine and cosine
+// are most of their FP64-pipe work, and this GPU's FP64 pipe runs at 1/64 of
+// the FP32 rate.
+struct TrigDf {
+    static __device__ __forceinline__ void sincos_of(double x, double *s, double *c) {
+        if (!(fabs(x) < (double)kDfMaxPhase)) {
+            sincos(x, s, c);
+            return;
+        }
+        dev::df sd, cd;
+        dd::sincos_df(dev::df_from_double(x), sd, cd);
+        *s = dev::f2d(sd.hi) + dev::f2d(sd.lo);
+        *c = dev::f2d(cd.hi) + dev::f2d(cd.lo);
+    }
+};
+
+namespace dd {
+
 // running sum of double-float terms with the error term carried in float
 // (renormalised once at the end of a pair)
 struct Acc {

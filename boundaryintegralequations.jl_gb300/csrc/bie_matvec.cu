@@ -93,7 +93,7 @@ __device__ __noinline__ PairDot pair_fp64_dot(const Fp64Rec &v, int64_t p, doubl
     const double *r = v.rec + (size_t)p * v.stride;
     const int c = dev::nearest_node<NP>(r, tx, ty, tz);
     double fr[NP], fi[NP], gr[NP], gi[NP];
-    dev::element_fp64<NP, CPLX>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP, tx,
+    dev::element_fp64<NP, CPLX, df64::TrigDf>(r + v.ri.off[c], v.ri.Q[c], v.phi + (size_t)c * v.qmax * NP, tx,
                                 ty, tz, kre, kim, fr, fi, gr, gi);
     const int32_t *nid = reinterpret_cast<const int32_t *>(r + v.nidx_off);
     double a0 = 0, a1 = 0, b0 = 0, b1 = 0;
@@ -332,7 +332,7 @@ matvec_correct_kernel(const int2 *__restrict__ defer, const unsigned int *__rest
         const int c = dev::nearest_node<NP>(r, tx, ty, tz);
         nqpe += ri.Q[c];
         double fr[NP], fi[NP], gr[NP], gi[NP];
-        dev::element_fp64<NP, CPLX_K>(r + ri.off[c], ri.Q[c], phi + (size_t)c * qmax * NP, tx, ty,
+        dev::element_fp64<NP, CPLX_K, df64::TrigDf>(r + ri.off[c], ri.Q[c], phi + (size_t)c * qmax * NP, tx, ty,
                                       tz, kre, kim, fr, fi, gr, gi);
         const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
         double yfr = 0, yfi = 0, ygr = 0, ygi = 0;
