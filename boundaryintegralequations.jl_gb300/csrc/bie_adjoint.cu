@@ -23,6 +23,7 @@
 // FP64 throughout.
 #include "bie_internal.h"
 #include "bie_device.cuh"
+#include "bie_df64.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -222,7 +223,9 @@ adjoint_grad_kernel(int64_t N, int64_t M, const double *__restrict__ src, const 
                 const double rinv = rsqrt(r2);
                 const double r = r2 * rinv;
                 double sn, cs;
-                sincos(kre * r, &sn, &cs);
+                // on the FP32 pipes in double-float (~2^-46 relative): the FP64
+                // sine and cosine would be a quarter of this loop's FP64 work
+                df64::TrigDf::sincos_of(kre * r, &sn, &cs);
                 if (CPLX_K) {
                     const double dmp = exp(-kim * r);
                     sn *= dmp;
