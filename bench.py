@@ -627,7 +627,8 @@ def profile_case(name: str) -> None:
     sphere: complex128 FP64 products), `taylor` (ROSEBEM k-derivative
     assembly, 2562-node P2 sphere), `sweep` (mixed frequency sweep of the
     2562-node sphere, 8 wavenumbers, launch by launch: complex64 products and
-    the exact products of the refinement residuals), `lossy` (LossyGlobalOuter
+    the exact products of the refinement residuals), `mixedmv` (mixed-precision
+    matrix-free products F x, 5762-node P2 sphere), `lossy` (LossyGlobalOuter
     products on the 2562-node sphere at 100 Hz: the one-launch sparse GMRES
     solves and the rest of the product)."""
     import torch
@@ -669,6 +670,14 @@ def profile_case(name: str) -> None:
         mesh = bm.icosphere(16)
         w = np.random.default_rng(2).normal(size=mesh.n_sources) + 0j
         biegpu.sweep([mesh], np.linspace(0.5, 8.0, 8), [w], precision="mixed", eager=True, target_error=0)
+    elif name == "mixedmv":
+        mesh = bm.icosphere(12, geometry="quadratic")
+        ctx = biegpu.Context(mesh, n=2, m=2)
+        x = torch.randn(mesh.n_sources, dtype=torch.complex128, device=dev)
+        y = torch.empty_like(x)
+        for _ in range(4):
+            _capi.check(L.bie_matvec_device(ctx.handle, 4.0, 0.0, None, 0, x.data_ptr(), None, y.data_ptr(), None,
+                                            _capi.BIE_PREC_MIXED))
     elif name == "lossy":
         mesh = bm.icosphere(16)
         Lo = biegpu.LossyGlobalOuter(mesh, 100.0, depth=1, n=3)
