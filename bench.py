@@ -882,7 +882,7 @@ def main():
                                     "d2h_bytes_per_step": int(Fh.nbytes + Gh.nbytes + Ch.nbytes),
                                     "steps": n_e2e, "call": "bie_assemble (host buffers, pinned), df64"}
 
-    # ---- batched frequency sweep (configs[2]): sweep solves/s ---------------
+    # ---- batched frequency sweep (3 meshes x 64 wavenumbers): solves/s -----
     sweep = None
     if not args.no_sweep:
         progress("frequency sweep")
