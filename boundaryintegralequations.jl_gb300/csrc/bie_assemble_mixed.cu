@@ -664,6 +664,49 @@ __global__ void df_widen_kernel(double2 *__restrict__ F, int64_t M, int64_t N,
 #endif
 constexpr int kK9Unroll = BIE_K9_UNROLL;
 
+// FP64 integration of one pair of the double-float assembly whose deferred
+// list is full, with its writes; returns the pair's C term.  Out of line so
+// that this rare path does not sit in the middle of the kernel's hot loop
+// (instruction fetch).
+template <int NP, bool CPLX_K>
+__device__ __noinline__ double k9_pair_inplace(const Fp64View &v64, int64_t p, double tx, double ty, double tz,
+                                               double kre, double kim, const double2 *__restrict__ gweight,
+                                               bool doF, bool doG, int64_t M, int64_t i, double2 *__restrict__ F,
+                                               double2 *__restrict__ G, uint32_t m) {
+    const double *r64 = v64.rec + (size_t)p * v64.stride;
+    const int cn = dev::nearest_node<NP>(r64, tx, ty, tz);
+    double fr[NP], fi[NP], gr[NP], gi[NP];
+    const double ce = dev::element_fp64<NP, CPLX_K, df64::TrigDf>(r64 + v64.ri.off[cn], v64.ri.Q[cn],
+                                                                  v64.phi + (size_t)cn * v64.qmax * NP, tx, ty, tz,
+                                                                  kre, kim, fr, fi, gr, gi);
+    if (gweight && doG) {
+        const double2 w = gweight[p];
+#pragma unroll
+        for (int a = 0; a < NP; ++a) {
+            const double t = gr[a] * w.x - gi[a] * w.y;
+            gi[a] = gr[a] * w.y + gi[a] * w.x;
+            gr[a] = t;
+        }
+    }
+    const int32_t *nid = reinterpret_cast<const int32_t *>(r64 + v64.nidx_off);
+    auto acc_of = [](double x) {
+        const dev::df t = dd::to_df(x);
+        return dd::Acc{t.hi, t.lo};
+    };
+#pragma unroll
+    for (int a = 0; a < NP; ++a) {
+        const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
+        if ((m >> a) & 1u) {
+            if (doF) add_entry(F + off, fr[a], fi[a]);
+            if (doG) add_entry(G + off, gr[a], gi[a]);
+        } else {   // float-pair entry (see the kernel)
+            if (doF) dd_rmw(reinterpret_cast<float4 *>(F + off), acc_of(fr[a]), acc_of(fi[a]));
+            if (doG) dd_rmw(reinterpret_cast<float4 *>(G + off), acc_of(gr[a]), acc_of(gi[a]));
+        }
+    }
+    return ce;
+}
+
 template <int NP, bool CPLX_K>
 __global__ void __launch_bounds__(kThreads, BIE_K9_MIN_BLOCKS)
 assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, int64_t E, int S,
@@ -733,39 +776,9 @@ assemble_df64_kernel(const float *__restrict__ rec, int stride, int nidx_off, in
                     continue;
                 }
                 // list full: the pair in FP64 here (slower, same result)
-                const double *r64 = v64.rec + (size_t)(cb + el) * v64.stride;
-                const int cn = dev::nearest_node<NP>(r64, tx, ty, tz);
-                double fr[NP], fi[NP], gr[NP], gi[NP];
-                const double ce = dev::element_fp64<NP, CPLX_K, df64::TrigDf>(r64 + v64.ri.off[cn], v64.ri.Q[cn],
-                                                                 v64.phi + (size_t)cn * v64.qmax * NP, tx, ty,
-                                                                 tz, kre, kim, fr, fi, gr, gi);
-                if (gweight && doG) {
-                    const double2 w = gweight[cb + el];
-#pragma unroll
-                    for (int a = 0; a < NP; ++a) {
-                        const double t = gr[a] * w.x - gi[a] * w.y;
-                        gi[a] = gr[a] * w.y + gi[a] * w.x;
-                        gr[a] = t;
-                    }
-                }
+                const double ce = k9_pair_inplace<NP, CPLX_K>(v64, cb + el, tx, ty, tz, kre, kim, gweight, doF, doG,
+                                                              M, i, F, G, s_mask[el]);
                 dd::acc_add(cacc, dd::to_df(ce));
-                const int32_t *nid = reinterpret_cast<const int32_t *>(r64 + v64.nidx_off);
-                const uint32_t m = s_mask[el];
-                auto acc_of = [](double x) {
-                    const df t = dd::to_df(x);
-                    return dd::Acc{t.hi, t.lo};
-                };
-#pragma unroll
-                for (int a = 0; a < NP; ++a) {
-                    const size_t off = (size_t)nid[a] * (size_t)M + (size_t)i;
-                    if ((m >> a) & 1u) {
-                        if (doF) add_entry(F + off, fr[a], fi[a]);
-                        if (doG) add_entry(G + off, gr[a], gi[a]);
-                    } else {   // float-pair entry (see below)
-                        if (doF) dd_rmw(reinterpret_cast<float4 *>(F + off), acc_of(fr[a]), acc_of(fi[a]));
-                        if (doG) dd_rmw(reinterpret_cast<float4 *>(G + off), acc_of(gr[a]), acc_of(gi[a]));
-                    }
-                }
                 continue;
             }
             df E0r, E0i;
