@@ -67,14 +67,16 @@ def test_mixed_flags():
     check(bm.icosphere(5), 2.0, fOn=False, cOn=False)
 
 
-def test_mixed_rows_full_size_rigid_sphere():
+@pytest.mark.parametrize("precision,tol", [("mixed", TOL_MIXED), ("fp64", 1e-12), ("df64", 1e-12)])
+def test_rows_full_size_rigid_sphere(precision, tol):
     """Bench workload (f=17 P2 sphere, 11562 nodes) at ka = 10: 48 sampled rows
-    of the mixed matrices against the oracle."""
+    of the full GPU matrices against the oracle, for the mixed path (1e-6),
+    the plain FP64 path and the double-float FP64-grade path (1e-12)."""
     mesh = bm.icosphere(17, geometry="quadratic")
     ctx = biegpu.get_context(mesh, n=2, m=2)
-    F, G, C = ctx.assemble(10.0, precision="mixed")
+    F, G, C = ctx.assemble(10.0, precision=precision)
     rows = np.random.default_rng(11).choice(mesh.n_sources, 48, replace=False)
     Fo, Go, Co = oracle.assemble(mesh, 10.0, targets=mesh.sources[:, rows], n=2, m=2)
-    assert rel(F[rows], Fo) <= TOL_MIXED
-    assert rel(G[rows], Go) <= TOL_MIXED
-    assert rel(C[rows], Co) <= TOL_MIXED
+    assert rel(F[rows], Fo) <= tol
+    assert rel(G[rows], Go) <= tol
+    assert rel(C[rows], Co) <= tol
