@@ -628,7 +628,12 @@ def profile_case(name: str) -> None:
     assembly, 2562-node P2 sphere), `sweep` (mixed frequency sweep of the
     2562-node sphere, 8 wavenumbers, launch by launch: complex64 products and
     the exact products of the refinement residuals), `mixedmv` (mixed-precision
-    matrix-free products F x, 5762-node P2 sphere), `lossy` (LossyGlobalOuter
+    matrix-free products F x, 5762-node P2 sphere), `multisolve` (64 right-hand
+    sides on the 5762-node P2 sphere), `sweepgraph` (the recorded-graph sweep of
+    the 2562-node sphere, 8 wavenumbers), `adjoint` (one gradient on a 1002-node
+    ellipsoid), `misc` (the remaining helper kernels: fast-operator product, the
+    standalone tensor-core GEMM, dense mixed GMRES on an odd-sized system, a
+    launch-per-operation lossy product), `lossy` (LossyGlobalOuter
     products on the 2562-node sphere at 100 Hz: the one-launch sparse GMRES
     solves and the rest of the product)."""
     import torch
@@ -670,6 +675,58 @@ def profile_case(name: str) -> None:
         mesh = bm.icosphere(16)
         w = np.random.default_rng(2).normal(size=mesh.n_sources) + 0j
         biegpu.sweep([mesh], np.linspace(0.5, 8.0, 8), [w], precision="mixed", eager=True, target_error=0)
+    elif name == "multisolve":
+        mesh = bm.icosphere(12, geometry="quadratic")
+        g = torch.Generator().manual_seed(3)
+        B = torch.complex(torch.randn(64, mesh.n_sources, generator=g, dtype=torch.float64),
+                          torch.randn(64, mesh.n_sources, generator=g, dtype=torch.float64)).to(dev).T
+        biegpu.solve_multi(mesh, 3.0, B)
+    elif name == "sweepgraph":
+        mesh = bm.icosphere(16)
+        w = np.random.default_rng(2).normal(size=mesh.n_sources) + 0j
+        biegpu.sweep([mesh], np.linspace(0.5, 8.0, 8), [w], precision="mixed", target_error=1e-6)
+    elif name == "adjoint":
+        P, T = bm.icosphere_arrays(10)
+        P = P * np.array([1.0, 2 / 3, 1 / 3])[:, None]
+        mesh = bm._finish(P, T + 1, "linear", "geometry")
+        rng = np.random.default_rng(1)
+        Z = 1.21 * 343.0 * np.exp(1j * rng.uniform(-1.0, 1.0, mesh.n_elements))
+        Xf = rng.normal(size=(3, 8))
+        Xf *= 10.0 / np.linalg.norm(Xf, axis=0)
+        biegpu.farfield_objective(mesh, 3.0, Z, Xf, rho_c=1.21 * 343.0)
+    elif name == "misc":
+        # the remaining helper kernels: fast-operator product (sparse near-field
+        # correction), the standalone tensor-core GEMM, dense mixed GMRES on an
+        # odd-sized system (complex64 rounding, one-row GEMV forms), and a
+        # launch-per-operation GMRES on vectors above 4096 entries
+        from biegpu import Diagonal, gmres
+        mesh = bm.icosphere(9)
+        xr = np.random.default_rng(1).normal(size=mesh.n_sources) + 0j
+        biegpu.FMMFOperator(mesh, 2.0) @ xr
+        ctx = biegpu.get_context(mesh, n=2, m=2)
+        # open curved plate of 41 x 41 = 1681 nodes (an odd count)
+        nx, h = 40, 0.05
+        xs, ys = np.meshgrid(np.arange(nx + 1) * h, np.arange(nx + 1) * h, indexing="xy")
+        c0 = 0.5 * nx * h
+        Pp = np.vstack([xs.ravel(), ys.ravel(), 0.5 * ((xs.ravel() - c0) ** 2 + (ys.ravel() - c0) ** 2)])
+        Tp = []
+        for j in range(nx):
+            for i in range(nx):
+                a = j * (nx + 1) + i
+                Tp += [[a, a + 1, a + nx + 2], [a, a + nx + 2, a + nx + 1]]
+        plate = bm._finish(Pp, np.array(Tp, dtype=np.int64).T + 1, "linear", "geometry")
+        Fp, _, Cp = biegpu.assemble_parallel(plate, 2.0, plate.sources, n=2, m=2, gOn=False)
+        gmres(Fp + Diagonal(1.0 - Cp), np.exp(2j * plate.sources[0]), refine=True, reltol=1e-10, maxiter=200,
+              ctx=biegpu.get_context(plate, n=2, m=2))
+        A = torch.randn(256, 512, device=dev, dtype=torch.float32)
+        Bm = torch.randn(384, 512, device=dev, dtype=torch.float32)
+        Cm = torch.empty(256, 384, device=dev, dtype=torch.float64)
+        _capi.check(L.bie_lowp_gemm_device(ctx.handle, _capi.PRECISION["fp16_split"], 256, 384, 512, A.data_ptr(),
+                                           Bm.data_ptr(), Cm.data_ptr()))
+        m16 = bm.icosphere(16)
+        Lo = biegpu.LossyGlobalOuter(m16, 100.0, depth=1, n=3)
+        Lo.set_one_launch(False)
+        Lo @ (np.random.default_rng(4).normal(size=m16.n_sources) + 0j)
     elif name == "mixedmv":
         mesh = bm.icosphere(12, geometry="quadratic")
         ctx = biegpu.Context(mesh, n=2, m=2)
