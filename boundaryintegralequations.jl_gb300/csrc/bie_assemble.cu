@@ -9,7 +9,7 @@
 //
 // Work decomposition (one GPU):
 //   grid.x  tiles of 128 target rows, one thread per row i
-//   grid.y  S element slices (contiguous ranges of the Morton-ordered element
+//   grid.y  S element slices (contiguous ranges of the bisection-ordered element
 //           records), so that even a few thousand rows fill all 152 SMs
 // Each block stages a chunk of element records (quadrature points, normals,
 // jacobian x weight for every clustered rule, the physics-node coordinates and

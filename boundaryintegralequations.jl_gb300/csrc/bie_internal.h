@@ -184,11 +184,11 @@ struct Ctx {
     std::vector<Rule> rules;
     std::vector<double> phi;             // R x qmax x NP
 
-    // element order (Morton order of centroids); records follow this order
+    // element order (recursive coordinate bisection of centroids); records follow this order
     std::vector<int32_t> order;
 
     // device data
-    double *d_records = nullptr;         // E x stride, Morton order
+    double *d_records = nullptr;         // E x stride, element order
     double *d_phi = nullptr;             // R x qmax x NP
     double *d_sources = nullptr;         // 3 x N (AoS)
     uint32_t *d_shared_mask = nullptr;   // kMaxLevels x E: bit a set -> node a is
@@ -215,10 +215,10 @@ struct Ctx {
     int64_t k2_widen_off[kMaxLevels] = {};   // d_k2_fix offset of the widening list
     int64_t k2_nwiden[kMaxLevels] = {};      // nodes of one slice with several contributions
     MixedLayout mlay;
-    float *d_mrecords = nullptr;         // E x mlay.stride words, Morton order
+    float *d_mrecords = nullptr;         // E x mlay.stride words, element order
     float *d_mphi = nullptr;             // R x qmax x NP (FP32)
     Df64Layout dlay;
-    float *d_drecords = nullptr;         // E x dlay.stride words, Morton order
+    float *d_drecords = nullptr;         // E x dlay.stride words, element order
     float *d_dphi = nullptr;             // R x qmax x NP (hi, lo) pairs
     double df_rho_max = 0.0;             // largest |x_q - c_e| over the mesh
     float *d_phase_tab = nullptr;        // e^{i j h} as (cos hi, lo, sin hi, lo), double-float kernels
@@ -289,7 +289,7 @@ struct AssembleArgs {
     double *F, *G, *C;       // device outputs (interleaved complex), may be null
     bool c64_out = false;    // mixed only: F, G are complex64 (float2) buffers, not widened
     const double *g_weight = nullptr;   // FP64 only: per-element complex factor on G
-                                        // (Morton record order), e.g. an element admittance
+                                        // (record order), e.g. an element admittance
     int taylor_m = -1;                  // FP64 only: >= 0 assembles the taylor_m-th
                                         // k-derivative (corner rules only)
     const double *k_dev = nullptr;      // device (re, im): the kernels read k here instead

@@ -521,13 +521,21 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
             physics_values(d.physics_kind, c.physics_beta, c.rules[r].u[q], c.rules[r].v[q],
                          &c.phi[((size_t)r * L.qmax + q) * NP]);
 
-    // ---- element order: Morton order of element centroids -------------------
+    // ---- element order: recursive coordinate bisection of centroids ---------
+    // The range of slice s at level l, [s*E/2^l, (s+1)*E/2^l), is split at
+    // the boundary of its two level-(l+1) halves across the longest side of
+    // its centroids' bounding box, so every slicing 2^l is a set of compact
+    // patches of equal size with short borders (fewer nodes shared between
+    // slices than a space-filling-curve order gives).  Ties break on the
+    // element index, and the elements of a range of at most two go in Morton
+    // order of their centroids, so the order is the same on every host.
     double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
     for (int64_t i = 0; i < d.n_coordinates; ++i)
         for (int k = 0; k < 3; ++k) {
             lo[k] = std::min(lo[k], c.coords[3 * i + k]);
             hi[k] = std::max(hi[k], c.coords[3 * i + k]);
         }
+    std::vector<double> cen((size_t)3 * E);
     std::vector<uint32_t> key(E);
     for (int64_t e = 0; e < E; ++e) {
         uint32_t code = 0;
@@ -535,6 +543,7 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
             double s = 0;
             for (int a = 0; a < 3; ++a) s += c.coords[3 * (int64_t)c.topo[NS * e + a] + k];
             s /= 3.0;
+            cen[3 * e + k] = s;
             double span = hi[k] - lo[k];
             double t = span > 0 ? (s - lo[k]) / span : 0.0;
             uint32_t qk = (uint32_t)std::min(1023.0, std::max(0.0, t * 1023.0));
@@ -544,8 +553,38 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     }
     c.order.resize(E);
     std::iota(c.order.begin(), c.order.end(), 0);
-    std::stable_sort(c.order.begin(), c.order.end(),
-                     [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+    {
+        struct Range { int64_t p0, p1, num, den; };   // [p0, p1) = [num*E/den, (num+1)*E/den)
+        std::vector<Range> todo{{0, E, 0, 1}};
+        while (!todo.empty()) {
+            const Range r = todo.back();
+            todo.pop_back();
+            auto b = c.order.begin();
+            if (r.p1 - r.p0 <= 2 || r.den > (int64_t(1) << 40)) {
+                std::sort(b + r.p0, b + r.p1, [&](int32_t x, int32_t y) {
+                    return key[x] != key[y] ? key[x] < key[y] : x < y;
+                });
+                continue;
+            }
+            double blo[3] = {1e300, 1e300, 1e300}, bhi[3] = {-1e300, -1e300, -1e300};
+            for (int64_t p = r.p0; p < r.p1; ++p)
+                for (int k = 0; k < 3; ++k) {
+                    blo[k] = std::min(blo[k], cen[3 * (int64_t)c.order[p] + k]);
+                    bhi[k] = std::max(bhi[k], cen[3 * (int64_t)c.order[p] + k]);
+                }
+            int ax = 0;
+            for (int k = 1; k < 3; ++k)
+                if (bhi[k] - blo[k] > bhi[ax] - blo[ax]) ax = k;
+            const int64_t den = 2 * r.den, left = 2 * r.num;
+            const int64_t mid = (int64_t)((__int128)(left + 1) * E / den);
+            std::nth_element(b + r.p0, b + mid, b + r.p1, [&](int32_t x, int32_t y) {
+                const double cx = cen[3 * (int64_t)x + ax], cy = cen[3 * (int64_t)y + ax];
+                return cx != cy ? cx < cy : x < y;
+            });
+            todo.push_back({mid, r.p1, left + 1, den});
+            todo.push_back({r.p0, mid, left, den});
+        }
+    }
 
     // ---- element records (quadrature geometry per rule) ---------------------
     std::vector<double> rec((size_t)E * L.stride, 0.0);
