@@ -145,19 +145,42 @@ __device__ __forceinline__ void red4(float4 *p, float4 v) { atomicAdd(p, v); }
 __device__ __forceinline__ void red2(float2 *p, float2 v) { atomicAdd(p, v); }
 
 // Output of one pair's per-node sums to node a of its element under the write
-// protocol (flag word fw: first / last / shared bits of the element's nodes).
-// Entries with several contributions keep float partial sums until the
-// widening pass (k2_widen_kernel).
-template <bool C64>
-__device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t side_slot, size_t off, int64_t i, int64_t M,
+// protocol (flag word fw: first / last / shared / ring bits of the element's
+// nodes; slot: the node's side slot or ring slot).  Ring nodes sum in the
+// thread's shared-memory slot (stride TPB float4s) and are written as final
+// complex128 entries at their last contribution; other entries with several
+// contributions keep float partial sums until the widening pass
+// (k2_widen_kernel).
+template <bool C64, int TPB>
+__device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t slot, size_t off, int64_t i, int64_t M,
                                          bool doF, bool doG, float fr, float fi, float gr, float gi,
-                                         void *__restrict__ Fo, void *__restrict__ Go, float4 *__restrict__ side) {
+                                         void *__restrict__ Fo, void *__restrict__ Go, float4 *__restrict__ side,
+                                         float4 *ring) {
     const bool first = (fw >> a) & 1u;
     if ((fw >> (16 + a)) & 1u) {   // shared node: this slice's sum in its side slot
-        float4 *q = side + (size_t)side_slot * (size_t)M + (size_t)i;
+        float4 *q = side + (size_t)slot * (size_t)M + (size_t)i;
         const float4 v = make_float4(fr, fi, gr, gi);
         if (first) *q = v;
         else red4(q, v);
+        return;
+    }
+    if (!C64 && ((fw >> (24 + a)) & 1u)) {   // ring node: partial sums in shared memory
+        float4 *q = ring + slot * TPB;
+        float4 v = make_float4(fr, fi, gr, gi);
+        if (!first) {
+            const float4 o = *q;
+            v.x = o.x + v.x;
+            v.y = o.y + v.y;
+            v.z = o.z + v.z;
+            v.w = o.w + v.w;
+        }
+        if ((fw >> (8 + a)) & 1u) {
+            double2 *pf = static_cast<double2 *>(Fo) + off, *pg = static_cast<double2 *>(Go) + off;
+            if (doF) __stcs(pf, widen2(v.x, v.y));
+            if (doG) __stcs(pg, widen2(v.z, v.w));
+        } else {
+            *q = v;
+        }
         return;
     }
     if (C64) {   // complex64 matrices: the entry accumulates its own sum
@@ -201,10 +224,13 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
         kim = kdev[1];
     }
     constexpr int NPP = PhiPad<NP>::value;
+    constexpr int kRing = C64 ? 0 : kK2RingSlots;
     extern __shared__ __align__(16) float smemf[];
     float *s_phi = smemf;                                   // nphi floats (padded to 4)
-    float *s_rec = smemf + ((nphi + 3) & ~3);               // chunk * stride floats
+    float4 *s_ring = reinterpret_cast<float4 *>(smemf + ((nphi + 3) & ~3));   // kRing x TPB
+    float *s_rec = reinterpret_cast<float *>(s_ring + kRing * TPB);            // chunk * stride floats
     uint32_t *s_flags = reinterpret_cast<uint32_t *>(s_rec + (size_t)chunk * stride);   // chunk
+    int32_t *s_slot = reinterpret_cast<int32_t *>(s_flags + chunk);                     // chunk * NP
 
     const int s = blockIdx.y;
     const int64_t e0 = (int64_t)s * E / S;
@@ -241,6 +267,7 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             const int n4 = n * stride / 4;
             for (int t = threadIdx.x; t < n4; t += TPB) dst[t] = src[t];
             for (int t = threadIdx.x; t < n; t += TPB) s_flags[t] = kflags[cb + t];
+            for (int t = threadIdx.x; t < n * NP; t += TPB) s_slot[t] = kside[cb * NP + t];
         }
         __syncthreads();
         if (!active) continue;
@@ -291,11 +318,12 @@ assemble_mixed_kernel(const float *__restrict__ rec, int stride, int nidx_off, i
             const int32_t *nid = reinterpret_cast<const int32_t *>(r + nidx_off);
 #pragma unroll
             for (int a = 0; a < NP; ++a) {
-                // a listed pair adds nothing: only its first stores (zero) remain
-                if (listed && !((fw >> a) & 1u)) continue;
-                const int32_t sslot = ((fw >> (16 + a)) & 1u) ? __ldg(kside + p * NP + a) : 0;
-                k2_write<C64>(a, fw, sslot, (size_t)nid[a] * (size_t)M + (size_t)i, i, M, doF, doG, fr[a],
-                              fi[a], gr[a], gi[a], Fo, Go, side);
+                // a listed pair adds nothing: only its first stores (zero) and
+                // a ring node's last contribution (the final write) remain
+                if (listed && !((fw >> a) & 1u) && !(kRing && ((fw >> (24 + a)) & (fw >> (8 + a)) & 1u)))
+                    continue;
+                k2_write<C64, TPB>(a, fw, s_slot[el * NP + a], (size_t)nid[a] * (size_t)M + (size_t)i, i, M, doF,
+                                   doG, fr[a], fi[a], gr[a], gi[a], Fo, Go, side, s_ring + threadIdx.x);
             }
         }
     }
@@ -561,13 +589,25 @@ void launch_assemble_mixed(Ctx &c, const AssembleArgs &a) {
 
     const int NPP = L.NP <= 4 ? 4 : 8;
     const size_t rec_bytes = (size_t)c.mlay.stride * sizeof(float);
-    const int chunk0 = (int)std::max<size_t>(1, std::min<size_t>(64, (24u << 10) / rec_bytes));
     const size_t phi_f = (size_t)((L.R * L.qmax * NPP + 3) & ~3);
+    // per element: record, flag word, NP slot indices; the ring of partial
+    // sums (complex128 outputs only) takes kK2RingSlots float4s per thread
+    const size_t el_bytes = rec_bytes + 4 + 4 * (size_t)L.NP;
+    const size_t ring128 = a.c64_out ? 0 : (size_t)kK2RingSlots * 128 * 16;
+    // four 128-thread blocks per SM: 228 KB of shared memory less 1 KB per block
+    const size_t blk_budget = (228u << 10) / 4 - (1u << 10);
+    const size_t fit = blk_budget > phi_f * 4 + ring128 ? (blk_budget - phi_f * 4 - ring128) / el_bytes : 1;
+    const int chunk0 = (int)std::max<size_t>(1, std::min<size_t>({64, (24u << 10) / rec_bytes, fit}));
     const bool cplx = a.k_im != 0.0;
     const bool fg = (a.flags & (BIE_F | BIE_G)) != 0;
     auto run = [&](const LaunchShape &sh) {
         const int level = sh.level, chunk = sh.chunk, tpb = sh.tpb;
-        const size_t smem = phi_f * sizeof(float) + (size_t)chunk * (rec_bytes + 4);
+        const size_t ring = a.c64_out ? 0 : (size_t)kK2RingSlots * tpb * 16;
+        const size_t smem = phi_f * sizeof(float) + ring + (size_t)chunk * el_bytes;
+        if (smem > (227u << 10))
+            fail(BIE_ERR_INVALID, "mixed assembly shape (chunk " + std::to_string(chunk) + ", " +
+                                      std::to_string(tpb) + " threads) needs " + std::to_string(smem) +
+                                      " bytes of shared memory per block, more than 232448");
         const int S = 1 << level;
         double *Cpart = static_cast<double *>(c.scratch(kScratchCpart, (size_t)S * a.M * sizeof(double)));
         float4 *side = fg ? static_cast<float4 *>(c.scratch(kScratchK2Side, (size_t)c.k2_nside[level] * a.M * 16))

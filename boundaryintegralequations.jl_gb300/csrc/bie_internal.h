@@ -69,6 +69,7 @@ constexpr int kMaxRules = 6;
 constexpr int kMaxNP = 6;
 constexpr int kMaxQ = 64;
 constexpr int kMaxLevels = 8;   // element slicings 1, 2, 4, ..., 128
+constexpr int kK2RingSlots = 16; // shared-memory partial-sum slots per thread in K2
 
 struct RecordLayout {
     int NP = 0;                 // physics nodes per element (3 or 6)
@@ -204,10 +205,16 @@ struct Ctx {
     // d_k2_side[l][p][a] (one slot per (slice, shared node)), and a fix-up pass
     // adds the slots of every shared node (d_k2_fix[l]: nodes | CSR pointers |
     // slots; nodes touched by no element get no slot and are written as zero);
-    // nodes of one slice with several contributions are widened by a
-    // streaming pass (their list follows at k2_widen_off[l]).
+    //   bit 24 + a : j has several contributions, all in slice s, and its
+    // partial sums live in ring slot d_k2_side[l][p][a] (< kK2RingSlots) of the
+    // block's shared memory from its first to its last position, where the
+    // sums become the final entries (slots are reused once a node closes; the
+    // host assigns them by earliest last position, which covers the most
+    // nodes).  The other nodes of one slice with several contributions keep
+    // float partial sums in their entries and are widened by a streaming pass
+    // (their list follows at k2_widen_off[l]).
     uint32_t *d_k2_flags = nullptr;      // kMaxLevels x E
-    int32_t *d_k2_side = nullptr;        // kMaxLevels x E x NP (-1: not shared)
+    int32_t *d_k2_side = nullptr;        // kMaxLevels x E x NP (side or ring slot, -1: neither)
     int32_t *d_k2_fix = nullptr;         // per level: nfix nodes, nfix + 1 pointers, slots
     int64_t k2_fix_off[kMaxLevels] = {};
     int64_t k2_nfix[kMaxLevels] = {};

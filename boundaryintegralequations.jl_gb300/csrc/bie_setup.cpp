@@ -14,6 +14,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <utility>
 
 namespace bie {
 
@@ -672,18 +673,22 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
     {
         const int64_t Nn = d.n_sources;
         std::vector<int64_t> stamp(Nn), fpos(Nn), lpos(Nn);
-        std::vector<int32_t> slot_of(Nn);
+        std::vector<int32_t> slot_of(Nn), ring_of(Nn);
         std::vector<std::vector<int32_t>> node_slots(Nn);
         std::vector<uint8_t> touched(Nn);
+        std::vector<int32_t> opened;
+        std::vector<std::pair<int64_t, int32_t>> spans;
         for (int l = 0; l < kMaxLevels; ++l) {
             const int64_t S = int64_t(1) << l;
             const uint8_t *sh = node_shared.data() + (size_t)l * Nn;
             std::fill(stamp.begin(), stamp.end(), -1);
             std::fill(touched.begin(), touched.end(), 0);
+            std::fill(ring_of.begin(), ring_of.end(), -1);
             for (auto &v : node_slots) v.clear();
             int64_t nside = 0;
             for (int64_t s = 0; s < S; ++s) {
                 const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
+                opened.clear();
                 for (int64_t p = p0; p < p1; ++p) {
                     const int64_t e = c.order[p];
                     for (int a = 0; a < NP; ++a) {
@@ -697,10 +702,31 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
                                 slot_of[nd] = (int32_t)nside;
                                 node_slots[nd].push_back((int32_t)nside);
                                 ++nside;
+                            } else {
+                                opened.push_back(nd);
                             }
                         }
                         lpos[nd] = p;
                     }
+                }
+                // ring slots for the slice's own nodes with several
+                // contributions: spans [fpos, lpos] in order of their last
+                // position, each to the slot that became free latest before
+                // the span opens (the most spans of any assignment)
+                spans.clear();
+                for (int32_t nd : opened)
+                    if (fpos[nd] != lpos[nd]) spans.push_back({lpos[nd], nd});
+                std::sort(spans.begin(), spans.end());
+                int64_t slot_end[kK2RingSlots];
+                std::fill(slot_end, slot_end + kK2RingSlots, int64_t(-1));
+                for (const auto &sp : spans) {
+                    const int32_t nd = sp.second;
+                    int best = -1;
+                    for (int k = 0; k < kK2RingSlots; ++k)
+                        if (slot_end[k] < fpos[nd] && (best < 0 || slot_end[k] > slot_end[best])) best = k;
+                    if (best < 0) continue;
+                    slot_end[best] = lpos[nd];
+                    ring_of[nd] = best;
                 }
                 for (int64_t p = p0; p < p1; ++p) {
                     const int64_t e = c.order[p];
@@ -712,6 +738,9 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
                         if (sh[nd]) {
                             w |= 1u << (16 + a);
                             k2_side[((size_t)l * E + p) * NP + a] = slot_of[nd];
+                        } else if (ring_of[nd] >= 0) {
+                            w |= 1u << (24 + a);
+                            k2_side[((size_t)l * E + p) * NP + a] = ring_of[nd];
                         }
                     }
                     k2_flags[(size_t)l * E + p] = w;
@@ -719,11 +748,12 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
             }
             // fix-up list: shared nodes with their slots, untouched nodes with
             // none; widening list: nodes of one slice with several contributions
-            // (their entries hold float partial sums until the widening pass)
+            // and no ring slot (their entries hold float partial sums until the
+            // widening pass)
             std::vector<int32_t> nodes, ptr{0}, slots, widen;
             for (int64_t nd = 0; nd < Nn; ++nd) {
                 if (touched[nd] && !sh[nd]) {
-                    if (fpos[nd] != lpos[nd]) widen.push_back((int32_t)nd);
+                    if (fpos[nd] != lpos[nd] && ring_of[nd] < 0) widen.push_back((int32_t)nd);
                     continue;
                 }
                 nodes.push_back((int32_t)nd);
