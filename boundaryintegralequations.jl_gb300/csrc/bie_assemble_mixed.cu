@@ -138,7 +138,13 @@ __device__ __forceinline__ void quad_loop(const float4 *g4, const float *phc, in
 #define BIE_K2_MIN_BLOCKS 4   // resident 128-thread blocks per SM (register budget)
 #endif
 
+// float -> double of an entry, two ways with the same (exact) result: integer
+// bit moves (dev::f2d) for the streaming passes, whose FP64 pipe would be their
+// bottleneck, and the conversion instruction for the assembly kernel, which
+// is bound by instruction issue and leaves its FP64 pipe idle (2.30 vs 2.48 ms
+// per assembly kernel at 11562 nodes with the integer form there)
 __device__ __forceinline__ double2 widen2(float re, float im) { return make_double2(dev::f2d(re), dev::f2d(im)); }
+__device__ __forceinline__ double2 widen2_cvt(float re, float im) { return make_double2((double)re, (double)im); }
 
 // fire-and-forget vector FP32 reductions (red.global.add.v4 / .v2)
 __device__ __forceinline__ void red4(float4 *p, float4 v) { atomicAdd(p, v); }
@@ -176,8 +182,8 @@ __device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t slot, size_
         }
         if ((fw >> (8 + a)) & 1u) {
             double2 *pf = static_cast<double2 *>(Fo) + off, *pg = static_cast<double2 *>(Go) + off;
-            if (doF) __stcs(pf, widen2(v.x, v.y));
-            if (doG) __stcs(pg, widen2(v.z, v.w));
+            if (doF) __stcs(pf, widen2_cvt(v.x, v.y));
+            if (doG) __stcs(pg, widen2_cvt(v.z, v.w));
         } else {
             *q = v;
         }
@@ -197,8 +203,8 @@ __device__ __forceinline__ void k2_write(int a, uint32_t fw, int32_t slot, size_
     }
     double2 *pf = static_cast<double2 *>(Fo) + off, *pg = static_cast<double2 *>(Go) + off;
     if (first && ((fw >> (8 + a)) & 1u)) {   // the only contribution: final value at once
-        if (doF) __stcs(pf, widen2(fr, fi));
-        if (doG) __stcs(pg, widen2(gr, gi));
+        if (doF) __stcs(pf, widen2_cvt(fr, fi));
+        if (doG) __stcs(pg, widen2_cvt(gr, gi));
         return;
     }
     // partial sums (F re, F im, G re, G im) in the 16 bytes of one entry
