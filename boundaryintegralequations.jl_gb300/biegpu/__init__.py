@@ -8,7 +8,8 @@ reference's Julia API for the path:
   * ``assemble_parallel`` -> (F, G, C)  (:mod:`biegpu.assembly`)
 """
 from ._capi import BIEError, lib, library_path  # noqa: F401
-from .assembly import Context, assemble_parallel, basis, get_context, quadrature_rule  # noqa: F401
+from .assembly import (Context, assemble_parallel, basis, element_slicing, get_context,  # noqa: F401
+                       quadrature_rule)
 from .mesh import Mesh3d, ellipsoid, icosphere, load_comsol, read_comsol  # noqa: F401
 from .operators import (Diagonal, FMMFOperator, FMMGOperator, GPUFOperator, GPUGOperator, I,  # noqa: F401
                         UniformScaling, gmres)

@@ -48,6 +48,43 @@ def basis(kind: str, u, v, beta: float = 0.0):
     return tuple(out)
 
 
+def mesh_desc(mesh: Mesh3d):
+    """A bie_mesh_desc of the mesh (quad_n = quad_m = 1) and the tuple of the
+    Fortran-ordered arrays it points at, to be kept alive while it is used."""
+    keep = (np.asfortranarray(mesh.coordinates, dtype=np.float64),
+            np.asfortranarray(mesh.topology, dtype=np.int64),
+            np.asfortranarray(mesh.physics_topology, dtype=np.int64),
+            np.asfortranarray(mesh.sources, dtype=np.float64))
+    d = _capi.MeshDesc(
+        n_coordinates=keep[0].shape[1], coordinates=keep[0].ctypes.data_as(C.POINTER(C.c_double)),
+        n_elements=keep[1].shape[1], shape_kind=_capi.KIND[mesh.shape_function],
+        physics_kind=_capi.KIND[mesh.physics_function], topology=keep[1].ctypes.data_as(C.POINTER(C.c_int64)),
+        physics_topology=keep[2].ctypes.data_as(C.POINTER(C.c_int64)), n_sources=keep[3].shape[1],
+        sources=keep[3].ctypes.data_as(C.POINTER(C.c_double)), quad_n=1, quad_m=1,
+        physics_beta=float(getattr(mesh, "physics_beta", 0.0)))
+    return d, keep
+
+
+SLICING_COUNTS = ("shared", "side_slots", "ring", "widened", "single", "untouched")
+
+
+def element_slicing(mesh: Mesh3d, level: int):
+    """The element slicing of the assembly kernels, computed on the host
+    (bie_element_slicing; no GPU): (order, counts).  order: the E 1-based
+    element numbers in the order the kernels process them (a recursive
+    coordinate bisection of the element centroids); counts: the nodes of each
+    kind at slicing level `level` (2^level slices), keyed by SLICING_COUNTS:
+    shared between slices (with their side slots), of one slice with several
+    contributions summed in the shared-memory ring or widened afterwards, with
+    one contribution, or touched by no element."""
+    d, keep = mesh_desc(mesh)
+    order = np.empty(mesh.topology.shape[1], dtype=np.int32)
+    counts = np.zeros(len(SLICING_COUNTS), dtype=np.int64)
+    _capi.check(_capi.lib().bie_element_slicing(C.byref(d), int(level), order.ctypes.data, counts.ctypes.data))
+    del keep
+    return order, dict(zip(SLICING_COUNTS, (int(v) for v in counts)))
+
+
 class Context:
     """A libbiegpu context: one mesh, one quadrature order (n, m), one device.
 

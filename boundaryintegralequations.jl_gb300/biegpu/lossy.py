@@ -23,6 +23,7 @@ import numpy as np
 
 from . import _capi
 from .assembly import Context, get_context
+from .assembly import mesh_desc as _mesh_desc
 from .mesh import Mesh3d
 
 AIR_20C = {"rho": 1.204, "c": 343.2, "mu": 1.81e-5, "alpha": 2.2e-5}
@@ -62,21 +63,6 @@ def visco_thermal_constants(freq=1000.0, S=-1.0, pa=101325.0, t=20.0, Hr=50.0):
     _capi.check(_capi.lib().bie_visco_thermal_constants(float(freq), float(S), float(pa), float(t), float(Hr),
                                                         C.byref(k)))
     return _constants_tuple(k)
-
-
-def _mesh_desc(mesh: Mesh3d):
-    keep = (np.asfortranarray(mesh.coordinates, dtype=np.float64),
-            np.asfortranarray(mesh.topology, dtype=np.int64),
-            np.asfortranarray(mesh.physics_topology, dtype=np.int64),
-            np.asfortranarray(mesh.sources, dtype=np.float64))
-    d = _capi.MeshDesc(
-        n_coordinates=keep[0].shape[1], coordinates=keep[0].ctypes.data_as(C.POINTER(C.c_double)),
-        n_elements=keep[1].shape[1], shape_kind=_capi.KIND[mesh.shape_function],
-        physics_kind=_capi.KIND[mesh.physics_function], topology=keep[1].ctypes.data_as(C.POINTER(C.c_int64)),
-        physics_topology=keep[2].ctypes.data_as(C.POINTER(C.c_int64)), n_sources=keep[3].shape[1],
-        sources=keep[3].ctypes.data_as(C.POINTER(C.c_double)), quad_n=1, quad_m=1,
-        physics_beta=float(getattr(mesh, "physics_beta", 0.0)))
-    return d, keep
 
 
 def tangential_derivatives(mesh: Mesh3d):

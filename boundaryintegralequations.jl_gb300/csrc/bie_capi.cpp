@@ -1031,6 +1031,49 @@ int bie_tangential_derivatives(const bie_mesh_desc *d, int64_t *nnz, int64_t *ro
     });
 }
 
+int bie_element_slicing(const bie_mesh_desc *d, int level, int32_t *order, int64_t *counts) {
+    return guarded([&] {
+        if (!d) bie::fail(BIE_ERR_INVALID, "mesh must not be NULL");
+        if (d->n_coordinates <= 0 || d->n_elements <= 0 || d->n_sources <= 0 || !d->coordinates || !d->topology ||
+            !d->physics_topology)
+            bie::fail(BIE_ERR_INVALID, "mesh sizes must be positive and its arrays given");
+        if (d->n_coordinates > INT32_MAX || d->n_sources > INT32_MAX || d->n_elements > INT32_MAX)
+            bie::fail(BIE_ERR_INVALID, "mesh too large for 32-bit node indices");
+        if (d->shape_kind != BIE_TRI_LINEAR && d->shape_kind != BIE_TRI_QUADRATIC)
+            bie::fail(BIE_ERR_UNSUPPORTED, "geometry must be 3- or 6-node triangles");
+        if (level < 0 || level >= bie::kMaxLevels)
+            bie::fail(BIE_ERR_INVALID, "level must be in 0.." + std::to_string(bie::kMaxLevels - 1));
+        const int NS = bie::n_nodes_of_kind(d->shape_kind), NP = bie::n_nodes_of_kind(d->physics_kind);
+        const int64_t E = d->n_elements, N = d->n_sources;
+        std::vector<int32_t> topo((size_t)NS * E), ptopo((size_t)NP * E);
+        for (int64_t i = 0; i < NS * E; ++i) {
+            const int64_t v = d->topology[i];
+            if (v < 1 || v > d->n_coordinates) bie::fail(BIE_ERR_INVALID, "topology index out of range");
+            topo[(size_t)i] = (int32_t)(v - 1);
+        }
+        for (int64_t i = 0; i < NP * E; ++i) {
+            const int64_t v = d->physics_topology[i];
+            if (v < 1 || v > N) bie::fail(BIE_ERR_INVALID, "physics_topology index out of range");
+            ptopo[(size_t)i] = (int32_t)(v - 1);
+        }
+        for (int64_t i = 0; i < 3 * d->n_coordinates; ++i)
+            if (!std::isfinite(d->coordinates[i])) bie::fail(BIE_ERR_INVALID, "non-finite coordinate");
+        const std::vector<int32_t> ord = bie::bisection_order(d->coordinates, d->n_coordinates, topo.data(), NS, E);
+        if (order)
+            for (int64_t p = 0; p < E; ++p) order[p] = ord[(size_t)p] + 1;
+        if (counts) {
+            bie::WriteProtocol w;
+            bie::build_write_protocol(ord.data(), E, ptopo.data(), NP, N, w);
+            counts[0] = w.nshared[level];
+            counts[1] = w.nside[level];
+            counts[2] = w.nring[level];
+            counts[3] = w.nwiden[level];
+            counts[4] = w.nsingle[level];
+            counts[5] = w.nuntouched[level];
+        }
+    });
+}
+
 int bie_lossy_create(bie_ctx *ctx, double freq, const bie_lossy_opts *opts, bie_lossy **out) {
     return guarded([&] {
         bie::Ctx &c = *as_ctx(ctx);

@@ -342,6 +342,29 @@ void launch_matvec_noalloc(Ctx &c, const MatvecArgs &a);
 // bie_matvec_device_noalloc call needs no module load and no stack growth.
 void prepare_noalloc(Ctx &c);
 
+// Host-side tables of the element slicings (no GPU): the element order and,
+// per slicing level l (S = 2^l slices of the ordered elements), the
+// shared-node masks of K1/K9 and the write protocol of K2 (flags, side or
+// ring slots, fix-up and widening lists; layout in Ctx::d_k2_flags) with
+// counts of each kind of node.
+struct WriteProtocol {
+    std::vector<uint32_t> masks;          // kMaxLevels x E
+    std::vector<uint8_t> node_shared;     // kMaxLevels x N
+    std::vector<uint32_t> k2_flags;       // kMaxLevels x E
+    std::vector<int32_t> k2_side;         // kMaxLevels x E x NP
+    std::vector<int32_t> k2_fix;          // per level: fix-up nodes | pointers | slots | widening nodes
+    int64_t fix_off[kMaxLevels] = {}, nfix[kMaxLevels] = {}, nside[kMaxLevels] = {};
+    int64_t widen_off[kMaxLevels] = {}, nwiden[kMaxLevels] = {};
+    int64_t nshared[kMaxLevels] = {};     // nodes touched by two or more slices
+    int64_t nring[kMaxLevels] = {};       // one slice, several contributions, a ring slot
+    int64_t nsingle[kMaxLevels] = {};     // exactly one contribution
+    int64_t nuntouched[kMaxLevels] = {};  // touched by no element
+};
+std::vector<int32_t> bisection_order(const double *coords, int64_t n_coords, const int32_t *topo, int NS,
+                                     int64_t E);
+void build_write_protocol(const int32_t *order, int64_t E, const int32_t *ptopo, int NP, int64_t Nn,
+                          WriteProtocol &w);
+
 // GMRES (bie_solver.cu); b, x device, N = n_sources
 void run_gmres(Ctx &c, const bie_operator &op, const double *b, double *x, const bie_gmres_opts &o,
                bie_gmres_info &info);

@@ -404,6 +404,237 @@ void Ctx::collect_timers() {
     ev_tensor.clear();
 }
 
+// Element order of the assembly kernels: recursive coordinate bisection of
+// the element centroids (topo: 0-based geometry nodes, NS per element).
+std::vector<int32_t> bisection_order(const double *coords, int64_t n_coords, const int32_t *topo, int NS,
+                                     int64_t E) {
+    std::vector<int32_t> order;
+    // The range of slice s at level l, [s*E/2^l, (s+1)*E/2^l), is split at
+    // the boundary of its two level-(l+1) halves across the longest side of
+    // its centroids' bounding box, so every slicing 2^l is a set of compact
+    // patches of equal size with short borders (fewer nodes shared between
+    // slices than a space-filling-curve order gives).  Ties break on the
+    // element index, and the elements of a range of at most two go in Morton
+    // order of their centroids, so the order is the same on every host.
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = 0; i < n_coords; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], coords[3 * i + k]);
+            hi[k] = std::max(hi[k], coords[3 * i + k]);
+        }
+    std::vector<double> cen((size_t)3 * E);
+    std::vector<uint32_t> key(E);
+    for (int64_t e = 0; e < E; ++e) {
+        uint32_t code = 0;
+        for (int k = 0; k < 3; ++k) {
+            double s = 0;
+            for (int a = 0; a < 3; ++a) s += coords[3 * (int64_t)topo[NS * e + a] + k];
+            s /= 3.0;
+            cen[3 * e + k] = s;
+            double span = hi[k] - lo[k];
+            double t = span > 0 ? (s - lo[k]) / span : 0.0;
+            uint32_t qk = (uint32_t)std::min(1023.0, std::max(0.0, t * 1023.0));
+            code |= spread10(qk) << k;
+        }
+        key[e] = code;
+    }
+    order.resize(E);
+    std::iota(order.begin(), order.end(), 0);
+    {
+        struct Range { int64_t p0, p1, num, den; };   // [p0, p1) = [num*E/den, (num+1)*E/den)
+        std::vector<Range> todo{{0, E, 0, 1}};
+        while (!todo.empty()) {
+            const Range r = todo.back();
+            todo.pop_back();
+            auto b = order.begin();
+            if (r.p1 - r.p0 <= 2 || r.den > (int64_t(1) << 40)) {
+                std::sort(b + r.p0, b + r.p1, [&](int32_t x, int32_t y) {
+                    return key[x] != key[y] ? key[x] < key[y] : x < y;
+                });
+                continue;
+            }
+            double blo[3] = {1e300, 1e300, 1e300}, bhi[3] = {-1e300, -1e300, -1e300};
+            for (int64_t p = r.p0; p < r.p1; ++p)
+                for (int k = 0; k < 3; ++k) {
+                    blo[k] = std::min(blo[k], cen[3 * (int64_t)order[p] + k]);
+                    bhi[k] = std::max(bhi[k], cen[3 * (int64_t)order[p] + k]);
+                }
+            int ax = 0;
+            for (int k = 1; k < 3; ++k)
+                if (bhi[k] - blo[k] > bhi[ax] - blo[ax]) ax = k;
+            const int64_t den = 2 * r.den, left = 2 * r.num;
+            const int64_t mid = (int64_t)((__int128)(left + 1) * E / den);
+            std::nth_element(b + r.p0, b + mid, b + r.p1, [&](int32_t x, int32_t y) {
+                const double cx = cen[3 * (int64_t)x + ax], cy = cen[3 * (int64_t)y + ax];
+                return cx != cy ? cx < cy : x < y;
+            });
+            todo.push_back({mid, r.p1, left + 1, den});
+            todo.push_back({r.p0, mid, left, den});
+        }
+    }
+    return order;
+}
+
+// Write protocol of the assembly kernels for every slicing level (order: the
+// element order, ptopo: 0-based physics nodes, NP per element, Nn nodes).
+void build_write_protocol(const int32_t *order, int64_t E, const int32_t *ptopo, int NP, int64_t Nn,
+                          WriteProtocol &w) {
+    // ---- shared-node masks for the element slicings S = 2^l ------------------
+    // Slice s of S covers sorted positions [s*E/S, (s+1)*E/S).  A node is shared
+    // at level l when elements of two different slices touch it; writes to a
+    // shared node use atomics, all other writes are plain read-modify-writes by
+    // the single thread that owns the (row, node) entry.
+    std::vector<uint32_t> &masks = w.masks;
+    masks.assign((size_t)kMaxLevels * E, 0u);
+    std::vector<int32_t> first(Nn);
+    std::vector<uint8_t> shared(Nn);
+    std::vector<uint8_t> &node_shared = w.node_shared;
+    node_shared.assign((size_t)kMaxLevels * Nn, 0);
+    for (int l = 0; l < kMaxLevels; ++l) {
+        const int64_t S = int64_t(1) << l;
+        std::fill(first.begin(), first.end(), -1);
+        std::fill(shared.begin(), shared.end(), 0);
+        for (int64_t s = 0; s < S; ++s) {
+            const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
+            for (int64_t p = p0; p < p1; ++p) {
+                const int64_t e = order[p];
+                for (int a = 0; a < NP; ++a) {
+                    int32_t nd = ptopo[NP * e + a];
+                    if (first[nd] < 0) first[nd] = (int32_t)s;
+                    else if (first[nd] != (int32_t)s) shared[nd] = 1;
+                }
+            }
+        }
+        for (int64_t p = 0; p < E; ++p) {
+            const int64_t e = order[p];
+            uint32_t m = 0;
+            for (int a = 0; a < NP; ++a)
+                if (shared[ptopo[NP * e + a]]) m |= 1u << a;
+            masks[(size_t)l * E + p] = m;
+        }
+        std::copy(shared.begin(), shared.end(), node_shared.begin() + (size_t)l * Nn);
+    }
+
+    // ---- write protocol of the mixed assembly per slicing level --------------
+    // Each (row, node) entry is written by the one thread that owns its row in
+    // the node's slice: its first contribution stores, later ones add, the last
+    // one converts; nodes shared between slices go through side slots.
+    std::vector<uint32_t> &k2_flags = w.k2_flags;
+    k2_flags.assign((size_t)kMaxLevels * E, 0u);
+    std::vector<int32_t> &k2_side = w.k2_side;
+    k2_side.assign((size_t)kMaxLevels * E * NP, -1);
+    std::vector<int32_t> &k2_fix = w.k2_fix;
+    k2_fix.clear();
+    {
+        std::vector<int64_t> stamp(Nn), fpos(Nn), lpos(Nn);
+        std::vector<int32_t> slot_of(Nn), ring_of(Nn);
+        std::vector<std::vector<int32_t>> node_slots(Nn);
+        std::vector<uint8_t> touched(Nn);
+        std::vector<int32_t> opened;
+        std::vector<std::pair<int64_t, int32_t>> spans;
+        for (int l = 0; l < kMaxLevels; ++l) {
+            const int64_t S = int64_t(1) << l;
+            const uint8_t *sh = node_shared.data() + (size_t)l * Nn;
+            std::fill(stamp.begin(), stamp.end(), -1);
+            std::fill(touched.begin(), touched.end(), 0);
+            std::fill(ring_of.begin(), ring_of.end(), -1);
+            for (auto &v : node_slots) v.clear();
+            int64_t nside = 0;
+            for (int64_t s = 0; s < S; ++s) {
+                const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
+                opened.clear();
+                for (int64_t p = p0; p < p1; ++p) {
+                    const int64_t e = order[p];
+                    for (int a = 0; a < NP; ++a) {
+                        const int32_t nd = ptopo[NP * e + a];
+                        touched[nd] = 1;
+                        if (stamp[nd] != s) {
+                            stamp[nd] = s;
+                            fpos[nd] = p;
+                            if (sh[nd]) {
+                                if (nside >= INT32_MAX) fail(BIE_ERR_INVALID, "mesh too large for the slot index");
+                                slot_of[nd] = (int32_t)nside;
+                                node_slots[nd].push_back((int32_t)nside);
+                                ++nside;
+                            } else {
+                                opened.push_back(nd);
+                            }
+                        }
+                        lpos[nd] = p;
+                    }
+                }
+                // ring slots for the slice's own nodes with several
+                // contributions: spans [fpos, lpos] in order of their last
+                // position, each to the slot that became free latest before
+                // the span opens (the most spans of any assignment)
+                spans.clear();
+                for (int32_t nd : opened)
+                    if (fpos[nd] != lpos[nd]) spans.push_back({lpos[nd], nd});
+                std::sort(spans.begin(), spans.end());
+                int64_t slot_end[kK2RingSlots];
+                std::fill(slot_end, slot_end + kK2RingSlots, int64_t(-1));
+                for (const auto &sp : spans) {
+                    const int32_t nd = sp.second;
+                    int best = -1;
+                    for (int k = 0; k < kK2RingSlots; ++k)
+                        if (slot_end[k] < fpos[nd] && (best < 0 || slot_end[k] > slot_end[best])) best = k;
+                    if (best < 0) continue;
+                    slot_end[best] = lpos[nd];
+                    ring_of[nd] = best;
+                }
+                for (int64_t p = p0; p < p1; ++p) {
+                    const int64_t e = order[p];
+                    uint32_t w = 0;
+                    for (int a = 0; a < NP; ++a) {
+                        const int32_t nd = ptopo[NP * e + a];
+                        if (fpos[nd] == p) w |= 1u << a;
+                        if (lpos[nd] == p) w |= 1u << (8 + a);
+                        if (sh[nd]) {
+                            w |= 1u << (16 + a);
+                            k2_side[((size_t)l * E + p) * NP + a] = slot_of[nd];
+                        } else if (ring_of[nd] >= 0) {
+                            w |= 1u << (24 + a);
+                            k2_side[((size_t)l * E + p) * NP + a] = ring_of[nd];
+                        }
+                    }
+                    k2_flags[(size_t)l * E + p] = w;
+                }
+            }
+            // fix-up list: shared nodes with their slots, untouched nodes with
+            // none; widening list: nodes of one slice with several contributions
+            // and no ring slot (their entries hold float partial sums until the
+            // widening pass)
+            std::vector<int32_t> nodes, ptr{0}, slots, widen;
+            int64_t nshared = 0, nring = 0, nsingle = 0;
+            for (int64_t nd = 0; nd < Nn; ++nd) {
+                if (touched[nd] && !sh[nd]) {
+                    if (fpos[nd] == lpos[nd]) ++nsingle;
+                    else if (ring_of[nd] >= 0) ++nring;
+                    else widen.push_back((int32_t)nd);
+                    continue;
+                }
+                if (sh[nd]) ++nshared;
+                nodes.push_back((int32_t)nd);
+                for (int32_t k : node_slots[nd]) slots.push_back(k);
+                ptr.push_back((int32_t)slots.size());
+            }
+            w.fix_off[l] = (int64_t)k2_fix.size();
+            w.nfix[l] = (int64_t)nodes.size();
+            w.nside[l] = nside;
+            w.nwiden[l] = (int64_t)widen.size();
+            w.nshared[l] = nshared;
+            w.nring[l] = nring;
+            w.nsingle[l] = nsingle;
+            w.nuntouched[l] = (int64_t)nodes.size() - nshared;
+            k2_fix.insert(k2_fix.end(), nodes.begin(), nodes.end());
+            k2_fix.insert(k2_fix.end(), ptr.begin(), ptr.end());
+            k2_fix.insert(k2_fix.end(), slots.begin(), slots.end());
+            w.widen_off[l] = (int64_t)k2_fix.size();
+            k2_fix.insert(k2_fix.end(), widen.begin(), widen.end());
+        }
+    }
+}
+
 void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
                    const std::vector<Rule> *explicit_rules) {
     // ---- validation -------------------------------------------------------
@@ -522,70 +753,8 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
             physics_values(d.physics_kind, c.physics_beta, c.rules[r].u[q], c.rules[r].v[q],
                          &c.phi[((size_t)r * L.qmax + q) * NP]);
 
-    // ---- element order: recursive coordinate bisection of centroids ---------
-    // The range of slice s at level l, [s*E/2^l, (s+1)*E/2^l), is split at
-    // the boundary of its two level-(l+1) halves across the longest side of
-    // its centroids' bounding box, so every slicing 2^l is a set of compact
-    // patches of equal size with short borders (fewer nodes shared between
-    // slices than a space-filling-curve order gives).  Ties break on the
-    // element index, and the elements of a range of at most two go in Morton
-    // order of their centroids, so the order is the same on every host.
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t i = 0; i < d.n_coordinates; ++i)
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = std::min(lo[k], c.coords[3 * i + k]);
-            hi[k] = std::max(hi[k], c.coords[3 * i + k]);
-        }
-    std::vector<double> cen((size_t)3 * E);
-    std::vector<uint32_t> key(E);
-    for (int64_t e = 0; e < E; ++e) {
-        uint32_t code = 0;
-        for (int k = 0; k < 3; ++k) {
-            double s = 0;
-            for (int a = 0; a < 3; ++a) s += c.coords[3 * (int64_t)c.topo[NS * e + a] + k];
-            s /= 3.0;
-            cen[3 * e + k] = s;
-            double span = hi[k] - lo[k];
-            double t = span > 0 ? (s - lo[k]) / span : 0.0;
-            uint32_t qk = (uint32_t)std::min(1023.0, std::max(0.0, t * 1023.0));
-            code |= spread10(qk) << k;
-        }
-        key[e] = code;
-    }
-    c.order.resize(E);
-    std::iota(c.order.begin(), c.order.end(), 0);
-    {
-        struct Range { int64_t p0, p1, num, den; };   // [p0, p1) = [num*E/den, (num+1)*E/den)
-        std::vector<Range> todo{{0, E, 0, 1}};
-        while (!todo.empty()) {
-            const Range r = todo.back();
-            todo.pop_back();
-            auto b = c.order.begin();
-            if (r.p1 - r.p0 <= 2 || r.den > (int64_t(1) << 40)) {
-                std::sort(b + r.p0, b + r.p1, [&](int32_t x, int32_t y) {
-                    return key[x] != key[y] ? key[x] < key[y] : x < y;
-                });
-                continue;
-            }
-            double blo[3] = {1e300, 1e300, 1e300}, bhi[3] = {-1e300, -1e300, -1e300};
-            for (int64_t p = r.p0; p < r.p1; ++p)
-                for (int k = 0; k < 3; ++k) {
-                    blo[k] = std::min(blo[k], cen[3 * (int64_t)c.order[p] + k]);
-                    bhi[k] = std::max(bhi[k], cen[3 * (int64_t)c.order[p] + k]);
-                }
-            int ax = 0;
-            for (int k = 1; k < 3; ++k)
-                if (bhi[k] - blo[k] > bhi[ax] - blo[ax]) ax = k;
-            const int64_t den = 2 * r.den, left = 2 * r.num;
-            const int64_t mid = (int64_t)((__int128)(left + 1) * E / den);
-            std::nth_element(b + r.p0, b + mid, b + r.p1, [&](int32_t x, int32_t y) {
-                const double cx = cen[3 * (int64_t)x + ax], cy = cen[3 * (int64_t)y + ax];
-                return cx != cy ? cx < cy : x < y;
-            });
-            todo.push_back({mid, r.p1, left + 1, den});
-            todo.push_back({r.p0, mid, left, den});
-        }
-    }
+    // ---- element order -------------------------------------------------------
+    c.order = bisection_order(c.coords.data(), d.n_coordinates, c.topo.data(), NS, E);
 
     // ---- element records (quadrature geometry per rule) ---------------------
     std::vector<double> rec((size_t)E * L.stride, 0.0);
@@ -629,148 +798,21 @@ void build_context(Ctx &c, const bie_mesh_desc &d, int device, int gauss_rule,
         for (int a = 0; a < NP; ++a) nid[a] = c.ptopo[NP * e + a];
     }
 
-    // ---- shared-node masks for the element slicings S = 2^l ------------------
-    // Slice s of S covers sorted positions [s*E/S, (s+1)*E/S).  A node is shared
-    // at level l when elements of two different slices touch it; writes to a
-    // shared node use atomics, all other writes are plain read-modify-writes by
-    // the single thread that owns the (row, node) entry.
-    std::vector<uint32_t> masks((size_t)kMaxLevels * E, 0u);
-    std::vector<int32_t> first(d.n_sources);
-    std::vector<uint8_t> shared(d.n_sources);
-    std::vector<uint8_t> node_shared((size_t)kMaxLevels * d.n_sources);
+    // ---- shared-node masks and the write protocol per slicing level ----------
+    WriteProtocol wp;
+    build_write_protocol(c.order.data(), E, c.ptopo.data(), NP, d.n_sources, wp);
     for (int l = 0; l < kMaxLevels; ++l) {
-        const int64_t S = int64_t(1) << l;
-        std::fill(first.begin(), first.end(), -1);
-        std::fill(shared.begin(), shared.end(), 0);
-        for (int64_t s = 0; s < S; ++s) {
-            const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
-            for (int64_t p = p0; p < p1; ++p) {
-                const int64_t e = c.order[p];
-                for (int a = 0; a < NP; ++a) {
-                    int32_t nd = c.ptopo[NP * e + a];
-                    if (first[nd] < 0) first[nd] = (int32_t)s;
-                    else if (first[nd] != (int32_t)s) shared[nd] = 1;
-                }
-            }
-        }
-        for (int64_t p = 0; p < E; ++p) {
-            const int64_t e = c.order[p];
-            uint32_t m = 0;
-            for (int a = 0; a < NP; ++a)
-                if (shared[c.ptopo[NP * e + a]]) m |= 1u << a;
-            masks[(size_t)l * E + p] = m;
-        }
-        std::copy(shared.begin(), shared.end(), node_shared.begin() + (size_t)l * d.n_sources);
+        c.k2_fix_off[l] = wp.fix_off[l];
+        c.k2_nfix[l] = wp.nfix[l];
+        c.k2_nside[l] = wp.nside[l];
+        c.k2_widen_off[l] = wp.widen_off[l];
+        c.k2_nwiden[l] = wp.nwiden[l];
     }
-
-    // ---- write protocol of the mixed assembly per slicing level --------------
-    // Each (row, node) entry is written by the one thread that owns its row in
-    // the node's slice: its first contribution stores, later ones add, the last
-    // one converts; nodes shared between slices go through side slots.
-    std::vector<uint32_t> k2_flags((size_t)kMaxLevels * E, 0u);
-    std::vector<int32_t> k2_side((size_t)kMaxLevels * E * NP, -1);
-    std::vector<int32_t> k2_fix;
-    {
-        const int64_t Nn = d.n_sources;
-        std::vector<int64_t> stamp(Nn), fpos(Nn), lpos(Nn);
-        std::vector<int32_t> slot_of(Nn), ring_of(Nn);
-        std::vector<std::vector<int32_t>> node_slots(Nn);
-        std::vector<uint8_t> touched(Nn);
-        std::vector<int32_t> opened;
-        std::vector<std::pair<int64_t, int32_t>> spans;
-        for (int l = 0; l < kMaxLevels; ++l) {
-            const int64_t S = int64_t(1) << l;
-            const uint8_t *sh = node_shared.data() + (size_t)l * Nn;
-            std::fill(stamp.begin(), stamp.end(), -1);
-            std::fill(touched.begin(), touched.end(), 0);
-            std::fill(ring_of.begin(), ring_of.end(), -1);
-            for (auto &v : node_slots) v.clear();
-            int64_t nside = 0;
-            for (int64_t s = 0; s < S; ++s) {
-                const int64_t p0 = s * E / S, p1 = (s + 1) * E / S;
-                opened.clear();
-                for (int64_t p = p0; p < p1; ++p) {
-                    const int64_t e = c.order[p];
-                    for (int a = 0; a < NP; ++a) {
-                        const int32_t nd = c.ptopo[NP * e + a];
-                        touched[nd] = 1;
-                        if (stamp[nd] != s) {
-                            stamp[nd] = s;
-                            fpos[nd] = p;
-                            if (sh[nd]) {
-                                if (nside >= INT32_MAX) fail(BIE_ERR_INVALID, "mesh too large for the slot index");
-                                slot_of[nd] = (int32_t)nside;
-                                node_slots[nd].push_back((int32_t)nside);
-                                ++nside;
-                            } else {
-                                opened.push_back(nd);
-                            }
-                        }
-                        lpos[nd] = p;
-                    }
-                }
-                // ring slots for the slice's own nodes with several
-                // contributions: spans [fpos, lpos] in order of their last
-                // position, each to the slot that became free latest before
-                // the span opens (the most spans of any assignment)
-                spans.clear();
-                for (int32_t nd : opened)
-                    if (fpos[nd] != lpos[nd]) spans.push_back({lpos[nd], nd});
-                std::sort(spans.begin(), spans.end());
-                int64_t slot_end[kK2RingSlots];
-                std::fill(slot_end, slot_end + kK2RingSlots, int64_t(-1));
-                for (const auto &sp : spans) {
-                    const int32_t nd = sp.second;
-                    int best = -1;
-                    for (int k = 0; k < kK2RingSlots; ++k)
-                        if (slot_end[k] < fpos[nd] && (best < 0 || slot_end[k] > slot_end[best])) best = k;
-                    if (best < 0) continue;
-                    slot_end[best] = lpos[nd];
-                    ring_of[nd] = best;
-                }
-                for (int64_t p = p0; p < p1; ++p) {
-                    const int64_t e = c.order[p];
-                    uint32_t w = 0;
-                    for (int a = 0; a < NP; ++a) {
-                        const int32_t nd = c.ptopo[NP * e + a];
-                        if (fpos[nd] == p) w |= 1u << a;
-                        if (lpos[nd] == p) w |= 1u << (8 + a);
-                        if (sh[nd]) {
-                            w |= 1u << (16 + a);
-                            k2_side[((size_t)l * E + p) * NP + a] = slot_of[nd];
-                        } else if (ring_of[nd] >= 0) {
-                            w |= 1u << (24 + a);
-                            k2_side[((size_t)l * E + p) * NP + a] = ring_of[nd];
-                        }
-                    }
-                    k2_flags[(size_t)l * E + p] = w;
-                }
-            }
-            // fix-up list: shared nodes with their slots, untouched nodes with
-            // none; widening list: nodes of one slice with several contributions
-            // and no ring slot (their entries hold float partial sums until the
-            // widening pass)
-            std::vector<int32_t> nodes, ptr{0}, slots, widen;
-            for (int64_t nd = 0; nd < Nn; ++nd) {
-                if (touched[nd] && !sh[nd]) {
-                    if (fpos[nd] != lpos[nd] && ring_of[nd] < 0) widen.push_back((int32_t)nd);
-                    continue;
-                }
-                nodes.push_back((int32_t)nd);
-                for (int32_t k : node_slots[nd]) slots.push_back(k);
-                ptr.push_back((int32_t)slots.size());
-            }
-            c.k2_fix_off[l] = (int64_t)k2_fix.size();
-            c.k2_nfix[l] = (int64_t)nodes.size();
-            c.k2_nside[l] = nside;
-            c.k2_nwiden[l] = (int64_t)widen.size();
-            k2_fix.insert(k2_fix.end(), nodes.begin(), nodes.end());
-            k2_fix.insert(k2_fix.end(), ptr.begin(), ptr.end());
-            k2_fix.insert(k2_fix.end(), slots.begin(), slots.end());
-            c.k2_widen_off[l] = (int64_t)k2_fix.size();
-            k2_fix.insert(k2_fix.end(), widen.begin(), widen.end());
-        }
-    }
+    const std::vector<uint32_t> &masks = wp.masks;
+    const std::vector<uint8_t> &node_shared = wp.node_shared;
+    const std::vector<uint32_t> &k2_flags = wp.k2_flags;
+    const std::vector<int32_t> &k2_side = wp.k2_side;
+    const std::vector<int32_t> &k2_fix = wp.k2_fix;
 
     // ---- device upload --------------------------------------------------------
     int ndev = 0;

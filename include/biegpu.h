@@ -711,6 +711,26 @@ BIE_API int bie_visco_thermal_constants(double freq, double S, double pa, double
 BIE_API int bie_tangential_derivatives(const bie_mesh_desc *mesh, int64_t *nnz, int64_t *row_ptr,
                                        int64_t *cols, double *Dx, double *Dy, double *Dz);
 
+/* Element slicing of the assembly kernels, on the host (no GPU, no context).
+ * The kernels process the elements in the order of a recursive coordinate
+ * bisection of their centroids and split that order into 2^l slices of
+ * consecutive elements (bie_ctx_get_shape reports the level l in use); the
+ * mixed assembly writes each node's entries by the rule of its kind below.
+ * order: E 1-based element numbers in processing order, or NULL.
+ * counts: 6 node counts for `level` (0..7), or NULL:
+ *   [0] nodes touched by elements of two or more slices (summed in side slots
+ *       and added by a fix-up pass),
+ *   [1] side slots: (slice, shared node) pairs,
+ *   [2] nodes of one slice with several contributions, summed in the
+ *       per-block shared-memory ring and written once,
+ *   [3] nodes of one slice with several contributions and no free ring slot
+ *       (float partial sums, then the widening pass),
+ *   [4] nodes with exactly one contribution,
+ *   [5] nodes touched by no element (written as zero).
+ * Replaces nothing in the reference: its assembly loops over collocation
+ * points (src/3d/assembly_collocation.jl:270-353) and has no element order. */
+BIE_API int bie_element_slicing(const bie_mesh_desc *mesh, int level, int32_t *order, int64_t *counts);
+
 typedef struct bie_lossy_opts {
     double  S;              /* sign convention of the constants (0: 1, as LossyGlobalOuter)    */
     int32_t custom_air;     /* 0: 101325 Pa, 20 C, 50 % humidity; 1: pa, t, Hr below          */
