@@ -6,6 +6,11 @@
 * total quadrature weight = sphere area 4 pi, test/3d/fmm_test.jl:11-28
 * rule weights sum to 1/2, test/3d/surface_functions_test.jl:16,37
 * mesh sizes, test/3d/meshing_test.jl:23
+* entry level: F, G, C at field points against an integration written here
+  from the integral definitions (greens3d!, freens3d!, freens3dk0!,
+  src/3d/kernels.jl:13-55; the normal -(x_u x x_v)/|x_u x x_v| of jacobian!,
+  src/3d/jacobian.jl:63-87; the bases of src/3d/surface_functions.jl:191-236),
+  independent of the oracle's rules, nearest-node choice and per-node sums
 """
 from __future__ import annotations
 
@@ -98,3 +103,73 @@ def test_oracle_taylor_derivatives_match_finite_differences():
     Fm, Gm, _ = oracle.assemble(mesh, k0 - h, n=2, m=2)
     assert np.linalg.norm((Fp - Fm) / (2 * h) - F[:, :, 1]) / np.linalg.norm(F[:, :, 1]) < 1e-8
     assert np.linalg.norm((Gp - Gm) / (2 * h) - G[:, :, 1]) / np.linalg.norm(G[:, :, 1]) < 1e-8
+
+
+# ---- entry-level pin --------------------------------------------------------
+
+def _tri_linear(u, v):
+    one, zero = np.ones_like(u), np.zeros_like(u)
+    return np.array([1 - u - v, u, v]), np.array([-one, one, zero]), np.array([-one, zero, one])
+
+
+def _tri_quadratic(u, v):
+    w = 1 - u - v
+    N = np.array([w * (1 - 2 * v - 2 * u), u * (2 * u - 1), v * (2 * v - 1), 4 * u * w, 4 * u * v, 4 * v * w])
+    dNu = np.array([-(2 * w - 1) - 2 * w, 4 * u - 1, 0 * u, 4 * w - 4 * u, 4 * v, -4 * v])
+    dNv = np.array([-(2 * w - 1) - 2 * w, 0 * u, 4 * v - 1, -4 * u, 4 * u, 4 * w - 4 * v])
+    return N, dNu, dNv
+
+
+def _integrate_definitions(mesh, k, targets, nq=16):
+    """F, G, C at off-surface targets by a collapsed nq x nq Gauss-Legendre
+    rule on every element (u = a (1 - b), v = a b, weight a)."""
+    x, w = np.polynomial.legendre.leggauss(nq)
+    x, w = (x + 1) / 2, w / 2
+    a, b = (g.ravel() for g in np.meshgrid(x, x, indexing="ij"))
+    wt = np.outer(w, w).ravel() * a
+    u, v = a * (1 - b), a * b
+    geo = _tri_linear if mesh.shape_function == "linear" else _tri_quadratic
+    phys = _tri_linear if mesh.physics_function == "linear" else _tri_quadratic
+    Ng, dNu, dNv = geo(u, v)
+    Np = phys(u, v)[0]
+    M, N = targets.shape[1], mesh.n_sources
+    F, G, C = np.zeros((M, N), complex), np.zeros((M, N), complex), np.zeros(M, complex)
+    topo, ptopo = mesh.topology - 1, mesh.physics_topology - 1
+    for e in range(topo.shape[1]):
+        X = mesh.coordinates[:, topo[:, e]]
+        xq, cr = X @ Ng, np.cross((X @ dNu).T, (X @ dNv).T).T
+        jac = np.linalg.norm(cr, axis=0)
+        nrm = -cr / jac
+        for i in range(M):
+            d = xq - targets[:, i:i + 1]
+            r = np.linalg.norm(d, axis=0)
+            dn = (d * nrm).sum(axis=0)
+            jw = jac * wt
+            G[i, ptopo[:, e]] += Np @ (np.exp(1j * k * r) / (4 * np.pi * r) * jw)
+            F[i, ptopo[:, e]] += Np @ (np.exp(1j * k * r) * (1j * k * r - 1) * dn / (4 * np.pi * r ** 3) * jw)
+            C[i] += np.sum(-dn / (4 * np.pi * r ** 3) * jw)
+    return F, G, C
+
+
+@pytest.mark.parametrize("k", [1.5, 2.0 + 0.3j])
+@pytest.mark.parametrize("geometry,physics,f,tol", [("linear", "geometry", 3, 1e-11),
+                                                    ("quadratic", "geometry", 2, 1e-8),
+                                                    ("quadratic", "linear", 2, 1e-8)])
+def test_oracle_entries_match_integral_definitions(geometry, physics, f, tol, k):
+    mesh = bm.icosphere(f, geometry=geometry, physics=physics)
+    rng = np.random.default_rng(3)
+    d = rng.normal(size=(3, 6))
+    targets = d / np.linalg.norm(d, axis=0) * np.array([2.0, 2.5, 3.0, 1.6, 4.0, 2.2])
+    Fi, Gi, Ci = _integrate_definitions(mesh, k, targets)
+    # 8 x 8 rules: the oracle's own quadrature error is below the tolerance
+    Fo, Go, Co = oracle.assemble(mesh, k, targets=targets, n=8, m=8)
+    assert np.linalg.norm(Fo - Fi) <= tol * np.linalg.norm(Fi)
+    assert np.linalg.norm(Go - Gi) <= tol * np.linalg.norm(Gi)
+    assert np.max(np.abs(Fo - Fi)) <= 5 * tol * np.max(np.abs(Fi))
+    # exterior points: the free term vanishes (Gauss's law) in both
+    assert np.max(np.abs(Co - Ci)) <= tol and np.max(np.abs(Ci)) <= 1e-12
+    # and the rules the assembly uses by default (n = m = 4) stay within their
+    # quadrature error of the definitions
+    F4, G4, _ = oracle.assemble(mesh, k, targets=targets, n=4, m=4)
+    assert np.linalg.norm(F4 - Fi) <= 2e-4 * np.linalg.norm(Fi)
+    assert np.linalg.norm(G4 - Gi) <= 5e-5 * np.linalg.norm(Gi)
