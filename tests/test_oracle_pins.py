@@ -9,7 +9,8 @@
 * entry level: F, G, C at field points against an integration written here
   from the integral definitions (greens3d!, freens3d!, freens3dk0!,
   src/3d/kernels.jl:13-55; the normal -(x_u x x_v)/|x_u x x_v| of jacobian!,
-  src/3d/jacobian.jl:63-87; the bases of src/3d/surface_functions.jl:191-236),
+  src/3d/jacobian.jl:63-87; the bases of src/3d/surface_functions.jl:191-300,
+  continuous and discontinuous),
   independent of the oracle's rules, nearest-node choice and per-node sums
 """
 from __future__ import annotations
@@ -120,6 +121,18 @@ def _tri_quadratic(u, v):
     return N, dNu, dNv
 
 
+def _disc_basis(kind, beta, u, v):
+    """Discontinuous triangle bases (src/3d/surface_functions.jl:242-300):
+    psi(s) = (s - beta) / (1 - 3 beta) of 1 - u - v, u, v."""
+    if kind == "disctriconstant":
+        return np.ones((1, u.size))
+    p3, pu, pv = ((s - beta) / (1 - 3 * beta) for s in (1 - u - v, u, v))
+    if kind == "disctrilinear":
+        return np.array([p3, pu, pv])
+    return np.array([p3 * (2 * p3 - 1), pu * (2 * pu - 1), pv * (2 * pv - 1), 4 * pu * p3, 4 * pu * pv,
+                     4 * pv * p3])
+
+
 def _integrate_definitions(mesh, k, targets, nq=16):
     """F, G, C at off-surface targets by a collapsed nq x nq Gauss-Legendre
     rule on every element (u = a (1 - b), v = a b, weight a)."""
@@ -129,9 +142,11 @@ def _integrate_definitions(mesh, k, targets, nq=16):
     wt = np.outer(w, w).ravel() * a
     u, v = a * (1 - b), a * b
     geo = _tri_linear if mesh.shape_function == "linear" else _tri_quadratic
-    phys = _tri_linear if mesh.physics_function == "linear" else _tri_quadratic
     Ng, dNu, dNv = geo(u, v)
-    Np = phys(u, v)[0]
+    if mesh.physics_function.startswith("disctri"):
+        Np = _disc_basis(mesh.physics_function, mesh.physics_beta, u, v)
+    else:
+        Np = (_tri_linear if mesh.physics_function == "linear" else _tri_quadratic)(u, v)[0]
     M, N = targets.shape[1], mesh.n_sources
     F, G, C = np.zeros((M, N), complex), np.zeros((M, N), complex), np.zeros(M, complex)
     topo, ptopo = mesh.topology - 1, mesh.physics_topology - 1
@@ -154,7 +169,11 @@ def _integrate_definitions(mesh, k, targets, nq=16):
 @pytest.mark.parametrize("k", [1.5, 2.0 + 0.3j])
 @pytest.mark.parametrize("geometry,physics,f,tol", [("linear", "geometry", 3, 1e-11),
                                                     ("quadratic", "geometry", 2, 1e-8),
-                                                    ("quadratic", "linear", 2, 1e-8)])
+                                                    ("quadratic", "linear", 2, 1e-8),
+                                                    ("linear", "disctriconstant", 3, 1e-11),
+                                                    ("linear", "disctrilinear", 3, 1e-11),
+                                                    ("linear", "disctriquadratic", 2, 1e-9),
+                                                    ("quadratic", "disctrilinear", 2, 1e-8)])
 def test_oracle_entries_match_integral_definitions(geometry, physics, f, tol, k):
     mesh = bm.icosphere(f, geometry=geometry, physics=physics)
     rng = np.random.default_rng(3)
