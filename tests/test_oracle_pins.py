@@ -11,7 +11,9 @@
   src/3d/kernels.jl:13-55; the normal -(x_u x x_v)/|x_u x x_v| of jacobian!,
   src/3d/jacobian.jl:63-87; the bases of src/3d/surface_functions.jl:191-300,
   continuous and discontinuous),
-  independent of the oracle's rules, nearest-node choice and per-node sums
+  independent of the oracle's rules, nearest-node choice and per-node sums;
+  at the mesh's own nodes too (continuous physics), with the singular and
+  near-singular elements integrated by rules collapsed at the target
 """
 from __future__ import annotations
 
@@ -192,3 +194,76 @@ def test_oracle_entries_match_integral_definitions(geometry, physics, f, tol, k)
     F4, G4, _ = oracle.assemble(mesh, k, targets=targets, n=4, m=4)
     assert np.linalg.norm(F4 - Fi) <= 2e-4 * np.linalg.norm(Fi)
     assert np.linalg.norm(G4 - Gi) <= 5e-5 * np.linalg.norm(Gi)
+
+
+# physics node positions of the continuous triangles (get_nodal_nodes_u/v,
+# src/3d/SurfaceFunction.jl:426-429)
+_NODE_UV = {3: [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0)],
+            6: [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0), (0.5, 0.0), (0.5, 0.5), (0.0, 0.5)]}
+
+
+def _collapsed_rule(P, nq):
+    """Points and weights on the reference triangle, split into triangles
+    with the common vertex P, each Duffy-collapsed there (integrable 1/r at P)."""
+    x, w = np.polynomial.legendre.leggauss(nq)
+    x, w = (x + 1) / 2, w / 2
+    a, b = (g.ravel() for g in np.meshgrid(x, x, indexing="ij"))
+    wt = np.outer(w, w).ravel() * a
+    P = np.asarray(P, dtype=float)
+    corners = [np.array(c) for c in [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0)]]
+    U, V, W = [], [], []
+    for i in range(3):
+        A, B = corners[i] - P, corners[(i + 1) % 3] - P
+        det = abs(A[0] * B[1] - A[1] * B[0])
+        if det > 1e-14:
+            pts = P[:, None] + a * (A[:, None] * (1 - b) + B[:, None] * b)
+            U.append(pts[0]), V.append(pts[1]), W.append(wt * det)
+    return np.concatenate(U), np.concatenate(V), np.concatenate(W)
+
+
+def _integrate_collocation(mesh, k, nq=24):
+    """F, G, C at the mesh's own nodes: every element's rule is collapsed at
+    the target's node if the element has it, else at the element's node
+    nearest the target (near-singular neighbours)."""
+    geo = _tri_linear if mesh.shape_function == "linear" else _tri_quadratic
+    phys = _tri_linear if mesh.physics_function == "linear" else _tri_quadratic
+    topo, ptopo = mesh.topology - 1, mesh.physics_topology - 1
+    S, N = mesh.sources, mesh.n_sources
+    nuv = _NODE_UV[ptopo.shape[0]]
+    F, G, C = np.zeros((N, N), complex), np.zeros((N, N), complex), np.zeros(N, complex)
+    for e in range(topo.shape[1]):
+        X = mesh.coordinates[:, topo[:, e]]
+        for i in range(N):
+            own = np.flatnonzero(ptopo[:, e] == i)
+            if own.size:
+                P = nuv[own[0]]
+            else:
+                P = nuv[int(np.argmin(np.linalg.norm(S[:, ptopo[:, e]] - S[:, i:i + 1], axis=0)))]
+            u, v, wt = _collapsed_rule(P, nq)
+            Ng, dNu, dNv = geo(u, v)
+            Np = phys(u, v)[0]
+            xq, cr = X @ Ng, np.cross((X @ dNu).T, (X @ dNv).T).T
+            jac = np.linalg.norm(cr, axis=0)
+            d = xq - S[:, i:i + 1]
+            r = np.linalg.norm(d, axis=0)
+            dn = (d * (-cr / jac)).sum(axis=0)
+            jw = jac * wt
+            G[i, ptopo[:, e]] += Np @ (np.exp(1j * k * r) / (4 * np.pi * r) * jw)
+            F[i, ptopo[:, e]] += Np @ (np.exp(1j * k * r) * (1j * k * r - 1) * dn / (4 * np.pi * r ** 3) * jw)
+            C[i] += np.sum(-dn / (4 * np.pi * r ** 3) * jw)
+    return F, G, C
+
+
+@pytest.mark.parametrize("geometry,physics,f,tol", [("linear", "geometry", 2, 1e-12),
+                                                    ("quadratic", "geometry", 1, 2e-9),
+                                                    ("quadratic", "linear", 1, 1e-11)])
+def test_oracle_collocation_entries_match_integral_definitions(geometry, physics, f, tol):
+    # on-surface targets: the singular element (Duffy rule at a vertex, two
+    # half-Duffy triangles at an edge midpoint) and its near neighbours
+    mesh = bm.icosphere(f, geometry=geometry, physics=physics)
+    k = 1.5 + 0.2j
+    Fi, Gi, Ci = _integrate_collocation(mesh, k)
+    Fo, Go, Co = oracle.assemble(mesh, k, n=12, m=12)
+    assert np.linalg.norm(Fo - Fi) <= tol * np.linalg.norm(Fi)
+    assert np.linalg.norm(Go - Gi) <= tol * np.linalg.norm(Gi)
+    assert np.max(np.abs(Co - Ci)) <= tol
