@@ -328,8 +328,11 @@ BIE_API int bie_matvec_device(bie_ctx *ctx, double k_re, double k_im,
  * executions overlap on the GPU race and must be serialised by the caller.
  * Inputs and outputs are device pointers as in bie_matvec_device; the call is
  * asynchronous on the context stream.  Results agree with bie_matvec_device
- * to the mixed-precision tolerance (same deferred-pair capacity, M*64+4096
- * pairs integrated by the FP64 correction kernel).
+ * to the mixed-precision tolerance: near pairs go to the FP64 correction
+ * kernel up to the same capacity (M*64+4096 pairs) where the array has room
+ * for it, shrunk for large meshes down to M*16+1024 pairs; pairs beyond it are
+ * integrated in FP64 inside the product kernel (slower, with both halves of
+ * each FP64 value added to the double-float row sums).
  */
 BIE_API int bie_matvec_device_noalloc(bie_ctx *ctx, double k_re, double k_im,
                                       const double *d_targets, int64_t n_targets,
