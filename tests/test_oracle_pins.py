@@ -13,7 +13,9 @@
   continuous and discontinuous),
   independent of the oracle's rules, nearest-node choice and per-node sums;
   at the mesh's own nodes too (continuous physics), with the singular and
-  near-singular elements integrated by rules collapsed at the target
+  near-singular elements integrated by rules collapsed at the target, and
+  the near field of sparse_assemble_parallel! (adaptive subdivision) within
+  the adaptive scheme's accuracy
 """
 from __future__ import annotations
 
@@ -267,3 +269,44 @@ def test_oracle_collocation_entries_match_integral_definitions(geometry, physics
     assert np.linalg.norm(Fo - Fi) <= tol * np.linalg.norm(Fi)
     assert np.linalg.norm(Go - Gi) <= tol * np.linalg.norm(Gi)
     assert np.max(np.abs(Co - Ci)) <= tol
+
+
+@pytest.mark.parametrize("geometry,physics,f", [("linear", "geometry", 3), ("quadratic", "geometry", 2),
+                                                ("quadratic", "linear", 2)])
+def test_oracle_near_field_matches_integral_definitions(geometry, physics, f):
+    # sparse_assemble_parallel! at depth 1 (src/3d/assembly_collocation_losses.jl:
+    # 200-405): each node's own elements by adaptive subdivision towards it
+    # (singular_triangle_integration, src/3d/adaptive_integration.jl:172-246,
+    # 3-point rules, TolE 1e-6), against the same entries integrated here by
+    # rules collapsed at the node; the adaptive scheme's accuracy sets the bound
+    mesh = bm.icosphere(f, geometry=geometry, physics=physics)
+    k = 1.5 + 0.2j
+    topo, ptopo = mesh.topology - 1, mesh.physics_topology - 1
+    geo = _tri_linear if geometry == "linear" else _tri_quadratic
+    phys = _tri_linear if mesh.physics_function == "linear" else _tri_quadratic
+    nuv = _NODE_UV[ptopo.shape[0]]
+    S, N = mesh.sources, mesh.n_sources
+    Fi, Gi = np.zeros((N, N), complex), np.zeros((N, N), complex)
+    for e in range(topo.shape[1]):
+        X = mesh.coordinates[:, topo[:, e]]
+        for a, i in enumerate(ptopo[:, e]):
+            u, v, wt = _collapsed_rule(nuv[a], 24)
+            Ng, dNu, dNv = geo(u, v)
+            Np = phys(u, v)[0]
+            xq, cr = X @ Ng, np.cross((X @ dNu).T, (X @ dNv).T).T
+            jac = np.linalg.norm(cr, axis=0)
+            d = xq - S[:, i:i + 1]
+            r = np.linalg.norm(d, axis=0)
+            dn = (d * (-cr / jac)).sum(axis=0)
+            Gi[i, ptopo[:, e]] += Np @ (np.exp(1j * k * r) / (4 * np.pi * r) * jac * wt)
+            Fi[i, ptopo[:, e]] += Np @ (np.exp(1j * k * r) * (1j * k * r - 1) * dn / (4 * np.pi * r ** 3) * jac * wt)
+    rp, cols, Fv, Gv = oracle.nearfield(mesh, k, depth=1)
+    Fo, Go = np.zeros((N, N), complex), np.zeros((N, N), complex)
+    for i in range(N):
+        Fo[i, cols[rp[i]:rp[i + 1]]] = Fv[rp[i]:rp[i + 1]]
+        Go[i, cols[rp[i]:rp[i + 1]]] = Gv[rp[i]:rp[i + 1]]
+    assert np.linalg.norm(Go - Gi) <= 3e-4 * np.linalg.norm(Gi)
+    if geometry == "linear":   # flat elements: (x - y).n = 0 on a node's own elements
+        assert np.max(np.abs(Fo)) <= 1e-7 * np.max(np.abs(Go)) and np.max(np.abs(Fi)) <= 1e-12
+    else:
+        assert np.linalg.norm(Fo - Fi) <= 3e-4 * np.linalg.norm(Fi)
