@@ -442,10 +442,10 @@ std::vector<int32_t> bisection_order(const double *coords, int64_t n_coords, con
     std::iota(order.begin(), order.end(), 0);
     {
         struct Range { int64_t p0, p1, num, den; };   // [p0, p1) = [num*E/den, (num+1)*E/den)
-        std::vector<Range> todo{{0, E, 0, 1}};
-        while (!todo.empty()) {
-            const Range r = todo.back();
-            todo.pop_back();
+        std::vector<Range> pending{{0, E, 0, 1}};
+        while (!pending.empty()) {
+            const Range r = pending.back();
+            pending.pop_back();
             auto b = order.begin();
             if (r.p1 - r.p0 <= 2 || r.den > (int64_t(1) << 40)) {
                 std::sort(b + r.p0, b + r.p1, [&](int32_t x, int32_t y) {
@@ -468,8 +468,8 @@ std::vector<int32_t> bisection_order(const double *coords, int64_t n_coords, con
                 const double cx = cen[3 * (int64_t)x + ax], cy = cen[3 * (int64_t)y + ax];
                 return cx != cy ? cx < cy : x < y;
             });
-            todo.push_back({mid, r.p1, left + 1, den});
-            todo.push_back({r.p0, mid, left, den});
+            pending.push_back({mid, r.p1, left + 1, den});
+            pending.push_back({r.p0, mid, left, den});
         }
     }
     return order;

@@ -47,9 +47,9 @@ def bisection_order(mesh):
         q = np.clip(t * 1023.0, 0.0, 1023.0).astype(np.uint32)
         key |= (_spread10(q) << k).astype(np.uint64)
     order = np.arange(E)
-    todo = [(0, E, 0, 1)]
-    while todo:
-        p0, p1, num, den = todo.pop()
+    pending = [(0, E, 0, 1)]
+    while pending:
+        p0, p1, num, den = pending.pop()
         seg = order[p0:p1]
         if p1 - p0 <= 2:
             order[p0:p1] = seg[np.lexsort((seg, key[seg]))]
@@ -59,8 +59,8 @@ def bisection_order(mesh):
         ax = int(np.argmax(ext))   # first of equal extents, as the strict > of the library
         mid = (2 * num + 1) * E // (2 * den)
         order[p0:p1] = seg[np.lexsort((seg, cen[ax, seg]))]
-        todo.append((mid, p1, 2 * num + 1, 2 * den))
-        todo.append((p0, mid, 2 * num, 2 * den))
+        pending.append((mid, p1, 2 * num + 1, 2 * den))
+        pending.append((p0, mid, 2 * num, 2 * den))
     return order
 
 
