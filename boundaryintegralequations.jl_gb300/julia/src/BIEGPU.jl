@@ -765,8 +765,38 @@ gmres_gpu(L::GPULossyGlobalOuter, b; kwargs...) = gmres_gpu(GPULossyBlock(L, Cin
 
 version() = unsafe_string(ccall((:bie_version, libbiegpu), Cstring, ()))
 
+"""
+    order, counts = element_slicing(mesh, level)
+
+The element slicing of the assembly kernels, computed on the host
+(`bie_element_slicing`, no GPU): `order` holds the 1-based element numbers in
+the order the kernels process them (a recursive coordinate bisection of the
+element centroids); `counts` the nodes of each kind at slicing level `level`
+(2^level slices, 0..7) as a NamedTuple: shared between slices (with their
+side slots), of one slice with several contributions summed in the
+shared-memory ring or widened afterwards, with one contribution, untouched.
+"""
+function element_slicing(mesh, level::Integer)
+    coords = Matrix{Float64}(mesh.coordinates)
+    topo = Matrix{Int64}(mesh.topology)
+    ptopo = Matrix{Int64}(mesh.physics_topology)
+    src = Matrix{Float64}(mesh.sources)
+    pk, pb = physics_kind(mesh.physics_function, size(ptopo, 1))
+    order = Vector{Int32}(undef, size(topo, 2))
+    counts = zeros(Int64, 6)
+    GC.@preserve coords topo ptopo src begin
+        desc = Ref(MeshDesc(size(coords, 2), pointer(coords), size(topo, 2), element_kind(size(topo, 1)), pk,
+                            pointer(topo), pointer(ptopo), size(src, 2), pointer(src), Int32(1), Int32(1), pb))
+        check(ccall((:bie_element_slicing, libbiegpu), Cint, (Ref{MeshDesc}, Cint, Ptr{Int32}, Ptr{Int64}),
+                    desc, level, order, counts))
+    end
+    return order, (shared=counts[1], side_slots=counts[2], ring=counts[3], widened=counts[4],
+                   single=counts[5], untouched=counts[6])
+end
+
 export GPU, Context, reference_rules, assemble_parallel_gpu!, GPUFOperator, GPUGOperator, evaluate_targets,
        sparse_assemble_parallel_gpu!, sweep_gpu, farfield_objective, FastFOperator, FastGOperator,
-       taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu, solve_multi_gpu, set_one_launch!
+       taylor_assemble_gpu!, GPULossyGlobalOuter, GPULossyBlock, gmres_gpu, solve_multi_gpu, set_one_launch!,
+       element_slicing
 
 end # module

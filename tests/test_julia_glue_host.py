@@ -1,0 +1,127 @@
+"""The Julia glue's `ccall`s against the C header and the built library.
+
+Julia is not installed here, so the glue (julia/src/BIEGPU.jl and the
+package extension) cannot run; this test reads it as text.  Every
+`ccall((:name, libbiegpu), Ret, (T1, ..., Tn), ...)` must name an entry point
+that include/biegpu.h declares and libbiegpu.so exports, with one argument
+type per declared parameter and of the same kind (32- or 64-bit integer,
+float, double, pointer).  The struct layouts the calls pass are checked in
+test_abi_layout.py.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+from biegpu import _capi
+
+ROOT = Path(__file__).resolve().parent.parent
+JULIA_DIR = ROOT / "boundaryintegralequations.jl_gb300" / "julia"
+HEADER = ROOT / "include" / "biegpu.h"
+
+
+def _split_top(text: str) -> list[str]:
+    """Split at commas outside (), {} and []; drop empty trailing parts."""
+    parts, depth, cur = [], 0, []
+    for ch in text:
+        if ch in "({[":
+            depth += 1
+        elif ch in ")}]":
+            depth -= 1
+        if ch == "," and depth == 0:
+            parts.append("".join(cur).strip())
+            cur = []
+        else:
+            cur.append(ch)
+    parts.append("".join(cur).strip())
+    return [p for p in parts if p]
+
+
+def _balanced(text: str, start: int) -> tuple[str, int]:
+    """Contents of the parenthesised group opening at text[start] and the index after it."""
+    assert text[start] == "("
+    depth = 0
+    for i in range(start, len(text)):
+        depth += text[i] == "("
+        depth -= text[i] == ")"
+        if depth == 0:
+            return text[start + 1:i], i + 1
+    raise ValueError("unbalanced parentheses")
+
+
+def julia_ccalls() -> dict[str, set[tuple[str, ...]]]:
+    """Per entry point, the argument kinds of every call site."""
+    src = "\n".join(re.sub(r"#.*", "", p.read_text()) for p in sorted(JULIA_DIR.rglob("*.jl")))
+    calls: dict[str, set[tuple[str, ...]]] = {}
+    for m in re.finditer(r"ccall\(\(:(\w+),\s*libbiegpu\),", src):
+        rest = src[m.end():]
+        # return type, then the argument type tuple
+        i = 0
+        depth = 0
+        while not (rest[i] == "," and depth == 0):
+            depth += rest[i] in "({["
+            depth -= rest[i] in ")}]"
+            i += 1
+        j = i + 1
+        while rest[j].isspace():
+            j += 1
+        types, _ = _balanced(rest, j)
+        calls.setdefault(m.group(1), set()).add(tuple(_julia_kind(t) for t in _split_top(types)))
+    return calls
+
+
+_JULIA_SCALARS = {"Cint": "i32", "Int32": "i32", "Cuint": "i32", "UInt32": "i32", "Int64": "i64",
+                  "Clonglong": "i64", "UInt64": "i64", "Csize_t": "i64", "Cdouble": "f64", "Float64": "f64",
+                  "Cfloat": "f32", "Float32": "f32"}
+
+
+def _julia_kind(t: str) -> str:
+    t = t.strip()
+    if t.startswith(("Ptr{", "Ref{")) or t in ("Cstring", "Ptr"):
+        return "ptr"
+    return _JULIA_SCALARS.get(t, "?" + t)
+
+
+def _c_kind(param: str) -> str:
+    p = re.sub(r"\bconst\b", "", param).strip()
+    if "*" in p or "[" in p:
+        return "ptr"
+    base = p.rsplit(None, 1)[0] if len(p.split()) > 1 else p
+    return {"int": "i32", "unsigned": "i32", "int32_t": "i32", "uint32_t": "i32", "int64_t": "i64",
+            "uint64_t": "i64", "size_t": "i64", "double": "f64", "float": "f32"}.get(base, "?" + base)
+
+
+def header_decls() -> dict[str, tuple[str, ...]]:
+    """Per declared entry point, the kinds of its parameters."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    decls = {}
+    for m in re.finditer(r"BIE_API\s+[\w\s\*]+?\b(bie_\w+)\s*\(", text):
+        params, _ = _balanced(text, m.end() - 1)
+        p = _split_top(params)
+        decls[m.group(1)] = () if p == ["void"] else tuple(_c_kind(x) for x in p)
+    return decls
+
+
+def test_every_julia_ccall_matches_a_declared_exported_entry():
+    calls = julia_ccalls()
+    decls = header_decls()
+    lib = C.CDLL(str(_capi.library_path()))
+    assert len(calls) >= 20, sorted(calls)
+    for name, sites in sorted(calls.items()):
+        assert name in decls, f"{name} is called from Julia but not declared in biegpu.h"
+        assert hasattr(lib, name), f"{name} is not exported by libbiegpu.so"
+        for kinds in sites:
+            assert kinds == decls[name], f"{name}: Julia passes {kinds}, C takes {decls[name]}"
+
+
+def test_parser_reads_known_signatures():
+    decls = header_decls()
+    assert decls["bie_version"] == ()
+    assert decls["bie_element_slicing"] == ("ptr", "i32", "ptr", "ptr")
+    assert decls["bie_ctx_create"] == ("ptr", "ptr", "i32")
+    assert decls["bie_assemble"][1:3] == ("f64", "f64")
+    assert all("?" not in k for kinds in decls.values() for k in kinds), decls
+    calls = julia_ccalls()
+    assert calls["bie_ctx_destroy"] == {("ptr",)}
+    assert calls["bie_element_slicing"] == {("ptr", "i32", "ptr", "ptr")}
