@@ -35,6 +35,24 @@ def test_library_exports_every_declared_symbol():
     assert set(declared_symbols()) <= set(_capi.SIGNATURES)
 
 
+def _ctypes_kind(t) -> str:
+    if t in (C.c_void_p, C.c_char_p) or (isinstance(t, type) and issubclass(t, C._Pointer)):
+        return "ptr"
+    return {C.c_int32: "i32", C.c_uint32: "i32", C.c_int64: "i64", C.c_uint64: "i64", C.c_double: "f64",
+            C.c_float: "f32"}.get(t, "?" + getattr(t, "__name__", str(t)))
+
+
+def test_ctypes_signatures_match_the_header():
+    # each ctypes argument of the same kind (32/64-bit integer, float,
+    # double, pointer) as the declared parameter
+    from _c_header import header_decls
+    decls = header_decls()
+    for name, (_res, args) in _capi.SIGNATURES.items():
+        assert name in decls, f"{name} has a ctypes signature but no declaration"
+        kinds = tuple(_ctypes_kind(a) for a in args)
+        assert kinds == decls[name], f"{name}: ctypes {kinds}, C {decls[name]}"
+
+
 def test_version_and_empty_error():
     L = _capi.lib()
     assert L.bie_version().decode().startswith("biegpu")
