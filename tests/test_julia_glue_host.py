@@ -10,7 +10,6 @@ test_abi_layout.py.
 """
 from __future__ import annotations
 
-import ctypes as C
 import re
 from pathlib import Path
 
@@ -57,7 +56,7 @@ def _julia_kind(t: str) -> str:
 def test_every_julia_ccall_matches_a_declared_exported_entry():
     calls = julia_ccalls()
     decls = header_decls()
-    lib = C.CDLL(str(_capi.library_path()))
+    lib = _capi.lib()   # builds the library first if it is missing
     assert len(calls) >= 20, sorted(calls)
     for name, sites in sorted(calls.items()):
         assert name in decls, f"{name} is called from Julia but not declared in biegpu.h"
