@@ -270,7 +270,7 @@ SIGNATURES = {
     "bie_ambient_to_properties": (_I, [_D, _D, _D, _D, _P]),
     "bie_visco_thermal_constants": (_I, [_D, _D, _D, _D, _D, C.POINTER(LossyConstants)]),
     "bie_tangential_derivatives": (_I, [C.POINTER(MeshDesc), C.POINTER(_I64), _P, _P, _P, _P, _P]),
-    "bie_element_slicing": (_I, [C.POINTER(MeshDesc), _I, _P, _P]),
+    "bie_element_slicing": (_I, [C.POINTER(MeshDesc), _I, _P, _P, _P, _P]),
     "bie_lossy_create": (_I, [_P, _D, C.POINTER(LossyOpts), C.POINTER(_P)]),
     "bie_lossy_destroy": (_I, [_P]),
     "bie_lossy_constants_of": (_I, [_P, C.POINTER(LossyConstants)]),

@@ -68,7 +68,7 @@ def mesh_desc(mesh: Mesh3d):
 SLICING_COUNTS = ("shared", "side_slots", "ring", "widened", "single", "untouched")
 
 
-def element_slicing(mesh: Mesh3d, level: int):
+def element_slicing(mesh: Mesh3d, level: int, tables: bool = False):
     """The element slicing of the assembly kernels, computed on the host
     (bie_element_slicing; no GPU): (order, counts).  order: the E 1-based
     element numbers in the order the kernels process them (a recursive
@@ -76,13 +76,22 @@ def element_slicing(mesh: Mesh3d, level: int):
     kind at slicing level `level` (2^level slices), keyed by SLICING_COUNTS:
     shared between slices (with their side slots), of one slice with several
     contributions summed in the shared-memory ring or widened afterwards, with
-    one contribution, or touched by no element."""
+    one contribution, or touched by no element.  tables=True adds the write
+    protocol of the mixed assembly: (order, counts, flags, slots) with flags
+    (E uint32; per position p and local node a: bit a first, 8+a last, 16+a
+    shared, 24+a ring) and slots (n_phys x E int32: side slot, ring slot or -1)."""
     d, keep = mesh_desc(mesh)
-    order = np.empty(mesh.topology.shape[1], dtype=np.int32)
+    E, NP = mesh.topology.shape[1], mesh.physics_topology.shape[0]
+    order = np.empty(E, dtype=np.int32)
     counts = np.zeros(len(SLICING_COUNTS), dtype=np.int64)
-    _capi.check(_capi.lib().bie_element_slicing(C.byref(d), int(level), order.ctypes.data, counts.ctypes.data))
+    flags = np.empty(E, dtype=np.uint32) if tables else None
+    slots = np.empty((E, NP), dtype=np.int32) if tables else None
+    _capi.check(_capi.lib().bie_element_slicing(C.byref(d), int(level), order.ctypes.data, counts.ctypes.data,
+                                                None if flags is None else flags.ctypes.data,
+                                                None if slots is None else slots.ctypes.data))
     del keep
-    return order, dict(zip(SLICING_COUNTS, (int(v) for v in counts)))
+    out = (order, dict(zip(SLICING_COUNTS, (int(v) for v in counts))))
+    return out + (flags, slots.T.copy()) if tables else out
 
 
 class Context:

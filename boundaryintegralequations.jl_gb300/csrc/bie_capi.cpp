@@ -1031,7 +1031,8 @@ int bie_tangential_derivatives(const bie_mesh_desc *d, int64_t *nnz, int64_t *ro
     });
 }
 
-int bie_element_slicing(const bie_mesh_desc *d, int level, int32_t *order, int64_t *counts) {
+int bie_element_slicing(const bie_mesh_desc *d, int level, int32_t *order, int64_t *counts, uint32_t *flags,
+                        int32_t *slots) {
     return guarded([&] {
         if (!d) bie::fail(BIE_ERR_INVALID, "mesh must not be NULL");
         if (d->n_coordinates <= 0 || d->n_elements <= 0 || d->n_sources <= 0 || !d->coordinates || !d->topology ||
@@ -1061,15 +1062,19 @@ int bie_element_slicing(const bie_mesh_desc *d, int level, int32_t *order, int64
         const std::vector<int32_t> ord = bie::bisection_order(d->coordinates, d->n_coordinates, topo.data(), NS, E);
         if (order)
             for (int64_t p = 0; p < E; ++p) order[p] = ord[(size_t)p] + 1;
-        if (counts) {
+        if (counts || flags || slots) {
             bie::WriteProtocol w;
             bie::build_write_protocol(ord.data(), E, ptopo.data(), NP, N, w);
-            counts[0] = w.nshared[level];
-            counts[1] = w.nside[level];
-            counts[2] = w.nring[level];
-            counts[3] = w.nwiden[level];
-            counts[4] = w.nsingle[level];
-            counts[5] = w.nuntouched[level];
+            if (counts) {
+                counts[0] = w.nshared[level];
+                counts[1] = w.nside[level];
+                counts[2] = w.nring[level];
+                counts[3] = w.nwiden[level];
+                counts[4] = w.nsingle[level];
+                counts[5] = w.nuntouched[level];
+            }
+            if (flags) std::copy_n(w.k2_flags.begin() + (size_t)level * E, E, flags);
+            if (slots) std::copy_n(w.k2_side.begin() + (size_t)level * E * NP, E * NP, slots);
         }
     });
 }

@@ -787,8 +787,9 @@ function element_slicing(mesh, level::Integer)
     GC.@preserve coords topo ptopo src begin
         desc = Ref(MeshDesc(size(coords, 2), pointer(coords), size(topo, 2), element_kind(size(topo, 1)), pk,
                             pointer(topo), pointer(ptopo), size(src, 2), pointer(src), Int32(1), Int32(1), pb))
-        check(ccall((:bie_element_slicing, libbiegpu), Cint, (Ref{MeshDesc}, Cint, Ptr{Int32}, Ptr{Int64}),
-                    desc, level, order, counts))
+        check(ccall((:bie_element_slicing, libbiegpu), Cint,
+                    (Ref{MeshDesc}, Cint, Ptr{Int32}, Ptr{Int64}, Ptr{UInt32}, Ptr{Int32}),
+                    desc, level, order, counts, C_NULL, C_NULL))
     end
     return order, (shared=counts[1], side_slots=counts[2], ring=counts[3], widened=counts[4],
                    single=counts[5], untouched=counts[6])

@@ -730,9 +730,16 @@ BIE_API int bie_tangential_derivatives(const bie_mesh_desc *mesh, int64_t *nnz, 
  *       (float partial sums, then the widening pass),
  *   [4] nodes with exactly one contribution,
  *   [5] nodes touched by no element (written as zero).
+ * flags: E words, or NULL: for the element at position p of the order and
+ *   its local node a: bit a = p is the node's first position in its slice,
+ *   bit 8+a = its last, bit 16+a = the node is shared, bit 24+a = it has a
+ *   ring slot.
+ * slots: E x n_phys indices, or NULL: the node's side slot (shared nodes,
+ *   numbered over all slices), its ring slot (0..15), else -1.
  * Replaces nothing in the reference: its assembly loops over collocation
  * points (src/3d/assembly_collocation.jl:270-353) and has no element order. */
-BIE_API int bie_element_slicing(const bie_mesh_desc *mesh, int level, int32_t *order, int64_t *counts);
+BIE_API int bie_element_slicing(const bie_mesh_desc *mesh, int level, int32_t *order, int64_t *counts,
+                                uint32_t *flags, int32_t *slots);
 
 typedef struct bie_lossy_opts {
     double  S;              /* sign convention of the constants (0: 1, as LossyGlobalOuter)    */

@@ -68,10 +68,10 @@ def test_every_julia_ccall_matches_a_declared_exported_entry():
 def test_parser_reads_known_signatures():
     decls = header_decls()
     assert decls["bie_version"] == ()
-    assert decls["bie_element_slicing"] == ("ptr", "i32", "ptr", "ptr")
+    assert decls["bie_element_slicing"] == ("ptr", "i32", "ptr", "ptr", "ptr", "ptr")
     assert decls["bie_ctx_create"] == ("ptr", "ptr", "i32")
     assert decls["bie_assemble"][1:3] == ("f64", "f64")
     assert all("?" not in k for kinds in decls.values() for k in kinds), decls
     calls = julia_ccalls()
     assert calls["bie_ctx_destroy"] == {("ptr",)}
-    assert calls["bie_element_slicing"] == {("ptr", "i32", "ptr", "ptr")}
+    assert calls["bie_element_slicing"] == {("ptr", "i32", "ptr", "ptr", "ptr", "ptr")}

@@ -2,6 +2,10 @@
 no GPU): the element order and the node counts of the mixed assembly's write
 protocol, against a numpy restatement written here.
 
+The emulation at the end drives one row of the mixed assembly through the
+flags and slot indices the library builds and checks that every entry gets
+its plain sum, written once.
+
 The kernels process elements in the order of a recursive coordinate bisection
 of their centroids: the range [num*E/den, (num+1)*E/den) is split at
 (2 num + 1)*E/(2 den) across the longest side of its centroids' bounding box
@@ -195,3 +199,91 @@ def test_invalid_arguments_are_reported():
     bad.coordinates[0, 1] = np.nan
     with pytest.raises(biegpu.BIEError, match="non-finite"):
         biegpu.element_slicing(bad, 0)
+
+
+def emulate_write_protocol(mesh, level):
+    """One row of the mixed assembly under the write protocol the library
+    builds (flags and slots of bie_element_slicing), with integer
+    contributions so that sums are exact: slices in order, each element's
+    nodes through a side slot, a ring slot, the entry's partial sums or a
+    direct final write; then the widening and fix-up passes and the zero
+    columns.  Returns (entries, expected sums, final writes per node, counts)."""
+    order, counts, flags, slots = biegpu.element_slicing(mesh, level, tables=True)
+    order = order - 1
+    ptopo = mesh.physics_topology - 1
+    NP, E = ptopo.shape
+    N = mesh.n_sources
+    S = 1 << level
+    rng = np.random.default_rng(1000 + level)
+    contrib = rng.integers(1, 1 << 20, size=(E, NP)).astype(np.float64)
+    entry = np.zeros(N)
+    writes = np.zeros(N, dtype=np.int64)
+    partial = {}
+    side, side_of = {}, {}
+    seen = np.zeros(N, dtype=bool)
+    for s in range(S):
+        ring = [None] * RING_SLOTS        # (node, sum) while open
+        for p in range(s * E // S, (s + 1) * E // S):
+            w = int(flags[p])
+            for a in range(NP):
+                nd, c = ptopo[a, order[p]], contrib[p, a]
+                seen[nd] = True
+                first, last = (w >> a) & 1, (w >> (8 + a)) & 1
+                shared, ringed = (w >> (16 + a)) & 1, (w >> (24 + a)) & 1
+                k = int(slots[a, p])
+                assert not (shared and ringed)
+                if shared:
+                    assert 0 <= k < counts["side_slots"]
+                    assert side_of.setdefault(k, (s, nd)) == (s, nd), "side slot reused"
+                    assert first or k in side
+                    side[k] = c if first else side[k] + c
+                elif ringed:
+                    assert 0 <= k < RING_SLOTS and not (first and last)
+                    if first:
+                        assert ring[k] is None, "ring slot still open"
+                        ring[k] = (nd, c)
+                    else:
+                        assert ring[k] is not None and ring[k][0] == nd, "ring slot lost"
+                        ring[k] = (nd, ring[k][1] + c)
+                    if last:
+                        entry[nd] = ring[k][1]
+                        writes[nd] += 1
+                        ring[k] = None
+                else:
+                    assert k == -1
+                    if first and last:
+                        entry[nd] = c
+                        writes[nd] += 1
+                    else:
+                        assert first or nd in partial
+                        partial[nd] = c if first else partial[nd] + c
+        assert all(r is None for r in ring), "ring slot open at the end of its slice"
+    for nd, v in partial.items():          # widening pass
+        entry[nd] = v
+        writes[nd] += 1
+    fix = {}
+    for k, (_, nd) in side_of.items():     # fix-up pass
+        fix[nd] = fix.get(nd, 0.0) + side[k]
+    for nd, v in fix.items():
+        entry[nd] = v
+        writes[nd] += 1
+    writes[~seen] += 1                     # untouched nodes: zero columns
+    want = np.zeros(N)
+    np.add.at(want, ptopo[:, order].T.ravel(), contrib.ravel())
+    return entry, want, writes, counts
+
+
+@pytest.mark.parametrize("level", range(8))
+def test_write_protocol_gives_each_entry_its_sum_once(mesh, level):
+    entry, want, writes, counts = emulate_write_protocol(mesh, level)
+    assert np.all(writes == 1)
+    assert np.array_equal(entry, want)
+
+
+def test_write_protocol_with_ring_overflow():
+    # few slices: more nodes open at once than a block has ring slots, so
+    # some nodes take the float partial sums and the widening pass
+    mesh = bm.icosphere(12, geometry="quadratic")
+    entry, want, writes, counts = emulate_write_protocol(mesh, 2)
+    assert counts["widened"] > 0 and counts["ring"] > 0 and counts["shared"] > 0
+    assert np.all(writes == 1) and np.array_equal(entry, want)
